@@ -1,0 +1,36 @@
+"""GB300-native (sm_103a) geometry evaluation for tetraloma (tbetcke/gridcl) meshes.
+
+For every cell block of a mesh the native library gathers each cell's geometry nodes through
+the dofmap and contracts them with the Lagrange basis and its reference gradients at the
+quadrature points, producing physical points, Jacobians, det J (or the area element and unit
+normals on manifolds) and the (pseudo-)inverse Jacobian, in the reference's tiled QuadField
+layout. The C ABI is ``include/tlgeom.h``; this package is its host-side mirror of
+tetraloma-geometry's API.
+"""
+
+from ._lib import GridError, lib
+from .geometry import (
+    CoordinateElement,
+    Geometry,
+    GeometryBlock,
+    PointSet,
+    QuadField,
+    QuadRule,
+    detj_block,
+    facet_normals_block,
+    facet_point_set,
+    geometric_factors_block,
+    jacobians_block,
+    measure_block,
+    normals_block,
+    physical_points_block,
+    pseudo_inverse_block,
+)
+from . import meshes, refcell
+
+__all__ = [
+    "CoordinateElement", "Geometry", "GeometryBlock", "GridError", "PointSet", "QuadField",
+    "QuadRule", "detj_block", "facet_normals_block", "facet_point_set",
+    "geometric_factors_block", "jacobians_block", "lib", "measure_block", "meshes", "normals_block",
+    "physical_points_block", "pseudo_inverse_block", "refcell",
+]

@@ -1,0 +1,372 @@
+// The C ABI of include/tlgeom.h: argument checks with the reference's error kinds, device
+// tables, and the launches of the evaluation and E-vector kernels.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/tlgeom.h"
+#include "eval_launch.cuh"
+#include "refcell.h"
+#include "status.h"
+
+struct tlg_tables {
+  int cell, degree, family, td, gd, dtype;
+  int64_t k, q;
+  bool has_refn;
+  unsigned char* dev = nullptr;  // phi [Q][K] | dphi [Q][K][TD] | refn [Q][TD] | error word
+  uint32_t bytes = 0;            // staged bytes (multiple of 16), error word excluded
+  uint32_t off_dphi = 0, off_refn = 0;
+  int* err = nullptr;
+  std::vector<unsigned char> host;  // host copy of the staged bytes
+};
+
+namespace {
+thread_local std::string g_error;
+}  // namespace
+
+namespace tlg {
+
+tlg_status fail(tlg_status s, const std::string& msg) {
+  g_error = msg;
+  return s;
+}
+
+tlg_status ok() {
+  g_error.clear();
+  return TLG_OK;
+}
+
+tlg_status cuda_fail(cudaError_t e, const char* what) {
+  return fail(TLG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace tlg
+
+namespace {
+
+using tlg::cuda_fail;
+using tlg::fail;
+using tlg::ok;
+
+// Runs `f`, turning the refcell's exceptions into status codes.
+template <typename Fn>
+tlg_status guarded(Fn f) {
+  try {
+    return f();
+  } catch (const std::invalid_argument& e) {
+    return fail(TLG_ERR_INVALID_ARGUMENT, e.what());
+  } catch (const std::domain_error& e) {
+    return fail(TLG_ERR_UNSUPPORTED, e.what());
+  } catch (const std::exception& e) {
+    return fail(TLG_ERR_INVALID_ARGUMENT, e.what());
+  }
+}
+
+uint32_t align16(size_t x) { return (uint32_t)((x + 15) / 16 * 16); }
+
+int tile_shift(int tile) {
+  switch (tile) {
+    case 1: return 0;
+    case 2: return 1;
+    case 4: return 2;
+    case 8: return 3;
+    case 16: return 4;
+  }
+  return -1;
+}
+
+template <typename F>
+void narrow_into(std::vector<unsigned char>& buf, size_t off, const double* src, size_t n) {
+  F* dst = reinterpret_cast<F*>(buf.data() + off);
+  for (size_t i = 0; i < n; ++i) dst[i] = (F)src[i];
+}
+
+template <typename F>
+tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                      cudaStream_t stream) {
+  tlg::EvalArgs<F> a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = static_cast<const F*>(b->nodes);
+  a.dofmap = b->dofmap;
+  a.flags = b->flags;
+  a.tab = t->dev;
+  void* outs[6] = {o->points, o->jacobian, o->detj, o->pinv, o->normals, o->facet_normals};
+  for (int i = 0; i < 6; ++i) a.out[i] = static_cast<F*>(outs[i]);
+  for (int g = 0; g < 3; ++g) a.origin[g] = (F)b->origin[g];
+  a.err = t->err;
+  const int shift = tile_shift(o->tile);
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + o->tile - 1) / o->tile * o->tile;
+  a.out_first_cell = o->out_first_cell;
+  a.last_cell = b->num_cells - 1;
+  const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
+  a.last_flag = nflags - 1;
+  a.last_node = (uint32_t)(b->num_nodes - 1);
+  a.tab_bytes = t->bytes;
+  a.off_dphi = t->off_dphi;
+  a.off_refn = t->off_refn;
+  a.mask = mask;
+  a.num_points = (int)t->q;
+  a.tile_shift = shift;
+  a.k_runtime = (int)t->k;
+  bool direct = false;
+  cudaError_t e;
+  if constexpr (sizeof(F) == 4)
+    e = tlg::launch_eval_f32(t->td, t->gd, (int)t->k, a, t->bytes, stream, &direct);
+  else
+    e = tlg::launch_eval_f64(t->td, t->gd, (int)t->k, a, t->bytes, stream, &direct);
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  return ok();
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* tlg_last_error(void) { return g_error.c_str(); }
+
+int tlg_abi_version(void) { return TLG_ABI_VERSION; }
+
+int64_t tlg_num_lagrange_nodes(int cell, int degree) {
+  if (!tlg::valid_cell(cell) || degree < 0) return -1;
+  return tlg::num_lagrange_nodes(cell, degree);
+}
+
+tlg_status tlg_lagrange_points(int cell, int degree, int family, double* out, int64_t cap) {
+  return guarded([&] {
+    if (!out) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_lagrange_points: out is NULL");
+    const std::vector<double> p = tlg::lagrange_points(cell, degree, family);
+    if ((int64_t)p.size() > cap)
+      return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_lagrange_points: capacity " + std::to_string(cap) +
+                                               " below " + std::to_string(p.size()));
+    std::memcpy(out, p.data(), p.size() * sizeof(double));
+    return ok();
+  });
+}
+
+tlg_status tlg_collapsed_rule(int cell, const int* counts, double* points, double* weights,
+                              int64_t cap_points, int64_t* num_points) {
+  return guarded([&] {
+    if (!counts || !points || !weights || !num_points)
+      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_collapsed_rule: NULL argument");
+    const int td = tlg::tdim(cell);
+    for (int d = 0; d < td; ++d)
+      if (counts[d] < 1 || counts[d] > 64)
+        return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_collapsed_rule: point counts must be 1..64");
+    std::vector<double> p, w;
+    tlg::collapsed_rule(cell, counts, p, w);
+    if ((int64_t)w.size() > cap_points)
+      return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_collapsed_rule: capacity below the point count");
+    std::memcpy(points, p.data(), p.size() * sizeof(double));
+    std::memcpy(weights, w.data(), w.size() * sizeof(double));
+    *num_points = (int64_t)w.size();
+    return ok();
+  });
+}
+
+tlg_status tlg_tabulate(int cell, int degree, int family, const double* points, int64_t npoints,
+                        int nderivs, double* out, int64_t cap) {
+  return guarded([&] {
+    if ((!points && npoints > 0) || !out || npoints < 0)
+      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tabulate: bad points or output");
+    const std::vector<double> t = tlg::tabulate(cell, degree, family, points, (long)npoints, nderivs);
+    if ((int64_t)t.size() > cap) return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_tabulate: capacity too small");
+    std::memcpy(out, t.data(), t.size() * sizeof(double));
+    return ok();
+  });
+}
+
+tlg_status tlg_reference_facet_normals(int cell, double* out, int64_t cap) {
+  return guarded([&] {
+    if (!out) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_reference_facet_normals: out is NULL");
+    const std::vector<double> n = tlg::reference_facet_normals(cell);
+    if ((int64_t)n.size() > cap) return fail(TLG_ERR_LENGTH_MISMATCH, "capacity too small");
+    std::memcpy(out, n.data(), n.size() * sizeof(double));
+    return ok();
+  });
+}
+
+tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dtype,
+                             const double* points, int64_t npoints, const double* ref_normals,
+                             tlg_tables** out) {
+  return guarded([&]() -> tlg_status {
+    if (!out) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: out is NULL");
+    *out = nullptr;
+    if (!tlg::valid_cell(cell) || cell == tlg::kPoint)
+      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: no cell type " + std::to_string(cell));
+    if (cell == tlg::kPyramid)
+      return fail(TLG_ERR_UNSUPPORTED, "tlg_tables_create: pyramids are not supported by this build");
+    const int td = tlg::tdim(cell);
+    if (gdim < td || gdim > 3)
+      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: gdim " + std::to_string(gdim) +
+                                                " with tdim " + std::to_string(td));
+    if (dtype != TLG_F32 && dtype != TLG_F64)
+      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: dtype must be 4 or 8");
+    if (degree < 1) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: degree must be >= 1");
+    if (npoints < 0 || (npoints > 0 && !points))
+      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: bad points");
+    const int64_t k = tlg::num_lagrange_nodes(cell, degree);
+    if (k > 1024) return fail(TLG_ERR_UNSUPPORTED, "tlg_tables_create: more than 1024 nodes per cell");
+    std::vector<double> tab = tlg::tabulate(cell, degree, family, points, (long)npoints, 1);
+    auto t = new tlg_tables();
+    t->cell = cell;
+    t->degree = degree;
+    t->family = family;
+    t->td = td;
+    t->gd = gdim;
+    t->dtype = dtype;
+    t->k = k;
+    t->q = npoints;
+    t->has_refn = ref_normals != nullptr;
+    const size_t es = (size_t)dtype;
+    const size_t n_phi = (size_t)npoints * k, n_dphi = n_phi * td, n_refn = (size_t)npoints * td;
+    t->off_dphi = align16(n_phi * es);
+    t->off_refn = align16(t->off_dphi + n_dphi * es);
+    const size_t total = align16(t->off_refn + std::max<size_t>(n_refn, 1) * es);
+    if (total + 16 > (size_t)200 * 1024) {
+      delete t;
+      return fail(TLG_ERR_ALLOCATION_TOO_LARGE,
+                  "tlg_tables_create: the tabulation (" + std::to_string(total) +
+                      " bytes) exceeds the shared-memory budget of 200 KiB");
+    }
+    t->bytes = (uint32_t)total;
+    t->host.assign(total, 0);
+    // Reorder [deriv][q][k] into phi [q][k] and dphi [q][k][d].
+    std::vector<double> phi(n_phi), dphi(n_dphi), refn(n_refn, 0.0);
+    for (int64_t q = 0; q < npoints; ++q)
+      for (int64_t i = 0; i < k; ++i) {
+        phi[q * k + i] = tab[q * k + i];
+        for (int d = 0; d < td; ++d) dphi[(q * k + i) * td + d] = tab[((1 + d) * npoints + q) * k + i];
+      }
+    if (ref_normals) std::memcpy(refn.data(), ref_normals, n_refn * sizeof(double));
+    if (dtype == TLG_F32) {
+      narrow_into<float>(t->host, 0, phi.data(), n_phi);
+      narrow_into<float>(t->host, t->off_dphi, dphi.data(), n_dphi);
+      narrow_into<float>(t->host, t->off_refn, refn.data(), n_refn);
+    } else {
+      narrow_into<double>(t->host, 0, phi.data(), n_phi);
+      narrow_into<double>(t->host, t->off_dphi, dphi.data(), n_dphi);
+      narrow_into<double>(t->host, t->off_refn, refn.data(), n_refn);
+    }
+    cudaError_t e = cudaMalloc(&t->dev, total + 16);
+    if (e != cudaSuccess) {
+      delete t;
+      return cuda_fail(e, "tlg_tables_create: cudaMalloc");
+    }
+    t->err = reinterpret_cast<int*>(t->dev + total);
+    e = cudaMemcpy(t->dev, t->host.data(), total, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(t->err, 0, 16);
+    if (e != cudaSuccess) {
+      cudaFree(t->dev);
+      delete t;
+      return cuda_fail(e, "tlg_tables_create: upload");
+    }
+    *out = t;
+    return ok();
+  });
+}
+
+tlg_status tlg_tables_destroy(tlg_tables* t) {
+  if (!t) return ok();
+  cudaError_t e = cudaFree(t->dev);
+  delete t;
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_tables_destroy");
+  return ok();
+}
+
+int64_t tlg_tables_num_points(const tlg_tables* t) { return t ? t->q : -1; }
+
+int64_t tlg_tables_nodes_per_cell(const tlg_tables* t) { return t ? t->k : -1; }
+
+tlg_status tlg_tables_device_status(const tlg_tables* t, void* stream) {
+  if (!t) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_device_status: NULL tables");
+  int flag = 0;
+  cudaError_t e = cudaMemcpyAsync(&flag, t->err, sizeof(int), cudaMemcpyDeviceToHost,
+                                  static_cast<cudaStream_t>(stream));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_tables_device_status");
+  if (flag != 0) {
+    cudaMemsetAsync(t->err, 0, sizeof(int), static_cast<cudaStream_t>(stream));
+    return fail(TLG_ERR_DEVICE_TIMEOUT, "a bounded device wait expired in an evaluation kernel");
+  }
+  return ok();
+}
+
+tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o,
+                          void* stream) {
+  if (!t || !b || !o) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: NULL argument");
+  if (b->dtype != t->dtype)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: block and tables differ in dtype");
+  if (b->gdim != t->gd)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: block gdim " + std::to_string(b->gdim) +
+                                              " but tables for gdim " + std::to_string(t->gd));
+  if (tile_shift(o->tile) < 0)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: tile " + std::to_string(o->tile) +
+                                              " is not 1, 2, 4, 8 or 16");
+  if (o->first_cell < 0 || o->num_cells < 0 || o->out_first_cell < 0 ||
+      o->first_cell + o->num_cells > b->num_cells)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: cell range outside the block");
+  if (o->out_first_cell % o->tile != 0)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: out_first_cell is not a multiple of the tile");
+  uint32_t mask = 0;
+  if (o->points) mask |= tlg::kOutPoints;
+  if (o->jacobian) mask |= tlg::kOutJacobian;
+  if (o->detj) mask |= tlg::kOutDetJ;
+  if (o->pinv) mask |= tlg::kOutPinv;
+  if (o->normals) mask |= tlg::kOutNormals;
+  if (o->facet_normals) mask |= tlg::kOutFacetNormals;
+  if (o->normals && t->td + 1 != t->gd)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: normals need a block of codimension 1");
+  if (o->facet_normals && (t->td != t->gd || !t->has_refn))
+    return fail(TLG_ERR_INVALID_ARGUMENT,
+                "tlg_eval_block: facet normals need codimension 0 and tables with reference normals");
+  if (o->num_cells == 0 || t->q == 0 || mask == 0) return ok();  // layout.rs:509-511
+  if (!b->nodes || !b->dofmap) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: NULL nodes or dofmap");
+  if (b->num_nodes < 1)  // Geometry::new rejects cells without nodes (geometry.rs:268-275)
+    return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_eval_block: cells but no nodes");
+  if (b->num_nodes > (int64_t)UINT32_MAX + 1 || b->num_cells > (int64_t)UINT32_MAX)
+    return fail(TLG_ERR_TOO_LARGE, "tlg_eval_block: node or cell count does not fit u32");
+  if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, static_cast<cudaStream_t>(stream));
+  return eval_typed<double>(t, b, o, mask, static_cast<cudaStream_t>(stream));
+}
+
+tlg_status tlg_evector(const tlg_block* b, int nodes_per_cell, int64_t first_cell, int64_t chunk_cells,
+                       int64_t stride, void* out, void* stream) {
+  if (!b || !out) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_evector: NULL argument");
+  if (b->dtype != TLG_F32 && b->dtype != TLG_F64)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_evector: dtype must be 4 or 8");
+  if (nodes_per_cell < 1 || b->gdim < 1 || b->gdim > 3)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_evector: bad nodes_per_cell or gdim");
+  if (first_cell < 0 || chunk_cells < 0 || first_cell + chunk_cells > b->num_cells)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_evector: chunk outside the block");
+  const int64_t padded = (chunk_cells + 15) / 16 * 16;  // VECTOR_PAD
+  if (stride < padded) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_evector: stride below the padded chunk");
+  if (chunk_cells == 0) return ok();
+  if (!b->nodes || !b->dofmap) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_evector: NULL nodes or dofmap");
+  if (b->num_nodes < 1) return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_evector: cells but no nodes");
+  if (b->num_nodes > (int64_t)UINT32_MAX + 1)
+    return fail(TLG_ERR_TOO_LARGE, "tlg_evector: node count does not fit u32");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int threads = 256;
+  int64_t blocks = (padded + threads - 1) / threads;
+  if (blocks > 65535LL * 16) blocks = 65535LL * 16;
+  const uint32_t last_node = (uint32_t)(b->num_nodes - 1);
+  if (b->dtype == TLG_F32)
+    tlg::evector_kernel<uint32_t><<<(unsigned)blocks, threads, 0, s>>>(
+        static_cast<const uint32_t*>(b->nodes), b->dofmap, static_cast<uint32_t*>(out), first_cell,
+        b->num_cells - 1, last_node, nodes_per_cell, b->gdim, padded, stride);
+  else
+    tlg::evector_kernel<uint64_t><<<(unsigned)blocks, threads, 0, s>>>(
+        static_cast<const uint64_t*>(b->nodes), b->dofmap, static_cast<uint64_t*>(out), first_cell,
+        b->num_cells - 1, last_node, nodes_per_cell, b->gdim, padded, stride);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_evector launch");
+  return ok();
+}
+
+}  // extern "C"

@@ -1,0 +1,48 @@
+// Launch helpers of the evaluation kernels: persistent grid sizing and the dispatch from run-time
+// (TD, GD, K) to the compiled instantiations.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "eval.cuh"
+
+namespace tlg {
+
+// Grid of persistent CTAs: enough to cover the range, at most the resident CTAs of the device.
+template <typename Kernel>
+inline int persistent_grid(Kernel kern, size_t smem, int64_t work_items, int threads) {
+  static thread_local int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int64_t need = (work_items + threads - 1) / threads;
+  const int64_t cap = (int64_t)sms * per_sm;
+  return (int)(need < cap ? (need > 0 ? need : 1) : cap);
+}
+
+template <typename Kernel, typename Args>
+inline cudaError_t launch_persistent(Kernel kern, const Args& a, int64_t work, size_t smem,
+                                     cudaStream_t s) {
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const int grid = persistent_grid(kern, smem, work, kEvalThreads);
+  kern<<<grid, kEvalThreads, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+// Defined in eval_f32.cu / eval_f64.cu. `direct` receives whether an unrolled kernel ran.
+cudaError_t launch_eval_f32(int td, int gd, int k, const EvalArgs<float>& a, size_t smem,
+                            cudaStream_t s, bool* direct);
+cudaError_t launch_eval_f64(int td, int gd, int k, const EvalArgs<double>& a, size_t smem,
+                            cudaStream_t s, bool* direct);
+
+}  // namespace tlg

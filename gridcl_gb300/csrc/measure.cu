@@ -1,0 +1,138 @@
+// Measure of a block: per-cell sums of det J * w over the points, then sums of 64 consecutive
+// values, level by level, down to one value (tetraloma-geometry/src/measure.rs:15-102). Each
+// value is summed in F in a fixed order, so the result is the same on every run and for every
+// grid shape.
+#include <cstdint>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/tlgeom.h"
+#include "status.h"
+
+namespace tlg {
+
+constexpr int kSumBlock = 64;  // measure.rs:44
+
+template <typename F>
+__global__ void __launch_bounds__(256) cell_sums_kernel(const F* detj, const F* weights, F* out,
+                                                        int64_t num_cells, int num_points,
+                                                        int tile_shift) {
+  const int64_t mask = (1 << tile_shift) - 1;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < num_cells;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t base = (((c >> tile_shift) * num_points) << tile_shift) + (c & mask);
+    F acc = detj[base] * weights[0];
+    for (int q = 1; q < num_points; ++q) acc = fma(detj[base + ((int64_t)q << tile_shift)], weights[q], acc);
+    out[c] = acc;
+  }
+}
+
+template <typename F>
+__global__ void __launch_bounds__(256) block_sum_kernel(const F* x, F* out, int64_t len, int64_t num_out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < num_out;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t start = i * kSumBlock;
+    const int64_t end = start + kSumBlock < len ? start + kSumBlock : len;
+    F acc = x[start];
+    for (int64_t j = start + 1; j < end; ++j) acc += x[j];
+    out[i] = acc;
+  }
+}
+
+inline unsigned grid_for(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  if (b < 1) b = 1;
+  if (b > 152 * 64) b = 152 * 64;
+  return (unsigned)b;
+}
+
+// Elements of the level buffers of a tree over n values: ceil(n/64) + ceil(n/64^2) + ... down
+// to one value.
+inline int64_t tree_elems(int64_t n) {
+  int64_t total = 0;
+  while (n > 1) {
+    n = (n + kSumBlock - 1) / kSumBlock;
+    total += n;
+  }
+  return total;
+}
+
+template <typename F>
+cudaError_t sum_tree(const F* x, int64_t n, F* work, F* result, cudaStream_t s) {
+  if (n == 1) return cudaMemcpyAsync(result, x, sizeof(F), cudaMemcpyDeviceToDevice, s);
+  const F* cur = x;
+  F* next = work;
+  while (n > 1) {
+    const int64_t m = (n + kSumBlock - 1) / kSumBlock;
+    F* dst = m == 1 ? result : next;
+    block_sum_kernel<F><<<grid_for(m, 256), 256, 0, s>>>(cur, dst, n, m);
+    cur = dst;
+    next = dst + m;
+    n = m;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace tlg
+
+
+extern "C" {
+
+int64_t tlg_sum_workspace_bytes(int dtype, int64_t n) {
+  if ((dtype != TLG_F32 && dtype != TLG_F64) || n < 0) return -1;
+  return tlg::tree_elems(n) * dtype;
+}
+
+tlg_status tlg_measure_cell_sums(const void* detj, int dtype, int64_t num_cells, int64_t num_points,
+                                 int tile, const void* weights, void* sums, void* stream) {
+  int shift = -1;
+  for (int s = 0; s <= 4; ++s)
+    if (tile == (1 << s)) shift = s;
+  if (shift < 0 || (dtype != TLG_F32 && dtype != TLG_F64) || num_cells < 0 || num_points < 0 ||
+      num_points > (1 << 30))
+    return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_measure_cell_sums: bad tile, dtype or sizes");
+  if (num_cells == 0) return tlg::ok();
+  if (!detj || !sums || (num_points > 0 && !weights))
+    return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_measure_cell_sums: NULL pointer");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (num_points == 0) {
+    cudaError_t e = cudaMemsetAsync(sums, 0, (size_t)num_cells * dtype, s);
+    return e == cudaSuccess ? tlg::ok() : tlg::cuda_fail(e, "tlg_measure_cell_sums");
+  }
+  if (dtype == TLG_F32)
+    tlg::cell_sums_kernel<float><<<tlg::grid_for(num_cells, 256), 256, 0, s>>>(
+        static_cast<const float*>(detj), static_cast<const float*>(weights), static_cast<float*>(sums),
+        num_cells, (int)num_points, shift);
+  else
+    tlg::cell_sums_kernel<double><<<tlg::grid_for(num_cells, 256), 256, 0, s>>>(
+        static_cast<const double*>(detj), static_cast<const double*>(weights),
+        static_cast<double*>(sums), num_cells, (int)num_points, shift);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? tlg::ok() : tlg::cuda_fail(e, "tlg_measure_cell_sums launch");
+}
+
+tlg_status tlg_sum(const void* x, int dtype, int64_t n, void* workspace, int64_t workspace_bytes,
+                   void* result, void* stream) {
+  if ((dtype != TLG_F32 && dtype != TLG_F64) || n < 0 || !result)
+    return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_sum: bad dtype, length or result");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (n == 0) {
+    cudaError_t e = cudaMemsetAsync(result, 0, dtype, s);
+    return e == cudaSuccess ? tlg::ok() : tlg::cuda_fail(e, "tlg_sum");
+  }
+  if (!x) return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_sum: NULL input");
+  if (workspace_bytes < tlg::tree_elems(n) * dtype || (tlg::tree_elems(n) > 0 && !workspace))
+    return tlg::fail(TLG_ERR_LENGTH_MISMATCH,
+                     "tlg_sum: workspace of " + std::to_string(workspace_bytes) + " bytes, " +
+                         std::to_string(tlg::tree_elems(n) * dtype) + " needed");
+  cudaError_t e =
+      dtype == TLG_F32
+          ? tlg::sum_tree<float>(static_cast<const float*>(x), n, static_cast<float*>(workspace),
+                                 static_cast<float*>(result), s)
+          : tlg::sum_tree<double>(static_cast<const double*>(x), n, static_cast<double*>(workspace),
+                                  static_cast<double*>(result), s);
+  return e == cudaSuccess ? tlg::ok() : tlg::cuda_fail(e, "tlg_sum launch");
+}
+
+}  // extern "C"

@@ -1,0 +1,410 @@
+"""The host side of the geometry path, mirroring tetraloma-geometry's public API over the C ABI.
+
+Names, argument meaning and error kinds follow the reference (paths inside its project):
+
+- :class:`CoordinateElement`, :class:`GeometryBlock` — tetraloma-geometry/src/element.rs:29-154;
+- :class:`Geometry` — tetraloma-geometry/src/geometry.rs:187-288: node L-vector relative to the
+  origin, per-block dofmaps, the E-vector cache; ``Geometry.new`` checks lengths only;
+- :class:`PointSet`, :class:`QuadRule` — point_set.rs:57-398 and rule.rs:49-104; a point set
+  caches its device tables per (element, scalar type, gdim), as the reference caches its
+  tabulations;
+- :class:`QuadField` — field.rs:162-409, one tiled chunk per field (or several when
+  ``max_chunk_cells`` is given), ``to_host_cell_major`` undoes the tiling;
+- ``physical_points_block``, ``jacobians_block``, ``detj_block``, ``pseudo_inverse_block``,
+  ``normals_block``, ``facet_normals_block`` — points_jac.rs:637,685, detj_pinv.rs:739,787,
+  facets.rs:46,107, all through one launcher like ``launch_factor`` (layout.rs:488-772);
+  ``geometric_factors_block`` computes several factors in one fused launch.
+
+Device memory, streams and tensors come from PyTorch; every computation runs in the native
+library (``libtlgeom.so``). Mesh arrays are torch tensors on the current CUDA device.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+from typing import Iterable
+
+import numpy as np
+import torch
+
+from . import refcell
+from ._lib import CELL_IDS, FAMILY_IDS, GridError, TlgBlock, TlgOutputs, check, lib
+
+VECTOR_PAD = 16  # tetraloma-device/src/buffer.rs:28
+GPU_QUAD_TILE = 16  # tetraloma-device/vector-policy.toml:59
+
+FACTOR_LEN = {
+    "points": lambda td, gd: gd,
+    "jacobian": lambda td, gd: td * gd,
+    "detj": lambda td, gd: 1,
+    "pinv": lambda td, gd: td * gd,
+    "normals": lambda td, gd: gd,
+    "facet_normals": lambda td, gd: gd,
+}
+
+_DTYPES = {torch.float32: 4, torch.float64: 8}
+
+
+def current_stream_handle() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+@dataclasses.dataclass(frozen=True)
+class CoordinateElement:
+    cell: str
+    degree: int
+    family: str = "Equispaced"
+
+    @property
+    def nodes_per_cell(self) -> int:
+        return refcell.num_lagrange_nodes(self.cell, self.degree)
+
+    @property
+    def tdim(self) -> int:
+        return refcell.tdim(self.cell)
+
+
+@dataclasses.dataclass
+class GeometryBlock:
+    """One cell block: its coordinate element, dofmap ``[cells][K]`` (u32 bit patterns held in an
+    int32 tensor) and cell flags (bit 0 flips normals)."""
+
+    element: CoordinateElement
+    dofmap: torch.Tensor
+    flags: torch.Tensor | None = None
+
+    @property
+    def num_cells(self) -> int:
+        return self.dofmap.shape[0]
+
+
+@dataclasses.dataclass
+class EVectorChunk:
+    first_cell: int
+    num_cells: int
+    data: torch.Tensor  # [K][GD][stride]
+
+
+class Geometry:
+    """Blocks of one grid, the node L-vector relative to `origin`, and the E-vector cache."""
+
+    def __init__(self, blocks: list, nodes: torch.Tensor, origin):
+        gd = nodes.shape[1] if nodes.dim() == 2 else 0
+        if nodes.dtype not in _DTYPES:
+            raise GridError(1, f"nodes must be float32 or float64, not {nodes.dtype}")
+        if not nodes.is_cuda:
+            raise GridError(1, "nodes must be a CUDA tensor")
+        for b in blocks:
+            k = b.element.nodes_per_cell
+            if b.dofmap.dim() != 2 or b.dofmap.shape[1] != k:
+                raise GridError(2, f"LengthMismatch {{ expected: {k}, found: {tuple(b.dofmap.shape)} }}")
+            if nodes.shape[0] == 0 and b.dofmap.numel() != 0:
+                raise GridError(2, "LengthMismatch { expected: 0 cells without nodes }")
+            if b.dofmap.dtype != torch.int32 or not b.dofmap.is_cuda or not b.dofmap.is_contiguous():
+                raise GridError(1, "dofmap must be a contiguous int32 CUDA tensor of u32 indices")
+        self.blocks = blocks
+        self.nodes = nodes.contiguous()
+        self.gdim = gd
+        self.origin = tuple(float(x) for x in origin) + (0.0,) * (3 - len(tuple(origin)))
+        self._evectors: dict[int, list[EVectorChunk]] = {}
+
+    @property
+    def dtype(self) -> torch.dtype:
+        return self.nodes.dtype
+
+    @classmethod
+    def from_host(cls, mesh, dtype=torch.float64, device="cuda", flags=None) -> "Geometry":
+        """Uploads a host mesh: origin = centre of the bounding box, nodes stored as
+        F(x - origin) (tetraloma/src/pipeline/nodes.rs:39-45, upload.rs:65-73)."""
+        x = np.asarray(mesh.nodes, dtype=np.float64)
+        if x.shape[0]:
+            origin = 0.5 * (x.min(axis=0) + x.max(axis=0))
+        else:
+            origin = np.zeros(mesh.gdim)
+        rel = x - origin
+        nodes = torch.from_numpy(np.ascontiguousarray(rel)).to(dtype=dtype).to(device)
+        blocks = []
+        for i, hb in enumerate(mesh.blocks):
+            dm = torch.from_numpy(np.ascontiguousarray(hb.cells.astype(np.uint32).view(np.int32))).to(device)
+            fl = None
+            if flags is not None and flags[i] is not None:
+                fl = torch.from_numpy(np.ascontiguousarray(np.asarray(flags[i], dtype=np.uint32).view(np.int32))).to(device)
+            blocks.append(GeometryBlock(CoordinateElement(hb.cell, hb.degree, hb.family), dm, fl))
+        return cls(blocks, nodes, origin)
+
+    def block_desc(self, b: int) -> TlgBlock:
+        blk = self.blocks[b]
+        d = TlgBlock()
+        d.dtype = _DTYPES[self.dtype]
+        d.gdim = self.gdim
+        d.num_cells = blk.num_cells
+        d.num_nodes = self.nodes.shape[0]
+        d.nodes = self.nodes.data_ptr()
+        d.dofmap = blk.dofmap.data_ptr()
+        d.flags = blk.flags.data_ptr() if blk.flags is not None else None
+        d.num_flags = blk.flags.numel() if blk.flags is not None else 0
+        for g in range(3):
+            d.origin[g] = self.origin[g]
+        return d
+
+    def evector(self, b: int, max_chunk_cells: int | None = None) -> list[EVectorChunk]:
+        """Block b's E-vector, built on first use and cached (geometry.rs:462-488): chunks of
+        ``[K][GD][stride]`` with stride = chunk cells rounded up to 16, padding lanes
+        repeating the block's last cell (evector.rs:296-390)."""
+        if b in self._evectors and max_chunk_cells is None:
+            return self._evectors[b]
+        blk = self.blocks[b]
+        k, gd, n = blk.element.nodes_per_cell, self.gdim, blk.num_cells
+        per = n if max_chunk_cells is None else max(VECTOR_PAD, max_chunk_cells // VECTOR_PAD * VECTOR_PAD)
+        chunks = []
+        desc = self.block_desc(b)
+        first = 0
+        while first < n:
+            cnt = min(per, n - first)
+            stride = -(-cnt // VECTOR_PAD) * VECTOR_PAD
+            data = torch.empty((k, gd, stride), dtype=self.dtype, device=self.nodes.device)
+            check(lib().tlg_evector(ctypes.byref(desc), k, first, cnt, stride, data.data_ptr(),
+                                    current_stream_handle()))
+            chunks.append(EVectorChunk(first, cnt, data))
+            first += cnt
+        if max_chunk_cells is None:
+            self._evectors[b] = chunks
+        return chunks
+
+
+class PointSet:
+    """Reference points and weights of one cell type; caches the device tables of each element
+    it is tabulated for (point_set.rs:57-398)."""
+
+    def __init__(self, cell: str, points, weights, ref_normals=None):
+        td = refcell.tdim(cell)
+        self.cell = cell
+        self.points = np.ascontiguousarray(np.asarray(points, dtype=np.float64).reshape(-1, td))
+        self.weights = np.ascontiguousarray(np.asarray(weights, dtype=np.float64).reshape(-1))
+        if self.points.shape[0] != self.weights.shape[0]:
+            raise GridError(2, "points and weights differ in count")
+        self.ref_normals = None if ref_normals is None else np.ascontiguousarray(
+            np.asarray(ref_normals, dtype=np.float64).reshape(-1, td))
+        self._tables: dict = {}
+        self._weights_dev: dict = {}
+
+    def __len__(self) -> int:
+        return self.points.shape[0]
+
+    def tables(self, element: CoordinateElement, gdim: int, dtype: torch.dtype):
+        key = (element, gdim, dtype)
+        t = self._tables.get(key)
+        if t is None:
+            if element.cell != self.cell:
+                raise GridError(1, f"a {self.cell} point set cannot tabulate a {element.cell} element")
+            h = ctypes.c_void_p()
+            pts = self.points if len(self) else np.zeros(1)
+            rn = None if self.ref_normals is None else self.ref_normals.ctypes.data_as(ctypes.c_void_p)
+            check(lib().tlg_tables_create(CELL_IDS[element.cell], element.degree,
+                                          FAMILY_IDS[element.family], gdim, _DTYPES[dtype],
+                                          pts.ctypes.data_as(ctypes.c_void_p), len(self), rn,
+                                          ctypes.byref(h)))
+            t = _Tables(h)
+            self._tables[key] = t
+        return t
+
+    def weights_device(self, dtype: torch.dtype, device="cuda") -> torch.Tensor:
+        w = self._weights_dev.get(dtype)
+        if w is None:
+            w = torch.from_numpy(self.weights).to(dtype=dtype).to(device)
+            self._weights_dev[dtype] = w
+        return w
+
+
+class _Tables:
+    def __init__(self, handle: ctypes.c_void_p):
+        self.handle = handle
+
+    def __del__(self):
+        try:
+            lib().tlg_tables_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class QuadRule:
+    """One point set per distinct cell type (rule.rs:49-104)."""
+
+    def __init__(self, sets: Iterable[PointSet]):
+        self.sets = list(sets)
+
+    @classmethod
+    def gauss(cls, cells: Iterable[str], degree: int) -> "QuadRule":
+        out = []
+        for c in dict.fromkeys(cells):
+            pts, w = refcell.gauss_rule(c, degree)
+            out.append(PointSet(c, pts, w))
+        return cls(out)
+
+    @classmethod
+    def for_grid(cls, g: Geometry, degree: int) -> "QuadRule":
+        return cls.gauss([b.element.cell for b in g.blocks], degree)
+
+    def get(self, cell: str) -> PointSet:
+        for s in self.sets:
+            if s.cell == cell:
+                return s
+        raise GridError(1, f"CellNotInRule({cell})")
+
+
+@dataclasses.dataclass
+class QuadChunk:
+    first_cell: int
+    num_cells: int
+    data: torch.Tensor  # flat, padded cells * Q * LEN
+
+
+class QuadField:
+    """Values at the points of one block, tiled: component k at point q of cell c at
+    ((c / tile) Q LEN + q LEN + k) tile + c % tile within its chunk (field.rs:121-162)."""
+
+    def __init__(self, chunks, num_cells: int, num_points: int, length: int, tile: int):
+        self.chunks = chunks
+        self.num_cells = num_cells
+        self.num_points = num_points
+        self.length = length
+        self.tile = tile
+
+    @classmethod
+    def uninit(cls, num_cells: int, num_points: int, length: int, tile: int, dtype,
+               device="cuda", max_chunk_cells: int | None = None) -> "QuadField":
+        if tile not in (1, 2, 4, 8, 16):
+            raise GridError(1, f"QuadField::uninit: tile {tile} is not 1, 2, 4, 8 or 16")
+        per = num_cells if not max_chunk_cells else max(tile, max_chunk_cells // tile * tile)
+        chunks, first = [], 0
+        while first < num_cells:
+            n = min(per, num_cells - first)
+            padded = -(-n // tile) * tile
+            chunks.append(QuadChunk(first, n, torch.empty(padded * num_points * length,
+                                                          dtype=dtype, device=device)))
+            first += n
+        return cls(chunks, num_cells, num_points, length, tile)
+
+    def to_host_cell_major(self) -> np.ndarray:
+        """``[cell][point][component]`` on the host, padding excluded (field.rs:380-408)."""
+        parts = []
+        for ch in self.chunks:
+            t, q, l = self.tile, self.num_points, self.length
+            nt = -(-ch.num_cells // t)
+            a = ch.data.detach().cpu().numpy().reshape(nt, q, l, t).transpose(0, 3, 1, 2)
+            parts.append(a.reshape(nt * t, q, l)[: ch.num_cells])
+        if not parts:
+            return np.zeros((0, self.num_points, self.length))
+        return np.concatenate(parts, axis=0)
+
+
+def _factor_names(g: Geometry, b: int, factors) -> list:
+    td = g.blocks[b].element.tdim
+    names = list(factors)
+    for f in names:
+        if f not in FACTOR_LEN:
+            raise GridError(1, f"unknown factor {f}")
+    if "normals" in names and td + 1 != g.gdim:
+        raise GridError(1, "normals need a block of codimension 1")
+    if "facet_normals" in names and td != g.gdim:
+        raise GridError(1, "facet normals need a block of codimension 0")
+    return names
+
+
+def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points", "jacobian", "detj", "pinv"),
+                            tile: int = GPU_QUAD_TILE, max_chunk_cells: int | None = None,
+                            out: dict | None = None) -> dict:
+    """Every factor in `factors` of block b at the points of `pts`, in one fused launch per
+    chunk; returns ``{factor: QuadField}``. `out` may pass preallocated fields."""
+    blk = g.blocks[b]
+    names = _factor_names(g, b, factors)
+    td, gd = blk.element.tdim, g.gdim
+    nq = len(pts)
+    tables = pts.tables(blk.element, gd, g.dtype)
+    fields = out if out is not None else {
+        f: QuadField.uninit(blk.num_cells, nq, FACTOR_LEN[f](td, gd), tile, g.dtype,
+                            g.nodes.device, max_chunk_cells)
+        for f in names}
+    desc = g.block_desc(b)
+    stream = current_stream_handle()
+    nchunks = len(next(iter(fields.values())).chunks) if fields else 0
+    for ci in range(nchunks):
+        o = TlgOutputs()
+        ch0 = fields[names[0]].chunks[ci]
+        o.first_cell = ch0.first_cell
+        o.num_cells = ch0.num_cells
+        o.out_first_cell = 0
+        o.tile = tile
+        for f in names:
+            setattr(o, f if f != "points" else "points", fields[f].chunks[ci].data.data_ptr())
+        check(lib().tlg_eval_block(tables.handle, ctypes.byref(desc), ctypes.byref(o), stream))
+    return fields
+
+
+def physical_points_block(g: Geometry, b: int, pts: PointSet, **kw) -> QuadField:
+    return geometric_factors_block(g, b, pts, ("points",), **kw)["points"]
+
+
+def jacobians_block(g: Geometry, b: int, pts: PointSet, **kw) -> QuadField:
+    return geometric_factors_block(g, b, pts, ("jacobian",), **kw)["jacobian"]
+
+
+def detj_block(g: Geometry, b: int, pts: PointSet, **kw) -> QuadField:
+    return geometric_factors_block(g, b, pts, ("detj",), **kw)["detj"]
+
+
+def pseudo_inverse_block(g: Geometry, b: int, pts: PointSet, **kw) -> QuadField:
+    return geometric_factors_block(g, b, pts, ("pinv",), **kw)["pinv"]
+
+
+def normals_block(g: Geometry, b: int, pts: PointSet, **kw) -> QuadField:
+    return geometric_factors_block(g, b, pts, ("normals",), **kw)["normals"]
+
+
+def facet_normals_block(g: Geometry, b: int, pts: PointSet, **kw) -> QuadField:
+    if pts.ref_normals is None:
+        raise GridError(1, "facet normals need a facet point set (with reference normals)")
+    return geometric_factors_block(g, b, pts, ("facet_normals",), **kw)["facet_normals"]
+
+
+def facet_point_set(cell: str, degree: int) -> PointSet:
+    """The facet Gauss rule of `cell` mapped to the cell, facet by facet, with each point's
+    reference facet normal (tetraloma-geometry/src/facet_rule.rs:16-70)."""
+    td = refcell.tdim(cell)
+    normals = refcell.reference_facet_normals(cell)
+    from ._facets import facet_points_to_cell, facet_types
+    pts, w, rn = [], [], []
+    for f, ft in enumerate(facet_types(cell)):
+        fp, fw = refcell.gauss_rule(ft, degree)
+        pts.append(facet_points_to_cell(cell, f, fp))
+        w.append(fw)
+        rn.append(np.repeat(normals[f:f + 1], fw.size, axis=0))
+    return PointSet(cell, np.concatenate(pts).reshape(-1, td), np.concatenate(w),
+                    np.concatenate(rn).reshape(-1, td))
+
+
+def measure_block(g: Geometry, b: int, pts: PointSet, detj: QuadField | None = None) -> float:
+    """The measure of block b: sum over cells and points of det J * w, per cell then by a tree of
+    64-value sums, all on the device in F, read back once (tetraloma-geometry/src/measure.rs:
+    141-185). `detj` may pass an already computed det J field of the same point set."""
+    blk = g.blocks[b]
+    if blk.num_cells == 0 or len(pts) == 0:
+        return 0.0
+    if detj is None:
+        detj = detj_block(g, b, pts)
+    es = _DTYPES[g.dtype]
+    dev = g.nodes.device
+    sums = torch.empty(blk.num_cells, dtype=g.dtype, device=dev)
+    w = pts.weights_device(g.dtype, dev)
+    stream = current_stream_handle()
+    for ch in detj.chunks:
+        check(lib().tlg_measure_cell_sums(ch.data.data_ptr(), es, ch.num_cells, detj.num_points,
+                                          detj.tile, w.data_ptr(),
+                                          sums.data_ptr() + ch.first_cell * es, stream))
+    nbytes = int(lib().tlg_sum_workspace_bytes(es, blk.num_cells))
+    work = torch.empty(max(nbytes, es), dtype=torch.uint8, device=dev)
+    result = torch.empty(1, dtype=g.dtype, device=dev)
+    check(lib().tlg_sum(sums.data_ptr(), es, blk.num_cells, work.data_ptr(), nbytes,
+                        result.data_ptr(), stream))
+    return float(result.item())

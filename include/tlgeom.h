@@ -1,0 +1,187 @@
+/*
+ * tlgeom: GB300-native (sm_103a) evaluation of the geometric factors of unstructured-mesh cell
+ * blocks, behind a plain C ABI.
+ *
+ * This is the boundary a host program binds to replace the device kernels of tetraloma's
+ * geometry path (tbetcke/gridcl). Every entry point takes plain pointers and sizes: device
+ * pointers for mesh data and outputs, host pointers for reference points and small tables,
+ * and a CUDA stream (`cudaStream_t`, passed as `void*`). No entry point of the evaluation
+ * itself allocates device memory; `tlg_tables_create` allocates once per (element, point set)
+ * and `tlg_tables_destroy` frees it.
+ *
+ * Status codes mirror `GridError` (tetraloma-device/src/error.rs:80-105):
+ * TooLarge, LengthMismatch{expected, found}, AllocationTooLarge, Server(..). The message of
+ * the last failure on the calling thread is `tlg_last_error()`.
+ *
+ * Data layouts (all as in the reference):
+ *  - nodes: the node L-vector `[node][gdim]` of F, relative to the grid's origin
+ *    (tetraloma/src/pipeline/upload.rs:65-73);
+ *  - dofmap: `[cell][K]` u32 node indices of one block in the reference's Lagrange node order
+ *    (tetraloma-refcell/src/lagrange.rs:163-266); indices past the last node read the last node
+ *    (tetraloma-geometry/src/evector.rs:221-222);
+ *  - outputs: QuadField chunks (tetraloma-geometry/src/field.rs:121-162): component k at point q
+ *    of cell c at ((c / tile) * Q * LEN + q * LEN + k) * tile + c % tile, counted from the chunk's
+ *    first cell; cells are padded to whole tiles and padding lanes hold the block's last cell;
+ *  - J(g, d) at component d * GD + g (column-major GD x TD); K = J^+ (t, g) at g * TD + t;
+ *    det J one component (sqrt(det(J^T J)) when TD < GD); normals and points GD components
+ *    (tetraloma-geometry/src/layout.rs:91-131, 133-369).
+ */
+#ifndef TLGEOM_H
+#define TLGEOM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TLG_ABI_VERSION 1
+
+typedef enum tlg_status {
+  TLG_OK = 0,
+  TLG_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad tile, bad dimension pair, ... */
+  TLG_ERR_LENGTH_MISMATCH = 2,  /* GridError::LengthMismatch */
+  TLG_ERR_TOO_LARGE = 3,        /* GridError::TooLarge: a count does not fit the kernel's u32 */
+  TLG_ERR_UNSUPPORTED = 4,      /* cell type / degree / factor this build has no kernel for */
+  TLG_ERR_CUDA = 5,             /* GridError::Server: a CUDA runtime failure */
+  TLG_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait expired; the context is intact */
+  TLG_ERR_ALLOCATION_TOO_LARGE = 7 /* GridError::AllocationTooLarge */
+} tlg_status;
+
+/* Scalar type of nodes and outputs: the byte size of F. */
+typedef enum tlg_dtype { TLG_F32 = 4, TLG_F64 = 8 } tlg_dtype;
+
+/* tetraloma_dims::CellType (tetraloma-dims/src/dim.rs). */
+typedef enum tlg_cell {
+  TLG_POINT = 0,
+  TLG_INTERVAL = 1,
+  TLG_TRIANGLE = 2,
+  TLG_QUADRILATERAL = 3,
+  TLG_TETRAHEDRON = 4,
+  TLG_HEXAHEDRON = 5,
+  TLG_PRISM = 6,
+  TLG_PYRAMID = 7
+} tlg_cell;
+
+/* tetraloma_refcell::NodeFamily (tetraloma-refcell/src/lagrange.rs:22-27). */
+typedef enum tlg_family { TLG_EQUISPACED = 0, TLG_GLL = 1 } tlg_family;
+
+/* Thread-local message of the last failing call on this thread ("" after success). */
+const char* tlg_last_error(void);
+int tlg_abi_version(void);
+
+/* ---------------------------------------------------------------------------------------
+ * Reference cells (host, f64). Replace tetraloma-refcell's public functions
+ * (tetraloma-refcell/src/lib.rs:58-69) for callers without the Rust crate.
+ * ------------------------------------------------------------------------------------- */
+
+/* num_lagrange_nodes (tetraloma-refcell/src/lagrange.rs:59-78); -1 for an unknown cell. */
+int64_t tlg_num_lagrange_nodes(int cell, int degree);
+
+/* lagrange_points (lagrange.rs:163-266): `[node][tdim]` into out (capacity `cap` doubles). */
+tlg_status tlg_lagrange_points(int cell, int degree, int family, double* out, int64_t cap);
+
+/* gauss_rule (tetraloma-refcell/src/quadrature.rs:77-128) with `counts[d]` points in collapsed
+ * direction d (counts all equal to degree / 2 + 1 gives the reference's rule). Points
+ * `[q][tdim]`, weights `[q]`; *num_points receives Q. */
+tlg_status tlg_collapsed_rule(int cell, const int* counts, double* points, double* weights,
+                              int64_t cap_points, int64_t* num_points);
+
+/* LagrangeElement::tabulate (tetraloma-refcell/src/tabulation.rs:266): `[deriv][q][k]`,
+ * deriv 0 the values, 1 + d the derivative in reference direction d (nderivs 0 or 1). */
+tlg_status tlg_tabulate(int cell, int degree, int family, const double* points, int64_t npoints,
+                        int nderivs, double* out, int64_t cap);
+
+/* reference_facet_normals (tetraloma-refcell/src/facet.rs): `[facet][tdim]`. */
+tlg_status tlg_reference_facet_normals(int cell, double* out, int64_t cap);
+
+/* ---------------------------------------------------------------------------------------
+ * Tables: the device-resident tabulation of one coordinate element at one point set, in F.
+ * Replaces PointSet::tabulate / tabulate_derivatives and their per-element cache
+ * (tetraloma-geometry/src/point_set.rs:312-398). Created once, read by every launch.
+ * ------------------------------------------------------------------------------------- */
+typedef struct tlg_tables tlg_tables;
+
+/* `points` `[q][tdim]` in reference coordinates; `ref_normals` `[q][tdim]` or NULL (the
+ * per-point reference facet normals of a FacetPointSet, facet_rule.rs). gdim is the
+ * geometric dimension of the grids the tables will serve. Allocates device memory. */
+tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dtype,
+                             const double* points, int64_t npoints, const double* ref_normals,
+                             tlg_tables** out);
+tlg_status tlg_tables_destroy(tlg_tables* tables);
+int64_t tlg_tables_num_points(const tlg_tables* tables);
+/* Synchronises `stream` and reports TLG_ERR_DEVICE_TIMEOUT (then clears it) if a kernel that read
+ * these tables gave up a bounded wait for its table copy; TLG_OK otherwise. */
+tlg_status tlg_tables_device_status(const tlg_tables* tables, void* stream);
+int64_t tlg_tables_nodes_per_cell(const tlg_tables* tables);
+
+/* ---------------------------------------------------------------------------------------
+ * One cell block of a Geometry (tetraloma-geometry/src/geometry.rs:187-288,
+ * element.rs:29-154).
+ * ------------------------------------------------------------------------------------- */
+typedef struct tlg_block {
+  int dtype;              /* tlg_dtype of nodes and outputs */
+  int gdim;               /* 1, 2 or 3 */
+  int64_t num_cells;      /* cells of the block */
+  int64_t num_nodes;      /* nodes of the L-vector */
+  const void* nodes;      /* device [num_nodes][gdim] F, relative to the origin */
+  const uint32_t* dofmap; /* device [num_cells][K] */
+  const uint32_t* flags;  /* device [num_flags] cell flags (bit 0 flips normals), or NULL */
+  int64_t num_flags;
+  double origin[3];       /* host; narrowed to F and added to physical points */
+} tlg_block;
+
+/* Outputs of one evaluation: one QuadField chunk range. NULL pointers are not computed. */
+typedef struct tlg_outputs {
+  int64_t first_cell;     /* first cell of the range, in the block */
+  int64_t num_cells;      /* cells of the range, padding excluded */
+  int64_t out_first_cell; /* the range's first cell within the output chunks; a multiple of tile */
+  int tile;               /* cells per tile: 1, 2, 4, 8 or 16 (the GPU policy's 16) */
+  void* points;           /* X, GD components */
+  void* jacobian;         /* J, TD * GD */
+  void* detj;             /* det J, 1 */
+  void* pinv;             /* K, TD * GD */
+  void* normals;          /* codimension 1: unit normals, GD */
+  void* facet_normals;    /* codimension 0: K^T n_ref / |K^T n_ref|, GD (tables need ref_normals) */
+} tlg_outputs;
+
+/* Fused evaluation of every requested factor of one block range in one launch: the
+ * connectivity gather, J at each point, and X / J / det J / K / normals / facet normals from
+ * it. Replaces `launch_factor` (tetraloma-geometry/src/layout.rs:488-772), which launches one
+ * kernel per factor over a gathered E-vector; a single non-NULL output gives exactly that
+ * factor. Empty ranges or point sets launch nothing (layout.rs:509-511). */
+tlg_status tlg_eval_block(const tlg_tables* tables, const tlg_block* block,
+                          const tlg_outputs* outputs, void* stream);
+
+/* The E-vector chunk of cells [first_cell, first_cell + chunk_cells): out[(k * gdim + g) * stride
+ * + c] for c < roundup(chunk_cells, 16) <= stride, padding lanes repeating the block's last cell
+ * and node indices clamped to the last node; a bit-exact gather
+ * (tetraloma-geometry/src/evector.rs:195-236, 296-390). */
+tlg_status tlg_evector(const tlg_block* block, int nodes_per_cell, int64_t first_cell,
+                       int64_t chunk_cells, int64_t stride, void* out, void* stream);
+
+/* ---------------------------------------------------------------------------------------
+ * Measure (tetraloma-geometry/src/measure.rs:15-185): per-cell sums of det J * w over the
+ * points of a det J QuadField chunk, then a sum tree of 64-value blocks, all in F and in a
+ * fixed order. The caller reads the F result (the reference finishes it in f64 on the host).
+ * ------------------------------------------------------------------------------------- */
+
+/* sums[c] = sum_q detj(c, q) * weights[q] for the chunk's cells (cell_sums_kernel, measure.rs:
+ * 15-41); detj is a QuadField chunk of tile `tile`, weights device [num_points] of F. */
+tlg_status tlg_measure_cell_sums(const void* detj, int dtype, int64_t num_cells, int64_t num_points,
+                                 int tile, const void* weights, void* sums, void* stream);
+
+/* Bytes of workspace tlg_sum needs for n values (-1 for a bad dtype). */
+int64_t tlg_sum_workspace_bytes(int dtype, int64_t n);
+
+/* result[0] = the sum of x[0..n) by levels of 64-value block sums (measure.rs:44-102); result
+ * and workspace are device memory; an empty input sums to 0. */
+tlg_status tlg_sum(const void* x, int dtype, int64_t n, void* workspace, int64_t workspace_bytes,
+                   void* result, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TLGEOM_H */

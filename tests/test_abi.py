@@ -1,0 +1,59 @@
+"""The C-ABI library loads on a CPU-only host and exports every entry point the header
+declares; argument checks run before any device call (CPU)."""
+
+import ctypes
+import pathlib
+import re
+
+import numpy as np
+
+from gridcl_gb300 import _lib
+from gridcl_gb300._lib import TlgBlock, TlgOutputs, lib
+
+HEADER = pathlib.Path(__file__).resolve().parents[1] / "include" / "tlgeom.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tlg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported():
+    names = declared_functions()
+    assert len(names) >= 14
+    handle = ctypes.CDLL(str(_lib.LIB_PATH))
+    for n in names:
+        assert hasattr(handle, n), n
+    assert sorted(n for n, _, _ in _lib.SIGNATURES) == names
+
+
+def test_abi_version():
+    assert lib().tlg_abi_version() == 1
+
+
+def test_argument_errors_before_device_work():
+    L = lib()
+    assert L.tlg_eval_block(None, None, None, None) == 1
+    b = TlgBlock()
+    o = TlgOutputs()
+    assert L.tlg_evector(ctypes.byref(b), 4, 0, 0, 16, None, None) == 1
+    h = ctypes.c_void_p()
+    pts = np.zeros((1, 3))
+    p = pts.ctypes.data_as(ctypes.c_void_p)
+    # gdim below tdim, unknown dtype, pyramids, degree 0: all rejected on the host
+    assert L.tlg_tables_create(4, 1, 0, 2, 8, p, 1, None, ctypes.byref(h)) == 1
+    assert L.tlg_tables_create(4, 1, 0, 3, 2, p, 1, None, ctypes.byref(h)) == 1
+    assert L.tlg_tables_create(7, 1, 0, 3, 8, p, 1, None, ctypes.byref(h)) == 4
+    assert L.tlg_tables_create(4, 0, 0, 3, 8, p, 1, None, ctypes.byref(h)) == 1
+    assert b"degree" in L.tlg_last_error()
+    assert h.value is None
+    del o
+
+
+def test_refcell_entry_points_report_capacity():
+    L = lib()
+    out = np.zeros(3)
+    assert L.tlg_lagrange_points(4, 2, 0, out.ctypes.data_as(ctypes.c_void_p), 3) == 2
+    assert L.tlg_num_lagrange_nodes(4, 2) == 10
+    assert L.tlg_num_lagrange_nodes(99, 2) == -1

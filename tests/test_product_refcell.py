@@ -1,0 +1,55 @@
+"""The product's native reference-cell tables against the golden fixtures and the oracle (CPU)."""
+
+import json
+import pathlib
+
+import numpy as np
+import pytest
+
+from gridcl_gb300 import refcell as pr
+from oracle import refcell as rc
+
+GOLDEN = pathlib.Path(__file__).resolve().parent / "golden"
+CELLS = ["Interval", "Triangle", "Quadrilateral", "Tetrahedron", "Hexahedron", "Prism"]
+
+
+def test_lagrange_points_match_fixture():
+    fixture = json.loads((GOLDEN / "lagrange_points.json").read_text())
+    for name, families in fixture.items():
+        for family, degrees in families.items():
+            for p, want in degrees.items():
+                ours = pr.lagrange_points(name, int(p), family).ravel()
+                assert np.abs(ours - np.array(want)).max() <= 1e-14, (name, family, p)
+
+
+@pytest.mark.parametrize("cell", CELLS)
+def test_rules_match_the_oracle(cell):
+    for n in range(0, 16):
+        a, b = pr.gauss_rule(cell, n), rc.gauss_rule(cell, n)
+        assert np.abs(a[0] - b[0]).max() < 1e-14 and np.abs(a[1] - b[1]).max() < 1e-14
+
+
+@pytest.mark.parametrize("cell", CELLS)
+def test_tabulation_matches_the_oracle(cell):
+    # Degrees of the benchmark elements and below; the product's Vandermonde route loses
+    # accuracy on simplices above degree 4.
+    for p in range(1, 5):
+        pts, _ = rc.gauss_rule(cell, 2 * p)
+        for fam in (["Equispaced", "Gll"] if cell in ("Interval", "Quadrilateral", "Hexahedron") else ["Equispaced"]):
+            err = np.abs(pr.tabulate(cell, p, pts, 1, fam) - rc.tabulate(cell, p, pts, 1, fam)).max()
+            assert err < 5e-13, (cell, p, fam, err)
+
+
+@pytest.mark.parametrize("cell", CELLS)
+def test_facet_normals_match_the_oracle(cell):
+    assert np.array_equal(pr.reference_facet_normals(cell), rc.reference_facet_normals(cell))
+
+
+def test_unsupported_and_bad_input():
+    from gridcl_gb300 import GridError
+
+    with pytest.raises(GridError) as e:
+        pr.lagrange_points("Triangle", 2, "Gll")
+    assert e.value.kind == "InvalidArgument"
+    with pytest.raises(GridError):
+        pr.tabulate("Pyramid", 1, np.zeros((1, 3)))
