@@ -145,7 +145,7 @@ def test_invariance_to_tile_chunks_and_repeats(cuda):
     base = tg.geometric_factors_block(g, 0, ps, ("points", "detj", "pinv"))
     again = tg.geometric_factors_block(g, 0, ps, ("points", "detj", "pinv"))
     tile1 = tg.geometric_factors_block(g, 0, ps, ("points", "detj", "pinv"), tile=1)
-    chunks = tg.geometric_factors_block(g, 0, ps, ("points", "detj", "pinv"), max_chunk_cells=4)
+    chunks = tg.geometric_factors_block(g, 0, ps, ("points", "detj", "pinv"), tile=1, max_chunk_cells=4)
     assert len(chunks["detj"].chunks) == 7
     for k in base:
         ref = base[k].to_host_cell_major()
