@@ -90,6 +90,8 @@ SIGNATURES = [
     ("tlg_measure_cell_sums", _I, [_P, _I, _L, _L, _I, _P, _P, _P]),
     ("tlg_sum_workspace_bytes", _L, [_I, _L]),
     ("tlg_sum", _I, [_P, _I, _L, _P, _L, _P, _P]),
+    ("tlg_measure_static", _I, [_P, _I, _L, _L, _I, _P, _P, _P]),
+    ("tlg_measure_static_max_cells", _L, []),
 ]
 
 _lib = None

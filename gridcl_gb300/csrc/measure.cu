@@ -3,6 +3,7 @@
 // value is summed in F in a fixed order, so the result is the same on every run and for every
 // grid shape.
 #include <cstdint>
+#include <mutex>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -74,8 +75,75 @@ cudaError_t sum_tree(const F* x, int64_t n, F* work, F* result, cudaStream_t s) 
   return cudaGetLastError();
 }
 
+// ----------------------------------------------------------------------------------------
+// Measure without any allocation: the sum-tree levels live in a fixed device array of this
+// library. Level 1 (sums of 64 consecutive cell sums) is produced directly from the det J
+// field, in the order cell_sums_kernel followed by block_sum_kernel would use, so the result is
+// the same bits as the allocating path.
+
+constexpr int64_t kStaticMaxCells = int64_t(1) << 24;  // 16,777,216 cells
+// tree_elems(kStaticMaxCells) = 262144 + 4096 + 64 + 1 values, rounded up to a multiple of 64.
+constexpr int64_t kStaticScratchElems = 266368;
+static __device__ __align__(256) double g_measure_scratch[kStaticScratchElems];  // 2,130,944 bytes
+
+template <typename F>
+__global__ void __launch_bounds__(256) cell_block_sums_kernel(const F* detj, const F* weights, F* out,
+                                                              int64_t num_cells, int num_points,
+                                                              int tile_shift) {
+  __shared__ F sums[256];
+  const int64_t mask = (1 << tile_shift) - 1;
+  const int64_t nblocks = (num_cells + kSumBlock - 1) / kSumBlock;
+  for (int64_t base_cell = (int64_t)blockIdx.x * 256; base_cell < num_cells;
+       base_cell += (int64_t)gridDim.x * 256) {
+    const int64_t c = base_cell + threadIdx.x;
+    if (c < num_cells) {
+      const int64_t base = (((c >> tile_shift) * num_points) << tile_shift) + (c & mask);
+      F acc = detj[base] * weights[0];
+      for (int q = 1; q < num_points; ++q) acc = fma(detj[base + ((int64_t)q << tile_shift)], weights[q], acc);
+      sums[threadIdx.x] = acc;
+    }
+    __syncthreads();
+    if (threadIdx.x < 256 / kSumBlock) {
+      const int64_t i = base_cell / kSumBlock + threadIdx.x;  // level-1 value index
+      const int64_t start = i * kSumBlock;
+      if (i < nblocks) {
+        const int64_t end = start + kSumBlock < num_cells ? start + kSumBlock : num_cells;
+        const int local = (int)(start - base_cell);
+        F acc = sums[local];
+        for (int64_t j = start + 1; j < end; ++j) acc += sums[local + (int)(j - start)];
+        out[i] = acc;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 }  // namespace tlg
 
+namespace {
+
+// Device address of g_measure_scratch for each device, found once per device (with that device
+// current) by the first call made on it.
+std::mutex g_scratch_mutex;
+void* g_scratch_ptr[64] = {};
+
+tlg_status static_scratch(void** ptr) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return tlg::cuda_fail(e, "tlg_measure_static: cudaGetDevice");
+  if (dev < 0 || dev >= 64) return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_measure_static: device ordinal above 63");
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (!g_scratch_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, tlg::g_measure_scratch);
+    if (e != cudaSuccess) return tlg::cuda_fail(e, "tlg_measure_static: cudaGetSymbolAddress");
+    g_scratch_ptr[dev] = p;
+  }
+  *ptr = g_scratch_ptr[dev];
+  return TLG_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -133,6 +201,51 @@ tlg_status tlg_sum(const void* x, int dtype, int64_t n, void* workspace, int64_t
           : tlg::sum_tree<double>(static_cast<const double*>(x), n, static_cast<double*>(workspace),
                                   static_cast<double*>(result), s);
   return e == cudaSuccess ? tlg::ok() : tlg::cuda_fail(e, "tlg_sum launch");
+}
+
+int64_t tlg_measure_static_max_cells(void) { return tlg::kStaticMaxCells; }
+
+tlg_status tlg_measure_static(const void* detj, int dtype, int64_t num_cells, int64_t num_points,
+                              int tile, const void* weights, void* result, void* stream) {
+  int shift = -1;
+  for (int s = 0; s <= 4; ++s)
+    if (tile == (1 << s)) shift = s;
+  if (shift < 0 || (dtype != TLG_F32 && dtype != TLG_F64) || num_cells < 0 || num_points < 0 ||
+      num_points > (1 << 30) || !result)
+    return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_measure_static: bad tile, dtype, sizes or result");
+  if (num_cells > tlg::kStaticMaxCells)
+    return tlg::fail(TLG_ERR_ALLOCATION_TOO_LARGE,
+                     "tlg_measure_static: " + std::to_string(num_cells) +
+                         " cells exceed the fixed scratch's maximum of " +
+                         std::to_string(tlg::kStaticMaxCells));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (num_cells == 0 || num_points == 0) {
+    cudaError_t e = cudaMemsetAsync(result, 0, dtype, s);
+    return e == cudaSuccess ? tlg::ok() : tlg::cuda_fail(e, "tlg_measure_static");
+  }
+  if (!detj || !weights) return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_measure_static: NULL input");
+  void* scratch = nullptr;
+  tlg_status st = static_scratch(&scratch);
+  if (st != TLG_OK) return st;
+  const int64_t level1 = (num_cells + tlg::kSumBlock - 1) / tlg::kSumBlock;
+  const unsigned grid = tlg::grid_for(num_cells, 256);
+  cudaError_t e = cudaSuccess;
+  if (dtype == TLG_F32) {
+    float* l1 = level1 == 1 ? static_cast<float*>(result) : static_cast<float*>(scratch);
+    tlg::cell_block_sums_kernel<float><<<grid, 256, 0, s>>>(
+        static_cast<const float*>(detj), static_cast<const float*>(weights), l1, num_cells,
+        (int)num_points, shift);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && level1 > 1) e = tlg::sum_tree<float>(l1, level1, l1 + level1, static_cast<float*>(result), s);
+  } else {
+    double* l1 = level1 == 1 ? static_cast<double*>(result) : static_cast<double*>(scratch);
+    tlg::cell_block_sums_kernel<double><<<grid, 256, 0, s>>>(
+        static_cast<const double*>(detj), static_cast<const double*>(weights), l1, num_cells,
+        (int)num_points, shift);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && level1 > 1) e = tlg::sum_tree<double>(l1, level1, l1 + level1, static_cast<double*>(result), s);
+  }
+  return e == cudaSuccess ? tlg::ok() : tlg::cuda_fail(e, "tlg_measure_static launch");
 }
 
 }  // extern "C"

@@ -180,6 +180,26 @@ int64_t tlg_sum_workspace_bytes(int dtype, int64_t n);
 tlg_status tlg_sum(const void* x, int dtype, int64_t n, void* workspace, int64_t workspace_bytes,
                    void* result, void* stream);
 
+/* The measure of one det J chunk without any device allocation, for callers that cannot call
+ * cudaMalloc: hosts whose device memory is owned by another allocator (a caching allocator or a
+ * pool that reserves the free memory up front, as PyTorch's and CubeCL's runtimes do), where an
+ * extra cudaMalloc can fail and a cudaFree synchronises the whole device. No counterpart in the
+ * reference, whose measure_block allocates its per-cell sums (measure.rs:141-185).
+ *
+ * Same inputs and the same result bits as tlg_measure_cell_sums followed by tlg_sum: the caller
+ * passes det J (a QuadField chunk), the weights and a device result of F. The sum tree's
+ * levels live in one fixed array of 2,130,944 bytes inside this library, which every GPU that
+ * loads the library holds until the process exits; chunks of more than
+ * tlg_measure_static_max_cells() = 16,777,216 cells are rejected with
+ * TLG_ERR_ALLOCATION_TOO_LARGE. The first call on each device looks up the array's device
+ * address (with that device current); make that first call before any stream capture. Every call
+ * shares the array: calls whose kernels may overlap on the GPU (other streams, other threads)
+ * race and must be serialised by the caller. No value of the array needs to start at zero:
+ * each is written before it is read. */
+tlg_status tlg_measure_static(const void* detj, int dtype, int64_t num_cells, int64_t num_points,
+                              int tile, const void* weights, void* result, void* stream);
+int64_t tlg_measure_static_max_cells(void);
+
 #ifdef __cplusplus
 }
 #endif
