@@ -8,6 +8,11 @@ det J and K = J^-1 at every point (22 values). One step = one evaluation of the 
 device; `e2e` adds, every step, the host-to-device copy of the node and dofmap arrays from
 pinned host memory, the evaluation, the measure (sum of det J * w) and its read back.
 
+Modes (`--mode`): `split` (default): the f64 mesh evaluated in FP32 on cell-shifted
+coordinates into f32 fields, FP64 recompute at near-degenerate points; its error against the
+plain FP64 GPU path is measured per output in the same run and reported with it, together with
+that path's own rate. `f64`: the plain per-block FP64 path. `f32`: an f32 mesh in FP32.
+
 `--impl reference` times the CPU restatement of the reference's f64 evaluation (the oracle,
 C + OpenMP) on the host cores over the same workload.
 
@@ -44,7 +49,7 @@ def parse():
     p.add_argument("--steps", type=int, default=40)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--dtype", choices=["f64", "f32"], default="f64")
+    p.add_argument("--mode", choices=["split", "f64", "f32"], default="split")
     p.add_argument("--n", type=int, default=64, help="subcells per direction")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
@@ -191,13 +196,27 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def time_steps(step, steps, flush, stream):
+    """CUDA-event time of each step (L2 flushed before each, outside the events); mean ms."""
+    import torch
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for i in range(steps):
+        flush.zero_()
+        starts[i].record(stream)
+        step()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    times = [a.elapsed_time(b) for a, b in zip(starts, ends)]
+    return sum(times) / len(times)
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
 
     import gridcl_gb300 as tg
-    from gridcl_gb300 import _lib
-    from gridcl_gb300.geometry import current_stream_handle
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -205,23 +224,25 @@ def run_ours(args):
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl")
-    dtype = torch.float64 if args.dtype == "f64" else torch.float32
-    es = 8 if args.dtype == "f64" else 4
+    mesh_dtype = torch.float32 if args.mode == "f32" else torch.float64
+    precision = "split" if args.mode == "split" else "native"
+    out_es = 8 if args.mode == "f64" else 4
 
     mesh = build_mesh(args.n)
     pts, w = rule()
-    g = tg.Geometry.from_host(mesh, dtype=dtype)
+    g = tg.Geometry.from_host(mesh, dtype=mesh_dtype)
     ps = tg.PointSet("Tetrahedron", pts, w)
     cells, k = mesh.blocks[0].cells.shape
     nq = pts.shape[0]
     qpts = cells * nq
     factors = ("points", "jacobian", "detj", "pinv")
-    out = tg.geometric_factors_block(g, 0, ps, factors)  # allocates the fields once
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    out = tg.geometric_factors_block(g, 0, ps, factors, precision=precision, recomputed=count)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
 
     def step():
-        tg.geometric_factors_block(g, 0, ps, factors, out=out)
+        tg.geometric_factors_block(g, 0, ps, factors, out=out, precision=precision, recomputed=count)
 
     for _ in range(args.warmup):
         step()
@@ -232,37 +253,51 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     t_wall0 = time.time()
-    for i in range(args.steps):
-        flush.zero_()  # L2 flush between steps, outside the timed events
-        starts[i].record(stream)
-        step()
-        ends[i].record(stream)
-    torch.cuda.synchronize()
+    ms = time_steps(step, args.steps, flush, stream)
     t_wall1 = time.time()
     if world > 1:
         dist.barrier()
     sampler.mark(t_wall0, t_wall1)
-    times = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = sum(times) / len(times)
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     ms_max = float(t.item())
+
+    # The plain FP64 GPU path on the same mesh: its rate, and the split path's error against it.
+    plain = None
+    if args.mode == "split":
+        ref = tg.geometric_factors_block(g, 0, ps, factors)
+
+        def plain_step():
+            tg.geometric_factors_block(g, 0, ps, factors, out=ref)
+
+        plain_step()
+        torch.cuda.synchronize()
+        plain_ms = time_steps(plain_step, max(3, min(args.steps, 5)), flush, stream)
+        errs = {}
+        for f in factors:
+            a = out[f].chunks[0].data.double()
+            b = ref[f].chunks[0].data
+            errs[f] = float((a - b).abs().max() / b.abs().max())
+        plain = {"ms_per_step": plain_ms, "value": world * qpts / (plain_ms * 1e-3),
+                 "rel_err_vs_fp64": errs,
+                 "speedup": plain_ms / ms}
+        del ref
+    recomputed = int(count.item())
 
     # End to end through the public API: pinned host inputs copied in every step, measure read back.
     host_nodes = g.nodes.cpu().pin_memory()
     host_dofmap = g.blocks[0].dofmap.cpu().pin_memory()
     h2d = host_nodes.numel() * host_nodes.element_size() + host_dofmap.numel() * 4
     e2e_steps = max(3, min(args.steps, 10))
+    meas_geom = g
 
     def e2e_step():
         g.nodes.copy_(host_nodes, non_blocking=True)
         g.blocks[0].dofmap.copy_(host_dofmap, non_blocking=True)
-        f = tg.geometric_factors_block(g, 0, ps, factors, out=out)
-        return tg.measure_block(g, 0, ps, detj=f["detj"])
+        f = tg.geometric_factors_block(g, 0, ps, factors, out=out, precision=precision)
+        return measure_of(tg, meas_geom, ps, f["detj"])
 
     for _ in range(2):
         vol = e2e_step()
@@ -282,7 +317,8 @@ def run_ours(args):
 
     if rank == 0:
         nout = 3 + 9 + 1 + 9
-        alg = algorithmic_bytes(cells, k, g.nodes.shape[0], 3, qpts, es, nout)
+        node_es = 4 if args.mode == "f32" else 8
+        alg = cells * k * 4 + g.nodes.shape[0] * 3 * node_es + qpts * nout * out_es
         peaks = {}
         try:
             peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -290,26 +326,31 @@ def run_ours(args):
             pass
         peak = float(peaks.get("hbm_gbs", 6800.0))
         achieved = alg / (ms * 1e-3) / 1e9
+        dtype = {"split": "f32", "f64": "f64", "f32": "f32"}[args.mode]
         line = {
             "metric": METRIC, "value": world * qpts / (ms_max * 1e-3), "unit": "qpoints/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic (seeded sin-mapped, jittered P2 tetrahedral box)",
-            "config": {"workload": WORKLOAD, "cells": int(cells), "nodes_per_cell": int(k),
+            "config": {"workload": WORKLOAD, "mode": args.mode, "mesh_dtype": str(mesh_dtype),
+                       "cells": int(cells), "nodes_per_cell": int(k),
                        "nodes": int(g.nodes.shape[0]), "points": int(nq), "qpoints": int(qpts),
-                       "outputs_per_qpoint": nout, "tile": 16,
+                       "outputs_per_qpoint": nout, "output_bytes": out_es, "tile": 16,
                        "l2": "256 MiB flush between steps (outside the timed events); outputs exceed L2",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None,
                          "algorithmic_bytes_per_launch": alg,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"},
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in peaks else "fallback 6800"},
             "e2e": {"value": world * qpts / (e2e_ms * 1e-3), "unit": "qpoints/s",
-                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": es, "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": out_es, "ms_per_step": e2e_ms,
                     "measure": vol},
             "gpu_launches": args.steps,
             "clocks": sampler.summary(),
         }
+        if plain is not None:
+            line["plain_fp64_gpu"] = plain
+            line["recomputed_points"] = recomputed
         if not args.no_cpu_baseline:
             v, threads, passes = cpu_baseline(mesh, pts)
             line["cpu_baseline"] = {"value": v, "unit": "qpoints/s", "cores": threads, "kind": "port",
@@ -317,6 +358,28 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def measure_of(tg, g, ps, detj):
+    """The measure from a det J field (f32 or f64) through the native sum tree."""
+    import torch
+
+    from gridcl_gb300._lib import check, lib
+    from gridcl_gb300.geometry import current_stream_handle
+
+    dt = detj.chunks[0].data.dtype
+    es = 4 if dt == torch.float32 else 8
+    sums = torch.empty(detj.num_cells, dtype=dt, device="cuda")
+    wd = ps.weights_device(dt)
+    stream = current_stream_handle()
+    ch = detj.chunks[0]
+    check(lib().tlg_measure_cell_sums(ch.data.data_ptr(), es, ch.num_cells, detj.num_points, detj.tile,
+                                      wd.data_ptr(), sums.data_ptr(), stream))
+    nbytes = int(lib().tlg_sum_workspace_bytes(es, detj.num_cells))
+    work = torch.empty(max(nbytes, es), dtype=torch.uint8, device="cuda")
+    res = torch.empty(1, dtype=dt, device="cuda")
+    check(lib().tlg_sum(sums.data_ptr(), es, detj.num_cells, work.data_ptr(), nbytes, res.data_ptr(), stream))
+    return float(res.item())
 
 
 def main():

@@ -65,6 +65,8 @@ class TlgOutputs(ctypes.Structure):
         ("pinv", ctypes.c_void_p),
         ("normals", ctypes.c_void_p),
         ("facet_normals", ctypes.c_void_p),
+        ("cond_limit", ctypes.c_double),
+        ("recomputed", ctypes.c_void_p),
     ]
 
 

@@ -20,7 +20,7 @@ struct tlg_tables {
   bool has_refn;
   unsigned char* dev = nullptr;  // phi [Q][K] | dphi [Q][K][TD] | refn [Q][TD] | error word
   uint32_t bytes = 0;            // staged bytes (multiple of 16), error word excluded
-  uint32_t off_dphi = 0, off_refn = 0;
+  uint32_t off_dphi = 0, off_refn = 0, off_dphi64 = 0;
   int* err = nullptr;
   std::vector<unsigned char> host;  // host copy of the staged bytes
 };
@@ -124,6 +124,43 @@ tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs
   return ok();
 }
 
+tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                      cudaStream_t stream) {
+  tlg::SplitArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = static_cast<const double*>(b->nodes);
+  a.dofmap = b->dofmap;
+  a.flags = b->flags;
+  a.tab = t->dev;
+  void* outs[6] = {o->points, o->jacobian, o->detj, o->pinv, o->normals, o->facet_normals};
+  for (int i = 0; i < 6; ++i) a.out[i] = static_cast<float*>(outs[i]);
+  a.err = t->err;
+  a.recomputed = o->recomputed;
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + o->tile - 1) / o->tile * o->tile;
+  a.out_first_cell = o->out_first_cell;
+  a.last_cell = b->num_cells - 1;
+  const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
+  a.last_flag = nflags - 1;
+  for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
+  a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 1e3f;
+  a.last_node = (uint32_t)(b->num_nodes - 1);
+  a.tab_bytes = t->bytes;
+  a.off_dphi = t->off_dphi;
+  a.off_refn = t->off_refn;
+  a.off_dphi64 = t->off_dphi64;
+  a.mask = mask;
+  a.num_points = (int)t->q;
+  a.tile_shift = tile_shift(o->tile);
+  bool found = false;
+  cudaError_t e = tlg::launch_eval_split(t->td, t->gd, (int)t->k, a, t->bytes, stream, &found);
+  if (!found)
+    return fail(TLG_ERR_UNSUPPORTED, "tlg_eval_block: no split-precision kernel for this element (tdim " +
+                                         std::to_string(t->td) + ", " + std::to_string(t->k) + " nodes)");
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  return ok();
+}
+
 }  // namespace
 
 extern "C" {
@@ -205,8 +242,8 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
     if (gdim < td || gdim > 3)
       return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: gdim " + std::to_string(gdim) +
                                                 " with tdim " + std::to_string(td));
-    if (dtype != TLG_F32 && dtype != TLG_F64)
-      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: dtype must be 4 or 8");
+    if (dtype != TLG_F32 && dtype != TLG_F64 && dtype != TLG_SPLIT32)
+      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: dtype must be 4, 8 or 12");
     if (degree < 1) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: degree must be >= 1");
     if (npoints < 0 || (npoints > 0 && !points))
       return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: bad points");
@@ -223,11 +260,15 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
     t->k = k;
     t->q = npoints;
     t->has_refn = ref_normals != nullptr;
-    const size_t es = (size_t)dtype;
+    const size_t es = dtype == TLG_SPLIT32 ? 4 : (size_t)dtype;
     const size_t n_phi = (size_t)npoints * k, n_dphi = n_phi * td, n_refn = (size_t)npoints * td;
     t->off_dphi = align16(n_phi * es);
     t->off_refn = align16(t->off_dphi + n_dphi * es);
-    const size_t total = align16(t->off_refn + std::max<size_t>(n_refn, 1) * es);
+    size_t total = align16(t->off_refn + std::max<size_t>(n_refn, 1) * es);
+    if (dtype == TLG_SPLIT32) {  // the f64 derivative table of the FP64 recompute follows
+      t->off_dphi64 = (uint32_t)total;
+      total = align16(total + std::max<size_t>(n_dphi, 1) * 8);
+    }
     if (total + 16 > (size_t)200 * 1024) {
       delete t;
       return fail(TLG_ERR_ALLOCATION_TOO_LARGE,
@@ -244,7 +285,8 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
         for (int d = 0; d < td; ++d) dphi[(q * k + i) * td + d] = tab[((1 + d) * npoints + q) * k + i];
       }
     if (ref_normals) std::memcpy(refn.data(), ref_normals, n_refn * sizeof(double));
-    if (dtype == TLG_F32) {
+    if (dtype == TLG_SPLIT32) narrow_into<double>(t->host, t->off_dphi64, dphi.data(), n_dphi);
+    if (dtype != TLG_F64) {
       narrow_into<float>(t->host, 0, phi.data(), n_phi);
       narrow_into<float>(t->host, t->off_dphi, dphi.data(), n_dphi);
       narrow_into<float>(t->host, t->off_refn, refn.data(), n_refn);
@@ -300,7 +342,7 @@ tlg_status tlg_tables_device_status(const tlg_tables* t, void* stream) {
 tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o,
                           void* stream) {
   if (!t || !b || !o) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: NULL argument");
-  if (b->dtype != t->dtype)
+  if (b->dtype != (t->dtype == TLG_SPLIT32 ? TLG_F64 : t->dtype))
     return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: block and tables differ in dtype");
   if (b->gdim != t->gd)
     return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: block gdim " + std::to_string(b->gdim) +
@@ -331,6 +373,7 @@ tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_out
     return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_eval_block: cells but no nodes");
   if (b->num_nodes > (int64_t)UINT32_MAX + 1 || b->num_cells > (int64_t)UINT32_MAX)
     return fail(TLG_ERR_TOO_LARGE, "tlg_eval_block: node or cell count does not fit u32");
+  if (t->dtype == TLG_SPLIT32) return eval_split(t, b, o, mask, static_cast<cudaStream_t>(stream));
   if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, static_cast<cudaStream_t>(stream));
   return eval_typed<double>(t, b, o, mask, static_cast<cudaStream_t>(stream));
 }

@@ -349,6 +349,176 @@ __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_
 }
 
 // ----------------------------------------------------------------------------------------
+// The split-precision kernel: f64 mesh in, FP32 arithmetic, f32 fields out.
+//
+// Each cell's nodes are shifted by its node 0 in f64 (x_k - x_0, FP64 subtractions once per
+// cell), then rounded to f32: the shifted coordinates have the size of the cell, so their f32
+// rounding is relative to the cell, not to the distance from the origin. J = sum_{k>=1} (x_k - x_0)
+// dphi_k (the k = 0 term vanishes; sum_k dphi_k = 0), X = x_0 + sum_{k>=1} (x_k - x_0) phi_k with
+// x_0 carried as an f32 pair. det J and K follow in f32. A condition estimate
+// kappa = |J|_F |K|_F / TD flags near-degenerate points (kappa above `cond_limit`, or not
+// finite); for those J, det J and K are recomputed in FP64 from the f64 nodes and the f64
+// derivative table, then rounded to f32, and a device counter records how many points were
+// recomputed.
+
+struct SplitArgs {
+  const double* nodes;
+  const uint32_t* dofmap;
+  const uint32_t* flags;
+  const unsigned char* tab;  // phi32 | dphi32 | refn32 | dphi64
+  float* out[6];
+  int* err;
+  unsigned long long* recomputed;  // may be null
+  int64_t first_cell, padded, out_first_cell, last_cell, last_flag;
+  double origin[3];
+  float cond_limit;
+  uint32_t last_node, tab_bytes, off_dphi, off_refn, off_dphi64, mask;
+  int num_points, tile_shift;
+};
+
+template <int TD, int GD>
+__device__ __forceinline__ float frob(const float* m) {
+  float s = m[0] * m[0];
+#pragma unroll
+  for (int i = 1; i < TD * GD; ++i) s = fmaf(m[i], m[i], s);
+  return sqrtf(s);
+}
+
+template <int TD, int GD, int K>
+__global__ void __launch_bounds__(kEvalThreads) eval_split_kernel(const __grid_constant__ SplitArgs a) {
+  __shared__ uint64_t bar;
+  extern __shared__ __align__(16) unsigned char smem[];
+  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  const float* phi = reinterpret_cast<const float*>(smem);
+  const float* dphi = reinterpret_cast<const float*>(smem + a.off_dphi);
+  const float* refn = reinterpret_cast<const float*>(smem + a.off_refn);
+  const double* dphi64 = reinterpret_cast<const double*>(smem + a.off_dphi64);
+  const int nq = a.num_points;
+  const uint32_t mask = a.mask;
+  const bool want_j = (mask & ~kOutPoints) != 0;
+  constexpr int LJ = TD * GD;
+  const int tile_mask = (1 << a.tile_shift) - 1;
+  using M = Factors<float, TD, GD>;
+  using M64 = Factors<double, TD, GD>;
+
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cell = min(a.first_cell + c, a.last_cell);
+    uint32_t idx[K];
+    load_row<K>(a.dofmap + cell * K, idx);
+#pragma unroll
+    for (int k = 0; k < K; ++k) idx[k] = min(idx[k], a.last_node);
+    double x0[GD];
+#pragma unroll
+    for (int g = 0; g < GD; ++g) x0[g] = __ldg(a.nodes + (int64_t)idx[0] * GD + g);
+    float y[K][GD];
+#pragma unroll
+    for (int k = 1; k < K; ++k)
+#pragma unroll
+      for (int g = 0; g < GD; ++g)
+        y[k][g] = __double2float_rn(__ldg(a.nodes + (int64_t)idx[k] * GD + g) - x0[g]);
+    // x_0 + origin as an f32 pair (hi + lo), for the physical points.
+    float xh[GD], xl[GD];
+    if (mask & kOutPoints) {
+#pragma unroll
+      for (int g = 0; g < GD; ++g) {
+        const double v = x0[g] + a.origin[g];
+        xh[g] = __double2float_rn(v);
+        xl[g] = __double2float_rn(v - (double)xh[g]);
+      }
+    }
+    float sign = 1.0f;
+    if ((mask & kOutNormals) && a.flags != nullptr && a.last_flag >= 0) {
+      const uint32_t f = __ldg(a.flags + min(a.first_cell + c, a.last_flag));
+      sign = (f & 1u) ? -1.0f : 1.0f;
+    }
+    const int64_t o = a.out_first_cell + c;
+    const int64_t tile_idx = o >> a.tile_shift;
+    const int lane = (int)(o & tile_mask);
+
+    for (int q = 0; q < nq; ++q) {
+      if (mask & kOutPoints) {
+        float s[GD];
+        const float* w = phi + q * K;
+#pragma unroll
+        for (int g = 0; g < GD; ++g) s[g] = y[1][g] * w[1];
+#pragma unroll
+        for (int k = 2; k < K; ++k) {
+          const float wk = w[k];
+#pragma unroll
+          for (int g = 0; g < GD; ++g) s[g] = fmaf(y[k][g], wk, s[g]);
+        }
+#pragma unroll
+        for (int g = 0; g < GD; ++g) s[g] = xh[g] + (xl[g] + s[g]);
+        store_point(a.out[0], tile_idx, q, nq, GD, lane, a.tile_shift, s, GD);
+      }
+      if (!want_j) continue;
+      float j[LJ];
+      const float* dq = dphi + q * K * TD;
+#pragma unroll
+      for (int d = 0; d < TD; ++d) {
+        const float w1 = dq[TD + d];
+#pragma unroll
+        for (int g = 0; g < GD; ++g) j[d * GD + g] = y[1][g] * w1;
+      }
+#pragma unroll
+      for (int k = 2; k < K; ++k) {
+#pragma unroll
+        for (int d = 0; d < TD; ++d) {
+          const float w = dq[k * TD + d];
+#pragma unroll
+          for (int g = 0; g < GD; ++g) j[d * GD + g] = fmaf(y[k][g], w, j[d * GD + g]);
+        }
+      }
+      float kk[LJ];
+      M::pinv(j, kk);
+      float dj = M::detj(j);
+      const float kappa = frob<TD, GD>(j) * frob<TD, GD>(kk) * (1.0f / TD);
+      if (!(kappa <= a.cond_limit)) {
+        // Near-degenerate point: J, det J and K again in FP64 from the f64 nodes.
+        double jd[LJ], kd[LJ];
+#pragma unroll
+        for (int i = 0; i < LJ; ++i) jd[i] = 0.0;
+        const double* d64 = dphi64 + q * K * TD;
+        for (int k = 1; k < K; ++k) {
+#pragma unroll
+          for (int g = 0; g < GD; ++g) {
+            const double yk = __ldg(a.nodes + (int64_t)idx[k] * GD + g) - x0[g];
+#pragma unroll
+            for (int d = 0; d < TD; ++d) jd[d * GD + g] = fma(yk, d64[k * TD + d], jd[d * GD + g]);
+          }
+        }
+        M64::pinv(jd, kd);
+        dj = (float)M64::detj(jd);
+#pragma unroll
+        for (int i = 0; i < LJ; ++i) {
+          j[i] = (float)jd[i];
+          kk[i] = (float)kd[i];
+        }
+        if (a.recomputed) atomicAdd(a.recomputed, 1ull);
+      }
+      if (mask & kOutJacobian) store_point(a.out[1], tile_idx, q, nq, LJ, lane, a.tile_shift, j, LJ);
+      if (mask & kOutDetJ) store_point(a.out[2], tile_idx, q, nq, 1, lane, a.tile_shift, &dj, 1);
+      if (mask & kOutPinv) store_point(a.out[3], tile_idx, q, nq, LJ, lane, a.tile_shift, kk, LJ);
+      if constexpr (TD == GD) {
+        if (mask & kOutFacetNormals) {
+          float n[GD];
+          M::facet_normal(kk, refn + q * TD, n);
+          store_point(a.out[5], tile_idx, q, nq, GD, lane, a.tile_shift, n, GD);
+        }
+      }
+      if constexpr (TD + 1 == GD) {
+        if (mask & kOutNormals) {
+          float n[GD];
+          M::normal(j, sign, n);
+          store_point(a.out[4], tile_idx, q, nq, GD, lane, a.tile_shift, n, GD);
+        }
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------------------
 // The loops kernel: any K (run time), TD and GD at compile time; node coordinates re-read
 // through L1 at each point. Same values as the direct kernel.
 

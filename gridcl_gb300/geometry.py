@@ -192,8 +192,11 @@ class PointSet:
     def __len__(self) -> int:
         return self.points.shape[0]
 
-    def tables(self, element: CoordinateElement, gdim: int, dtype: torch.dtype):
-        key = (element, gdim, dtype)
+    def tables(self, element: CoordinateElement, gdim: int, dtype):
+        """Device tables for `element`; `dtype` is a torch dtype or the ABI code 12 for the
+        split-precision tables (f32 tables plus the f64 derivative table)."""
+        code = dtype if isinstance(dtype, int) else _DTYPES[dtype]
+        key = (element, gdim, code)
         t = self._tables.get(key)
         if t is None:
             if element.cell != self.cell:
@@ -202,7 +205,7 @@ class PointSet:
             pts = self.points if len(self) else np.zeros(1)
             rn = None if self.ref_normals is None else self.ref_normals.ctypes.data_as(ctypes.c_void_p)
             check(lib().tlg_tables_create(CELL_IDS[element.cell], element.degree,
-                                          FAMILY_IDS[element.family], gdim, _DTYPES[dtype],
+                                          FAMILY_IDS[element.family], gdim, code,
                                           pts.ctypes.data_as(ctypes.c_void_p), len(self), rn,
                                           ctypes.byref(h)))
             t = _Tables(h)
@@ -312,18 +315,36 @@ def _factor_names(g: Geometry, b: int, factors) -> list:
     return names
 
 
+SPLIT32 = 12  # ABI code of the split-precision tables
+
+
 def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points", "jacobian", "detj", "pinv"),
                             tile: int = GPU_QUAD_TILE, max_chunk_cells: int | None = None,
-                            out: dict | None = None) -> dict:
+                            out: dict | None = None, precision: str = "native",
+                            cond_limit: float = 0.0, recomputed: torch.Tensor | None = None) -> dict:
     """Every factor in `factors` of block b at the points of `pts`, in one fused launch per
-    chunk; returns ``{factor: QuadField}``. `out` may pass preallocated fields."""
+    chunk; returns ``{factor: QuadField}``. `out` may pass preallocated fields.
+
+    ``precision="native"`` computes in the mesh's scalar type. ``precision="split"`` (f64 meshes)
+    computes in FP32 on cell-shifted coordinates and returns f32 fields; points whose condition
+    estimate exceeds `cond_limit` (0: 1e3) get det J and K from FP64, and `recomputed` (an int64
+    CUDA tensor of one element) counts them."""
     blk = g.blocks[b]
     names = _factor_names(g, b, factors)
     td, gd = blk.element.tdim, g.gdim
     nq = len(pts)
-    tables = pts.tables(blk.element, gd, g.dtype)
+    if precision == "split":
+        if g.dtype != torch.float64:
+            raise GridError(1, "split precision evaluates f64 meshes")
+        tables = pts.tables(blk.element, gd, SPLIT32)
+        out_dtype = torch.float32
+    elif precision == "native":
+        tables = pts.tables(blk.element, gd, g.dtype)
+        out_dtype = g.dtype
+    else:
+        raise GridError(1, f"unknown precision {precision!r}")
     fields = out if out is not None else {
-        f: QuadField.uninit(blk.num_cells, nq, FACTOR_LEN[f](td, gd), tile, g.dtype,
+        f: QuadField.uninit(blk.num_cells, nq, FACTOR_LEN[f](td, gd), tile, out_dtype,
                             g.nodes.device, max_chunk_cells)
         for f in names}
     desc = g.block_desc(b)
@@ -336,8 +357,10 @@ def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points
         o.num_cells = ch0.num_cells
         o.out_first_cell = 0
         o.tile = tile
+        o.cond_limit = cond_limit
+        o.recomputed = recomputed.data_ptr() if recomputed is not None else None
         for f in names:
-            setattr(o, f if f != "points" else "points", fields[f].chunks[ci].data.data_ptr())
+            setattr(o, f, fields[f].chunks[ci].data.data_ptr())
         check(lib().tlg_eval_block(tables.handle, ctypes.byref(desc), ctypes.byref(o), stream))
     return fields
 

@@ -49,8 +49,10 @@ typedef enum tlg_status {
   TLG_ERR_ALLOCATION_TOO_LARGE = 7 /* GridError::AllocationTooLarge */
 } tlg_status;
 
-/* Scalar type of nodes and outputs: the byte size of F. */
-typedef enum tlg_dtype { TLG_F32 = 4, TLG_F64 = 8 } tlg_dtype;
+/* Scalar type of nodes and outputs: the byte size of F. TLG_SPLIT32 (tables only) selects the
+ * split-precision evaluation: an f64 mesh, FP32 arithmetic on cell-shifted coordinates, f32
+ * outputs, FP64 recompute of det J and K at points flagged by a condition estimate. */
+typedef enum tlg_dtype { TLG_F32 = 4, TLG_F64 = 8, TLG_SPLIT32 = 12 } tlg_dtype;
 
 /* tetraloma_dims::CellType (tetraloma-dims/src/dim.rs). */
 typedef enum tlg_cell {
@@ -144,6 +146,11 @@ typedef struct tlg_outputs {
   void* pinv;             /* K, TD * GD */
   void* normals;          /* codimension 1: unit normals, GD */
   void* facet_normals;    /* codimension 0: K^T n_ref / |K^T n_ref|, GD (tables need ref_normals) */
+  /* Split precision only (TLG_SPLIT32 tables): points whose condition estimate
+   * |J|_F |K|_F / TD exceeds cond_limit (or is not finite) get det J and K from FP64; 0 selects
+   * 1e3. `recomputed` (device u64, may be NULL) is incremented once per such point. */
+  double cond_limit;
+  unsigned long long* recomputed;
 } tlg_outputs;
 
 /* Fused evaluation of every requested factor of one block range in one launch: the

@@ -1,0 +1,117 @@
+"""Split precision (f64 mesh, FP32 arithmetic on cell-shifted coordinates, f32 fields, FP64
+recompute at flagged points) against the f64 oracle, with the error stated per output (GPU)."""
+
+import numpy as np
+import pytest
+import torch
+
+import gridcl_gb300 as tg
+from gridcl_gb300 import meshes
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+# Per-output relative error bounds of the split path against the f64 oracle (max abs error
+# over the block / max abs value, reference.rs:805-817), for well-conditioned curved cells.
+SPLIT_TOL = {"points": 2e-7, "jacobian": 2e-6, "detj": 4e-6, "pinv": 4e-6, "normals": 4e-6}
+
+
+def oracle(mesh, g, cell, degree, pts, factors, flags=None):
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[: g.gdim])
+    return orc.eval_block(cell, degree, absx, mesh.blocks[0].cells, pts, factors=factors, flags=flags)
+
+
+KEYS = {"points": "x", "jacobian": "j", "detj": "detj", "pinv": "k", "normals": "normals"}
+
+
+@pytest.mark.parametrize("cell,n,degree,rdeg", [("Tetrahedron", 4, 2, 4), ("Tetrahedron", 3, 1, 4),
+                                                ("Hexahedron", 3, 2, 4), ("Prism", 3, 2, 4),
+                                                ("Tetrahedron", 2, 3, 6)])
+def test_split_volume_errors_are_stated_per_output(cuda, cell, n, degree, rdeg):
+    mesh = meshes.curved_box(cell, n, degree, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    got = tg.geometric_factors_block(g, 0, ps, ("points", "jacobian", "detj", "pinv"),
+                                     precision="split", recomputed=count)
+    want = oracle(mesh, g, cell, degree, pts, ("x", "j", "detj", "k"))
+    for f, field in got.items():
+        assert field.chunks[0].data.dtype == torch.float32
+        err = orc.rel_err(field.to_host_cell_major(), want[KEYS[f]])
+        assert err < SPLIT_TOL[f], (f, err)
+    assert int(count.item()) == 0  # no point of these meshes is near-degenerate
+
+
+def test_split_is_more_accurate_than_plain_f32(cuda):
+    """Shifting by the cell's first node in f64 before rounding keeps J's rounding relative to
+    the cell size; plain f32 rounds coordinates relative to their distance from the origin."""
+    mesh = meshes.curved_box("Tetrahedron", 8, 2, jitter=0.02)
+    pts, _ = tg.refcell.gauss_rule("Tetrahedron", 4)
+    ps = tg.PointSet("Tetrahedron", pts, np.ones(len(pts)))
+    g64 = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    g32 = tg.Geometry.from_host(mesh, dtype=torch.float32)
+    want = oracle(mesh, g64, "Tetrahedron", 2, pts, ("j", "detj"))
+    split = tg.geometric_factors_block(g64, 0, ps, ("jacobian", "detj"), precision="split")
+    plain = tg.geometric_factors_block(g32, 0, ps, ("jacobian", "detj"))
+    for f in ("jacobian", "detj"):
+        es = orc.rel_err(split[f].to_host_cell_major(), want[KEYS[f]])
+        ep = orc.rel_err(plain[f].to_host_cell_major(), want[KEYS[f]])
+        assert es < ep / 4, (f, es, ep)
+
+
+def test_near_degenerate_points_are_recomputed_in_f64(cuda):
+    """A sliver tetrahedron (height 1e-6) next to a regular one: its points exceed the condition
+    limit and get det J and K from FP64; their det J is then exact to f32 rounding."""
+    nodes = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.3, 0.3, 1e-6],
+                      [0.0, 0.0, 1.0]]) + 100.0
+    cells = np.array([[0, 1, 2, 3], [0, 1, 2, 4]], dtype=np.uint32)
+    mesh = meshes.HostMesh(3, nodes, [meshes.HostBlock("Tetrahedron", 1, cells)])
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, _ = tg.refcell.gauss_rule("Tetrahedron", 2)
+    ps = tg.PointSet("Tetrahedron", pts, np.ones(len(pts)))
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    got = tg.geometric_factors_block(g, 0, ps, ("detj", "pinv"), precision="split", recomputed=count)
+    want = oracle(mesh, g, "Tetrahedron", 1, pts, ("detj", "k"))
+    assert int(count.item()) == len(pts)  # every point of the sliver, none of the other cell
+    d = got["detj"].to_host_cell_major()[..., 0]
+    assert np.all(np.abs(d[0] - want["detj"][0, :, 0]) <= 2e-7 * np.abs(want["detj"][0, :, 0]))
+    k = got["pinv"].to_host_cell_major()
+    assert orc.rel_err(k[0], want["k"][0]) < 1e-6
+
+
+@pytest.mark.parametrize("degree", [2, 4])
+def test_split_surface_errors(cuda, degree):
+    mesh = meshes.perturbed_radius(meshes.sphere(2, degree), 0.02)
+    flags = (np.arange(mesh.blocks[0].num_cells) % 2).astype(np.uint32)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64, flags=[flags])
+    pts, _ = tg.refcell.gauss_rule("Triangle", 2 * degree)
+    ps = tg.PointSet("Triangle", pts, np.ones(len(pts)))
+    got = tg.geometric_factors_block(g, 0, ps, ("points", "jacobian", "detj", "pinv", "normals"),
+                                     precision="split")
+    want = oracle(mesh, g, "Triangle", degree, pts, ("x", "j", "detj", "k", "normals"), flags=flags)
+    for f, field in got.items():
+        err = orc.rel_err(field.to_host_cell_major(), want[KEYS[f]])
+        assert err < SPLIT_TOL[f], (f, err)
+
+
+def test_split_is_deterministic_and_matches_per_factor_launches(cuda):
+    mesh = meshes.curved_box("Hexahedron", 3, 2, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, _ = tg.refcell.gauss_rule("Hexahedron", 4)
+    ps = tg.PointSet("Hexahedron", pts, np.ones(len(pts)))
+    a = tg.geometric_factors_block(g, 0, ps, ("points", "detj", "pinv"), precision="split")
+    b = tg.geometric_factors_block(g, 0, ps, ("points", "detj", "pinv"), precision="split")
+    c = tg.geometric_factors_block(g, 0, ps, ("detj",), precision="split")
+    for k in a:
+        assert torch.equal(a[k].chunks[0].data, b[k].chunks[0].data)
+    assert torch.equal(a["detj"].chunks[0].data, c["detj"].chunks[0].data)
+
+
+def test_split_rejects_f32_meshes(cuda):
+    mesh = meshes.cube_box("Tetrahedron", 1, 1)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float32)
+    pts, _ = tg.refcell.gauss_rule("Tetrahedron", 2)
+    with pytest.raises(tg.GridError):
+        tg.geometric_factors_block(g, 0, tg.PointSet("Tetrahedron", pts, np.ones(len(pts))),
+                                   ("detj",), precision="split")
