@@ -20,7 +20,7 @@ struct tlg_tables {
   bool has_refn;
   unsigned char* dev = nullptr;  // phi [Q][K] | dphi [Q][K][TD] | refn [Q][TD] | error word
   uint32_t bytes = 0;            // staged bytes (multiple of 16), error word excluded
-  uint32_t off_dphi = 0, off_refn = 0, off_dphi64 = 0;
+  uint32_t off_dphi = 0, off_refn = 0, off_phi2 = 0, off_dphi2 = 0, off_dphi64 = 0;
   int* err = nullptr;
   std::vector<unsigned char> host;  // host copy of the staged bytes
 };
@@ -86,6 +86,54 @@ void narrow_into(std::vector<unsigned char>& buf, size_t off, const double* src,
   for (size_t i = 0; i < n; ++i) dst[i] = (F)src[i];
 }
 
+// The paired-FP32 kernel: an f32 mesh (split = false) or split precision (split = true).
+// `found` is false when no paired kernel exists for the element (nothing launched).
+tlg_status eval_pair(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                     bool split, cudaStream_t stream, bool* found) {
+  tlg::PairArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = b->nodes;
+  a.dofmap = b->dofmap;
+  a.flags = b->flags;
+  a.tab = t->dev;
+  void* outs[6] = {o->points, o->jacobian, o->detj, o->pinv, o->normals, o->facet_normals};
+  for (int i = 0; i < 6; ++i) a.out[i] = static_cast<float*>(outs[i]);
+  a.err = t->err;
+  a.recomputed = o->recomputed;
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + o->tile - 1) / o->tile * o->tile;
+  a.out_first_cell = o->out_first_cell;
+  a.last_cell = b->num_cells - 1;
+  const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
+  a.last_flag = nflags - 1;
+  for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
+  a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 1e3f;
+  a.last_node = (uint32_t)(b->num_nodes - 1);
+  a.tab_bytes = t->bytes;
+  a.off_refn = t->off_refn;
+  a.off_phi2 = t->off_phi2;
+  a.off_dphi2 = t->off_dphi2;
+  a.off_dphi64 = t->off_dphi64;
+  a.mask = mask;
+  a.num_points = (int)t->q;
+  cudaError_t e = tlg::launch_eval_pair(split, t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
+  if (!*found) return TLG_ERR_UNSUPPORTED;
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  return ok();
+}
+
+tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                      cudaStream_t stream) {
+  bool found = false;
+  tlg_status st = o->tile == 16 ? eval_pair(t, b, o, mask, true, stream, &found) : TLG_ERR_UNSUPPORTED;
+  if (!found)
+    return fail(TLG_ERR_UNSUPPORTED, "tlg_eval_block: no split-precision kernel for this element (tdim " +
+                                         std::to_string(t->td) + ", " + std::to_string(t->k) +
+                                         " nodes) and tile " + std::to_string(o->tile) +
+                                         " (split precision runs with tile 16)");
+  return st;
+}
+
 template <typename F>
 tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
                       cudaStream_t stream) {
@@ -116,47 +164,15 @@ tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs
   a.k_runtime = (int)t->k;
   bool direct = false;
   cudaError_t e;
-  if constexpr (sizeof(F) == 4)
+  if constexpr (sizeof(F) == 4) {
+    if (shift == 4) {  // the GPU tile: the paired-FP32 kernel, when one is compiled for the element
+      tlg_status st = eval_pair(t, b, o, mask, false, stream, &direct);
+      if (direct) return st;
+    }
     e = tlg::launch_eval_f32(t->td, t->gd, (int)t->k, a, t->bytes, stream, &direct);
-  else
+  } else {
     e = tlg::launch_eval_f64(t->td, t->gd, (int)t->k, a, t->bytes, stream, &direct);
-  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
-  return ok();
-}
-
-tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
-                      cudaStream_t stream) {
-  tlg::SplitArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.nodes = static_cast<const double*>(b->nodes);
-  a.dofmap = b->dofmap;
-  a.flags = b->flags;
-  a.tab = t->dev;
-  void* outs[6] = {o->points, o->jacobian, o->detj, o->pinv, o->normals, o->facet_normals};
-  for (int i = 0; i < 6; ++i) a.out[i] = static_cast<float*>(outs[i]);
-  a.err = t->err;
-  a.recomputed = o->recomputed;
-  a.first_cell = o->first_cell;
-  a.padded = (o->num_cells + o->tile - 1) / o->tile * o->tile;
-  a.out_first_cell = o->out_first_cell;
-  a.last_cell = b->num_cells - 1;
-  const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
-  a.last_flag = nflags - 1;
-  for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
-  a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 1e3f;
-  a.last_node = (uint32_t)(b->num_nodes - 1);
-  a.tab_bytes = t->bytes;
-  a.off_dphi = t->off_dphi;
-  a.off_refn = t->off_refn;
-  a.off_dphi64 = t->off_dphi64;
-  a.mask = mask;
-  a.num_points = (int)t->q;
-  a.tile_shift = tile_shift(o->tile);
-  bool found = false;
-  cudaError_t e = tlg::launch_eval_split(t->td, t->gd, (int)t->k, a, t->bytes, stream, &found);
-  if (!found)
-    return fail(TLG_ERR_UNSUPPORTED, "tlg_eval_block: no split-precision kernel for this element (tdim " +
-                                         std::to_string(t->td) + ", " + std::to_string(t->k) + " nodes)");
+  }
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
   return ok();
 }
@@ -265,6 +281,15 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
     t->off_dphi = align16(n_phi * es);
     t->off_refn = align16(t->off_dphi + n_dphi * es);
     size_t total = align16(t->off_refn + std::max<size_t>(n_refn, 1) * es);
+    // Point pairs for the paired-FP32 kernels: phi2 [QP][K][2], dphi2 [QP][K][TD][2], f32; an odd
+    // last point is paired with itself.
+    const int64_t qp = (npoints + 1) / 2;
+    if (dtype != TLG_F64) {
+      t->off_phi2 = (uint32_t)total;
+      total = align16(total + std::max<size_t>((size_t)qp * k * 2, 1) * 4);
+      t->off_dphi2 = (uint32_t)total;
+      total = align16(total + std::max<size_t>((size_t)qp * k * td * 2, 1) * 4);
+    }
     if (dtype == TLG_SPLIT32) {  // the f64 derivative table of the FP64 recompute follows
       t->off_dphi64 = (uint32_t)total;
       total = align16(total + std::max<size_t>(n_dphi, 1) * 8);
@@ -286,6 +311,20 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       }
     if (ref_normals) std::memcpy(refn.data(), ref_normals, n_refn * sizeof(double));
     if (dtype == TLG_SPLIT32) narrow_into<double>(t->host, t->off_dphi64, dphi.data(), n_dphi);
+    if (dtype != TLG_F64) {
+      std::vector<double> phi2((size_t)qp * k * 2), dphi2((size_t)qp * k * td * 2);
+      for (int64_t p = 0; p < qp; ++p)
+        for (int h = 0; h < 2; ++h) {
+          const int64_t q = std::min<int64_t>(2 * p + h, npoints - 1);
+          for (int64_t i = 0; i < k; ++i) {
+            phi2[(p * k + i) * 2 + h] = phi[q * k + i];
+            for (int d = 0; d < td; ++d)
+              dphi2[((p * k + i) * td + d) * 2 + h] = dphi[(q * k + i) * td + d];
+          }
+        }
+      narrow_into<float>(t->host, t->off_phi2, phi2.data(), phi2.size());
+      narrow_into<float>(t->host, t->off_dphi2, dphi2.data(), dphi2.size());
+    }
     if (dtype != TLG_F64) {
       narrow_into<float>(t->host, 0, phi.data(), n_phi);
       narrow_into<float>(t->host, t->off_dphi, dphi.data(), n_dphi);

@@ -1,20 +1,30 @@
 // Fused geometry-evaluation kernels for sm_103a.
 //
-// One thread per cell of a block range. Each CTA stages the element's tabulation (values
-// [Q][K], derivatives [Q][K][TD], reference facet normals [Q][TD], all in F) from global memory
-// into its own shared memory with one bulk asynchronous copy (cp.async.bulk completing on an
-// mbarrier); every thread then reads table entries at warp-uniform addresses, which shared
-// memory broadcasts. A thread gathers its cell's K nodes through the dofmap (index clamped to
-// the last node, the cell clamped to the block's last cell, tetraloma-geometry/src/evector.rs:
-// 221-222) into registers and walks the Q points: J, then every requested factor from J, each
-// stored straight into its QuadField chunk at ((cell / tile) * Q * LEN + q * LEN + k) * tile +
-// cell % tile (tetraloma-geometry/src/field.rs:121-162). Consecutive threads are consecutive
-// cells, so each warp store covers whole tile rows.
+// One thread per cell of a block range; persistent CTAs (a grid-stride loop). Each CTA stages
+// the element's tabulation from global memory into its own shared memory with one bulk
+// asynchronous copy (cp.async.bulk completing on an mbarrier); threads then read table entries
+// at warp-uniform addresses, which shared memory broadcasts. A thread gathers its cell's K nodes
+// through the dofmap (index clamped to the last node, the cell clamped to the block's last cell,
+// tetraloma-geometry/src/evector.rs:221-222) into registers and walks the Q points: J, then
+// every requested factor from J, each stored straight into its QuadField chunk at
+// ((cell / tile) * Q * LEN + q * LEN + k) * tile + cell % tile
+// (tetraloma-geometry/src/field.rs:121-162). Consecutive threads are consecutive cells, so each
+// warp store covers whole tile rows.
 //
 // Arithmetic follows tetraloma-geometry/src/layout.rs:133-369: J(g, d) is the sum over the
 // nodes in ascending k starting with the k = 0 product; det J and K by the same cofactor
-// formulas; normals as s (J0 x J1) / |J0 x J1|. The CTAs are persistent (a grid-stride loop),
-// so the table is staged once per CTA.
+// formulas; normals as s (J0 x J1) / |J0 x J1|. Every operation is an explicitly rounded
+// intrinsic (no compiler contraction), written once for scalars and for f32 pairs, so the
+// kernels below give the same bits for the same point whichever of them runs.
+//
+// Kernels:
+//  - eval_pair_kernel<SPLIT, TD, GD, K>: f32 arithmetic on two quadrature points at once with
+//    Blackwell's paired FP32 instructions (FFMA2 / FMUL2 / FADD2). SPLIT = false: an f32 mesh.
+//    SPLIT = true: an f64 mesh, each cell shifted by its node 0 in f64 before rounding to f32,
+//    f32 fields, and an FP64 recompute of J, det J and K at points whose condition estimate
+//    exceeds a limit (counted in a device counter).
+//  - eval_direct_kernel<F, TD, GD, K, TILE>: scalar, everything unrolled (the f64 path).
+//  - eval_loops_kernel<F, TD, GD>: K and the tile at run time (every other element and tile).
 #pragma once
 
 #include <cstdint>
@@ -51,12 +61,28 @@ struct EvalArgs {
   int64_t last_flag;         // last readable flag index, or -1
   uint32_t last_node;        // node count - 1
   uint32_t tab_bytes;
-  uint32_t off_dphi;         // byte offset of the derivative table
-  uint32_t off_refn;         // byte offset of the reference normals
+  uint32_t off_dphi;         // byte offset of the derivative table [Q][K][TD]
+  uint32_t off_refn;         // byte offset of the reference normals [Q][TD]
   uint32_t mask;             // kOut* bits
   int num_points;            // Q
   int tile_shift;            // log2(tile)
   int k_runtime;             // K for the loops kernel
+};
+
+// Arguments of the paired kernels (f32 arithmetic; nodes f32, or f64 with SPLIT).
+struct PairArgs {
+  const void* nodes;
+  const uint32_t* dofmap;
+  const uint32_t* flags;
+  const unsigned char* tab;  // phi | dphi | refn | phi2 [QP][K][2] | dphi2 [QP][K][TD][2] | dphi64
+  float* out[6];
+  int* err;
+  unsigned long long* recomputed;  // may be null
+  int64_t first_cell, padded, out_first_cell, last_cell, last_flag;
+  double origin[3];
+  float cond_limit;
+  uint32_t last_node, tab_bytes, off_refn, off_phi2, off_dphi2, off_dphi64, mask;
+  int num_points;
 };
 
 // ----------------------------------------------------------------------------------------
@@ -105,114 +131,186 @@ __device__ __forceinline__ bool stage_table(const unsigned char* src, unsigned c
 }
 
 // ----------------------------------------------------------------------------------------
-// Factor math on J (column-major GD x TD), tetraloma-geometry/src/layout.rs:166-369.
+// Explicitly rounded arithmetic on scalars and f32 pairs.
 
-template <typename F, int TD, int GD>
+template <typename V>
+struct Ar;
+
+template <>
+struct Ar<float> {
+  using S = float;
+  __device__ static float splat(float s) { return s; }
+  __device__ static float mul(float a, float b) { return __fmul_rn(a, b); }
+  __device__ static float add(float a, float b) { return __fadd_rn(a, b); }
+  __device__ static float sub(float a, float b) { return __fsub_rn(a, b); }
+  __device__ static float fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+  __device__ static float neg(float a) { return -a; }
+  __device__ static float rcp(float a) { return __frcp_rn(a); }
+  __device__ static float div(float a, float b) { return __fdiv_rn(a, b); }
+  __device__ static float sqrt(float a) { return __fsqrt_rn(a); }
+};
+
+template <>
+struct Ar<double> {
+  using S = double;
+  __device__ static double splat(double s) { return s; }
+  __device__ static double mul(double a, double b) { return __dmul_rn(a, b); }
+  __device__ static double add(double a, double b) { return __dadd_rn(a, b); }
+  __device__ static double sub(double a, double b) { return __dsub_rn(a, b); }
+  __device__ static double fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+  __device__ static double neg(double a) { return -a; }
+  __device__ static double rcp(double a) { return __drcp_rn(a); }
+  __device__ static double div(double a, double b) { return __ddiv_rn(a, b); }
+  __device__ static double sqrt(double a) { return __dsqrt_rn(a); }
+};
+
+// Two quadrature points at once: .x is point q, .y point q + 1.
+template <>
+struct Ar<float2> {
+  using S = float;
+  __device__ static float2 splat(float s) { return make_float2(s, s); }
+  __device__ static float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+  __device__ static float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+  __device__ static float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
+  __device__ static float2 sub(float2 a, float2 b) { return __fadd2_rn(a, neg(b)); }
+  __device__ static float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+  __device__ static float2 rcp(float2 a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
+  __device__ static float2 div(float2 a, float2 b) {
+    return make_float2(__fdiv_rn(a.x, b.x), __fdiv_rn(a.y, b.y));
+  }
+  __device__ static float2 sqrt(float2 a) { return make_float2(__fsqrt_rn(a.x), __fsqrt_rn(a.y)); }
+};
+
+// ----------------------------------------------------------------------------------------
+// Factor math on J (column-major GD x TD), tetraloma-geometry/src/layout.rs:166-369, in the
+// value type V. a*b - c*d is fma(a, b, -(c*d)) throughout.
+
+template <typename V, int TD, int GD>
 struct Factors {
-  __device__ static F column_dot(const F* j, int a, int b) {
-    F acc = j[a * GD] * j[b * GD];
+  using A = Ar<V>;
+  __device__ static V cross(V a, V b, V c, V d) { return A::fma(a, b, A::neg(A::mul(c, d))); }
+
+  __device__ static V column_dot(const V* j, int a, int b) {
+    V acc = A::mul(j[a * GD], j[b * GD]);
 #pragma unroll
-    for (int g = 1; g < GD; ++g) acc = fma(j[a * GD + g], j[b * GD + g], acc);
+    for (int g = 1; g < GD; ++g) acc = A::fma(j[a * GD + g], j[b * GD + g], acc);
     return acc;
   }
 
-  __device__ static F square_det(const F* j) {
+  __device__ static V square_det(const V* j) {
     if constexpr (TD == 1) {
       return j[0];
     } else if constexpr (TD == 2) {
-      return j[0] * j[3] - j[2] * j[1];
+      return cross(j[0], j[3], j[2], j[1]);
     } else {
-      return j[0] * (j[4] * j[8] - j[7] * j[5]) - j[3] * (j[1] * j[8] - j[7] * j[2]) +
-             j[6] * (j[1] * j[5] - j[4] * j[2]);
+      // j0 (j4 j8 - j7 j5) - j3 (j1 j8 - j7 j2) + j6 (j1 j5 - j4 j2)
+      const V c0 = cross(j[4], j[8], j[7], j[5]);
+      const V c1 = cross(j[1], j[8], j[7], j[2]);
+      const V c2 = cross(j[1], j[5], j[4], j[2]);
+      return A::fma(j[6], c2, A::fma(j[0], c0, A::neg(A::mul(j[3], c1))));
     }
   }
 
-  __device__ static F detj(const F* j) {
+  __device__ static V detj(const V* j) {
     if constexpr (TD == GD) {
       return square_det(j);
     } else if constexpr (TD == 1) {
-      return sqrt(column_dot(j, 0, 0));
+      return A::sqrt(column_dot(j, 0, 0));
     } else {
-      const F a = column_dot(j, 0, 0), b = column_dot(j, 0, 1), c = column_dot(j, 1, 1);
-      return sqrt(a * c - b * b);
+      const V a = column_dot(j, 0, 0), b = column_dot(j, 0, 1), c = column_dot(j, 1, 1);
+      return A::sqrt(cross(a, c, b, b));
     }
   }
 
   // K(t, g) at g * TD + t.
-  __device__ static void pinv(const F* j, F* k) {
+  __device__ static void pinv(const V* j, V* k) {
     if constexpr (TD == GD) {
-      const F inv = F(1) / square_det(j);
+      const V inv = A::rcp(square_det(j));
       if constexpr (TD == 1) {
         k[0] = inv;
       } else if constexpr (TD == 2) {
-        k[0] = j[3] * inv;
-        k[2] = -j[2] * inv;
-        k[1] = -j[1] * inv;
-        k[3] = j[0] * inv;
+        k[0] = A::mul(j[3], inv);
+        k[2] = A::mul(A::neg(j[2]), inv);
+        k[1] = A::mul(A::neg(j[1]), inv);
+        k[3] = A::mul(j[0], inv);
       } else {
-        k[0] = (j[4] * j[8] - j[7] * j[5]) * inv;
-        k[3] = (j[6] * j[5] - j[3] * j[8]) * inv;
-        k[6] = (j[3] * j[7] - j[6] * j[4]) * inv;
-        k[1] = (j[7] * j[2] - j[1] * j[8]) * inv;
-        k[4] = (j[0] * j[8] - j[6] * j[2]) * inv;
-        k[7] = (j[6] * j[1] - j[0] * j[7]) * inv;
-        k[2] = (j[1] * j[5] - j[4] * j[2]) * inv;
-        k[5] = (j[3] * j[2] - j[0] * j[5]) * inv;
-        k[8] = (j[0] * j[4] - j[3] * j[1]) * inv;
+        k[0] = A::mul(cross(j[4], j[8], j[7], j[5]), inv);
+        k[3] = A::mul(cross(j[6], j[5], j[3], j[8]), inv);
+        k[6] = A::mul(cross(j[3], j[7], j[6], j[4]), inv);
+        k[1] = A::mul(cross(j[7], j[2], j[1], j[8]), inv);
+        k[4] = A::mul(cross(j[0], j[8], j[6], j[2]), inv);
+        k[7] = A::mul(cross(j[6], j[1], j[0], j[7]), inv);
+        k[2] = A::mul(cross(j[1], j[5], j[4], j[2]), inv);
+        k[5] = A::mul(cross(j[3], j[2], j[0], j[5]), inv);
+        k[8] = A::mul(cross(j[0], j[4], j[3], j[1]), inv);
       }
     } else if constexpr (TD == 1) {
-      const F inv = F(1) / column_dot(j, 0, 0);
+      const V inv = A::rcp(column_dot(j, 0, 0));
 #pragma unroll
-      for (int g = 0; g < GD; ++g) k[g] = j[g] * inv;
+      for (int g = 0; g < GD; ++g) k[g] = A::mul(j[g], inv);
     } else {
-      const F a = column_dot(j, 0, 0), b = column_dot(j, 0, 1), c = column_dot(j, 1, 1);
-      const F inv = F(1) / (a * c - b * b);
-      const F g00 = c * inv, g01 = -b * inv, g11 = a * inv;
+      const V a = column_dot(j, 0, 0), b = column_dot(j, 0, 1), c = column_dot(j, 1, 1);
+      const V inv = A::rcp(cross(a, c, b, b));
+      const V g00 = A::mul(c, inv), g01 = A::mul(A::neg(b), inv), g11 = A::mul(a, inv);
 #pragma unroll
       for (int g = 0; g < GD; ++g) {
-        k[g * TD] = g00 * j[g] + g01 * j[GD + g];
-        k[g * TD + 1] = g01 * j[g] + g11 * j[GD + g];
+        k[g * TD] = A::fma(g00, j[g], A::mul(g01, j[GD + g]));
+        k[g * TD + 1] = A::fma(g01, j[g], A::mul(g11, j[GD + g]));
       }
     }
   }
 
   // Codimension 1: s (J0_y, -J0_x) / |J0| or s (J0 x J1) / |J0 x J1|.
-  __device__ static void normal(const F* j, F s, F* n) {
-    F v[GD];
+  __device__ static void normal(const V* j, V s, V* n) {
+    V v[GD];
     if constexpr (GD == 2) {
       v[0] = j[1];
-      v[1] = -j[0];
+      v[1] = A::neg(j[0]);
     } else {
-      v[0] = j[1] * j[5] - j[2] * j[4];
-      v[1] = j[2] * j[3] - j[0] * j[5];
-      v[2] = j[0] * j[4] - j[1] * j[3];
+      v[0] = cross(j[1], j[5], j[2], j[4]);
+      v[1] = cross(j[2], j[3], j[0], j[5]);
+      v[2] = cross(j[0], j[4], j[1], j[3]);
     }
-    F s2 = v[0] * v[0];
+    V s2 = A::mul(v[0], v[0]);
 #pragma unroll
-    for (int g = 1; g < GD; ++g) s2 = fma(v[g], v[g], s2);
-    const F norm = sqrt(s2);
+    for (int g = 1; g < GD; ++g) s2 = A::fma(v[g], v[g], s2);
+    const V norm = A::sqrt(s2);
 #pragma unroll
-    for (int g = 0; g < GD; ++g) n[g] = (s * v[g]) / norm;
+    for (int g = 0; g < GD; ++g) n[g] = A::div(A::mul(s, v[g]), norm);
   }
 
-  // Codimension 0: m = K^T n_ref, m / |m|.
-  __device__ static void facet_normal(const F* k, const F* nref, F* n) {
-    F m[GD];
+  // Codimension 0: m = K^T n_ref, m / |m| (nref: the reference normal of each point).
+  __device__ static void facet_normal(const V* k, const V* nref, V* n) {
+    V m[GD];
 #pragma unroll
     for (int g = 0; g < GD; ++g) {
-      F acc = k[g * TD] * nref[0];
+      V acc = A::mul(k[g * TD], nref[0]);
 #pragma unroll
-      for (int t = 1; t < TD; ++t) acc = fma(k[g * TD + t], nref[t], acc);
+      for (int t = 1; t < TD; ++t) acc = A::fma(k[g * TD + t], nref[t], acc);
       m[g] = acc;
     }
-    F s2 = m[0] * m[0];
+    V s2 = A::mul(m[0], m[0]);
 #pragma unroll
-    for (int g = 1; g < GD; ++g) s2 = fma(m[g], m[g], s2);
-    const F norm = sqrt(s2);
+    for (int g = 1; g < GD; ++g) s2 = A::fma(m[g], m[g], s2);
+    const V norm = A::sqrt(s2);
 #pragma unroll
-    for (int g = 0; g < GD; ++g) n[g] = m[g] / norm;
+    for (int g = 0; g < GD; ++g) n[g] = A::div(m[g], norm);
+  }
+
+  // |J|_F |K|_F / TD, the Frobenius condition estimate (tetraloma-testing/src/reference.rs:237).
+  __device__ static V condition(const V* j, const V* k) {
+    V a = A::mul(j[0], j[0]), b = A::mul(k[0], k[0]);
+#pragma unroll
+    for (int i = 1; i < TD * GD; ++i) {
+      a = A::fma(j[i], j[i], a);
+      b = A::fma(k[i], k[i], b);
+    }
+    return A::mul(A::sqrt(A::mul(a, b)), A::splat((typename A::S)(1.0 / TD)));
   }
 };
+
+// ----------------------------------------------------------------------------------------
+// Stores.
 
 // Stores `len` components of one point of one cell: element (tile, q, comp, lane).
 template <typename F>
@@ -221,6 +319,31 @@ __device__ __forceinline__ void store_point(F* out, int64_t tile_idx, int q, int
   F* base = out + ((((tile_idx * nq + q) * len) << tile_shift) + lane);
   for (int c = 0; c < n; ++c) base[(int64_t)c << tile_shift] = v[c];
 }
+
+// Output cursor of one field for one cell of a kernel with a compile-time tile: points at
+// (tile, q, 0, lane); `put` stores one point's LEN components (immediate offsets c * TILE) and
+// advances; `put2` stores two consecutive points (the second only when `both`).
+template <typename F, int LEN, int TILE>
+struct Cursor {
+  F* p;
+  __device__ __forceinline__ void init(F* out, int64_t tile_idx, int nq, int lane) {
+    p = out + tile_idx * (int64_t)nq * (LEN * TILE) + lane;
+  }
+  __device__ __forceinline__ void put(const F* v) {
+#pragma unroll
+    for (int c = 0; c < LEN; ++c) p[c * TILE] = v[c];
+    p += LEN * TILE;
+  }
+  __device__ __forceinline__ void put2(const float2* v, bool both) {
+#pragma unroll
+    for (int c = 0; c < LEN; ++c) p[c * TILE] = v[c].x;
+    if (both) {
+#pragma unroll
+      for (int c = 0; c < LEN; ++c) p[(LEN + c) * TILE] = v[c].y;
+    }
+    p += 2 * LEN * TILE;
+  }
+};
 
 // Loads the K node indices of one cell with the widest aligned vector loads.
 template <int K>
@@ -248,9 +371,211 @@ __device__ __forceinline__ void load_row(const uint32_t* row, uint32_t* idx) {
 }
 
 // ----------------------------------------------------------------------------------------
-// The direct kernel: K, TD, GD at compile time, everything unrolled over nodes and dimensions.
+// FP64 recompute of one point of the split kernel: J from the f64 nodes shifted by node 0 and
+// the f64 derivative row of the point, then det J and K, rounded to f32 and stored over the
+// f32 values at the given addresses (component stride `stride`). Not inlined: it runs only at
+// flagged points, and its FP64 registers stay out of the kernel body.
+template <int TD, int GD, int K>
+__device__ __noinline__ void recompute_f64(const double* __restrict__ nodes, const uint32_t* row,
+                                           uint32_t last_node, const double* d64, float* pj,
+                                           float* pd, float* pk, int stride) {
+  constexpr int LJ = TD * GD;
+  using M64 = Factors<double, TD, GD>;
+  double jd[LJ], kd[LJ], x0[GD];
+  const uint32_t n0 = min(__ldg(row), last_node);
+#pragma unroll
+  for (int g = 0; g < GD; ++g) x0[g] = __ldg(nodes + (int64_t)n0 * GD + g);
+#pragma unroll
+  for (int i = 0; i < LJ; ++i) jd[i] = 0.0;
+  for (int k = 1; k < K; ++k) {
+    const uint32_t nk = min(__ldg(row + k), last_node);
+#pragma unroll
+    for (int g = 0; g < GD; ++g) {
+      const double yk = __ldg(nodes + (int64_t)nk * GD + g) - x0[g];
+#pragma unroll
+      for (int d = 0; d < TD; ++d) jd[d * GD + g] = __fma_rn(yk, d64[k * TD + d], jd[d * GD + g]);
+    }
+  }
+  M64::pinv(jd, kd);
+  if (pd) *pd = (float)M64::detj(jd);
+#pragma unroll
+  for (int i = 0; i < LJ; ++i) {
+    if (pj) pj[i * stride] = (float)jd[i];
+    if (pk) pk[i * stride] = (float)kd[i];
+  }
+}
 
-template <typename F, int TD, int GD, int K>
+// ----------------------------------------------------------------------------------------
+// The paired f32 kernel (tile 16).
+
+template <bool SPLIT, int TD, int GD, int K>
+__global__ void __launch_bounds__(kEvalThreads) eval_pair_kernel(const __grid_constant__ PairArgs a) {
+  constexpr int TILE = 16;
+  constexpr int LJ = TD * GD;
+  using A = Ar<float2>;
+  using M = Factors<float2, TD, GD>;
+  __shared__ uint64_t bar;
+  extern __shared__ __align__(16) unsigned char smem[];
+  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  const float2* phi2 = reinterpret_cast<const float2*>(smem + a.off_phi2);
+  const float2* dphi2 = reinterpret_cast<const float2*>(smem + a.off_dphi2);
+  const float* refn = reinterpret_cast<const float*>(smem + a.off_refn);
+  const double* dphi64 = reinterpret_cast<const double*>(smem + a.off_dphi64);
+  const int nq = a.num_points;
+  const int nqp = (nq + 1) / 2;
+  const uint32_t mask = a.mask;
+  const bool want_j = (mask & ~kOutPoints) != 0;
+  constexpr int K0 = SPLIT ? 1 : 0;  // the split kernel's node-0 term vanishes
+
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cell = min(a.first_cell + c, a.last_cell);
+    uint32_t idx[K];
+    load_row<K>(a.dofmap + cell * K, idx);
+    float x[K][GD];  // f32 nodes, or (SPLIT) x_k - x_0 rounded to f32 for k >= 1
+    float xh[GD], xl[GD];  // the origin (f32 mesh) or x_0 + origin as an f32 pair (SPLIT)
+    if constexpr (SPLIT) {
+      const double* nodes = static_cast<const double*>(a.nodes);
+      double x0[GD];
+      const uint32_t n0 = min(idx[0], a.last_node);
+#pragma unroll
+      for (int g = 0; g < GD; ++g) x0[g] = __ldg(nodes + (int64_t)n0 * GD + g);
+#pragma unroll
+      for (int k = 1; k < K; ++k) {
+        const uint32_t n = min(idx[k], a.last_node);
+#pragma unroll
+        for (int g = 0; g < GD; ++g) x[k][g] = __double2float_rn(__ldg(nodes + (int64_t)n * GD + g) - x0[g]);
+      }
+#pragma unroll
+      for (int g = 0; g < GD; ++g) {
+        const double v = x0[g] + a.origin[g];
+        xh[g] = __double2float_rn(v);
+        xl[g] = __double2float_rn(v - (double)xh[g]);
+      }
+    } else {
+      const float* nodes = static_cast<const float*>(a.nodes);
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const uint32_t n = min(idx[k], a.last_node);
+#pragma unroll
+        for (int g = 0; g < GD; ++g) x[k][g] = __ldg(nodes + (int64_t)n * GD + g);
+      }
+#pragma unroll
+      for (int g = 0; g < GD; ++g) {
+        xh[g] = (float)a.origin[g];
+        xl[g] = 0.0f;
+      }
+    }
+    float2 sign = A::splat(1.0f);
+    if ((mask & kOutNormals) && a.flags != nullptr && a.last_flag >= 0) {
+      const uint32_t f = __ldg(a.flags + min(a.first_cell + c, a.last_flag));
+      sign = A::splat((f & 1u) ? -1.0f : 1.0f);
+    }
+    const int64_t o = a.out_first_cell + c;
+    const int64_t tile_idx = o / TILE;
+    const int lane = (int)(o % TILE);
+    Cursor<float, GD, TILE> cx, cn, cf;
+    Cursor<float, LJ, TILE> cj, ck;
+    Cursor<float, 1, TILE> cd;
+    if (mask & kOutPoints) cx.init(a.out[0], tile_idx, nq, lane);
+    if (mask & kOutJacobian) cj.init(a.out[1], tile_idx, nq, lane);
+    if (mask & kOutDetJ) cd.init(a.out[2], tile_idx, nq, lane);
+    if (mask & kOutPinv) ck.init(a.out[3], tile_idx, nq, lane);
+    if (mask & kOutNormals) cn.init(a.out[4], tile_idx, nq, lane);
+    if (mask & kOutFacetNormals) cf.init(a.out[5], tile_idx, nq, lane);
+
+    for (int qp = 0; qp < nqp; ++qp) {
+      const bool both = 2 * qp + 1 < nq;
+      if (mask & kOutPoints) {
+        float2 s[GD];
+        const float2* w = phi2 + qp * K;
+#pragma unroll
+        for (int g = 0; g < GD; ++g) s[g] = A::mul(A::splat(x[K0][g]), w[K0]);
+#pragma unroll
+        for (int k = K0 + 1; k < K; ++k) {
+          const float2 wk = w[k];
+#pragma unroll
+          for (int g = 0; g < GD; ++g) s[g] = A::fma(A::splat(x[k][g]), wk, s[g]);
+        }
+#pragma unroll
+        for (int g = 0; g < GD; ++g) {
+          if constexpr (SPLIT) s[g] = A::add(A::splat(xh[g]), A::add(A::splat(xl[g]), s[g]));
+          else s[g] = A::add(s[g], A::splat(xh[g]));
+        }
+        cx.put2(s, both);
+      }
+      if (!want_j) continue;
+      float2 j[LJ];
+      const float2* dq = dphi2 + qp * K * TD;
+#pragma unroll
+      for (int d = 0; d < TD; ++d) {
+        const float2 w0 = dq[K0 * TD + d];
+#pragma unroll
+        for (int g = 0; g < GD; ++g) j[d * GD + g] = A::mul(A::splat(x[K0][g]), w0);
+      }
+#pragma unroll
+      for (int k = K0 + 1; k < K; ++k) {
+#pragma unroll
+        for (int d = 0; d < TD; ++d) {
+          const float2 w = dq[k * TD + d];
+#pragma unroll
+          for (int g = 0; g < GD; ++g) j[d * GD + g] = A::fma(A::splat(x[k][g]), w, j[d * GD + g]);
+        }
+      }
+      float2 kk[LJ];
+      const bool want_k = (mask & (kOutPinv | kOutFacetNormals)) != 0 || SPLIT;
+      if (want_k) M::pinv(j, kk);
+      float* pj = (mask & kOutJacobian) ? cj.p : nullptr;
+      float* pd = (mask & kOutDetJ) ? cd.p : nullptr;
+      float* pk = (mask & kOutPinv) ? ck.p : nullptr;
+      if (mask & kOutJacobian) cj.put2(j, both);
+      if (mask & kOutDetJ) {
+        const float2 dj = M::detj(j);
+        cd.put2(&dj, both);
+      }
+      if (mask & kOutPinv) ck.put2(kk, both);
+      if constexpr (TD == GD) {
+        if (mask & kOutFacetNormals) {
+          float2 nr[TD], n[GD];
+#pragma unroll
+          for (int t = 0; t < TD; ++t)
+            nr[t] = make_float2(refn[(2 * qp) * TD + t], refn[min(2 * qp + 1, nq - 1) * TD + t]);
+          M::facet_normal(kk, nr, n);
+          cf.put2(n, both);
+        }
+      }
+      if constexpr (TD + 1 == GD) {
+        if (mask & kOutNormals) {
+          float2 n[GD];
+          M::normal(j, sign, n);
+          cn.put2(n, both);
+        }
+      }
+      if constexpr (SPLIT) {
+        // Near-degenerate points (or non-finite estimates) again in FP64.
+        const float2 kap = M::condition(j, kk);
+        if ((pj || pd || pk) && (!(kap.x <= a.cond_limit) || (both && !(kap.y <= a.cond_limit)))) {
+          const double* nodes = static_cast<const double*>(a.nodes);
+          const uint32_t* row = a.dofmap + cell * K;
+          for (int h = 0; h < (both ? 2 : 1); ++h) {
+            const float kp = h == 0 ? kap.x : kap.y;
+            if (kp <= a.cond_limit) continue;
+            const int shift = h * LJ * TILE;
+            recompute_f64<TD, GD, K>(nodes, row, a.last_node, dphi64 + (2 * qp + h) * K * TD,
+                                     pj ? pj + shift : nullptr, pd ? pd + h * TILE : nullptr,
+                                     pk ? pk + shift : nullptr, TILE);
+            if (a.recomputed) atomicAdd(a.recomputed, 1ull);
+          }
+        }
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------------------
+// The direct kernel: scalar, K, TD, GD and the tile at compile time.
+
+template <typename F, int TD, int GD, int K, int TILE>
 __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_constant__ EvalArgs<F> a) {
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -262,7 +587,8 @@ __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_
   const uint32_t mask = a.mask;
   const bool want_j = (mask & ~kOutPoints) != 0;
   constexpr int LJ = TD * GD;
-  const int tile_mask = (1 << a.tile_shift) - 1;
+  using A = Ar<F>;
+  using M = Factors<F, TD, GD>;
 
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
        c += (int64_t)gridDim.x * blockDim.x) {
@@ -282,24 +608,33 @@ __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_
       sign = (f & 1u) ? F(-1) : F(1);
     }
     const int64_t o = a.out_first_cell + c;
-    const int64_t tile_idx = o >> a.tile_shift;
-    const int lane = (int)(o & tile_mask);
+    const int64_t tile_idx = o / TILE;
+    const int lane = (int)(o % TILE);
+    Cursor<F, GD, TILE> cx, cn, cf;
+    Cursor<F, LJ, TILE> cj, ck;
+    Cursor<F, 1, TILE> cd;
+    if (mask & kOutPoints) cx.init(a.out[0], tile_idx, nq, lane);
+    if (mask & kOutJacobian) cj.init(a.out[1], tile_idx, nq, lane);
+    if (mask & kOutDetJ) cd.init(a.out[2], tile_idx, nq, lane);
+    if (mask & kOutPinv) ck.init(a.out[3], tile_idx, nq, lane);
+    if (mask & kOutNormals) cn.init(a.out[4], tile_idx, nq, lane);
+    if (mask & kOutFacetNormals) cf.init(a.out[5], tile_idx, nq, lane);
 
     for (int q = 0; q < nq; ++q) {
       if (mask & kOutPoints) {
         F xp[GD];
         const F* w = phi + q * K;
 #pragma unroll
-        for (int g = 0; g < GD; ++g) xp[g] = x[0][g] * w[0];
+        for (int g = 0; g < GD; ++g) xp[g] = A::mul(x[0][g], w[0]);
 #pragma unroll
         for (int k = 1; k < K; ++k) {
           const F wk = w[k];
 #pragma unroll
-          for (int g = 0; g < GD; ++g) xp[g] = fma(x[k][g], wk, xp[g]);
+          for (int g = 0; g < GD; ++g) xp[g] = A::fma(x[k][g], wk, xp[g]);
         }
 #pragma unroll
-        for (int g = 0; g < GD; ++g) xp[g] = xp[g] + a.origin[g];
-        store_point(a.out[0], tile_idx, q, nq, GD, lane, a.tile_shift, xp, GD);
+        for (int g = 0; g < GD; ++g) xp[g] = A::add(xp[g], a.origin[g]);
+        cx.put(xp);
       }
       if (!want_j) continue;
       F j[LJ];
@@ -308,7 +643,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_
       for (int d = 0; d < TD; ++d) {
         const F w0 = dq[d];
 #pragma unroll
-        for (int g = 0; g < GD; ++g) j[d * GD + g] = x[0][g] * w0;
+        for (int g = 0; g < GD; ++g) j[d * GD + g] = A::mul(x[0][g], w0);
       }
 #pragma unroll
       for (int k = 1; k < K; ++k) {
@@ -316,24 +651,23 @@ __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_
         for (int d = 0; d < TD; ++d) {
           const F w = dq[k * TD + d];
 #pragma unroll
-          for (int g = 0; g < GD; ++g) j[d * GD + g] = fma(x[k][g], w, j[d * GD + g]);
+          for (int g = 0; g < GD; ++g) j[d * GD + g] = A::fma(x[k][g], w, j[d * GD + g]);
         }
       }
-      using M = Factors<F, TD, GD>;
-      if (mask & kOutJacobian) store_point(a.out[1], tile_idx, q, nq, LJ, lane, a.tile_shift, j, LJ);
+      if (mask & kOutJacobian) cj.put(j);
       if (mask & kOutDetJ) {
         const F dj = M::detj(j);
-        store_point(a.out[2], tile_idx, q, nq, 1, lane, a.tile_shift, &dj, 1);
+        cd.put(&dj);
       }
       if (mask & (kOutPinv | kOutFacetNormals)) {
         F k[LJ];
         M::pinv(j, k);
-        if (mask & kOutPinv) store_point(a.out[3], tile_idx, q, nq, LJ, lane, a.tile_shift, k, LJ);
+        if (mask & kOutPinv) ck.put(k);
         if constexpr (TD == GD) {
           if (mask & kOutFacetNormals) {
             F n[GD];
             M::facet_normal(k, refn + q * TD, n);
-            store_point(a.out[5], tile_idx, q, nq, GD, lane, a.tile_shift, n, GD);
+            cf.put(n);
           }
         }
       }
@@ -341,7 +675,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_
         if (mask & kOutNormals) {
           F n[GD];
           M::normal(j, sign, n);
-          store_point(a.out[4], tile_idx, q, nq, GD, lane, a.tile_shift, n, GD);
+          cn.put(n);
         }
       }
     }
@@ -349,178 +683,8 @@ __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_
 }
 
 // ----------------------------------------------------------------------------------------
-// The split-precision kernel: f64 mesh in, FP32 arithmetic, f32 fields out.
-//
-// Each cell's nodes are shifted by its node 0 in f64 (x_k - x_0, FP64 subtractions once per
-// cell), then rounded to f32: the shifted coordinates have the size of the cell, so their f32
-// rounding is relative to the cell, not to the distance from the origin. J = sum_{k>=1} (x_k - x_0)
-// dphi_k (the k = 0 term vanishes; sum_k dphi_k = 0), X = x_0 + sum_{k>=1} (x_k - x_0) phi_k with
-// x_0 carried as an f32 pair. det J and K follow in f32. A condition estimate
-// kappa = |J|_F |K|_F / TD flags near-degenerate points (kappa above `cond_limit`, or not
-// finite); for those J, det J and K are recomputed in FP64 from the f64 nodes and the f64
-// derivative table, then rounded to f32, and a device counter records how many points were
-// recomputed.
-
-struct SplitArgs {
-  const double* nodes;
-  const uint32_t* dofmap;
-  const uint32_t* flags;
-  const unsigned char* tab;  // phi32 | dphi32 | refn32 | dphi64
-  float* out[6];
-  int* err;
-  unsigned long long* recomputed;  // may be null
-  int64_t first_cell, padded, out_first_cell, last_cell, last_flag;
-  double origin[3];
-  float cond_limit;
-  uint32_t last_node, tab_bytes, off_dphi, off_refn, off_dphi64, mask;
-  int num_points, tile_shift;
-};
-
-template <int TD, int GD>
-__device__ __forceinline__ float frob(const float* m) {
-  float s = m[0] * m[0];
-#pragma unroll
-  for (int i = 1; i < TD * GD; ++i) s = fmaf(m[i], m[i], s);
-  return sqrtf(s);
-}
-
-template <int TD, int GD, int K>
-__global__ void __launch_bounds__(kEvalThreads) eval_split_kernel(const __grid_constant__ SplitArgs a) {
-  __shared__ uint64_t bar;
-  extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
-  const float* phi = reinterpret_cast<const float*>(smem);
-  const float* dphi = reinterpret_cast<const float*>(smem + a.off_dphi);
-  const float* refn = reinterpret_cast<const float*>(smem + a.off_refn);
-  const double* dphi64 = reinterpret_cast<const double*>(smem + a.off_dphi64);
-  const int nq = a.num_points;
-  const uint32_t mask = a.mask;
-  const bool want_j = (mask & ~kOutPoints) != 0;
-  constexpr int LJ = TD * GD;
-  const int tile_mask = (1 << a.tile_shift) - 1;
-  using M = Factors<float, TD, GD>;
-  using M64 = Factors<double, TD, GD>;
-
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t cell = min(a.first_cell + c, a.last_cell);
-    uint32_t idx[K];
-    load_row<K>(a.dofmap + cell * K, idx);
-#pragma unroll
-    for (int k = 0; k < K; ++k) idx[k] = min(idx[k], a.last_node);
-    double x0[GD];
-#pragma unroll
-    for (int g = 0; g < GD; ++g) x0[g] = __ldg(a.nodes + (int64_t)idx[0] * GD + g);
-    float y[K][GD];
-#pragma unroll
-    for (int k = 1; k < K; ++k)
-#pragma unroll
-      for (int g = 0; g < GD; ++g)
-        y[k][g] = __double2float_rn(__ldg(a.nodes + (int64_t)idx[k] * GD + g) - x0[g]);
-    // x_0 + origin as an f32 pair (hi + lo), for the physical points.
-    float xh[GD], xl[GD];
-    if (mask & kOutPoints) {
-#pragma unroll
-      for (int g = 0; g < GD; ++g) {
-        const double v = x0[g] + a.origin[g];
-        xh[g] = __double2float_rn(v);
-        xl[g] = __double2float_rn(v - (double)xh[g]);
-      }
-    }
-    float sign = 1.0f;
-    if ((mask & kOutNormals) && a.flags != nullptr && a.last_flag >= 0) {
-      const uint32_t f = __ldg(a.flags + min(a.first_cell + c, a.last_flag));
-      sign = (f & 1u) ? -1.0f : 1.0f;
-    }
-    const int64_t o = a.out_first_cell + c;
-    const int64_t tile_idx = o >> a.tile_shift;
-    const int lane = (int)(o & tile_mask);
-
-    for (int q = 0; q < nq; ++q) {
-      if (mask & kOutPoints) {
-        float s[GD];
-        const float* w = phi + q * K;
-#pragma unroll
-        for (int g = 0; g < GD; ++g) s[g] = y[1][g] * w[1];
-#pragma unroll
-        for (int k = 2; k < K; ++k) {
-          const float wk = w[k];
-#pragma unroll
-          for (int g = 0; g < GD; ++g) s[g] = fmaf(y[k][g], wk, s[g]);
-        }
-#pragma unroll
-        for (int g = 0; g < GD; ++g) s[g] = xh[g] + (xl[g] + s[g]);
-        store_point(a.out[0], tile_idx, q, nq, GD, lane, a.tile_shift, s, GD);
-      }
-      if (!want_j) continue;
-      float j[LJ];
-      const float* dq = dphi + q * K * TD;
-#pragma unroll
-      for (int d = 0; d < TD; ++d) {
-        const float w1 = dq[TD + d];
-#pragma unroll
-        for (int g = 0; g < GD; ++g) j[d * GD + g] = y[1][g] * w1;
-      }
-#pragma unroll
-      for (int k = 2; k < K; ++k) {
-#pragma unroll
-        for (int d = 0; d < TD; ++d) {
-          const float w = dq[k * TD + d];
-#pragma unroll
-          for (int g = 0; g < GD; ++g) j[d * GD + g] = fmaf(y[k][g], w, j[d * GD + g]);
-        }
-      }
-      float kk[LJ];
-      M::pinv(j, kk);
-      float dj = M::detj(j);
-      const float kappa = frob<TD, GD>(j) * frob<TD, GD>(kk) * (1.0f / TD);
-      if (!(kappa <= a.cond_limit)) {
-        // Near-degenerate point: J, det J and K again in FP64 from the f64 nodes.
-        double jd[LJ], kd[LJ];
-#pragma unroll
-        for (int i = 0; i < LJ; ++i) jd[i] = 0.0;
-        const double* d64 = dphi64 + q * K * TD;
-        for (int k = 1; k < K; ++k) {
-#pragma unroll
-          for (int g = 0; g < GD; ++g) {
-            const double yk = __ldg(a.nodes + (int64_t)idx[k] * GD + g) - x0[g];
-#pragma unroll
-            for (int d = 0; d < TD; ++d) jd[d * GD + g] = fma(yk, d64[k * TD + d], jd[d * GD + g]);
-          }
-        }
-        M64::pinv(jd, kd);
-        dj = (float)M64::detj(jd);
-#pragma unroll
-        for (int i = 0; i < LJ; ++i) {
-          j[i] = (float)jd[i];
-          kk[i] = (float)kd[i];
-        }
-        if (a.recomputed) atomicAdd(a.recomputed, 1ull);
-      }
-      if (mask & kOutJacobian) store_point(a.out[1], tile_idx, q, nq, LJ, lane, a.tile_shift, j, LJ);
-      if (mask & kOutDetJ) store_point(a.out[2], tile_idx, q, nq, 1, lane, a.tile_shift, &dj, 1);
-      if (mask & kOutPinv) store_point(a.out[3], tile_idx, q, nq, LJ, lane, a.tile_shift, kk, LJ);
-      if constexpr (TD == GD) {
-        if (mask & kOutFacetNormals) {
-          float n[GD];
-          M::facet_normal(kk, refn + q * TD, n);
-          store_point(a.out[5], tile_idx, q, nq, GD, lane, a.tile_shift, n, GD);
-        }
-      }
-      if constexpr (TD + 1 == GD) {
-        if (mask & kOutNormals) {
-          float n[GD];
-          M::normal(j, sign, n);
-          store_point(a.out[4], tile_idx, q, nq, GD, lane, a.tile_shift, n, GD);
-        }
-      }
-    }
-  }
-}
-
-// ----------------------------------------------------------------------------------------
-// The loops kernel: any K (run time), TD and GD at compile time; node coordinates re-read
-// through L1 at each point. Same values as the direct kernel.
+// The loops kernel: any K and tile (run time), TD and GD at compile time; node coordinates
+// re-read through L1 at each point. The same operations as the kernels above.
 
 template <typename F, int TD, int GD>
 __global__ void __launch_bounds__(kEvalThreads) eval_loops_kernel(const __grid_constant__ EvalArgs<F> a) {
@@ -536,6 +700,8 @@ __global__ void __launch_bounds__(kEvalThreads) eval_loops_kernel(const __grid_c
   const bool want_j = (mask & ~kOutPoints) != 0;
   constexpr int LJ = TD * GD;
   const int tile_mask = (1 << a.tile_shift) - 1;
+  using A = Ar<F>;
+  using M = Factors<F, TD, GD>;
 
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
        c += (int64_t)gridDim.x * blockDim.x) {
@@ -563,7 +729,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_loops_kernel(const __grid_c
         if (mask & kOutPoints) {
           const F w = phi[q * K + k];
 #pragma unroll
-          for (int g = 0; g < GD; ++g) xp[g] = k == 0 ? xk[g] * w : fma(xk[g], w, xp[g]);
+          for (int g = 0; g < GD; ++g) xp[g] = k == 0 ? A::mul(xk[g], w) : A::fma(xk[g], w, xp[g]);
         }
         if (want_j) {
 #pragma unroll
@@ -571,17 +737,16 @@ __global__ void __launch_bounds__(kEvalThreads) eval_loops_kernel(const __grid_c
             const F w = dphi[(q * K + k) * TD + d];
 #pragma unroll
             for (int g = 0; g < GD; ++g)
-              j[d * GD + g] = k == 0 ? xk[g] * w : fma(xk[g], w, j[d * GD + g]);
+              j[d * GD + g] = k == 0 ? A::mul(xk[g], w) : A::fma(xk[g], w, j[d * GD + g]);
           }
         }
       }
       if (mask & kOutPoints) {
 #pragma unroll
-        for (int g = 0; g < GD; ++g) xp[g] = xp[g] + a.origin[g];
+        for (int g = 0; g < GD; ++g) xp[g] = A::add(xp[g], a.origin[g]);
         store_point(a.out[0], tile_idx, q, nq, GD, lane, a.tile_shift, xp, GD);
       }
       if (!want_j) continue;
-      using M = Factors<F, TD, GD>;
       if (mask & kOutJacobian) store_point(a.out[1], tile_idx, q, nq, LJ, lane, a.tile_shift, j, LJ);
       if (mask & kOutDetJ) {
         const F dj = M::detj(j);

@@ -1,16 +1,19 @@
-// Instantiation list of the evaluation kernels for one scalar type (included by eval_f32.cu and
-// eval_f64.cu with TLG_F and TLG_LAUNCH defined). Unrolled kernels exist for the elements of the
-// benchmark meshes and the low degrees; every other (TD, GD, K) runs the loops kernel.
+// Instantiation list of the scalar evaluation kernels for one scalar type (included by
+// eval_f32.cu and eval_f64.cu with TLG_F and TLG_LAUNCH defined). Unrolled direct kernels exist
+// for f64 at the elements of the benchmark meshes and the low degrees (f32 at tile 16 runs the
+// paired kernel of eval_pair.cu); every other (TD, GD, K, tile) runs the loops kernel.
 #include "eval_launch.cuh"
 
 namespace tlg {
 
 cudaError_t TLG_LAUNCH(int td, int gd, int k, const EvalArgs<TLG_F>& a, size_t smem,
                        cudaStream_t s, bool* direct) {
-  *direct = true;
+#ifdef TLG_WITH_DIRECT
+  // Unrolled kernels are compiled for f64 and the GPU tile of 16 cells.
+  *direct = a.tile_shift == 4;
 #define TLG_DIRECT(TD, GD, K) \
-  if (td == TD && gd == GD && k == K) \
-    return launch_persistent(eval_direct_kernel<TLG_F, TD, GD, K>, a, a.padded, smem, s);
+  if (*direct && td == TD && gd == GD && k == K) \
+    return launch_persistent(eval_direct_kernel<TLG_F, TD, GD, K, 16>, a, a.padded, smem, s);
   // Tetrahedra P1-P3, hexahedra Q1-Q2, prisms P1-P2.
   TLG_DIRECT(3, 3, 4)
   TLG_DIRECT(3, 3, 10)
@@ -40,6 +43,7 @@ cudaError_t TLG_LAUNCH(int td, int gd, int k, const EvalArgs<TLG_F>& a, size_t s
   TLG_DIRECT(1, 2, 3)
   TLG_DIRECT(1, 3, 3)
 #undef TLG_DIRECT
+#endif
   *direct = false;
 #define TLG_LOOPS(TD, GD) \
   if (td == TD && gd == GD) return launch_persistent(eval_loops_kernel<TLG_F, TD, GD>, a, a.padded, smem, s);

@@ -44,8 +44,9 @@ cudaError_t launch_eval_f32(int td, int gd, int k, const EvalArgs<float>& a, siz
                             cudaStream_t s, bool* direct);
 cudaError_t launch_eval_f64(int td, int gd, int k, const EvalArgs<double>& a, size_t smem,
                             cudaStream_t s, bool* direct);
-// Defined in eval_split.cu; `found` is false when no split kernel exists for (td, gd, k).
-cudaError_t launch_eval_split(int td, int gd, int k, const SplitArgs& a, size_t smem, cudaStream_t s,
-                              bool* found);
+// Defined in eval_pair.cu: the paired-FP32 kernel for an f32 mesh (split = false) or split
+// precision (split = true), tile 16; `found` is false when none exists for (td, gd, k).
+cudaError_t launch_eval_pair(bool split, int td, int gd, int k, const PairArgs& a, size_t smem,
+                             cudaStream_t s, bool* found);
 
 }  // namespace tlg

@@ -46,7 +46,7 @@ def test_split_volume_errors_are_stated_per_output(cuda, cell, n, degree, rdeg):
 def test_split_is_more_accurate_than_plain_f32(cuda):
     """Shifting by the cell's first node in f64 before rounding keeps J's rounding relative to
     the cell size; plain f32 rounds coordinates relative to their distance from the origin."""
-    mesh = meshes.curved_box("Tetrahedron", 8, 2, jitter=0.02)
+    mesh = meshes.curved_box("Tetrahedron", 16, 2, jitter=0.02)
     pts, _ = tg.refcell.gauss_rule("Tetrahedron", 4)
     ps = tg.PointSet("Tetrahedron", pts, np.ones(len(pts)))
     g64 = tg.Geometry.from_host(mesh, dtype=torch.float64)
@@ -57,7 +57,7 @@ def test_split_is_more_accurate_than_plain_f32(cuda):
     for f in ("jacobian", "detj"):
         es = orc.rel_err(split[f].to_host_cell_major(), want[KEYS[f]])
         ep = orc.rel_err(plain[f].to_host_cell_major(), want[KEYS[f]])
-        assert es < ep / 4, (f, es, ep)
+        assert es < ep / 3, (f, es, ep)
 
 
 def test_near_degenerate_points_are_recomputed_in_f64(cuda):
@@ -72,12 +72,18 @@ def test_near_degenerate_points_are_recomputed_in_f64(cuda):
     ps = tg.PointSet("Tetrahedron", pts, np.ones(len(pts)))
     count = torch.zeros(1, dtype=torch.int64, device="cuda")
     got = tg.geometric_factors_block(g, 0, ps, ("detj", "pinv"), precision="split", recomputed=count)
-    want = oracle(mesh, g, "Tetrahedron", 1, pts, ("detj", "k"))
+    want = oracle(mesh, g, "Tetrahedron", 1, pts, ("detj", "j"))
     assert int(count.item()) == len(pts)  # every point of the sliver, none of the other cell
     d = got["detj"].to_host_cell_major()[..., 0]
     assert np.all(np.abs(d[0] - want["detj"][0, :, 0]) <= 2e-7 * np.abs(want["detj"][0, :, 0]))
+    # K by a pivoted LU inverse of the f64 J: the normal-equations route of the host reference
+    # (reference.rs:197-235) squares the condition number (1e12 here) and is not an oracle for K
+    # of a sliver.
+    jm = want["j"][0].reshape(-1, 3, 3)  # [q][d][g] = J(g, d)
+    kref = np.linalg.inv(np.transpose(jm, (0, 2, 1)))  # [q][t][g]
+    kref = np.transpose(kref, (0, 2, 1)).reshape(-1, 9)  # K(t, g) at g * 3 + t
     k = got["pinv"].to_host_cell_major()
-    assert orc.rel_err(k[0], want["k"][0]) < 1e-6
+    assert orc.rel_err(k[0], kref) < 1e-6
 
 
 @pytest.mark.parametrize("degree", [2, 4])
