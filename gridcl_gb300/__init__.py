@@ -22,9 +22,11 @@ from .geometry import (
     geometric_factors_block,
     jacobians_block,
     measure_block,
+    node_incidence,
     normals_block,
     physical_points_block,
     pseudo_inverse_block,
+    vjp_block,
 )
 from . import meshes, refcell
 
@@ -32,5 +34,5 @@ __all__ = [
     "CoordinateElement", "Geometry", "GeometryBlock", "GridError", "PointSet", "QuadField",
     "QuadRule", "detj_block", "facet_normals_block", "facet_point_set",
     "geometric_factors_block", "jacobians_block", "lib", "measure_block", "meshes", "normals_block",
-    "physical_points_block", "pseudo_inverse_block", "refcell",
+    "node_incidence", "physical_points_block", "pseudo_inverse_block", "refcell", "vjp_block",
 ]

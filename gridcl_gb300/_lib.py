@@ -70,6 +70,10 @@ class TlgOutputs(ctypes.Structure):
     ]
 
 
+class TlgCotangents(ctypes.Structure):
+    _fields_ = [("points", ctypes.c_void_p), ("detj", ctypes.c_void_p), ("pinv", ctypes.c_void_p)]
+
+
 # (name, restype, argtypes) of every entry point declared in include/tlgeom.h.
 _P = ctypes.c_void_p
 _I = ctypes.c_int
@@ -89,6 +93,11 @@ SIGNATURES = [
     ("tlg_tables_nodes_per_cell", _L, [_P]),
     ("tlg_eval_block", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs), _P]),
     ("tlg_evector", _I, [ctypes.POINTER(TlgBlock), _I, _L, _L, _L, _P, _P]),
+    ("tlg_csr_workspace_bytes", _L, [_L, _I]),
+    ("tlg_csr_build", _I, [_P, _L, _I, _L, _P, _L, _P, _P, _P]),
+    ("tlg_vjp_block", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs),
+                           ctypes.POINTER(TlgCotangents), _P, _L, _P]),
+    ("tlg_vjp_gather", _I, [_P, _P, _L, _I, _I, _P, _I, _L, _P, _P]),
     ("tlg_measure_cell_sums", _I, [_P, _I, _L, _L, _I, _P, _P, _P]),
     ("tlg_sum_workspace_bytes", _L, [_I, _L]),
     ("tlg_sum", _I, [_P, _I, _L, _P, _L, _P, _P]),

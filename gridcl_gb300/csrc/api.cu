@@ -13,6 +13,7 @@
 #include "eval_launch.cuh"
 #include "refcell.h"
 #include "status.h"
+#include "vjp.cuh"
 
 struct tlg_tables {
   int cell, degree, family, td, gd, dtype;
@@ -448,6 +449,72 @@ tlg_status tlg_evector(const tlg_block* b, int nodes_per_cell, int64_t first_cel
         b->num_cells - 1, last_node, nodes_per_cell, b->gdim, padded, stride);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "tlg_evector launch");
+  return ok();
+}
+
+tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o,
+                         const tlg_cotangents* ct, void* local, int64_t local_stride, void* stream) {
+  if (!t || !b || !o || !ct) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: NULL argument");
+  if (t->dtype != TLG_F64 && t->dtype != TLG_SPLIT32)
+    return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: the adjoint runs with f64 or split-precision tables");
+  if (b->dtype != TLG_F64) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: the adjoint reads f64 meshes");
+  if (t->td != t->gd || b->gdim != t->gd)
+    return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: the adjoint needs a block of codimension 0");
+  if (o->tile != 16) return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: the adjoint runs with tile 16");
+  if (o->normals || o->facet_normals)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: no normals in the fused forward");
+  if (o->first_cell < 0 || o->num_cells < 0 || o->first_cell + o->num_cells > b->num_cells ||
+      o->out_first_cell < 0 || o->out_first_cell % 16 != 0)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: bad cell range");
+  if (local_stride < b->num_cells) return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_vjp_block: local_stride below the block's cells");
+  if (o->num_cells == 0) return ok();
+  if (!b->nodes || !b->dofmap || !local) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: NULL nodes, dofmap or local");
+  if (b->num_nodes < 1) return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_vjp_block: cells but no nodes");
+  tlg::VjpArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = b->nodes;
+  a.dofmap = b->dofmap;
+  a.tab = t->dev;
+  a.ct[0] = ct->points;
+  a.ct[1] = ct->detj;
+  a.ct[2] = ct->pinv;
+  a.out[0] = o->points;
+  a.out[1] = o->jacobian;
+  a.out[2] = o->detj;
+  a.out[3] = o->pinv;
+  a.local = local;
+  a.err = t->err;
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + 15) / 16 * 16;
+  a.out_first_cell = o->out_first_cell;
+  a.last_cell = b->num_cells - 1;
+  a.range_end = o->first_cell + o->num_cells;
+  a.local_stride = local_stride;
+  for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
+  a.last_node = (uint32_t)(b->num_nodes - 1);
+  a.tab_bytes = t->bytes;
+  a.off_dphi = t->off_dphi;
+  a.num_points = (int)t->q;
+  if (t->q == 0) return ok();
+  bool found = false;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = t->dtype == TLG_SPLIT32 ? tlg::launch_vjp_split(t->td, (int)t->k, a, t->bytes, s, &found)
+                                          : tlg::launch_vjp_f64(t->td, (int)t->k, a, t->bytes, s, &found);
+  if (!found) return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: no adjoint kernel for this element");
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_block launch");
+  return ok();
+}
+
+tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int nodes_per_cell,
+                          int gdim, const void* local, int local_dtype, int64_t local_stride, double* grad,
+                          void* stream) {
+  if (!offsets || !grad || num_nodes < 0 || nodes_per_cell < 1 || gdim < 1 || gdim > 3 ||
+      (local_dtype != 4 && local_dtype != 8))
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_gather: bad arguments");
+  if (num_nodes == 0) return ok();
+  cudaError_t e = tlg::launch_vjp_gather(offsets, entries, num_nodes, nodes_per_cell, gdim, local, local_dtype,
+                                         local_stride, grad, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_gather launch");
   return ok();
 }
 

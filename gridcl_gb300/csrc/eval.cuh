@@ -188,16 +188,16 @@ struct Ar<float2> {
 template <typename V, int TD, int GD>
 struct Factors {
   using A = Ar<V>;
-  __device__ static V cross(V a, V b, V c, V d) { return A::fma(a, b, A::neg(A::mul(c, d))); }
+  __device__ __forceinline__ static V cross(V a, V b, V c, V d) { return A::fma(a, b, A::neg(A::mul(c, d))); }
 
-  __device__ static V column_dot(const V* j, int a, int b) {
+  __device__ __forceinline__ static V column_dot(const V* j, int a, int b) {
     V acc = A::mul(j[a * GD], j[b * GD]);
 #pragma unroll
     for (int g = 1; g < GD; ++g) acc = A::fma(j[a * GD + g], j[b * GD + g], acc);
     return acc;
   }
 
-  __device__ static V square_det(const V* j) {
+  __device__ __forceinline__ static V square_det(const V* j) {
     if constexpr (TD == 1) {
       return j[0];
     } else if constexpr (TD == 2) {
@@ -211,7 +211,7 @@ struct Factors {
     }
   }
 
-  __device__ static V detj(const V* j) {
+  __device__ __forceinline__ static V detj(const V* j) {
     if constexpr (TD == GD) {
       return square_det(j);
     } else if constexpr (TD == 1) {
@@ -223,7 +223,7 @@ struct Factors {
   }
 
   // K(t, g) at g * TD + t.
-  __device__ static void pinv(const V* j, V* k) {
+  __device__ __forceinline__ static void pinv(const V* j, V* k) {
     if constexpr (TD == GD) {
       const V inv = A::rcp(square_det(j));
       if constexpr (TD == 1) {
@@ -261,7 +261,7 @@ struct Factors {
   }
 
   // Codimension 1: s (J0_y, -J0_x) / |J0| or s (J0 x J1) / |J0 x J1|.
-  __device__ static void normal(const V* j, V s, V* n) {
+  __device__ __forceinline__ static void normal(const V* j, V s, V* n) {
     V v[GD];
     if constexpr (GD == 2) {
       v[0] = j[1];
@@ -280,7 +280,7 @@ struct Factors {
   }
 
   // Codimension 0: m = K^T n_ref, m / |m| (nref: the reference normal of each point).
-  __device__ static void facet_normal(const V* k, const V* nref, V* n) {
+  __device__ __forceinline__ static void facet_normal(const V* k, const V* nref, V* n) {
     V m[GD];
 #pragma unroll
     for (int g = 0; g < GD; ++g) {
@@ -298,7 +298,7 @@ struct Factors {
   }
 
   // |J|_F |K|_F / TD, the Frobenius condition estimate (tetraloma-testing/src/reference.rs:237).
-  __device__ static V condition(const V* j, const V* k) {
+  __device__ __forceinline__ static V condition(const V* j, const V* k) {
     V a = A::mul(j[0], j[0]), b = A::mul(k[0], k[0]);
 #pragma unroll
     for (int i = 1; i < TD * GD; ++i) {

@@ -49,4 +49,12 @@ cudaError_t launch_eval_f64(int td, int gd, int k, const EvalArgs<double>& a, si
 cudaError_t launch_eval_pair(bool split, int td, int gd, int k, const PairArgs& a, size_t smem,
                              cudaStream_t s, bool* found);
 
+struct VjpArgs;
+// Defined in vjp_f64.cu / vjp_split.cu; `found` is false when no kernel exists for (d, k).
+cudaError_t launch_vjp_f64(int d, int k, const VjpArgs& a, size_t smem, cudaStream_t s, bool* found);
+cudaError_t launch_vjp_split(int d, int k, const VjpArgs& a, size_t smem, cudaStream_t s, bool* found);
+cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int k,
+                              int d, const void* local, int local_dtype, int64_t local_stride,
+                              double* grad, cudaStream_t s);
+
 }  // namespace tlg

@@ -1,0 +1,30 @@
+// Split-precision instantiations of the adjoint kernel, and the f64 node gather.
+#define TLG_VJP_SPLIT true
+#define TLG_VJP_LAUNCH launch_vjp_split
+#include "vjp_inst.cuh"
+
+namespace tlg {
+
+cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int k,
+                              int d, const void* local, int local_dtype, int64_t local_stride,
+                              double* grad, cudaStream_t s) {
+  int64_t blocks = (num_nodes + 255) / 256;
+  if (blocks < 1) blocks = 1;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+#define TLG_GATHER(L, DD) \
+  vjp_gather_kernel<L, DD><<<(unsigned)blocks, 256, 0, s>>>(offsets, entries, num_nodes, k, \
+                                                            static_cast<const L*>(local), local_stride, grad)
+  if (local_dtype == 4) {
+    if (d == 1) TLG_GATHER(float, 1);
+    else if (d == 2) TLG_GATHER(float, 2);
+    else TLG_GATHER(float, 3);
+  } else {
+    if (d == 1) TLG_GATHER(double, 1);
+    else if (d == 2) TLG_GATHER(double, 2);
+    else TLG_GATHER(double, 3);
+  }
+#undef TLG_GATHER
+  return cudaGetLastError();
+}
+
+}  // namespace tlg

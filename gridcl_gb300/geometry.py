@@ -431,3 +431,90 @@ def measure_block(g: Geometry, b: int, pts: PointSet, detj: QuadField | None = N
     check(lib().tlg_sum(sums.data_ptr(), es, blk.num_cells, work.data_ptr(), nbytes,
                         result.data_ptr(), stream))
     return float(result.item())
+
+
+@dataclasses.dataclass
+class NodeIncidence:
+    """Node-to-(cell, local node) CSR of one block: node n's dofmap entries e = cell * K + k
+    are ``entries[offsets[n]:offsets[n + 1]]`` in ascending e (u32 bit patterns in int32)."""
+
+    offsets: torch.Tensor
+    entries: torch.Tensor
+
+
+def node_incidence(g: Geometry, b: int) -> NodeIncidence:
+    """The block's CSR, built on the device by a stable radix sort and cached on the grid."""
+    cache = g.__dict__.setdefault("_incidence", {})
+    if b in cache:
+        return cache[b]
+    blk = g.blocks[b]
+    k = blk.element.nodes_per_cell
+    nn = g.nodes.shape[0]
+    dev = g.nodes.device
+    offsets = torch.empty(nn + 1, dtype=torch.int32, device=dev)
+    entries = torch.empty(max(blk.num_cells * k, 1), dtype=torch.int32, device=dev)
+    nbytes = int(lib().tlg_csr_workspace_bytes(blk.num_cells, k))
+    work = torch.empty(max(nbytes, 16), dtype=torch.uint8, device=dev)
+    check(lib().tlg_csr_build(blk.dofmap.data_ptr(), blk.num_cells, k, nn, work.data_ptr(), nbytes,
+                              offsets.data_ptr(), entries.data_ptr(), current_stream_handle()))
+    inc = NodeIncidence(offsets, entries)
+    cache[b] = inc
+    return inc
+
+
+def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: str = "native",
+              forward=(), out: dict | None = None, local: torch.Tensor | None = None):
+    """Cotangents of the node coordinates (``[node][GD]`` f64) for the cotangent fields
+    ``{"points", "detj", "pinv"}`` (QuadFields of tile 16, f64, or f32 with
+    ``precision="split"``; missing entries are zero) of block b, codimension 0. J, det J and K
+    are recomputed. The factors named in `forward` are evaluated in the same pass (fused
+    forward + adjoint) and returned: ``(grad, fields)``."""
+    from ._lib import TlgCotangents
+
+    blk = g.blocks[b]
+    td, gd = blk.element.tdim, g.gdim
+    if td != gd:
+        raise GridError(4, "the adjoint needs a block of codimension 0")
+    if g.dtype != torch.float64:
+        raise GridError(1, "the adjoint reads f64 meshes")
+    if precision == "split":
+        tables = pts.tables(blk.element, gd, SPLIT32)
+        fdt = torch.float32
+    elif precision == "native":
+        tables = pts.tables(blk.element, gd, g.dtype)
+        fdt = torch.float64
+    else:
+        raise GridError(1, f"unknown precision {precision!r}")
+    for name in forward:
+        if name not in ("points", "jacobian", "detj", "pinv"):
+            raise GridError(1, f"no fused forward factor {name}")
+    k = blk.element.nodes_per_cell
+    nq = len(pts)
+    dev = g.nodes.device
+    fields = out if out is not None else {
+        f: QuadField.uninit(blk.num_cells, nq, FACTOR_LEN[f](td, gd), GPU_QUAD_TILE, fdt, dev)
+        for f in forward}
+    if local is None:
+        local = torch.empty((k, gd, max(blk.num_cells, 1)), dtype=fdt, device=dev)
+    stride = local.shape[2]
+    ct = TlgCotangents()
+    for name in ("points", "detj", "pinv"):
+        f = cotangents.get(name)
+        if f is not None:
+            if f.tile != GPU_QUAD_TILE or len(f.chunks) != 1 or f.chunks[0].data.dtype != fdt:
+                raise GridError(1, f"cotangent {name}: one chunk of tile 16 and dtype {fdt} expected")
+            setattr(ct, name, f.chunks[0].data.data_ptr())
+    o = TlgOutputs()
+    o.first_cell, o.num_cells, o.out_first_cell, o.tile = 0, blk.num_cells, 0, GPU_QUAD_TILE
+    for name, f in fields.items():
+        setattr(o, name, f.chunks[0].data.data_ptr())
+    desc = g.block_desc(b)
+    stream = current_stream_handle()
+    check(lib().tlg_vjp_block(tables.handle, ctypes.byref(desc), ctypes.byref(o), ctypes.byref(ct),
+                              local.data_ptr(), stride, stream))
+    inc = node_incidence(g, b)
+    grad = torch.empty((g.nodes.shape[0], gd), dtype=torch.float64, device=dev)
+    check(lib().tlg_vjp_gather(inc.offsets.data_ptr(), inc.entries.data_ptr(), g.nodes.shape[0], k, gd,
+                               local.data_ptr(), 4 if fdt == torch.float32 else 8, stride,
+                               grad.data_ptr(), stream))
+    return grad, fields

@@ -169,6 +169,47 @@ tlg_status tlg_evector(const tlg_block* block, int nodes_per_cell, int64_t first
                        int64_t chunk_cells, int64_t stride, void* out, void* stream);
 
 /* ---------------------------------------------------------------------------------------
+ * Adjoint: cotangents of the geometric factors mapped back to the node coordinates, for shape
+ * optimisation (no counterpart kernel in the reference, which has no adjoint; the sums follow
+ * its node-to-cell incidence recipe, tetraloma-topology/src/connectivity.rs:1-3).
+ * ------------------------------------------------------------------------------------- */
+
+/* Bytes of workspace tlg_csr_build needs for num_cells cells of nodes_per_cell nodes. */
+int64_t tlg_csr_workspace_bytes(int64_t num_cells, int nodes_per_cell);
+
+/* The node-to-(cell, local node) incidence of a dofmap as CSR, by a stable device radix sort:
+ * node n's entries e = cell * K + k are entries[offsets[n] .. offsets[n + 1]) in ascending e
+ * (offsets has num_nodes + 1 values). Indices past the last node count for the last node, as
+ * in the gather. Deterministic. Device pointers; the workspace is caller-provided. */
+tlg_status tlg_csr_build(const uint32_t* dofmap, int64_t num_cells, int nodes_per_cell, int64_t num_nodes,
+                         void* workspace, int64_t workspace_bytes, uint32_t* offsets, uint32_t* entries,
+                         void* stream);
+
+/* Cotangent fields (QuadField chunks of the evaluated range, tile 16); NULL means zero. */
+typedef struct tlg_cotangents {
+  const void* points; /* dL/dx, GD components */
+  const void* detj;   /* dL/d(det J) */
+  const void* pinv;   /* dL/dK, TD * GD components, K(t, g) at g * TD + t */
+} tlg_cotangents;
+
+/* Per-cell contributions to the node cotangents of a codimension-0 block range (TD = GD),
+ * J, det J and K recomputed: local[(k * GD + g) * local_stride + cell] = sum_q phi_k(q) xbar(q, g)
+ * + sum_d Jbar(q)(g, d) dphi_k(q)[d], Jbar = dbar det J K^T - K^T Kbar K^T. With TLG_F64 tables
+ * everything is f64; with TLG_SPLIT32 tables the mesh is f64, the arithmetic FP32 on cell-shifted
+ * coordinates, and cotangents, contributions and any forward fields are f32. Forward pointers set
+ * in `outputs` (points, jacobian, detj, pinv) are written in the same pass (fused forward +
+ * adjoint); outputs->tile must be 16. */
+tlg_status tlg_vjp_block(const tlg_tables* tables, const tlg_block* block, const tlg_outputs* outputs,
+                         const tlg_cotangents* cotangents, void* local, int64_t local_stride,
+                         void* stream);
+
+/* grad[n * gdim + g] = sum over node n's CSR entries, in entry order, of the contributions, in
+ * f64 (local_dtype 4 or 8 is the contributions' type). Deterministic. */
+tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes,
+                          int nodes_per_cell, int gdim, const void* local, int local_dtype,
+                          int64_t local_stride, double* grad, void* stream);
+
+/* ---------------------------------------------------------------------------------------
  * Measure (tetraloma-geometry/src/measure.rs:15-185): per-cell sums of det J * w over the
  * points of a det J QuadField chunk, then a sum tree of 64-value blocks, all in F and in a
  * fixed order. The caller reads the F result (the reference finishes it in f64 on the host).

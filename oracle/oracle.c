@@ -213,6 +213,84 @@ double orc_measure(const double* detj, const double* weights, int64_t ncells, in
   return total;
 }
 
+/*
+ * Adjoint restated in f64 (no reference counterpart: the reference has no adjoint): for
+ * codimension 0 (td == gd), the node cotangents of L = sum_c sum_q [xbar . x + dbar det J +
+ * Kbar : K], accumulated cell by cell into grad [node][gd] (sequential, deterministic). K by the
+ * adjugate of J over det J. xbar [cell][q][gd], dbar [cell][q], kbar [cell][q][td * gd] (K(t, g)
+ * at g * td + t) may be NULL.
+ */
+int orc_vjp(int d, int k, int nq, int64_t ncells, const double* nodes, int64_t nnodes,
+            const uint32_t* dofmap, const double* tab, const double* xbar, const double* dbar,
+            const double* kbar, double* grad) {
+  if (d < 1 || d > 3 || k < 1 || k > 64 || nq < 0 || ncells < 0 || nnodes < 1) return ORC_BAD_ARGS;
+  for (int64_t i = 0; i < nnodes * d; ++i) grad[i] = 0.0;
+  double xc[64 * 3], gl[64 * 3];
+  for (int64_t c = 0; c < ncells; ++c) {
+    uint32_t idx[64];
+    for (int i = 0; i < k; ++i) {
+      uint32_t n = dofmap[c * k + i];
+      if ((int64_t)n >= nnodes) n = (uint32_t)(nnodes - 1);
+      idx[i] = n;
+      for (int g = 0; g < d; ++g) xc[i * d + g] = nodes[(int64_t)n * d + g];
+    }
+    for (int i = 0; i < k * d; ++i) gl[i] = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      const int64_t cq = c * nq + q;
+      double j[9], kk[9], det;
+      for (int dd = 0; dd < d; ++dd)
+        for (int g = 0; g < d; ++g) {
+          double s = 0.0;
+          for (int i = 0; i < k; ++i) s += xc[i * d + g] * tab[((int64_t)(1 + dd) * nq + q) * k + i];
+          j[dd * d + g] = s;
+        }
+      /* M(g, dd) = J(g, dd) = j[dd * d + g]; inverse by adjugate. */
+      if (d == 1) {
+        det = j[0];
+        kk[0] = 1.0 / det;
+      } else if (d == 2) {
+        det = j[0] * j[3] - j[2] * j[1];
+        kk[0] = j[3] / det;
+        kk[1] = -j[1] / det;
+        kk[2] = -j[2] / det;
+        kk[3] = j[0] / det;
+      } else {
+        det = detj_of(j, 3, 3);
+#define J_(g, dd) j[(dd) * 3 + (g)]
+        /* K(t, g) = cof(J)(g, t) / det, stored at g * 3 + t */
+        for (int g = 0; g < 3; ++g)
+          for (int t = 0; t < 3; ++t) {
+            const int r0 = (g + 1) % 3, r1 = (g + 2) % 3, c0 = (t + 1) % 3, c1 = (t + 2) % 3;
+            const double cof = J_(r0, c0) * J_(r1, c1) - J_(r0, c1) * J_(r1, c0);
+            kk[g * 3 + t] = cof / det;
+          }
+#undef J_
+      }
+      double jb[9];
+      for (int i = 0; i < d * d; ++i) jb[i] = 0.0;
+      /* Jbar(g, dd) = dbar det K(dd, g) - sum_{t,h} K(t, g) Kbar(t, h) K(dd, h) */
+      for (int g = 0; g < d; ++g)
+        for (int dd = 0; dd < d; ++dd) {
+          double v = dbar ? dbar[cq] * det * kk[g * d + dd] : 0.0;
+          if (kbar)
+            for (int t = 0; t < d; ++t)
+              for (int h = 0; h < d; ++h)
+                v -= kk[g * d + t] * kbar[cq * d * d + h * d + t] * kk[h * d + dd];
+          jb[dd * d + g] = v;
+        }
+      for (int i = 0; i < k; ++i)
+        for (int g = 0; g < d; ++g) {
+          double v = xbar ? tab[(int64_t)q * k + i] * xbar[cq * d + g] : 0.0;
+          for (int dd = 0; dd < d; ++dd) v += jb[dd * d + g] * tab[((int64_t)(1 + dd) * nq + q) * k + i];
+          gl[i * d + g] += v;
+        }
+    }
+    for (int i = 0; i < k; ++i)
+      for (int g = 0; g < d; ++g) grad[(int64_t)idx[i] * d + g] += gl[i * d + g];
+  }
+  return ORC_OK;
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -57,6 +57,9 @@ def load():
         lib.orc_measure.argtypes = [p, p, ctypes.c_int64, ctypes.c_int]
         lib.orc_measure.restype = ctypes.c_double
         lib.orc_max_threads.restype = ctypes.c_int
+        lib.orc_vjp.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64, p,
+                                ctypes.c_int64, p, p, p, p, p, p]
+        lib.orc_vjp.restype = ctypes.c_int
         _lib = lib
     return _lib
 
@@ -105,6 +108,28 @@ def eval_block(cell: str, degree: int, nodes_abs: np.ndarray, dofmap: np.ndarray
     if rc != 0:
         raise ValueError(f"orc_eval rejected its arguments ({rc})")
     return out
+
+
+def vjp(cell: str, degree: int, nodes_abs: np.ndarray, dofmap: np.ndarray, points: np.ndarray,
+        xbar=None, dbar=None, kbar=None, family: str = "Equispaced", tab=None) -> np.ndarray:
+    """Node cotangents ``[node][gdim]`` (f64) of sum(xbar . x + dbar det J + kbar : K) over a
+    codimension-0 block; cotangents cell-major ``[cell][q][...]`` or None."""
+    td = refcell.tdim(cell)
+    nodes_abs = np.ascontiguousarray(nodes_abs, dtype=np.float64)
+    dofmap = np.ascontiguousarray(dofmap, dtype=np.uint32)
+    ncells, k = dofmap.shape
+    points = np.asarray(points, dtype=np.float64).reshape(-1, td)
+    if tab is None:
+        tab = refcell.tabulate(cell, degree, points, 1, family)
+    tab = np.ascontiguousarray(tab, dtype=np.float64)
+    conv = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+    xbar, dbar, kbar = conv(xbar), conv(dbar), conv(kbar)
+    grad = np.zeros_like(nodes_abs)
+    rc = load().orc_vjp(td, k, points.shape[0], ncells, _ptr(nodes_abs), nodes_abs.shape[0],
+                        _ptr(dofmap), _ptr(tab), _ptr(xbar), _ptr(dbar), _ptr(kbar), _ptr(grad))
+    if rc != 0:
+        raise ValueError(f"orc_vjp rejected its arguments ({rc})")
+    return grad
 
 
 def evector(nodes_stored: np.ndarray, dofmap: np.ndarray, num_cells: int, k: int, gd: int,

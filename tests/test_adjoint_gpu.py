@@ -1,0 +1,124 @@
+"""Adjoint (node cotangents through the device CSR) against the f64 oracle and central finite
+differences; the CSR against a stable host sort (GPU)."""
+
+import numpy as np
+import pytest
+import torch
+
+import gridcl_gb300 as tg
+from gridcl_gb300 import meshes
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def stable_csr(dofmap, num_nodes):
+    keys = np.minimum(dofmap.ravel().astype(np.int64), num_nodes - 1)
+    order = np.argsort(keys, kind="stable")
+    counts = np.bincount(keys, minlength=num_nodes)
+    offsets = np.concatenate([[0], np.cumsum(counts)])
+    return offsets, order
+
+
+@pytest.mark.parametrize("cell,n,p", [("Tetrahedron", 3, 2), ("Hexahedron", 24, 2), ("Prism", 2, 1)])
+def test_csr_is_the_stable_sort(cuda, cell, n, p):
+    mesh = meshes.cube_box(cell, n, p)
+    g = tg.Geometry.from_host(mesh)
+    inc = tg.node_incidence(g, 0)
+    offsets, entries = stable_csr(mesh.blocks[0].cells, mesh.num_nodes)
+    assert np.array_equal(inc.offsets.cpu().numpy().view(np.uint32), offsets)
+    assert np.array_equal(inc.entries.cpu().numpy().view(np.uint32)[: entries.size], entries)
+
+
+def test_csr_with_unused_and_clamped_nodes(cuda):
+    nodes = np.random.default_rng(1).random((40, 3))
+    cells = np.array([[3, 5, 7, 9], [9, 3, 12, 77], [1, 2, 3, 4], [30, 31, 32, 39]], dtype=np.uint32)
+    mesh = meshes.HostMesh(3, nodes, [meshes.HostBlock("Tetrahedron", 1, cells)])
+    g = tg.Geometry.from_host(mesh)
+    inc = tg.node_incidence(g, 0)
+    offsets, entries = stable_csr(cells, 40)
+    assert np.array_equal(inc.offsets.cpu().numpy().view(np.uint32), offsets)
+    assert np.array_equal(inc.entries.cpu().numpy().view(np.uint32), entries)
+
+
+def cotangent_fields(rng, ncells, nq, dtype):
+    """Seeded standard-normal cotangents as tile-16 fields, with their cell-major copies."""
+    out, host = {}, {}
+    for name, length in (("points", 3), ("detj", 1), ("pinv", 9)):
+        f = tg.QuadField.uninit(ncells, nq, length, 16, dtype)
+        vals = rng.standard_normal(f.chunks[0].data.numel())
+        f.chunks[0].data.copy_(torch.from_numpy(vals).to(dtype))
+        out[name] = f
+        host[name] = f.to_host_cell_major().astype(np.float64)
+    return out, host
+
+
+@pytest.mark.parametrize("cell,n,degree,rdeg", [("Tetrahedron", 3, 2, 4), ("Hexahedron", 3, 2, 4),
+                                                ("Tetrahedron", 2, 3, 6), ("Prism", 2, 2, 4)])
+def test_vjp_matches_the_oracle(cuda, cell, n, degree, rdeg):
+    mesh = meshes.curved_box(cell, n, degree, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    ncells = mesh.blocks[0].num_cells
+    rng = np.random.default_rng(7)
+    ct64, host = cotangent_fields(rng, ncells, len(pts), torch.float64)
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
+    want = orc.vjp(cell, degree, absx, mesh.blocks[0].cells, pts, host["points"],
+                   host["detj"][..., 0], host["pinv"])
+    got, _ = tg.vjp_block(g, 0, ps, ct64)
+    assert orc.rel_err(got.cpu().numpy(), want) < 1e-11
+    again, _ = tg.vjp_block(g, 0, ps, ct64)
+    assert torch.equal(got, again)  # deterministic
+    # Split precision: f32 cotangents (the same values rounded), FP32 arithmetic.
+    ct32 = {k: tg.QuadField([tg.geometry.QuadChunk(0, ncells, v.chunks[0].data.float())], ncells,
+                            len(pts), v.length, 16) for k, v in ct64.items()}
+    host32 = {k: v.to_host_cell_major().astype(np.float64) for k, v in ct32.items()}
+    want32 = orc.vjp(cell, degree, absx, mesh.blocks[0].cells, pts, host32["points"],
+                     host32["detj"][..., 0], host32["pinv"])
+    got32, _ = tg.vjp_block(g, 0, ps, ct32, precision="split")
+    assert orc.rel_err(got32.cpu().numpy(), want32) < 2e-5
+
+
+@pytest.mark.parametrize("precision", ["native", "split"])
+def test_fused_forward_equals_the_forward_kernels(cuda, precision):
+    mesh = meshes.curved_box("Hexahedron", 3, 2, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, _ = tg.refcell.gauss_rule("Hexahedron", 4)
+    ps = tg.PointSet("Hexahedron", pts, np.ones(len(pts)))
+    dt = torch.float64 if precision == "native" else torch.float32
+    ct, _ = cotangent_fields(np.random.default_rng(3), mesh.blocks[0].num_cells, len(pts), dt)
+    names = ("points", "jacobian", "detj", "pinv")
+    _, fused = tg.vjp_block(g, 0, ps, ct, precision=precision, forward=names)
+    plain = tg.geometric_factors_block(g, 0, ps, names, precision=precision)
+    for k in names:
+        assert torch.equal(fused[k].chunks[0].data, plain[k].chunks[0].data), k
+
+
+def test_vjp_against_central_differences(cuda):
+    """Central differences (step 1e-6) of L = sum(xbar . x + dbar det J + kbar : K), evaluated by
+    the f64 forward kernels, at 12 seeded node coordinates."""
+    mesh = meshes.curved_box("Tetrahedron", 2, 2, jitter=0.02)
+    pts, _ = tg.refcell.gauss_rule("Tetrahedron", 4)
+    ps = tg.PointSet("Tetrahedron", pts, np.ones(len(pts)))
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    ct, host = cotangent_fields(np.random.default_rng(11), mesh.blocks[0].num_cells, len(pts),
+                                torch.float64)
+    grad, _ = tg.vjp_block(g, 0, ps, ct)
+    grad = grad.cpu().numpy()
+
+    def functional(nodes_rel):
+        gg = tg.Geometry(g.blocks, torch.from_numpy(nodes_rel).cuda(), g.origin)
+        f = tg.geometric_factors_block(gg, 0, ps, ("points", "detj", "pinv"))
+        return sum(float((f[k].to_host_cell_major() * host[k]).sum()) for k in ("points", "detj", "pinv"))
+
+    base = g.nodes.cpu().numpy()
+    rng = np.random.default_rng(5)
+    h = 1e-6
+    for n in rng.choice(mesh.num_nodes, 4, replace=False):
+        for c in range(3):
+            xp, xm = base.copy(), base.copy()
+            xp[n, c] += h
+            xm[n, c] -= h
+            fd = (functional(xp) - functional(xm)) / (2 * h)
+            assert abs(fd - grad[n, c]) <= 1e-6 * max(1.0, abs(grad[n, c])), (n, c, fd, grad[n, c])
