@@ -10,6 +10,7 @@ tetraloma-geometry's API.
 
 from ._lib import GridError, lib
 from .geometry import (
+    Batch,
     CoordinateElement,
     Geometry,
     GeometryBlock,
@@ -31,7 +32,7 @@ from .geometry import (
 from . import meshes, refcell
 
 __all__ = [
-    "CoordinateElement", "Geometry", "GeometryBlock", "GridError", "PointSet", "QuadField",
+    "Batch", "CoordinateElement", "Geometry", "GeometryBlock", "GridError", "PointSet", "QuadField",
     "QuadRule", "detj_block", "facet_normals_block", "facet_point_set",
     "geometric_factors_block", "jacobians_block", "lib", "measure_block", "meshes", "normals_block",
     "node_incidence", "physical_points_block", "pseudo_inverse_block", "refcell", "vjp_block",

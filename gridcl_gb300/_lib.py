@@ -92,6 +92,10 @@ SIGNATURES = [
     ("tlg_tables_device_status", _I, [_P, _P]),
     ("tlg_tables_nodes_per_cell", _L, [_P]),
     ("tlg_eval_block", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs), _P]),
+    ("tlg_batch_create", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs), _I, _P]),
+    ("tlg_batch_destroy", _I, [_P]),
+    ("tlg_batch_tune", _I, [_P, _P, _P]),
+    ("tlg_batch_launch", _I, [_P, _P]),
     ("tlg_evector", _I, [ctypes.POINTER(TlgBlock), _I, _L, _L, _L, _P, _P]),
     ("tlg_csr_workspace_bytes", _L, [_L, _I]),
     ("tlg_csr_build", _I, [_P, _L, _I, _L, _P, _L, _P, _P, _P]),

@@ -1,8 +1,11 @@
 // The C ABI of include/tlgeom.h: argument checks with the reference's error kinds, device
 // tables, and the launches of the evaluation and E-vector kernels.
 #include <cmath>
+#include <cstdio>
 #include <cstdint>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -14,6 +17,17 @@
 #include "refcell.h"
 #include "status.h"
 #include "vjp.cuh"
+
+struct tlg_batch {
+  std::vector<const tlg_tables*> tables;
+  std::vector<tlg_block> blocks;
+  std::vector<tlg_outputs> outputs;
+  std::vector<int> grid;  // launch grid per block (0: the kernel's persistent default)
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> events;  // fork, then one join per block
+  cudaStream_t capture = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
 
 struct tlg_tables {
   int cell, degree, family, td, gd, dtype;
@@ -515,6 +529,173 @@ tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int6
   cudaError_t e = tlg::launch_vjp_gather(offsets, entries, num_nodes, nodes_per_cell, gdim, local, local_dtype,
                                          local_stride, grad, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_gather launch");
+  return ok();
+}
+
+// ---------------------------------------------------------------------------------------
+// Batches: every block of a hybrid mesh in one CUDA graph launch, launch shapes autotuned.
+
+namespace {
+
+std::mutex g_tune_mutex;
+std::map<std::string, int> g_tune_cache;  // launch-shape key -> grid multiplier
+
+std::string tune_key(const tlg_tables* t, const tlg_outputs* o, int64_t cells) {
+  int bucket = 0;
+  while ((int64_t(1) << bucket) < cells) ++bucket;
+  char buf[160];
+  std::snprintf(buf, sizeof(buf), "d%d t%d g%d k%lld q%lld c%d o%d%d%d%d%d%d", t->dtype, t->td, t->gd,
+                (long long)t->k, (long long)t->q, bucket, o->points != nullptr, o->jacobian != nullptr,
+                o->detj != nullptr, o->pinv != nullptr, o->normals != nullptr, o->facet_normals != nullptr);
+  return buf;
+}
+
+void destroy_graph(tlg_batch* b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+}
+
+tlg_status eval_with_grid(tlg_batch* b, size_t i, cudaStream_t s, int grid) {
+  tlg::g_grid_override = grid;
+  tlg_status st = tlg_eval_block(b->tables[i], &b->blocks[i], &b->outputs[i], s);
+  tlg::g_grid_override = 0;
+  return st;
+}
+
+}  // namespace
+
+tlg_status tlg_batch_create(const tlg_tables* const* tables, const tlg_block* blocks, const tlg_outputs* outputs,
+                            int num_blocks, tlg_batch** out) {
+  if (!out || num_blocks < 0 || (num_blocks > 0 && (!tables || !blocks || !outputs)))
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_batch_create: NULL argument");
+  *out = nullptr;
+  auto b = new tlg_batch();
+  for (int i = 0; i < num_blocks; ++i) {
+    if (!tables[i]) {
+      delete b;
+      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_batch_create: NULL tables");
+    }
+    b->tables.push_back(tables[i]);
+    b->blocks.push_back(blocks[i]);
+    b->outputs.push_back(outputs[i]);
+    b->grid.push_back(0);
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
+  for (int i = 0; i < num_blocks && e == cudaSuccess; ++i) {
+    cudaStream_t s;
+    e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e == cudaSuccess) b->streams.push_back(s);
+  }
+  for (int i = 0; i < num_blocks + 1 && e == cudaSuccess; ++i) {
+    cudaEvent_t ev;
+    e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) b->events.push_back(ev);
+  }
+  if (e != cudaSuccess) {
+    tlg_batch_destroy(b);
+    return cuda_fail(e, "tlg_batch_create");
+  }
+  *out = b;
+  return ok();
+}
+
+tlg_status tlg_batch_destroy(tlg_batch* b) {
+  if (!b) return ok();
+  destroy_graph(b);
+  for (auto s : b->streams) cudaStreamDestroy(s);
+  for (auto ev : b->events) cudaEventDestroy(ev);
+  if (b->capture) cudaStreamDestroy(b->capture);
+  delete b;
+  return ok();
+}
+
+tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
+  if (!b) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_batch_tune: NULL batch");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int dev = 0, sms = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  for (size_t i = 0; i < b->tables.size(); ++i) {
+    const std::string key = tune_key(b->tables[i], &b->outputs[i], b->outputs[i].num_cells);
+    int mult = -1;
+    {
+      std::lock_guard<std::mutex> lock(g_tune_mutex);
+      auto it = g_tune_cache.find(key);
+      if (it != g_tune_cache.end()) mult = it->second;
+    }
+    if (mult < 0) {
+      // Candidates: CTAs per SM of the persistent grid (0: the occupancy limit); 3 timed runs each.
+      const int cands[] = {0, 1, 2, 3, 4, 6, 8};
+      float best = 1e30f;
+      mult = 0;
+      for (int c : cands) {
+        const int grid = c == 0 ? 0 : c * sms;
+        tlg_status st = eval_with_grid(b, i, s, grid);
+        if (st != TLG_OK) {
+          cudaEventDestroy(t0);
+          cudaEventDestroy(t1);
+          return st;
+        }
+        cudaEventRecord(t0, s);
+        for (int r = 0; r < 3; ++r) eval_with_grid(b, i, s, grid);
+        cudaEventRecord(t1, s);
+        cudaEventSynchronize(t1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, t0, t1);
+        if (ms < best) {
+          best = ms;
+          mult = c;
+        }
+      }
+      std::lock_guard<std::mutex> lock(g_tune_mutex);
+      g_tune_cache[key] = mult;
+    }
+    b->grid[i] = mult == 0 ? 0 : mult * sms;
+    if (grids) grids[i] = b->grid[i];
+  }
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  destroy_graph(b);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_batch_tune");
+  return ok();
+}
+
+tlg_status tlg_batch_launch(tlg_batch* b, void* stream) {
+  if (!b) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_batch_launch: NULL batch");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!b->exec) {
+    // Capture every block's launch as a parallel branch of one graph: fork from the capture
+    // stream, one stream per block, join back.
+    cudaError_t e = cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e, "tlg_batch_launch: begin capture");
+    tlg_status st = TLG_OK;
+    cudaEventRecord(b->events[0], b->capture);
+    for (size_t i = 0; i < b->tables.size() && st == TLG_OK; ++i) {
+      cudaStreamWaitEvent(b->streams[i], b->events[0], 0);
+      st = eval_with_grid(b, i, b->streams[i], b->grid[i]);
+      cudaEventRecord(b->events[i + 1], b->streams[i]);
+      cudaStreamWaitEvent(b->capture, b->events[i + 1], 0);
+    }
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(b->capture, &graph);
+    if (st != TLG_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return st;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "tlg_batch_launch: end capture");
+    e = cudaGraphInstantiate(&b->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      b->exec = nullptr;
+      return cuda_fail(e, "tlg_batch_launch: instantiate");
+    }
+  }
+  cudaError_t e = cudaGraphLaunch(b->exec, s);
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_batch_launch");
   return ok();
 }
 

@@ -67,6 +67,7 @@ struct EvalArgs {
   int num_points;            // Q
   int tile_shift;            // log2(tile)
   int k_runtime;             // K for the loops kernel
+  uint32_t tab_base;         // offset of these tables in a batch's staged tables (0 alone)
 };
 
 // Arguments of the paired kernels (f32 arithmetic; nodes f32, or f64 with SPLIT).
@@ -83,6 +84,7 @@ struct PairArgs {
   float cond_limit;
   uint32_t last_node, tab_bytes, off_refn, off_phi2, off_dphi2, off_dphi64, mask;
   int num_points;
+  uint32_t tab_base;  // offset of these tables in a batch's staged tables (0 alone)
 };
 
 // ----------------------------------------------------------------------------------------
@@ -408,27 +410,25 @@ __device__ __noinline__ void recompute_f64(const double* __restrict__ nodes, con
 // ----------------------------------------------------------------------------------------
 // The paired f32 kernel (tile 16).
 
+// Cells c0, c0 + step, ... below c_end of one block range, tables at `tabs` (shared memory).
 template <bool SPLIT, int TD, int GD, int K>
-__global__ void __launch_bounds__(kEvalThreads) eval_pair_kernel(const __grid_constant__ PairArgs a) {
+__device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned char* tabs, int64_t c0,
+                                           int64_t c_end, int64_t step) {
   constexpr int TILE = 16;
   constexpr int LJ = TD * GD;
   using A = Ar<float2>;
   using M = Factors<float2, TD, GD>;
-  __shared__ uint64_t bar;
-  extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
-  const float2* phi2 = reinterpret_cast<const float2*>(smem + a.off_phi2);
-  const float2* dphi2 = reinterpret_cast<const float2*>(smem + a.off_dphi2);
-  const float* refn = reinterpret_cast<const float*>(smem + a.off_refn);
-  const double* dphi64 = reinterpret_cast<const double*>(smem + a.off_dphi64);
+  const float2* phi2 = reinterpret_cast<const float2*>(tabs + a.off_phi2);
+  const float2* dphi2 = reinterpret_cast<const float2*>(tabs + a.off_dphi2);
+  const float* refn = reinterpret_cast<const float*>(tabs + a.off_refn);
+  const double* dphi64 = reinterpret_cast<const double*>(tabs + a.off_dphi64);
   const int nq = a.num_points;
   const int nqp = (nq + 1) / 2;
   const uint32_t mask = a.mask;
   const bool want_j = (mask & ~kOutPoints) != 0;
   constexpr int K0 = SPLIT ? 1 : 0;  // the split kernel's node-0 term vanishes
 
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
-       c += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t c = c0; c < c_end; c += step) {
     const int64_t cell = min(a.first_cell + c, a.last_cell);
     uint32_t idx[K];
     load_row<K>(a.dofmap + cell * K, idx);
@@ -572,17 +572,24 @@ __global__ void __launch_bounds__(kEvalThreads) eval_pair_kernel(const __grid_co
   }
 }
 
+template <bool SPLIT, int TD, int GD, int K>
+__global__ void __launch_bounds__(kEvalThreads) eval_pair_kernel(const __grid_constant__ PairArgs a) {
+  __shared__ uint64_t bar;
+  extern __shared__ __align__(16) unsigned char smem[];
+  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  pair_cells<SPLIT, TD, GD, K>(a, smem, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, a.padded,
+                               (int64_t)gridDim.x * blockDim.x);
+}
+
 // ----------------------------------------------------------------------------------------
 // The direct kernel: scalar, K, TD, GD and the tile at compile time.
 
 template <typename F, int TD, int GD, int K, int TILE>
-__global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_constant__ EvalArgs<F> a) {
-  __shared__ uint64_t bar;
-  extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
-  const F* phi = reinterpret_cast<const F*>(smem);
-  const F* dphi = reinterpret_cast<const F*>(smem + a.off_dphi);
-  const F* refn = reinterpret_cast<const F*>(smem + a.off_refn);
+__device__ __forceinline__ void direct_cells(const EvalArgs<F>& a, const unsigned char* tabs, int64_t c0,
+                                             int64_t c_end, int64_t step) {
+  const F* phi = reinterpret_cast<const F*>(tabs);
+  const F* dphi = reinterpret_cast<const F*>(tabs + a.off_dphi);
+  const F* refn = reinterpret_cast<const F*>(tabs + a.off_refn);
   const int nq = a.num_points;
   const uint32_t mask = a.mask;
   const bool want_j = (mask & ~kOutPoints) != 0;
@@ -590,8 +597,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_
   using A = Ar<F>;
   using M = Factors<F, TD, GD>;
 
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
-       c += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t c = c0; c < c_end; c += step) {
     const int64_t cell = min(a.first_cell + c, a.last_cell);
     uint32_t idx[K];
     load_row<K>(a.dofmap + cell * K, idx);
@@ -680,6 +686,15 @@ __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_
       }
     }
   }
+}
+
+template <typename F, int TD, int GD, int K, int TILE>
+__global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_constant__ EvalArgs<F> a) {
+  __shared__ uint64_t bar;
+  extern __shared__ __align__(16) unsigned char smem[];
+  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  direct_cells<F, TD, GD, K, TILE>(a, smem, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, a.padded,
+                                   (int64_t)gridDim.x * blockDim.x);
 }
 
 // ----------------------------------------------------------------------------------------

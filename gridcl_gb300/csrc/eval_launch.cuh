@@ -8,9 +8,14 @@
 
 namespace tlg {
 
-// Grid of persistent CTAs: enough to cover the range, at most the resident CTAs of the device.
+// A grid size chosen by the batch autotuner for the next launches on this thread (0: none).
+inline thread_local int g_grid_override = 0;
+
+// Grid of persistent CTAs: enough to cover the range, at most the resident CTAs of the device
+// (or the autotuner's choice).
 template <typename Kernel>
 inline int persistent_grid(Kernel kern, size_t smem, int64_t work_items, int threads) {
+  if (g_grid_override > 0) return g_grid_override;
   static thread_local int sms = 0;
   if (sms == 0) {
     int dev = 0;

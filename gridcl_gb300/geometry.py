@@ -518,3 +518,55 @@ def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: s
                                local.data_ptr(), 4 if fdt == torch.float32 else 8, stride,
                                grad.data_ptr(), stream))
     return grad, fields
+
+
+class Batch:
+    """Every block of `g` evaluated by one CUDA graph launch (``tlg_batch_*``): the point set of
+    each block from `rule`, the same factors and precision for all; fields allocated once
+    (``self.fields[b]``). ``tune()`` picks the launch shapes; ``launch()`` runs the graph."""
+
+    def __init__(self, g: Geometry, rule: "QuadRule", factors=("points", "jacobian", "detj", "pinv"),
+                 precision: str = "native"):
+        self.g, self.rule, self.precision = g, rule, precision
+        n = len(g.blocks)
+        out_dtype = torch.float32 if precision == "split" else g.dtype
+        code = SPLIT32 if precision == "split" else g.dtype
+        self.fields, self._tables = [], []
+        descs = (TlgBlock * max(n, 1))()
+        outs = (TlgOutputs * max(n, 1))()
+        handles = (ctypes.c_void_p * max(n, 1))()
+        for b, blk in enumerate(g.blocks):
+            pts = rule.get(blk.element.cell)
+            td, gd = blk.element.tdim, g.gdim
+            names = _factor_names(g, b, factors)
+            t = pts.tables(blk.element, gd, code)
+            self._tables.append(t)
+            f = {name: QuadField.uninit(blk.num_cells, len(pts), FACTOR_LEN[name](td, gd), GPU_QUAD_TILE,
+                                        out_dtype, g.nodes.device) for name in names}
+            self.fields.append(f)
+            descs[b] = g.block_desc(b)
+            o = outs[b]
+            o.first_cell, o.num_cells, o.out_first_cell, o.tile = 0, blk.num_cells, 0, GPU_QUAD_TILE
+            for name in names:
+                setattr(o, name, f[name].chunks[0].data.data_ptr() if f[name].chunks else None)
+            handles[b] = t.handle
+        self._descs, self._outs, self._handles = descs, outs, handles
+        h = ctypes.c_void_p()
+        check(lib().tlg_batch_create(handles, descs, outs, n, ctypes.byref(h)))
+        self.handle = h
+        self.grids = [0] * n
+
+    def tune(self) -> list:
+        grids = (ctypes.c_int * max(len(self.fields), 1))()
+        check(lib().tlg_batch_tune(self.handle, current_stream_handle(), grids))
+        self.grids = list(grids)[: len(self.fields)]
+        return self.grids
+
+    def launch(self) -> None:
+        check(lib().tlg_batch_launch(self.handle, current_stream_handle()))
+
+    def __del__(self):
+        try:
+            lib().tlg_batch_destroy(self.handle)
+        except Exception:
+            pass

@@ -301,3 +301,30 @@ def perturbed_radius(m: HostMesh, amplitude: float, seed: int = 2026) -> HostMes
     """Scales every node's radius by 1 + amplitude * U[0, 1) (seeded)."""
     u = 0.5 * (uniform(seed, (m.num_nodes,)) + 1.0)
     return HostMesh(m.gdim, m.nodes * (1.0 + amplitude * u)[:, None], m.blocks)
+
+
+def combine(parts, offsets) -> HostMesh:
+    """One mesh of the blocks of `parts` (3D meshes), each translated by its offset, with the
+    node arrays concatenated (the blocks share no nodes)."""
+    nodes, blocks, base = [], [], 0
+    for m, off in zip(parts, offsets):
+        nodes.append(m.nodes + np.asarray(off, dtype=np.float64))
+        for b in m.blocks:
+            blocks.append(HostBlock(b.cell, b.degree, (b.cells.astype(np.int64) + base).astype(np.uint32),
+                                    b.family))
+        base += m.num_nodes
+    return HostMesh(parts[0].gdim, np.concatenate(nodes), blocks)
+
+
+def hybrid_box(hexes: int, prisms: int, tets: int, jitter: float = 0.02, seed: int = 2026) -> HostMesh:
+    """A hybrid mesh of three blocks of uneven size: `hexes` Q2 hexahedra, `prisms` P2 prisms and
+    `tets` P3 tetrahedra, each the first cells of a sin-mapped, jittered box, the boxes side by
+    side along x."""
+    parts = []
+    for cell, p, count, per in (("Hexahedron", 2, hexes, 1), ("Prism", 2, prisms, 2), ("Tetrahedron", 3, tets, 6)):
+        n = 1
+        while per * n ** 3 < count:
+            n += 1
+        m = curved_box(cell, n, p, jitter=jitter, seed=seed)
+        parts.append(m.first_cells(count))
+    return combine(parts, [(0.0, 0.0, 0.0), (1.5, 0.0, 0.0), (3.0, 0.0, 0.0)])

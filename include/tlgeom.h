@@ -161,6 +161,29 @@ typedef struct tlg_outputs {
 tlg_status tlg_eval_block(const tlg_tables* tables, const tlg_block* block,
                           const tlg_outputs* outputs, void* stream);
 
+/* ---------------------------------------------------------------------------------------
+ * Batches: all blocks of a hybrid mesh (different cell types and degrees) evaluated by one CUDA
+ * graph launch, the blocks' persistent kernels running as parallel branches of the graph, their
+ * launch shapes picked by an autotuner. Replaces the host loop over blocks of Mesh::per_block
+ * (tetraloma/src/mesh.rs:249-257), which launches each factor of each block separately.
+ * ------------------------------------------------------------------------------------- */
+typedef struct tlg_batch tlg_batch;
+
+/* num_blocks (tables, block, outputs) triples, copied; the pointed-to device memory must stay
+ * valid while the batch is used. */
+tlg_status tlg_batch_create(const tlg_tables* const* tables, const tlg_block* blocks,
+                            const tlg_outputs* outputs, int num_blocks, tlg_batch** out);
+tlg_status tlg_batch_destroy(tlg_batch* batch);
+
+/* Times candidate persistent grids (0 and 1..8 CTAs per SM) for each block on `stream`, keeps the
+ * fastest, and caches the choice per launch shape for the process; grids[i] (may be NULL) receives
+ * block i's grid (0: the occupancy limit). Runs the blocks' kernels; call it outside stream
+ * capture. Rebuilds the graph on the next launch. */
+tlg_status tlg_batch_tune(tlg_batch* batch, void* stream, int* grids);
+
+/* Evaluates every block: one launch of a CUDA graph (captured on the first call). */
+tlg_status tlg_batch_launch(tlg_batch* batch, void* stream);
+
 /* The E-vector chunk of cells [first_cell, first_cell + chunk_cells): out[(k * gdim + g) * stride
  * + c] for c < roundup(chunk_cells, 16) <= stride, padding lanes repeating the block's last cell
  * and node indices clamped to the last node; a bit-exact gather
