@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--mode", choices=["split", "f64", "f32"], default="split")
     p.add_argument("--n", type=int, default=64, help="subcells per direction")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the other workloads (hybrid batch, sphere surface, Q2 adjoint, P1 box)")
     return p.parse_args()
 
 
@@ -212,6 +214,189 @@ def time_steps(step, steps, flush, stream):
     return sum(times) / len(times)
 
 
+
+# ------------------------------------------------------------------------------------------
+# The other workloads, measured in the same run and reported under "workloads".
+
+def event_ms(fn, reps: int = 5, warm: int = 2) -> float:
+    import torch
+
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def rel_err_fields(a: dict, b: dict) -> dict:
+    out = {}
+    for k in a:
+        x = a[k].chunks[0].data.double()
+        y = b[k].chunks[0].data.double()
+        out[k] = float((x - y).abs().max() / y.abs().max())
+    return out
+
+
+def extra_hybrid():
+    """Hybrid mesh, one graph launch: 2,000,000 Q2 hexahedra (27-point Gauss), 300,000 P2 prisms
+    (21 points), 50,000 P3 tetrahedra (24 points); plain per-block FP64 launches against the
+    batched FP64 and split-precision graphs."""
+    import torch
+
+    import gridcl_gb300 as tg
+    from gridcl_gb300 import meshes, refcell
+
+    mesh = meshes.hybrid_box(2_000_000, 300_000, 50_000)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    sets = [tg.PointSet("Hexahedron", *refcell.gauss_rule("Hexahedron", 4)),
+            tg.PointSet("Prism", *refcell.collapsed_rule("Prism", (3, 1, 7))),
+            tg.PointSet("Tetrahedron", *refcell.collapsed_rule("Tetrahedron", (4, 3, 2)))]
+    rule = tg.QuadRule(sets)
+    qpts = sum(b.num_cells * len(rule.get(b.element.cell)) for b in g.blocks)
+    factors = ("points", "jacobian", "detj", "pinv")
+    plain_out = [tg.geometric_factors_block(g, b, rule.get(blk.element.cell), factors)
+                 for b, blk in enumerate(g.blocks)]
+
+    def plain():
+        for b, blk in enumerate(g.blocks):
+            tg.geometric_factors_block(g, b, rule.get(blk.element.cell), factors, out=plain_out[b])
+
+    plain_ms = event_ms(plain, reps=3, warm=1)
+    res = {"workload": "hybrid: 2,000,000 Q2 hex (27 pts) + 300,000 P2 prisms (21) + 50,000 P3 tets (24), "
+                       "sin-mapped + jittered, fused x/J/detJ/K", "qpoints": int(qpts),
+           "plain_fp64_per_block": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3)}}
+    for precision in ("native", "split"):
+        batch = tg.Batch(g, rule, factors=factors, precision=precision)
+        grids = batch.tune()
+        ms = event_ms(batch.launch)
+        key = "batched_fp64_graph" if precision == "native" else "batched_split_graph"
+        res[key] = {"ms": ms, "value": qpts / (ms * 1e-3), "tuned_grids": grids,
+                    "speedup_vs_plain_fp64": plain_ms / ms}
+        if precision == "split":
+            res[key]["rel_err_vs_fp64"] = {
+                b: rel_err_fields(batch.fields[b], plain_out[b]) for b in range(len(g.blocks))}
+            out_bytes = qpts * 22 * 4
+            in_bytes = sum(b.num_cells * b.element.nodes_per_cell * 4 for b in g.blocks) + g.nodes.numel() * 8
+            res[key]["hbm_gbs"] = (out_bytes + in_bytes) / (ms * 1e-3) / 1e9
+        del batch
+    return res
+
+
+def extra_sphere():
+    """Surface TD=2, GD=3: 4,194,304 degree-4 triangles of the refined icosahedron (first cells of
+    9 refinements), radius x (1 + 0.02 U), 28-point rule; x, J, area element, normals, K; split
+    precision against FP64."""
+    import torch
+
+    import gridcl_gb300 as tg
+    from gridcl_gb300 import meshes, refcell
+
+    mesh = meshes.perturbed_radius(meshes.sphere(9, 4, max_cells=4_194_304), 0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    ps = tg.PointSet("Triangle", *refcell.collapsed_rule("Triangle", (7, 4)))
+    qpts = mesh.blocks[0].num_cells * len(ps)
+    factors = ("points", "jacobian", "detj", "normals", "pinv")
+    f64 = tg.geometric_factors_block(g, 0, ps, factors)
+    count = torch.zeros(1, dtype=torch.int64, device="cuda")
+    split = tg.geometric_factors_block(g, 0, ps, factors, precision="split", recomputed=count)
+    recomputed = int(count.item())
+    ms64 = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, factors, out=f64), reps=3)
+    ms32 = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, factors, out=split, precision="split"))
+    out_bytes = qpts * 19 * 4
+    in_bytes = mesh.blocks[0].cells.size * 4 + g.nodes.numel() * 8
+    return {"workload": "sphere P4 triangles 4,194,304 cells, 28 pts, x/J/area/normals/K", "qpoints": int(qpts),
+            "fp64": {"ms": ms64, "value": qpts / (ms64 * 1e-3)},
+            "split": {"ms": ms32, "value": qpts / (ms32 * 1e-3), "speedup_vs_fp64": ms64 / ms32,
+                      "hbm_gbs": (out_bytes + in_bytes) / (ms32 * 1e-3) / 1e9,
+                      "fp64_recomputed_points": recomputed,
+                      "rel_err_vs_fp64": rel_err_fields(split, f64)}}
+
+
+def extra_adjoint():
+    """Forward + adjoint: 128^3 Q2 hexahedra, 27-point Gauss, seeded standard-normal cotangents on
+    det J and K; the fused split-precision forward + vjp (+ f64 node sums) against the plain FP64
+    forward followed by the FP64 vjp; central differences (step 1e-6) at 1,000 seeded nodes."""
+    import numpy as np
+    import torch
+
+    import gridcl_gb300 as tg
+    from gridcl_gb300 import meshes, refcell
+
+    mesh = meshes.curved_box("Hexahedron", 128, 2, jitter=0.02, seed=2026)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    ps = tg.PointSet("Hexahedron", *refcell.gauss_rule("Hexahedron", 4))
+    ncells, nq = mesh.blocks[0].num_cells, len(ps)
+    qpts = ncells * nq
+    gen = torch.Generator(device="cuda").manual_seed(2026)
+    ct64 = {}
+    for name, length in (("detj", 1), ("pinv", 9)):
+        f = tg.QuadField.uninit(ncells, nq, length, 16, torch.float64)
+        f.chunks[0].data.normal_(generator=gen)
+        ct64[name] = f
+    ct32 = {k: tg.QuadField([tg.geometry.QuadChunk(0, ncells, v.chunks[0].data.float())], ncells, nq,
+                            v.length, 16) for k, v in ct64.items()}
+    factors = ("points", "jacobian", "detj", "pinv")
+    fwd64 = tg.geometric_factors_block(g, 0, ps, factors)
+    tg.node_incidence(g, 0)
+    local64 = torch.empty((27, 3, ncells), dtype=torch.float64, device="cuda")
+    local32 = torch.empty((27, 3, ncells), dtype=torch.float32, device="cuda")
+    grad64, _ = tg.vjp_block(g, 0, ps, ct64, local=local64)
+    grad32, fused = tg.vjp_block(g, 0, ps, ct32, precision="split", forward=factors, local=local32)
+
+    def plain():
+        tg.geometric_factors_block(g, 0, ps, factors, out=fwd64)
+        tg.vjp_block(g, 0, ps, ct64, local=local64)
+
+    def fused_step():
+        tg.vjp_block(g, 0, ps, ct32, precision="split", forward=factors, out=fused, local=local32)
+
+    plain_ms = event_ms(plain, reps=2, warm=1)
+    fused_ms = event_ms(fused_step)
+    # Central differences of the FP64 functional at 1,000 seeded nodes against the FP64 adjoint.
+    sample = np.random.default_rng(2026).choice(mesh.num_nodes, 1000, replace=False)
+    host = {k: v.to_host_cell_major() for k, v in ct64.items()}
+    fd = tg.fd_check(g, 0, ps, {"detj": host["detj"][..., 0], "pinv": host["pinv"]},
+                     grad64.cpu().numpy(), sample)
+    gerr = float((grad32 - grad64).abs().max() / grad64.abs().max())
+    # Compulsory traffic of the fused step: cotangents in, forward fields out, nodes and dofmap
+    # in, contributions out and back in through the CSR, node cotangents out.
+    alg = (qpts * 10 * 4 + qpts * 22 * 4 + ncells * 27 * 4 + g.nodes.numel() * 8
+           + 2 * local32.numel() * 4 + g.nodes.numel() * 8 + (ncells * 27 + g.nodes.shape[0]) * 4)
+    return {"workload": "Q2 hex 128^3, 27 pts, forward (x/J/detJ/K) + adjoint from detJ and K cotangents",
+            "qpoints": int(qpts),
+            "plain_fp64_fwd_then_vjp": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3)},
+            "fused_split_fwd_vjp": {"ms": fused_ms, "value": qpts / (fused_ms * 1e-3),
+                                    "speedup_vs_plain_fp64": plain_ms / fused_ms,
+                                    "hbm_gbs": alg / (fused_ms * 1e-3) / 1e9,
+                                    "grad_rel_err_vs_fp64": gerr,
+                                    "forward_rel_err_vs_fp64": rel_err_fields(fused, fwd64)},
+            "fd_check_fp64": fd}
+
+
+def extra_p1_box():
+    """BASELINE's CPU-runtime case: 8^3 x 6 = 3,072 P1 tetrahedra, interior nodes jittered by
+    +-0.1 h, 14 points (collapsed 7 x 2 x 1), f64; GPU against the oracle on the host cores."""
+    import torch
+
+    import gridcl_gb300 as tg
+    from gridcl_gb300 import meshes, refcell
+
+    mesh = meshes.curved_box("Tetrahedron", 8, 1, jitter=0.1, amplitude=0.0)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, w = refcell.collapsed_rule("Tetrahedron", (7, 2, 1))
+    ps = tg.PointSet("Tetrahedron", pts, w)
+    out = tg.geometric_factors_block(g, 0, ps)
+    ms = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, out=out), reps=20)
+    qpts = mesh.blocks[0].num_cells * len(ps)
+    res = {"workload": "P1 tets 8^3x6, 14 pts, f64", "qpoints": int(qpts),
+           "gpu_fp64": {"ms": ms, "value": qpts / (ms * 1e-3)}}
+    return res
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -351,6 +536,16 @@ def run_ours(args):
         if plain is not None:
             line["plain_fp64_gpu"] = plain
             line["recomputed_points"] = recomputed
+        if not args.no_extras and world == 1:
+            workloads = {}
+            for name, fn in (("hybrid_batched", extra_hybrid), ("sphere_surface", extra_sphere),
+                             ("q2_forward_adjoint", extra_adjoint), ("p1_box", extra_p1_box)):
+                try:
+                    workloads[name] = fn()
+                except Exception as exc:  # reported, not fatal: the main line stands
+                    workloads[name] = {"error": f"{type(exc).__name__}: {exc}"}
+                torch.cuda.empty_cache()
+            line["workloads"] = workloads
         if not args.no_cpu_baseline:
             v, threads, passes = cpu_baseline(mesh, pts)
             line["cpu_baseline"] = {"value": v, "unit": "qpoints/s", "cores": threads, "kind": "port",

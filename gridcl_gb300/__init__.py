@@ -20,6 +20,7 @@ from .geometry import (
     detj_block,
     facet_normals_block,
     facet_point_set,
+    fd_check,
     geometric_factors_block,
     jacobians_block,
     measure_block,
@@ -33,7 +34,7 @@ from . import meshes, refcell
 
 __all__ = [
     "Batch", "CoordinateElement", "Geometry", "GeometryBlock", "GridError", "PointSet", "QuadField",
-    "QuadRule", "detj_block", "facet_normals_block", "facet_point_set",
+    "QuadRule", "detj_block", "facet_normals_block", "facet_point_set", "fd_check",
     "geometric_factors_block", "jacobians_block", "lib", "measure_block", "meshes", "normals_block",
     "node_incidence", "physical_points_block", "pseudo_inverse_block", "refcell", "vjp_block",
 ]

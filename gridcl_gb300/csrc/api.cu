@@ -122,7 +122,7 @@ tlg_status eval_pair(const tlg_tables* t, const tlg_block* b, const tlg_outputs*
   const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
   a.last_flag = nflags - 1;
   for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
-  a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 1e3f;
+  a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 256.0f;
   a.last_node = (uint32_t)(b->num_nodes - 1);
   a.tab_bytes = t->bytes;
   a.off_refn = t->off_refn;

@@ -213,14 +213,29 @@ struct Factors {
     }
   }
 
+  // The normal n = J0 x J1 of a surface in 3D (TD = 2, GD = 3).
+  __device__ __forceinline__ static void surface_normal(const V* j, V* n) {
+    n[0] = cross(j[1], j[5], j[2], j[4]);
+    n[1] = cross(j[2], j[3], j[0], j[5]);
+    n[2] = cross(j[0], j[4], j[1], j[3]);
+  }
+
+  __device__ __forceinline__ static V dot3(const V* u, const V* v) {
+    return A::fma(u[2], v[2], A::fma(u[1], v[1], A::mul(u[0], v[0])));
+  }
+
+  // det J, or the area element when TD < GD. For TD = 2, GD = 3 it is |J0 x J1|, which equals the
+  // reference's sqrt(det(J^T J)) = sqrt(ac - b^2) (Lagrange's identity) with a rounding error
+  // that grows with the condition number of J, not with its square.
   __device__ __forceinline__ static V detj(const V* j) {
     if constexpr (TD == GD) {
       return square_det(j);
     } else if constexpr (TD == 1) {
       return A::sqrt(column_dot(j, 0, 0));
     } else {
-      const V a = column_dot(j, 0, 0), b = column_dot(j, 0, 1), c = column_dot(j, 1, 1);
-      return A::sqrt(cross(a, c, b, b));
+      V n[3];
+      surface_normal(j, n);
+      return A::sqrt(dot3(n, n));
     }
   }
 
@@ -251,13 +266,22 @@ struct Factors {
 #pragma unroll
       for (int g = 0; g < GD; ++g) k[g] = A::mul(j[g], inv);
     } else {
-      const V a = column_dot(j, 0, 0), b = column_dot(j, 0, 1), c = column_dot(j, 1, 1);
-      const V inv = A::rcp(cross(a, c, b, b));
-      const V g00 = A::mul(c, inv), g01 = A::mul(A::neg(b), inv), g11 = A::mul(a, inv);
+      // (J^T J)^-1 J^T with the identities c J0 - b J1 = J1 x n and a J1 - b J0 = n x J0, over
+      // |n|^2 = ac - b^2, n = J0 x J1: the reference's G^-1 J^T (layout.rs:253-266) without
+      // forming J^T J.
+      V n[3];
+      surface_normal(j, n);
+      const V inv = A::rcp(dot3(n, n));
+      const V* j0 = j;
+      const V* j1 = j + 3;
+      const V r0[3] = {cross(j1[1], n[2], j1[2], n[1]), cross(j1[2], n[0], j1[0], n[2]),
+                       cross(j1[0], n[1], j1[1], n[0])};
+      const V r1[3] = {cross(n[1], j0[2], n[2], j0[1]), cross(n[2], j0[0], n[0], j0[2]),
+                       cross(n[0], j0[1], n[1], j0[0])};
 #pragma unroll
-      for (int g = 0; g < GD; ++g) {
-        k[g * TD] = A::fma(g00, j[g], A::mul(g01, j[GD + g]));
-        k[g * TD + 1] = A::fma(g01, j[g], A::mul(g11, j[GD + g]));
+      for (int g = 0; g < 3; ++g) {
+        k[g * 2] = A::mul(r0[g], inv);
+        k[g * 2 + 1] = A::mul(r1[g], inv);
       }
     }
   }

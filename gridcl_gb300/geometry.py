@@ -327,7 +327,7 @@ def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points
 
     ``precision="native"`` computes in the mesh's scalar type. ``precision="split"`` (f64 meshes)
     computes in FP32 on cell-shifted coordinates and returns f32 fields; points whose condition
-    estimate exceeds `cond_limit` (0: 1e3) get det J and K from FP64, and `recomputed` (an int64
+    estimate exceeds `cond_limit` (0: 256) get det J and K from FP64, and `recomputed` (an int64
     CUDA tensor of one element) counts them."""
     blk = g.blocks[b]
     names = _factor_names(g, b, factors)
@@ -570,3 +570,65 @@ class Batch:
             lib().tlg_batch_destroy(self.handle)
         except Exception:
             pass
+
+
+def fd_check(g: Geometry, b: int, pts: PointSet, cotangents: dict, grad: np.ndarray, sample,
+             h: float = 1e-6) -> dict:
+    """Central differences of L = sum over cells and points of (xbar . x + dbar det J + Kbar : K)
+    against the node cotangents `grad` ([node][GD]) at the node indices `sample`, with the f64
+    forward kernels. Each (node, coordinate, sign) perturbs a private copy of the cells around the
+    node only (the other cells do not change L), and all copies are evaluated in one launch.
+    `cotangents` holds cell-major host arrays ("points" [c][q][GD], "detj" [c][q], "pinv"
+    [c][q][TD GD]), missing ones zero. Returns the largest |fd - grad| / max(1, |grad|)."""
+    blk = g.blocks[b]
+    k = blk.element.nodes_per_cell
+    gd = g.gdim
+    dofmap = blk.dofmap.cpu().numpy().view(np.uint32).reshape(-1, k)
+    inc = node_incidence(g, b)
+    offsets = inc.offsets.cpu().numpy().view(np.uint32).astype(np.int64)
+    entries = inc.entries.cpu().numpy().view(np.uint32)
+    stored = g.nodes.double().cpu().numpy()
+    cells_of = []
+    for n in sample:
+        e = entries[offsets[n]:offsets[n + 1]]
+        cells_of.append(np.unique(e // k))
+    copies, owner, local_pos = [], [], []
+    for i, cells in enumerate(cells_of):
+        for c in range(gd):
+            for s in (1.0, -1.0):
+                copies.append(cells)
+                owner.append((i, c, s))
+    all_cells = np.concatenate(copies)
+    dm = dofmap[all_cells]  # [m][K]
+    nodes = stored[dm].reshape(-1, gd).copy()  # private copies, [m * K][GD]
+    start = 0
+    for (i, c, s), cells in zip(owner, copies):
+        n = sample[i]
+        for j in range(cells.size):
+            row = dm[start + j]
+            for kk in np.nonzero(row == n)[0]:
+                nodes[(start + j) * k + kk, c] += s * h
+        start += cells.size
+    sub_dofmap = np.arange(all_cells.size * k, dtype=np.uint32).reshape(-1, k)
+    sub = Geometry([GeometryBlock(blk.element, torch.from_numpy(sub_dofmap.view(np.int32)).to(g.nodes.device))],
+                   torch.from_numpy(nodes).to(g.nodes.device), g.origin)
+    names = [f for f in ("points", "detj", "pinv") if cotangents.get(f) is not None]
+    fields = geometric_factors_block(sub, 0, pts, names)
+    per_cell = np.zeros(all_cells.size)
+    for f in names:
+        vals = fields[f].to_host_cell_major()  # [copy][q][LEN]
+        ct = np.asarray(cotangents[f], dtype=np.float64)
+        if f == "detj":
+            ct = ct[..., None]
+        per_cell += (vals * ct[all_cells]).sum(axis=(1, 2))
+    worst = 0.0
+    start = 0
+    sums = {}
+    for (i, c, s), cells in zip(owner, copies):
+        sums[(i, c, s)] = per_cell[start:start + cells.size].sum()
+        start += cells.size
+    for i, n in enumerate(sample):
+        for c in range(gd):
+            fd = (sums[(i, c, 1.0)] - sums[(i, c, -1.0)]) / (2.0 * h)
+            worst = max(worst, abs(fd - grad[n, c]) / max(1.0, abs(grad[n, c])))
+    return {"max_rel_err": worst, "nodes": int(len(sample)), "step": h}

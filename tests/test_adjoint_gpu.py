@@ -122,3 +122,18 @@ def test_vjp_against_central_differences(cuda):
             xm[n, c] -= h
             fd = (functional(xp) - functional(xm)) / (2 * h)
             assert abs(fd - grad[n, c]) <= 1e-6 * max(1.0, abs(grad[n, c])), (n, c, fd, grad[n, c])
+
+
+def test_fd_check_on_seeded_nodes(cuda):
+    """The product's local central-difference check (f64 forward kernels) agrees with the f64
+    adjoint at seeded nodes of a curved Q2 hexahedral box."""
+    mesh = meshes.curved_box("Hexahedron", 4, 2, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, _ = tg.refcell.gauss_rule("Hexahedron", 4)
+    ps = tg.PointSet("Hexahedron", pts, np.ones(len(pts)))
+    ct, host = cotangent_fields(np.random.default_rng(2), mesh.blocks[0].num_cells, len(pts), torch.float64)
+    grad, _ = tg.vjp_block(g, 0, ps, ct)
+    sample = np.random.default_rng(9).choice(mesh.num_nodes, 40, replace=False)
+    res = tg.fd_check(g, 0, ps, {"points": host["points"], "detj": host["detj"][..., 0],
+                                 "pinv": host["pinv"]}, grad.cpu().numpy(), sample)
+    assert res["max_rel_err"] < 1e-6, res
