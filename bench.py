@@ -343,8 +343,8 @@ def extra_adjoint():
     factors = ("points", "jacobian", "detj", "pinv")
     fwd64 = tg.geometric_factors_block(g, 0, ps, factors)
     tg.node_incidence(g, 0)
-    local64 = torch.empty((27, 3, ncells), dtype=torch.float64, device="cuda")
-    local32 = torch.empty((27, 3, ncells), dtype=torch.float32, device="cuda")
+    local64 = torch.empty((ncells, 27, 4), dtype=torch.float64, device="cuda")
+    local32 = torch.empty((ncells, 27, 4), dtype=torch.float32, device="cuda")
     grad64, _ = tg.vjp_block(g, 0, ps, ct64, local=local64)
     grad32, fused = tg.vjp_block(g, 0, ps, ct32, precision="split", forward=factors, local=local32)
 
@@ -366,7 +366,7 @@ def extra_adjoint():
     # Compulsory traffic of the fused step: cotangents in, forward fields out, nodes and dofmap
     # in, contributions out and back in through the CSR, node cotangents out.
     alg = (qpts * 10 * 4 + qpts * 22 * 4 + ncells * 27 * 4 + g.nodes.numel() * 8
-           + 2 * local32.numel() * 4 + g.nodes.numel() * 8 + (ncells * 27 + g.nodes.shape[0]) * 4)
+           + 2 * ncells * 27 * 3 * 4 + g.nodes.numel() * 8 + (ncells * 27 + g.nodes.shape[0]) * 4)
     return {"workload": "Q2 hex 128^3, 27 pts, forward (x/J/detJ/K) + adjoint from detJ and K cotangents",
             "qpoints": int(qpts),
             "plain_fp64_fwd_then_vjp": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3)},

@@ -101,7 +101,7 @@ SIGNATURES = [
     ("tlg_csr_build", _I, [_P, _L, _I, _L, _P, _L, _P, _P, _P]),
     ("tlg_vjp_block", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs),
                            ctypes.POINTER(TlgCotangents), _P, _L, _P]),
-    ("tlg_vjp_gather", _I, [_P, _P, _L, _I, _I, _P, _I, _L, _P, _P]),
+    ("tlg_vjp_gather", _I, [_P, _P, _L, _I, _P, _I, _P, _P]),
     ("tlg_measure_cell_sums", _I, [_P, _I, _L, _L, _I, _P, _P, _P]),
     ("tlg_sum_workspace_bytes", _L, [_I, _L]),
     ("tlg_sum", _I, [_P, _I, _L, _P, _L, _P, _P]),

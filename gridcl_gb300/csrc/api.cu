@@ -36,8 +36,12 @@ struct tlg_tables {
   unsigned char* dev = nullptr;  // phi [Q][K] | dphi [Q][K][TD] | refn [Q][TD] | error word
   uint32_t bytes = 0;            // staged bytes (multiple of 16), error word excluded
   uint32_t off_dphi = 0, off_refn = 0, off_phi2 = 0, off_dphi2 = 0, off_dphi64 = 0;
+  // The adjoint's table after the error word (codimension 0, f64 or split tables; 0 bytes when
+  // absent or too large to stage): per node of each point (f64) or point pair (split) the 32
+  // bytes phi, dphi_0 .. dphi_{TD-1}, zero padding, as f64 values or f32 pairs.
+  uint32_t off_vjp = 0, vjp_bytes = 0;
   int* err = nullptr;
-  std::vector<unsigned char> host;  // host copy of the staged bytes
+  std::vector<unsigned char> host;  // host copy of the device bytes
 };
 
 namespace {
@@ -316,7 +320,12 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
                       " bytes) exceeds the shared-memory budget of 200 KiB");
     }
     t->bytes = (uint32_t)total;
-    t->host.assign(total, 0);
+    t->off_vjp = (uint32_t)(total + 16);
+    if (td == gdim && dtype != TLG_F32) {
+      const size_t vb = (size_t)(dtype == TLG_SPLIT32 ? qp : npoints) * k * 32;
+      if (vb > 0 && vb <= (size_t)160 * 1024) t->vjp_bytes = (uint32_t)vb;
+    }
+    t->host.assign(t->off_vjp + t->vjp_bytes, 0);
     // Reorder [deriv][q][k] into phi [q][k] and dphi [q][k][d].
     std::vector<double> phi(n_phi), dphi(n_dphi), refn(n_refn, 0.0);
     for (int64_t q = 0; q < npoints; ++q)
@@ -340,6 +349,22 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       narrow_into<float>(t->host, t->off_phi2, phi2.data(), phi2.size());
       narrow_into<float>(t->host, t->off_dphi2, dphi2.data(), dphi2.size());
     }
+    if (t->vjp_bytes > 0) {
+      const int pn = dtype == TLG_SPLIT32 ? 2 : 1;  // points per table row
+      const int64_t rows = dtype == TLG_SPLIT32 ? qp : npoints;
+      std::vector<double> v((size_t)rows * k * 4 * pn, 0.0);
+      for (int64_t r = 0; r < rows; ++r)
+        for (int h = 0; h < pn; ++h) {
+          const int64_t q = std::min<int64_t>(r * pn + h, npoints - 1);
+          for (int64_t i = 0; i < k; ++i) {
+            double* row = v.data() + (r * k + i) * 4 * pn;
+            row[h] = phi[q * k + i];
+            for (int d = 0; d < td; ++d) row[(1 + d) * pn + h] = dphi[(q * k + i) * td + d];
+          }
+        }
+      if (dtype == TLG_SPLIT32) narrow_into<float>(t->host, t->off_vjp, v.data(), v.size());
+      else narrow_into<double>(t->host, t->off_vjp, v.data(), v.size());
+    }
     if (dtype != TLG_F64) {
       narrow_into<float>(t->host, 0, phi.data(), n_phi);
       narrow_into<float>(t->host, t->off_dphi, dphi.data(), n_dphi);
@@ -349,14 +374,13 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       narrow_into<double>(t->host, t->off_dphi, dphi.data(), n_dphi);
       narrow_into<double>(t->host, t->off_refn, refn.data(), n_refn);
     }
-    cudaError_t e = cudaMalloc(&t->dev, total + 16);
+    cudaError_t e = cudaMalloc(&t->dev, t->host.size());
     if (e != cudaSuccess) {
       delete t;
       return cuda_fail(e, "tlg_tables_create: cudaMalloc");
     }
     t->err = reinterpret_cast<int*>(t->dev + total);
-    e = cudaMemcpy(t->dev, t->host.data(), total, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemset(t->err, 0, 16);
+    e = cudaMemcpy(t->dev, t->host.data(), t->host.size(), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
       cudaFree(t->dev);
       delete t;
@@ -467,7 +491,7 @@ tlg_status tlg_evector(const tlg_block* b, int nodes_per_cell, int64_t first_cel
 }
 
 tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o,
-                         const tlg_cotangents* ct, void* local, int64_t local_stride, void* stream) {
+                         const tlg_cotangents* ct, void* local, int64_t local_cells, void* stream) {
   if (!t || !b || !o || !ct) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: NULL argument");
   if (t->dtype != TLG_F64 && t->dtype != TLG_SPLIT32)
     return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: the adjoint runs with f64 or split-precision tables");
@@ -480,7 +504,7 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
   if (o->first_cell < 0 || o->num_cells < 0 || o->first_cell + o->num_cells > b->num_cells ||
       o->out_first_cell < 0 || o->out_first_cell % 16 != 0)
     return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: bad cell range");
-  if (local_stride < b->num_cells) return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_vjp_block: local_stride below the block's cells");
+  if (local_cells < b->num_cells) return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_vjp_block: local_cells below the block's cells");
   if (o->num_cells == 0) return ok();
   if (!b->nodes || !b->dofmap || !local) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: NULL nodes, dofmap or local");
   if (b->num_nodes < 1) return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_vjp_block: cells but no nodes");
@@ -488,7 +512,7 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
   std::memset(&a, 0, sizeof(a));
   a.nodes = b->nodes;
   a.dofmap = b->dofmap;
-  a.tab = t->dev;
+  a.tab = t->dev + t->off_vjp;
   a.ct[0] = ct->points;
   a.ct[1] = ct->detj;
   a.ct[2] = ct->pinv;
@@ -503,31 +527,34 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
   a.out_first_cell = o->out_first_cell;
   a.last_cell = b->num_cells - 1;
   a.range_end = o->first_cell + o->num_cells;
-  a.local_stride = local_stride;
   for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
   a.last_node = (uint32_t)(b->num_nodes - 1);
-  a.tab_bytes = t->bytes;
-  a.off_dphi = t->off_dphi;
+  a.tab_bytes = t->vjp_bytes;
+  const bool split = t->dtype == TLG_SPLIT32;
   a.num_points = (int)t->q;
   if (t->q == 0) return ok();
+  if (t->vjp_bytes == 0)
+    return fail(TLG_ERR_ALLOCATION_TOO_LARGE, "tlg_vjp_block: the adjoint's table exceeds 160 KiB of shared memory");
+  const size_t smem = (t->vjp_bytes + 15) / 16 * 16 + tlg::vjp_stage_bytes(split, t->td, (int)t->k);
+  if (smem > (size_t)227 * 1024)
+    return fail(TLG_ERR_ALLOCATION_TOO_LARGE, "tlg_vjp_block: tables and staging (" + std::to_string(smem) +
+                                                  " bytes) exceed 227 KiB of shared memory");
   bool found = false;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = t->dtype == TLG_SPLIT32 ? tlg::launch_vjp_split(t->td, (int)t->k, a, t->bytes, s, &found)
-                                          : tlg::launch_vjp_f64(t->td, (int)t->k, a, t->bytes, s, &found);
+  cudaError_t e = split ? tlg::launch_vjp_split(t->td, (int)t->k, a, smem, s, &found)
+                        : tlg::launch_vjp_f64(t->td, (int)t->k, a, smem, s, &found);
   if (!found) return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: no adjoint kernel for this element");
   if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_block launch");
   return ok();
 }
 
-tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int nodes_per_cell,
-                          int gdim, const void* local, int local_dtype, int64_t local_stride, double* grad,
-                          void* stream) {
-  if (!offsets || !grad || num_nodes < 0 || nodes_per_cell < 1 || gdim < 1 || gdim > 3 ||
-      (local_dtype != 4 && local_dtype != 8))
+tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int gdim,
+                          const void* local, int local_dtype, double* grad, void* stream) {
+  if (!offsets || !grad || num_nodes < 0 || gdim < 1 || gdim > 3 || (local_dtype != 4 && local_dtype != 8))
     return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_gather: bad arguments");
   if (num_nodes == 0) return ok();
-  cudaError_t e = tlg::launch_vjp_gather(offsets, entries, num_nodes, nodes_per_cell, gdim, local, local_dtype,
-                                         local_stride, grad, static_cast<cudaStream_t>(stream));
+  cudaError_t e = tlg::launch_vjp_gather(offsets, entries, num_nodes, gdim, local, local_dtype, grad,
+                                         static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_gather launch");
   return ok();
 }

@@ -55,11 +55,11 @@ cudaError_t launch_eval_pair(bool split, int td, int gd, int k, const PairArgs& 
                              cudaStream_t s, bool* found);
 
 struct VjpArgs;
-// Defined in vjp_f64.cu / vjp_split.cu; `found` is false when no kernel exists for (d, k).
+// Defined in vjp_f64.cu / vjp_split.cu; `found` is false when no kernel exists for (d, k). `smem`
+// is the dynamic shared memory: the staged tables (rounded up to 16 bytes) and the staging slots.
 cudaError_t launch_vjp_f64(int d, int k, const VjpArgs& a, size_t smem, cudaStream_t s, bool* found);
 cudaError_t launch_vjp_split(int d, int k, const VjpArgs& a, size_t smem, cudaStream_t s, bool* found);
-cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int k,
-                              int d, const void* local, int local_dtype, int64_t local_stride,
-                              double* grad, cudaStream_t s);
+cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int d,
+                              const void* local, int local_dtype, double* grad, cudaStream_t s);
 
 }  // namespace tlg

@@ -7,15 +7,26 @@
 //   Jbar(g, d) = dbar det J K(d, g) - (K^T Kbar K^T)(g, d),
 // from d det J = det J tr(K dJ) and dK = -K dJ K. J, det J and K are recomputed here, not read.
 //
-// vjp_kernel writes each cell's contributions L(cell, k, g) (layout [k][g][cell], cells fastest,
-// as the E-vector) and, when asked, the forward fields of the same points in the same pass (the
-// fused forward + adjoint). vjp_gather then sums, for every node, the contributions listed by the
-// node's CSR entries in entry order, in f64: deterministic.
+// vjp_kernel writes each cell's contributions L(cell, k, g), cell-major in rows of R values
+// ([cell][k][R], R = 4 for D = 3 with a zero pad, else D), so that the entry e = cell * K + k
+// of the node CSR owns the aligned row at e * R, read by one vector load; and, when asked, the
+// forward fields of the same points in the same pass (the fused forward + adjoint). vjp_gather
+// then sums, for every node, the contributions listed by the node's CSR entries in entry order,
+// in f64: deterministic.
 //
-// Four lanes per cell: lane g < D owns coordinate g (its node coordinates, row g of J, its
-// contributions); J is assembled from the rows by shuffles inside the group, det J and K are
-// computed by every lane of the group. SPLIT: f64 nodes shifted by node 0 in f64, FP32
-// arithmetic, f32 cotangents, contributions and fields; otherwise f64 throughout.
+// Four lanes per cell split the cell's nodes: lane r owns the nodes k = r, r + 4, r + 8, ...
+// with all D coordinates. Each lane forms the partial J (and x) over its nodes; a two-level
+// butterfly (xor 1, then xor 2) sums the partials, and since IEEE addition commutes every lane
+// of the group ends with the same bits. det J, K and Jbar are then formed by every lane, and
+// each lane accumulates the contributions of its own nodes. One node row of the table (phi and
+// dphi of one point, or of a point pair) is 32 bytes: two 16-byte shared-memory loads. The
+// cotangents of the next step are loaded while the current step's contributions accumulate.
+// The eight cells of a warp are consecutive: their contributions are staged in shared memory
+// and written as one contiguous run.
+//
+// SPLIT: f64 nodes shifted by node 0 in f64, FP32 arithmetic on two points at a time (FFMA2,
+// FMUL2 and FADD2 over the pair (q, q + 1)), f32 cotangents, contributions and fields.
+// Otherwise f64 throughout, one point at a time.
 #pragma once
 
 #include <cstdint>
@@ -28,183 +39,365 @@ namespace tlg {
 struct VjpArgs {
   const void* nodes;
   const uint32_t* dofmap;
-  const unsigned char* tab;  // phi [Q][K] | dphi [Q][K][D] in F (F = float with SPLIT)
+  const unsigned char* tab;  // node rows [QV][K][4] of V: phi, dphi_0 .. dphi_{D-1}, padding
   const void* ct[3];         // cotangents: points, detj, pinv (tile 16 chunks) or null
   void* out[4];              // fused forward fields: points, jacobian, detj, pinv, or null
-  void* local;               // contributions [K][D][local_stride] of F
+  void* local;               // contributions [cell][K][R] of the arithmetic's scalar type
   int* err;
-  int64_t first_cell, padded, out_first_cell, last_cell, range_end, local_stride;
+  int64_t first_cell, padded, out_first_cell, last_cell, range_end;
   double origin[3];
-  uint32_t last_node, tab_bytes, off_dphi;
+  uint32_t last_node, tab_bytes;
   int num_points;
 };
 
 constexpr int kVjpGroup = 4;
+constexpr int kVjpCellsPerWarp = 32 / kVjpGroup;
+
+// Values per contribution row: D, padded to 4 for D = 3 so that rows are 16- or 32-byte aligned.
+__host__ __device__ constexpr int vjp_row(int d) { return d == 3 ? 4 : d; }
+
+// CTAs per SM the register allocation is bounded for: 4 where the kernel fits 128 registers
+// without spills, else 3 (168 registers; the 27-node hexahedron spills a few words there).
+__host__ __device__ constexpr int vjp_min_blocks(bool split, int d, int k) {
+  return d == 2 || k <= 8 || (split && k <= 10) ? 4 : 3;
+}
+
+template <bool SPLIT>
+struct VjpScalar;
+template <>
+struct VjpScalar<true> {
+  using S = float;
+  using V = float2;  // a point pair
+  static constexpr int P = 2;
+  __device__ static void row(const float2* p, float2 (&v)[4]) {
+    const float4 a = reinterpret_cast<const float4*>(p)[0];
+    const float4 b = reinterpret_cast<const float4*>(p)[1];
+    v[0] = make_float2(a.x, a.y);
+    v[1] = make_float2(a.z, a.w);
+    v[2] = make_float2(b.x, b.y);
+    v[3] = make_float2(b.z, b.w);
+  }
+  __device__ static float2 shfl_xor(float2 v, int m) {
+    return make_float2(__shfl_xor_sync(0xFFFFFFFFu, v.x, m), __shfl_xor_sync(0xFFFFFFFFu, v.y, m));
+  }
+};
+template <>
+struct VjpScalar<false> {
+  using S = double;
+  using V = double;
+  static constexpr int P = 1;
+  __device__ static void row(const double* p, double (&v)[4]) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0];
+    const double2 b = reinterpret_cast<const double2*>(p)[1];
+    v[0] = a.x;
+    v[1] = a.y;
+    v[2] = b.x;
+    v[3] = b.y;
+  }
+  __device__ static double shfl_xor(double v, int m) { return __shfl_xor_sync(0xFFFFFFFFu, v, m); }
+};
+
+// Shared memory past the staged table: one slot of 8 cells x K rows of contributions per warp.
+inline size_t vjp_stage_bytes(bool split, int d, int k) {
+  return (size_t)(kEvalThreads / 32) * kVjpCellsPerWarp * k * vjp_row(d) * (split ? 4 : 8);
+}
 
 template <bool SPLIT, int D, int K>
-__global__ void __launch_bounds__(kEvalThreads) vjp_kernel(const __grid_constant__ VjpArgs a) {
-  using F = typename std::conditional<SPLIT, float, double>::type;
-  using A = Ar<F>;
-  using M = Factors<F, D, D>;
+__global__ void __launch_bounds__(kEvalThreads, vjp_min_blocks(SPLIT, D, K))
+    vjp_kernel(const __grid_constant__ VjpArgs a) {
+  using T = VjpScalar<SPLIT>;
+  using S = typename T::S;
+  using V = typename T::V;
+  using A = Ar<V>;
+  using M = Factors<V, D, D>;
+  constexpr int P = T::P;
+  constexpr int G = kVjpGroup;
+  constexpr int NK = (K + G - 1) / G;  // node slots per lane
   constexpr int TILE = 16;
   constexpr int LJ = D * D;
-  constexpr int K0 = SPLIT ? 1 : 0;
+  constexpr int R = vjp_row(D);
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
   stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
-  const F* phi = reinterpret_cast<const F*>(smem);
-  const F* dphi = reinterpret_cast<const F*>(smem + a.off_dphi);
+  const V* tab = reinterpret_cast<const V*>(smem);
+  S* stage = reinterpret_cast<S*>(smem + (a.tab_bytes + 15) / 16 * 16) +
+             (threadIdx.x / 32) * (kVjpCellsPerWarp * K * R);
   const int nq = a.num_points;
+  const int nqv = (nq + P - 1) / P;
   const int lane = threadIdx.x % 32;
-  const int g = threadIdx.x % kVjpGroup;
-  const int gl = g < D ? g : D - 1;  // idle lanes mirror the last coordinate
-  const int group_base = lane & ~(kVjpGroup - 1);
-  const int cells_per_cta = kEvalThreads / kVjpGroup;
-  const F* ctx = static_cast<const F*>(a.ct[0]);
-  const F* ctd = static_cast<const F*>(a.ct[1]);
-  const F* ctk = static_cast<const F*>(a.ct[2]);
+  const int r = lane % G;               // this lane's nodes: k = r + G j, j < nown
+  const int nown = (K - r + G - 1) / G;
+  const int rl = r < D ? r : D - 1;     // the row of the forward fields this lane stores
+  const int slot = lane / G;
+  const int cells_per_cta = kEvalThreads / G;
+  const S* ctx = static_cast<const S*>(a.ct[0]);
+  const S* ctd = static_cast<const S*>(a.ct[1]);
+  const S* ctk = static_cast<const S*>(a.ct[2]);
+  const double* nodes = static_cast<const double*>(a.nodes);
 
-  for (int64_t c = (int64_t)blockIdx.x * cells_per_cta + threadIdx.x / kVjpGroup; c < a.padded;
+  // The trip count is uniform over a warp: padded is a multiple of 16 and a warp's cells are the
+  // 8 consecutive c of one aligned run.
+  for (int64_t c = (int64_t)blockIdx.x * cells_per_cta + threadIdx.x / G; c < a.padded;
        c += (int64_t)gridDim.x * cells_per_cta) {
     const int64_t cell = min(a.first_cell + c, a.last_cell);
-    const bool real = a.first_cell + c < a.range_end;
-    uint32_t idx[K];
-    load_row<K>(a.dofmap + cell * K, idx);
-    F xk[K];
-    F xh = F(0), xl = F(0);
+    const uint32_t* drow = a.dofmap + cell * K;
+    double x0[D];
+#pragma unroll
+    for (int g = 0; g < D; ++g) x0[g] = 0.0;
     if constexpr (SPLIT) {
-      const double* nodes = static_cast<const double*>(a.nodes);
-      const double x0 = __ldg(nodes + (int64_t)min(idx[0], a.last_node) * D + gl);
-      xk[0] = 0.0f;
+      const int64_t n0 = min(__ldg(drow), a.last_node);
 #pragma unroll
-      for (int k = 1; k < K; ++k)
-        xk[k] = __double2float_rn(__ldg(nodes + (int64_t)min(idx[k], a.last_node) * D + gl) - x0);
-      const double v = x0 + a.origin[gl];
-      xh = __double2float_rn(v);
-      xl = __double2float_rn(v - (double)xh);
-    } else {
-      const double* nodes = static_cast<const double*>(a.nodes);
-#pragma unroll
-      for (int k = 0; k < K; ++k) xk[k] = __ldg(nodes + (int64_t)min(idx[k], a.last_node) * D + gl);
-      xh = (F)a.origin[gl];
+      for (int g = 0; g < D; ++g) x0[g] = __ldg(nodes + n0 * D + g);
     }
-    const int64_t o = a.out_first_cell + c;
-    const int64_t tile_idx = o / TILE;
-    const int l16 = (int)(o % TILE);
-    // Element (tile, q, comp, l16) of a tiled field with `len` components:
-    // ((tile * Q + q) * len + comp) * 16 + l16.
-    const int64_t tq = tile_idx * nq;
-#define TLG_AT(q, len, comp) (((tq + (q)) * (len) + (comp)) * TILE + l16)
-    F lacc[K];
+    S xk[NK][D];
 #pragma unroll
-    for (int k = 0; k < K; ++k) lacc[k] = F(0);
+    for (int j = 0; j < NK; ++j) {
+      const bool own = j < nown;
+      const int64_t n = min(__ldg(drow + min(r + G * j, K - 1)), a.last_node);
+#pragma unroll
+      for (int g = 0; g < D; ++g) {
+        const double v = __ldg(nodes + n * D + g);
+        if constexpr (SPLIT) xk[j][g] = own ? __double2float_rn(v - x0[g]) : 0.0f;
+        else xk[j][g] = own ? v : 0.0;
+      }
+    }
+    // Absolute offset of this lane's row: split into two f32 values with SPLIT.
+    double xo = x0[0] + a.origin[0];
+#pragma unroll
+    for (int g = 1; g < D; ++g)
+      if (rl == g) xo = x0[g] + a.origin[g];
+    const S xh = (S)xo;
+    const S xl = SPLIT ? (S)(xo - (double)xh) : S(0);
 
-    for (int q = 0; q < nq; ++q) {
-      const F* dq = dphi + q * K * D;
-      F jr[D];
-#pragma unroll
-      for (int d = 0; d < D; ++d) jr[d] = A::mul(xk[K0], dq[K0 * D + d]);
-#pragma unroll
-      for (int k = K0 + 1; k < K; ++k)
-#pragma unroll
-        for (int d = 0; d < D; ++d) jr[d] = A::fma(xk[k], dq[k * D + d], jr[d]);
-      F j[LJ];
-#pragma unroll
-      for (int gg = 0; gg < D; ++gg)
-#pragma unroll
-        for (int d = 0; d < D; ++d) j[d * D + gg] = __shfl_sync(0xFFFFFFFFu, jr[d], group_base + gg);
-      F kinv[LJ];
-      M::pinv(j, kinv);
-      const F det = M::detj(j);
-      // Row gl of K^T: krow[t] = K(t, gl), selected with compile-time indices (no local memory).
-      F krow[D];
-#pragma unroll
-      for (int t = 0; t < D; ++t) krow[t] = kinv[t];
-#pragma unroll
-      for (int gg = 1; gg < D; ++gg)
-        if (gl == gg)
-#pragma unroll
-          for (int t = 0; t < D; ++t) krow[t] = kinv[gg * D + t];
-      if (g < D) {
-        if (a.out[0]) {
-          const F* w = phi + q * K;
-          F s = A::mul(xk[K0], w[K0]);
-#pragma unroll
-          for (int k = K0 + 1; k < K; ++k) s = A::fma(xk[k], w[k], s);
-          s = SPLIT ? A::add(xh, A::add(xl, s)) : A::add(s, xh);
-          static_cast<F*>(a.out[0])[TLG_AT(q, D, g)] = s;
-        }
-        if (a.out[1])
-#pragma unroll
-          for (int d = 0; d < D; ++d) static_cast<F*>(a.out[1])[TLG_AT(q, LJ, d * D + g)] = jr[d];
-        if (a.out[2] && g == 0) static_cast<F*>(a.out[2])[TLG_AT(q, 1, 0)] = det;
-        if (a.out[3])
-#pragma unroll
-          for (int t = 0; t < D; ++t) static_cast<F*>(a.out[3])[TLG_AT(q, LJ, g * D + t)] = krow[t];
+    const int64_t o = a.out_first_cell + c;
+    const int64_t tq = (o / TILE) * nq;
+    const int l16 = (int)(o % TILE);
+    // Element (tile, q, comp, l16) of a tiled field with `len` components.
+#define TLG_AT(q, len, comp) (((tq + (q)) * (len) + (comp)) * TILE + l16)
+    // Cotangents of step qv (zero for the repeated odd last point of a pair).
+    auto ld = [&](const S* p, int qv, int len, int comp) -> V {
+      if constexpr (SPLIT) {
+        const int q0 = qv * 2;
+        return make_float2(__ldg(p + TLG_AT(q0, len, comp)),
+                           q0 + 1 < nq ? __ldg(p + TLG_AT(q0 + 1, len, comp)) : 0.0f);
+      } else {
+        return __ldg(p + TLG_AT(qv, len, comp));
       }
-      // Jbar(gl, d) = dbar det K(d, gl) - sum_t K(t, gl) M(t, d), M(t, d) = sum_h Kbar(t, h) K(d, h).
-      F jbar[D];
+    };
+    V cx[D], cd, ck[LJ];
+    auto load_ct = [&](int qv) {
 #pragma unroll
-      for (int d = 0; d < D; ++d) jbar[d] = F(0);
-      if (ctd) {
-        const F s = A::mul(__ldg(ctd + TLG_AT(q, 1, 0)), det);
+      for (int g = 0; g < D; ++g) cx[g] = ctx ? ld(ctx, qv, D, g) : A::splat(S(0));
+      cd = ctd ? ld(ctd, qv, 1, 0) : A::splat(S(0));
 #pragma unroll
-        for (int d = 0; d < D; ++d) jbar[d] = A::mul(s, krow[d]);
+      for (int i = 0; i < LJ; ++i) ck[i] = ctk ? ld(ctk, qv, LJ, i) : A::splat(S(0));
+    };
+    load_ct(0);
+    V lacc[NK][D];
+#pragma unroll
+    for (int j = 0; j < NK; ++j)
+#pragma unroll
+      for (int g = 0; g < D; ++g) lacc[j][g] = A::splat(S(0));
+
+    for (int qv = 0; qv < nqv; ++qv) {
+      const V* tv = tab + (int64_t)qv * K * 4;
+      // Partial J(g, d) (at d * D + g) and x(g) over this lane's nodes.
+      V jp[LJ], xp[D];
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) jp[i] = A::splat(S(0));
+#pragma unroll
+      for (int g = 0; g < D; ++g) xp[g] = A::splat(S(0));
+#pragma unroll
+      for (int j = 0; j < NK; ++j) {
+        V t[4];
+        T::row(tv + min(r + G * j, K - 1) * 4, t);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+          for (int g = 0; g < D; ++g) jp[d * D + g] = A::fma(A::splat(xk[j][g]), t[1 + d], jp[d * D + g]);
+        if (a.out[0])
+#pragma unroll
+          for (int g = 0; g < D; ++g) xp[g] = A::fma(A::splat(xk[j][g]), t[0], xp[g]);
       }
-      if (ctk) {
-        F kb[LJ];
 #pragma unroll
-        for (int i = 0; i < LJ; ++i) kb[i] = __ldg(ctk + TLG_AT(q, LJ, i));
+      for (int m = 1; m < G; m *= 2) {
+#pragma unroll
+        for (int i = 0; i < LJ; ++i) jp[i] = A::add(jp[i], T::shfl_xor(jp[i], m));
+        if (a.out[0])
+#pragma unroll
+          for (int g = 0; g < D; ++g) xp[g] = A::add(xp[g], T::shfl_xor(xp[g], m));
+      }
+      V kinv[LJ];
+      M::pinv(jp, kinv);
+      const V det = M::detj(jp);
+      if (r < D) {
+        // Row rl of x, J and K^T, selected with compile-time indices (no local memory).
+        V xr = xp[0], jr[D], kr[D];
 #pragma unroll
         for (int d = 0; d < D; ++d) {
-          F acc = jbar[d];
-#pragma unroll
-          for (int t = 0; t < D; ++t) {
-            F m = A::mul(kb[t], kinv[d]);  // Kbar(t, 0) K(d, 0); K(t, h) at h * D + t
-#pragma unroll
-            for (int h = 1; h < D; ++h) m = A::fma(kb[h * D + t], kinv[h * D + d], m);
-            acc = A::fma(A::neg(krow[t]), m, acc);
-          }
-          jbar[d] = acc;
+          jr[d] = jp[d * D];
+          kr[d] = kinv[d];
         }
+#pragma unroll
+        for (int g = 1; g < D; ++g)
+          if (rl == g) {
+            xr = xp[g];
+#pragma unroll
+            for (int d = 0; d < D; ++d) {
+              jr[d] = jp[d * D + g];
+              kr[d] = kinv[g * D + d];
+            }
+          }
+        auto st = [&](void* p, int len, int comp, V v) {
+          S* f = static_cast<S*>(p);
+          if constexpr (SPLIT) {
+            f[TLG_AT(2 * qv, len, comp)] = v.x;
+            if (2 * qv + 1 < nq) f[TLG_AT(2 * qv + 1, len, comp)] = v.y;
+          } else {
+            f[TLG_AT(qv, len, comp)] = v;
+          }
+        };
+        if (a.out[0])
+          st(a.out[0], D, rl,
+             SPLIT ? A::add(A::splat(xh), A::add(A::splat(xl), xr)) : A::add(xr, A::splat(xh)));
+        if (a.out[1])
+#pragma unroll
+          for (int d = 0; d < D; ++d) st(a.out[1], LJ, d * D + rl, jr[d]);
+        if (a.out[2] && r == 0) st(a.out[2], 1, 0, det);
+        if (a.out[3])
+#pragma unroll
+          for (int t = 0; t < D; ++t) st(a.out[3], LJ, rl * D + t, kr[t]);
       }
-      F xb = F(0);
-      if (ctx) xb = __ldg(ctx + TLG_AT(q, D, gl));
-      const F* w = phi + q * K;
+      // Jbar(g, d) at g * D + d: dbar det K(d, g) - sum_t K(t, g) Mt(t, d), with
+      // Mt(t, d) = sum_h Kbar(t, h) K(d, h); K(t, h) and Kbar(t, h) at h * D + t.
+      V jb[LJ];
+      const V s = A::mul(cd, det);
 #pragma unroll
-      for (int k = 0; k < K; ++k) {
-        F acc = A::fma(w[k], xb, lacc[k]);
+      for (int g = 0; g < D; ++g)
 #pragma unroll
-        for (int d = 0; d < D; ++d) acc = A::fma(jbar[d], dq[k * D + d], acc);
-        lacc[k] = acc;
+        for (int d = 0; d < D; ++d) jb[g * D + d] = A::mul(s, kinv[g * D + d]);
+#pragma unroll
+      for (int t = 0; t < D; ++t)
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          V mt = A::mul(ck[t], kinv[d]);
+#pragma unroll
+          for (int h = 1; h < D; ++h) mt = A::fma(ck[h * D + t], kinv[h * D + d], mt);
+#pragma unroll
+          for (int g = 0; g < D; ++g) jb[g * D + d] = A::fma(A::neg(kinv[g * D + t]), mt, jb[g * D + d]);
+        }
+      // The next step's cotangents load while this step's contributions are accumulated.
+      V xb[D];
+#pragma unroll
+      for (int g = 0; g < D; ++g) xb[g] = cx[g];
+      if (qv + 1 < nqv) load_ct(qv + 1);
+#pragma unroll
+      for (int j = 0; j < NK; ++j) {
+        V t[4];
+        T::row(tv + min(r + G * j, K - 1) * 4, t);
+#pragma unroll
+        for (int g = 0; g < D; ++g) {
+          V acc = A::fma(t[0], xb[g], lacc[j][g]);
+#pragma unroll
+          for (int d = 0; d < D; ++d) acc = A::fma(jb[g * D + d], t[1 + d], acc);
+          lacc[j][g] = acc;
+        }
       }
     }
 #undef TLG_AT
-    if (real && g < D) {
-      F* loc = static_cast<F*>(a.local);
+    // Stage the group's contributions; the warp then writes its cells' rows as one run of
+    // 16-byte (8-byte for 2D f32 rows) stores.
 #pragma unroll
-      for (int k = 0; k < K; ++k) loc[((int64_t)k * D + g) * a.local_stride + cell] = lacc[k];
+    for (int j = 0; j < NK; ++j)
+      if (j < nown)
+#pragma unroll
+        for (int g = 0; g < R; ++g) {
+          S v = S(0);
+          if (g < D) {
+            if constexpr (SPLIT) v = __fadd_rn(lacc[j][g].x, lacc[j][g].y);
+            else v = lacc[j][g];
+          }
+          stage[(slot * K + r + G * j) * R + g] = v;
+        }
+    __syncwarp();
+    const int64_t cell0 = __shfl_sync(0xFFFFFFFFu, a.first_cell + c, 0);
+    const int64_t nreal = min((int64_t)kVjpCellsPerWarp, a.range_end - cell0);
+    if (nreal > 0) {
+      using U = typename std::conditional<(R * sizeof(S)) % 16 == 0, uint4, uint2>::type;
+      constexpr int UPR = (int)(R * sizeof(S) / sizeof(U));  // units per row
+      const U* src = reinterpret_cast<const U*>(stage);
+      U* dst = reinterpret_cast<U*>(static_cast<S*>(a.local) + cell0 * (K * R));
+      for (int i = lane; i < nreal * (K * UPR); i += 32) dst[i] = src[i];
     }
+    __syncwarp();
   }
 }
 
-// gbar(n, g) = sum over the CSR entries e of node n, in entry order, of L(e / K, e % K, g), in f64.
+// One contribution row (R values of L) as one vector value.
+template <typename L, int R>
+struct VjpRow;
+template <>
+struct VjpRow<float, 4> {
+  using T = float4;
+  __device__ static T load(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+  __device__ static float get(const T& v, int g) { return g == 0 ? v.x : g == 1 ? v.y : v.z; }
+};
+template <>
+struct VjpRow<float, 2> {
+  using T = float2;
+  __device__ static T load(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
+  __device__ static float get(const T& v, int g) { return g == 0 ? v.x : v.y; }
+};
+template <>
+struct VjpRow<double, 4> {
+  struct T {
+    double2 a, b;
+  };
+  __device__ static T load(const double* p) {
+    return {__ldg(reinterpret_cast<const double2*>(p)), __ldg(reinterpret_cast<const double2*>(p) + 1)};
+  }
+  __device__ static double get(const T& v, int g) { return g == 0 ? v.a.x : g == 1 ? v.a.y : v.b.x; }
+};
+template <>
+struct VjpRow<double, 2> {
+  using T = double2;
+  __device__ static T load(const double* p) { return __ldg(reinterpret_cast<const double2*>(p)); }
+  __device__ static double get(const T& v, int g) { return g == 0 ? v.x : v.y; }
+};
+template <typename L>
+struct VjpRow<L, 1> {
+  using T = L;
+  __device__ static T load(const L* p) { return __ldg(p); }
+  __device__ static L get(const T& v, int) { return v; }
+};
+
+// gbar(n, g) = sum over the CSR entries e of node n, in entry order, of local[e * R + g], in f64.
+// Entries are read four at a time so that their loads overlap; the sum stays in entry order.
 template <typename L, int D>
-__global__ void __launch_bounds__(256) vjp_gather_kernel(const uint32_t* offsets, const uint32_t* entries,
-                                                         int64_t num_nodes, int K, const L* local,
-                                                         int64_t local_stride, double* grad) {
+__global__ void __launch_bounds__(256, 4) vjp_gather_kernel(const uint32_t* offsets, const uint32_t* entries,
+                                                         int64_t num_nodes, const L* local, double* grad) {
+  constexpr int R = vjp_row(D);
+  using Row = VjpRow<L, R>;
   for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < num_nodes;
        n += (int64_t)gridDim.x * blockDim.x) {
     double acc[D];
 #pragma unroll
     for (int g = 0; g < D; ++g) acc[g] = 0.0;
-    const uint32_t b = offsets[n], e = offsets[n + 1];
-    for (uint32_t i = b; i < e; ++i) {
-      const uint32_t ent = entries[i];
-      const int64_t cell = ent / (uint32_t)K;
-      const int k = (int)(ent - (uint32_t)cell * (uint32_t)K);
+    const uint32_t b = __ldg(offsets + n), e = __ldg(offsets + n + 1);
+    uint32_t i = b;
+    for (; i + 4 <= e; i += 4) {
+      typename Row::T v[4];
 #pragma unroll
-      for (int g = 0; g < D; ++g) acc[g] += (double)local[((int64_t)k * D + g) * local_stride + cell];
+      for (int u = 0; u < 4; ++u) v[u] = Row::load(local + (int64_t)__ldg(entries + i + u) * R);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int g = 0; g < D; ++g) acc[g] += (double)Row::get(v[u], g);
+    }
+    for (; i < e; ++i) {
+      const typename Row::T v = Row::load(local + (int64_t)__ldg(entries + i) * R);
+#pragma unroll
+      for (int g = 0; g < D; ++g) acc[g] += (double)Row::get(v, g);
     }
 #pragma unroll
     for (int g = 0; g < D; ++g) grad[n * D + g] = acc[g];

@@ -495,8 +495,7 @@ def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: s
         f: QuadField.uninit(blk.num_cells, nq, FACTOR_LEN[f](td, gd), GPU_QUAD_TILE, fdt, dev)
         for f in forward}
     if local is None:
-        local = torch.empty((k, gd, max(blk.num_cells, 1)), dtype=fdt, device=dev)
-    stride = local.shape[2]
+        local = torch.empty((max(blk.num_cells, 1), k, 4 if gd == 3 else gd), dtype=fdt, device=dev)
     ct = TlgCotangents()
     for name in ("points", "detj", "pinv"):
         f = cotangents.get(name)
@@ -511,12 +510,11 @@ def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: s
     desc = g.block_desc(b)
     stream = current_stream_handle()
     check(lib().tlg_vjp_block(tables.handle, ctypes.byref(desc), ctypes.byref(o), ctypes.byref(ct),
-                              local.data_ptr(), stride, stream))
+                              local.data_ptr(), local.shape[0], stream))
     inc = node_incidence(g, b)
     grad = torch.empty((g.nodes.shape[0], gd), dtype=torch.float64, device=dev)
-    check(lib().tlg_vjp_gather(inc.offsets.data_ptr(), inc.entries.data_ptr(), g.nodes.shape[0], k, gd,
-                               local.data_ptr(), 4 if fdt == torch.float32 else 8, stride,
-                               grad.data_ptr(), stream))
+    check(lib().tlg_vjp_gather(inc.offsets.data_ptr(), inc.entries.data_ptr(), g.nodes.shape[0], gd,
+                               local.data_ptr(), 4 if fdt == torch.float32 else 8, grad.data_ptr(), stream))
     return grad, fields
 
 

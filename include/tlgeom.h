@@ -216,21 +216,24 @@ typedef struct tlg_cotangents {
 } tlg_cotangents;
 
 /* Per-cell contributions to the node cotangents of a codimension-0 block range (TD = GD),
- * J, det J and K recomputed: local[(k * GD + g) * local_stride + cell] = sum_q phi_k(q) xbar(q, g)
- * + sum_d Jbar(q)(g, d) dphi_k(q)[d], Jbar = dbar det J K^T - K^T Kbar K^T. With TLG_F64 tables
- * everything is f64; with TLG_SPLIT32 tables the mesh is f64, the arithmetic FP32 on cell-shifted
- * coordinates, and cotangents, contributions and any forward fields are f32. Forward pointers set
- * in `outputs` (points, jacobian, detj, pinv) are written in the same pass (fused forward +
- * adjoint); outputs->tile must be 16. */
+ * J, det J and K recomputed: local[(cell * K + k) * R + g] = sum_q phi_k(q) xbar(q, g)
+ * + sum_d Jbar(q)(g, d) dphi_k(q)[d], Jbar = dbar det J K^T - K^T Kbar K^T, for the cells of the
+ * range (cell = block cell index; rows of R = 4 values for GD = 3, the fourth zero, else R = GD;
+ * local holds local_cells >= block->num_cells cells, 16-byte aligned). With
+ * TLG_F64 tables everything is f64; with TLG_SPLIT32 tables the mesh is f64, the arithmetic FP32
+ * on cell-shifted coordinates, and cotangents, contributions and any forward fields are f32.
+ * Forward pointers set in `outputs` (points, jacobian, detj, pinv) are written in the same pass
+ * (fused forward + adjoint; no FP64 recompute of ill-conditioned points there);
+ * outputs->tile must be 16. */
 tlg_status tlg_vjp_block(const tlg_tables* tables, const tlg_block* block, const tlg_outputs* outputs,
-                         const tlg_cotangents* cotangents, void* local, int64_t local_stride,
+                         const tlg_cotangents* cotangents, void* local, int64_t local_cells,
                          void* stream);
 
-/* grad[n * gdim + g] = sum over node n's CSR entries, in entry order, of the contributions, in
- * f64 (local_dtype 4 or 8 is the contributions' type). Deterministic. */
+/* grad[n * gdim + g] = sum over node n's CSR entries e, in entry order, of local[e * R + g]
+ * (R as in tlg_vjp_block), in f64 (local_dtype 4 or 8 is the contributions' type).
+ * Deterministic. */
 tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes,
-                          int nodes_per_cell, int gdim, const void* local, int local_dtype,
-                          int64_t local_stride, double* grad, void* stream);
+                          int gdim, const void* local, int local_dtype, double* grad, void* stream);
 
 /* ---------------------------------------------------------------------------------------
  * Measure (tetraloma-geometry/src/measure.rs:15-185): per-cell sums of det J * w over the

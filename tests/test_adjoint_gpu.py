@@ -41,10 +41,10 @@ def test_csr_with_unused_and_clamped_nodes(cuda):
     assert np.array_equal(inc.entries.cpu().numpy().view(np.uint32), entries)
 
 
-def cotangent_fields(rng, ncells, nq, dtype):
+def cotangent_fields(rng, ncells, nq, dtype, gd=3):
     """Seeded standard-normal cotangents as tile-16 fields, with their cell-major copies."""
     out, host = {}, {}
-    for name, length in (("points", 3), ("detj", 1), ("pinv", 9)):
+    for name, length in (("points", gd), ("detj", 1), ("pinv", gd * gd)):
         f = tg.QuadField.uninit(ncells, nq, length, 16, dtype)
         vals = rng.standard_normal(f.chunks[0].data.numel())
         f.chunks[0].data.copy_(torch.from_numpy(vals).to(dtype))
@@ -54,16 +54,18 @@ def cotangent_fields(rng, ncells, nq, dtype):
 
 
 @pytest.mark.parametrize("cell,n,degree,rdeg", [("Tetrahedron", 3, 2, 4), ("Hexahedron", 3, 2, 4),
-                                                ("Tetrahedron", 2, 3, 6), ("Prism", 2, 2, 4)])
+                                                ("Tetrahedron", 2, 3, 6), ("Prism", 2, 2, 4),
+                                                ("Hexahedron", 2, 1, 3), ("Quadrilateral", 4, 2, 3),
+                                                ("Triangle", 5, 3, 4)])
 def test_vjp_matches_the_oracle(cuda, cell, n, degree, rdeg):
-    mesh = meshes.curved_box(cell, n, degree, jitter=0.02)
+    mesh = jittered_box(cell, n, degree)
     g = tg.Geometry.from_host(mesh, dtype=torch.float64)
     pts, _ = tg.refcell.gauss_rule(cell, rdeg)
     ps = tg.PointSet(cell, pts, np.ones(len(pts)))
     ncells = mesh.blocks[0].num_cells
     rng = np.random.default_rng(7)
-    ct64, host = cotangent_fields(rng, ncells, len(pts), torch.float64)
-    absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
+    ct64, host = cotangent_fields(rng, ncells, len(pts), torch.float64, g.gdim)
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[: g.gdim])
     want = orc.vjp(cell, degree, absx, mesh.blocks[0].cells, pts, host["points"],
                    host["detj"][..., 0], host["pinv"])
     got, _ = tg.vjp_block(g, 0, ps, ct64)
@@ -80,19 +82,38 @@ def test_vjp_matches_the_oracle(cuda, cell, n, degree, rdeg):
     assert orc.rel_err(got32.cpu().numpy(), want32) < 2e-5
 
 
+def jittered_box(cell, n, degree):
+    """The curved unit cube, or for 2D cells the unit square with interior nodes jittered."""
+    if cell in ("Quadrilateral", "Triangle"):
+        m = meshes.square_box(cell, n, degree)
+        m.nodes = meshes.jitter_interior(m.nodes, m.nodes, 0.02 / n, 2026)
+        return m
+    return meshes.curved_box(cell, n, degree, jitter=0.02)
+
+
 @pytest.mark.parametrize("precision", ["native", "split"])
-def test_fused_forward_equals_the_forward_kernels(cuda, precision):
-    mesh = meshes.curved_box("Hexahedron", 3, 2, jitter=0.02)
+@pytest.mark.parametrize("cell,n,degree,rdeg", [("Hexahedron", 3, 2, 4), ("Tetrahedron", 3, 3, 5),
+                                                ("Quadrilateral", 5, 2, 3), ("Triangle", 4, 1, 2)])
+def test_fused_forward_matches_the_forward_kernels(cuda, precision, cell, n, degree, rdeg):
+    """The fused forward sums J over the four lanes of a cell (a butterfly), the forward kernels
+    over the nodes in order: equal to rounding, and both within tolerance of the oracle."""
+    mesh = jittered_box(cell, n, degree)
     g = tg.Geometry.from_host(mesh, dtype=torch.float64)
-    pts, _ = tg.refcell.gauss_rule("Hexahedron", 4)
-    ps = tg.PointSet("Hexahedron", pts, np.ones(len(pts)))
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
     dt = torch.float64 if precision == "native" else torch.float32
-    ct, _ = cotangent_fields(np.random.default_rng(3), mesh.blocks[0].num_cells, len(pts), dt)
+    ct, _ = cotangent_fields(np.random.default_rng(3), mesh.blocks[0].num_cells, len(pts), dt, g.gdim)
     names = ("points", "jacobian", "detj", "pinv")
     _, fused = tg.vjp_block(g, 0, ps, ct, precision=precision, forward=names)
     plain = tg.geometric_factors_block(g, 0, ps, names, precision=precision)
-    for k in names:
-        assert torch.equal(fused[k].chunks[0].data, plain[k].chunks[0].data), k
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[: g.gdim])
+    want = orc.eval_block(cell, degree, absx, mesh.blocks[0].cells, pts)
+    tight = 1e-14 if precision == "native" else 2e-6
+    loose = 1e-12 if precision == "native" else 1e-5
+    for k, o in zip(names, ("x", "j", "detj", "k")):
+        f = fused[k].to_host_cell_major()
+        assert orc.rel_err(f, plain[k].to_host_cell_major()) < tight, k
+        assert orc.rel_err(f, want[o]) < loose, k
 
 
 def test_vjp_against_central_differences(cuda):
