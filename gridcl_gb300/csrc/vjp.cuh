@@ -371,36 +371,89 @@ struct VjpRow<L, 1> {
   __device__ static L get(const T& v, int) { return v; }
 };
 
-// gbar(n, g) = sum over the CSR entries e of node n, in entry order, of local[e * R + g], in f64.
-// Entries are read four at a time so that their loads overlap; the sum stays in entry order.
+// f32 -> f64 by exponent rebias in integer operations: exact for zero and normal numbers, which
+// are what the FP64 pipe (2 lanes per clock per SM on this part) is spared; subnormal, infinite
+// and NaN values take the conversion instruction.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xFFu;
+  const uint64_t sign = (uint64_t)(b >> 31) << 63;
+  if ((b << 1) == 0u) return __longlong_as_double((long long)sign);
+  if (e == 0u || e == 0xFFu) return (double)f;
+  return __longlong_as_double(
+      (long long)(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7FFFFFu) << 29)));
+}
+
+// A node's running sum of f32 contributions: f64 adds for f64 rows; for f32 rows an unevaluated
+// pair hi + lo kept by TwoSum (Knuth) in FP32, whose error per add is captured exactly, so the
+// FP64 pipe sees one add per coordinate and node instead of a conversion and an add per entry.
+template <typename L>
+struct GatherSum {
+  double s = 0.0;
+  __device__ __forceinline__ void add(L x) { s = __dadd_rn(s, x); }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct GatherSum<float> {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float s = __fadd_rn(hi, x);
+    const float bv = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bv)), __fsub_rn(x, bv));
+    hi = s;
+    lo = __fadd_rn(lo, err);
+  }
+  __device__ __forceinline__ double value() const { return __dadd_rn(f2d_exact(hi), f2d_exact(lo)); }
+};
+
+// gbar(n, g) = sum over the CSR entries e of node n, in entry order, of local[e * R + g]: in f64
+// for f64 rows, as an FP32 TwoSum pair rounded once to f64 for f32 rows.
+// A CTA owns 256 consecutive nodes, whose entries are contiguous in the CSR: all its threads
+// load the rows of up to 1024 of those entries at a time into shared memory (independent
+// vector loads, so many are in flight), then the thread of each node adds the rows of its own
+// entries in order. The sums, and their order, do not depend on the launch shape.
+constexpr int kGatherNodes = 256;
+constexpr int kGatherChunk = 1024;
+
 template <typename L, int D>
-__global__ void __launch_bounds__(256, 4) vjp_gather_kernel(const uint32_t* offsets, const uint32_t* entries,
-                                                         int64_t num_nodes, const L* local, double* grad) {
+__global__ void __launch_bounds__(kGatherNodes) vjp_gather_kernel(const uint32_t* offsets, const uint32_t* entries,
+                                                                  int64_t num_nodes, const L* local, double* grad) {
   constexpr int R = vjp_row(D);
   using Row = VjpRow<L, R>;
-  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < num_nodes;
-       n += (int64_t)gridDim.x * blockDim.x) {
-    double acc[D];
-#pragma unroll
-    for (int g = 0; g < D; ++g) acc[g] = 0.0;
-    const uint32_t b = __ldg(offsets + n), e = __ldg(offsets + n + 1);
-    uint32_t i = b;
-    for (; i + 4 <= e; i += 4) {
-      typename Row::T v[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) v[u] = Row::load(local + (int64_t)__ldg(entries + i + u) * R);
-#pragma unroll
-      for (int u = 0; u < 4; ++u)
-#pragma unroll
-        for (int g = 0; g < D; ++g) acc[g] += (double)Row::get(v[u], g);
+  __shared__ typename Row::T rows[kGatherChunk];
+  for (int64_t n0 = (int64_t)blockIdx.x * kGatherNodes; n0 < num_nodes; n0 += (int64_t)gridDim.x * kGatherNodes) {
+    const int64_t n = n0 + threadIdx.x;
+    const int64_t n_end = min(n0 + kGatherNodes, num_nodes);
+    const uint32_t e0 = offsets[n0], e1 = offsets[n_end];
+    uint32_t b = 0, e = 0;
+    if (n < num_nodes) {
+      b = offsets[n];
+      e = offsets[n + 1];
     }
-    for (; i < e; ++i) {
-      const typename Row::T v = Row::load(local + (int64_t)__ldg(entries + i) * R);
+    GatherSum<L> acc[D];
+    for (uint32_t c = e0; c < e1; c += kGatherChunk) {
+      const uint32_t cn = min((uint32_t)kGatherChunk, e1 - c);
+      uint32_t ent[kGatherChunk / kGatherNodes];
 #pragma unroll
-      for (int g = 0; g < D; ++g) acc[g] += (double)Row::get(v, g);
+      for (int u = 0; u < kGatherChunk / kGatherNodes; ++u) {
+        const uint32_t i = threadIdx.x + kGatherNodes * u;
+        ent[u] = i < cn ? entries[c + i] : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < kGatherChunk / kGatherNodes; ++u) {
+        const uint32_t i = threadIdx.x + kGatherNodes * u;
+        if (i < cn) rows[i] = Row::load(local + (int64_t)ent[u] * R);
+      }
+      __syncthreads();
+      const uint32_t lo = max(b, c), hi = min(e, c + cn);
+      for (uint32_t i = lo; i < hi; ++i)
+#pragma unroll
+        for (int g = 0; g < D; ++g) acc[g].add(Row::get(rows[i - c], g));
+      __syncthreads();
     }
+    if (n < num_nodes)
 #pragma unroll
-    for (int g = 0; g < D; ++g) grad[n * D + g] = acc[g];
+      for (int g = 0; g < D; ++g) grad[n * D + g] = acc[g].value();
   }
 }
 

@@ -230,8 +230,9 @@ tlg_status tlg_vjp_block(const tlg_tables* tables, const tlg_block* block, const
                          void* stream);
 
 /* grad[n * gdim + g] = sum over node n's CSR entries e, in entry order, of local[e * R + g]
- * (R as in tlg_vjp_block), in f64 (local_dtype 4 or 8 is the contributions' type).
- * Deterministic. */
+ * (R as in tlg_vjp_block; local_dtype 4 or 8 is the contributions' type): f64 sums of f64
+ * contributions; f32 contributions summed as an FP32 TwoSum pair (about 48 significant bits)
+ * rounded once to f64. Deterministic. */
 tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes,
                           int gdim, const void* local, int local_dtype, double* grad, void* stream);
 
