@@ -41,6 +41,13 @@ WORKLOAD = "curved P2 tetrahedra 64^3x6, 24-point rule, fused x/J/detJ/K"
 # have m^3 points; its nearest, gauss_rule(Tet, 4), has 27).
 RULE_COUNTS = (4, 3, 2)
 METRIC = "Jacobian qpoints/s (fwd, fwd+adjoint) vs plain FP64 GPU path at stated error"
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the evaluation
+# kernel on the 64^3 workload, measured on a GB300 by one-pass ncu captures of
+# `bench.py --no-extras --no-cpu-baseline --steps 3 --warmup 3 [--mode f64]` (-s 3 -c 1):
+# split eval_pair_kernel<1,3,3,10> 191.07 MB + 3.26 GB; f64 eval_direct_kernel<double,3,3,10,16>
+# 166.22 MB + 6.58 GB. Reported as roofline.traffic, scaled by quadrature points for other n.
+NCU_TRAFFIC_64 = {"split": 191.07e6 + 3.26e9, "f64": 166.22e6 + 6.58e9}
+QPOINTS_64 = 64 ** 3 * 6 * 24
 
 
 def parse():
@@ -54,6 +61,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the other workloads (hybrid batch, sphere surface, Q2 adjoint, P1 box)")
+    p.add_argument("--workload", choices=["main", *EXTRAS], default="main",
+                   help="run one of the other workloads alone and print its JSON object")
+    p.add_argument("--adjoint-n", type=int, default=128, help="Q2 hexahedra per direction (adjoint)")
     return p.parse_args()
 
 
@@ -198,6 +208,15 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def gpu_hold(ms: float = 1.0):
+    """Keeps the stream busy for about `ms` (a device spin) so that the host enqueues what follows
+    before the GPU reaches it: events recorded next then bracket device work only, not the host's
+    launch overhead."""
+    import torch
+
+    torch.cuda._sleep(int(ms * 2.0e6))
+
+
 def time_steps(step, steps, flush, stream):
     """CUDA-event time of each step (L2 flushed before each, outside the events); mean ms."""
     import torch
@@ -206,6 +225,7 @@ def time_steps(step, steps, flush, stream):
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     for i in range(steps):
         flush.zero_()
+        gpu_hold()
         starts[i].record(stream)
         step()
         ends[i].record(stream)
@@ -225,6 +245,7 @@ def event_ms(fn, reps: int = 5, warm: int = 2) -> float:
         fn()
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    gpu_hold(2.0)
     a.record()
     for _ in range(reps):
         fn()
@@ -317,9 +338,9 @@ def extra_sphere():
                       "rel_err_vs_fp64": rel_err_fields(split, f64)}}
 
 
-def extra_adjoint():
-    """Forward + adjoint: 128^3 Q2 hexahedra, 27-point Gauss, seeded standard-normal cotangents on
-    det J and K; the fused split-precision forward + vjp (+ f64 node sums) against the plain FP64
+def extra_adjoint(n: int = 128):
+    """Forward + adjoint: n^3 Q2 hexahedra, 27-point Gauss, seeded standard-normal cotangents on
+    det J and K; the fused split-precision forward + vjp (+ node sums) against the plain FP64
     forward followed by the FP64 vjp; central differences (step 1e-6) at 1,000 seeded nodes."""
     import numpy as np
     import torch
@@ -327,7 +348,7 @@ def extra_adjoint():
     import gridcl_gb300 as tg
     from gridcl_gb300 import meshes, refcell
 
-    mesh = meshes.curved_box("Hexahedron", 128, 2, jitter=0.02, seed=2026)
+    mesh = meshes.curved_box("Hexahedron", n, 2, jitter=0.02, seed=2026)
     g = tg.Geometry.from_host(mesh, dtype=torch.float64)
     ps = tg.PointSet("Hexahedron", *refcell.gauss_rule("Hexahedron", 4))
     ncells, nq = mesh.blocks[0].num_cells, len(ps)
@@ -367,7 +388,7 @@ def extra_adjoint():
     # in, contributions out and back in through the CSR, node cotangents out.
     alg = (qpts * 10 * 4 + qpts * 22 * 4 + ncells * 27 * 4 + g.nodes.numel() * 8
            + 2 * ncells * 27 * 3 * 4 + g.nodes.numel() * 8 + (ncells * 27 + g.nodes.shape[0]) * 4)
-    return {"workload": "Q2 hex 128^3, 27 pts, forward (x/J/detJ/K) + adjoint from detJ and K cotangents",
+    return {"workload": f"Q2 hex {n}^3, 27 pts, forward (x/J/detJ/K) + adjoint from detJ and K cotangents",
             "qpoints": int(qpts),
             "plain_fp64_fwd_then_vjp": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3)},
             "fused_split_fwd_vjp": {"ms": fused_ms, "value": qpts / (fused_ms * 1e-3),
@@ -524,7 +545,9 @@ def run_ours(args):
                        "l2": "256 MiB flush between steps (outside the timed events); outputs exceed L2",
                        "parallelism": f"replicas x{world}"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
+                         "frac": achieved / peak,
+                         "traffic": (NCU_TRAFFIC_64[args.mode] * qpts / QPOINTS_64
+                                     if args.mode in NCU_TRAFFIC_64 else None),
                          "algorithmic_bytes_per_launch": alg,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in peaks else "fallback 6800"},
             "e2e": {"value": world * qpts / (e2e_ms * 1e-3), "unit": "qpoints/s",
@@ -539,7 +562,8 @@ def run_ours(args):
         if not args.no_extras and world == 1:
             workloads = {}
             for name, fn in (("hybrid_batched", extra_hybrid), ("sphere_surface", extra_sphere),
-                             ("q2_forward_adjoint", extra_adjoint), ("p1_box", extra_p1_box)):
+                             ("q2_forward_adjoint", lambda: extra_adjoint(args.adjoint_n)),
+                             ("p1_box", extra_p1_box)):
                 try:
                     workloads[name] = fn()
                 except Exception as exc:  # reported, not fatal: the main line stands
@@ -577,10 +601,25 @@ def measure_of(tg, g, ps, detj):
     return float(res.item())
 
 
+EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "p1_box")
+
+
+def run_extra(args):
+    """One of the other workloads alone (for profiling): its JSON object on one line."""
+    import torch
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    fn = {"hybrid_batched": extra_hybrid, "sphere_surface": extra_sphere,
+          "q2_forward_adjoint": lambda: extra_adjoint(args.adjoint_n), "p1_box": extra_p1_box}[args.workload]
+    print(json.dumps(fn()), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "main":
+        run_extra(args)
     else:
         run_ours(args)
 

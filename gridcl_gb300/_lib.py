@@ -107,6 +107,7 @@ SIGNATURES = [
     ("tlg_sum", _I, [_P, _I, _L, _P, _L, _P, _P]),
     ("tlg_measure_static", _I, [_P, _I, _L, _L, _I, _P, _P, _P]),
     ("tlg_measure_static_max_cells", _L, []),
+    ("tlg_selftest_conversions", _I, [_P, _L, _P, _P]),
 ]
 
 _lib = None

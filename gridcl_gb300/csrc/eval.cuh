@@ -31,6 +31,8 @@
 
 #include <cuda_runtime.h>
 
+#include "convert.cuh"
+
 namespace tlg {
 
 constexpr int kEvalThreads = 128;
@@ -67,7 +69,6 @@ struct EvalArgs {
   int num_points;            // Q
   int tile_shift;            // log2(tile)
   int k_runtime;             // K for the loops kernel
-  uint32_t tab_base;         // offset of these tables in a batch's staged tables (0 alone)
 };
 
 // Arguments of the paired kernels (f32 arithmetic; nodes f32, or f64 with SPLIT).
@@ -84,7 +85,6 @@ struct PairArgs {
   float cond_limit;
   uint32_t last_node, tab_bytes, off_refn, off_phi2, off_dphi2, off_dphi64, mask;
   int num_points;
-  uint32_t tab_base;  // offset of these tables in a batch's staged tables (0 alone)
 };
 
 // ----------------------------------------------------------------------------------------
@@ -468,13 +468,13 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
       for (int k = 1; k < K; ++k) {
         const uint32_t n = min(idx[k], a.last_node);
 #pragma unroll
-        for (int g = 0; g < GD; ++g) x[k][g] = __double2float_rn(__ldg(nodes + (int64_t)n * GD + g) - x0[g]);
+        for (int g = 0; g < GD; ++g) x[k][g] = d2f_rn(__ldg(nodes + (int64_t)n * GD + g) - x0[g]);
       }
 #pragma unroll
       for (int g = 0; g < GD; ++g) {
         const double v = x0[g] + a.origin[g];
-        xh[g] = __double2float_rn(v);
-        xl[g] = __double2float_rn(v - (double)xh[g]);
+        xh[g] = d2f_rn(v);
+        xl[g] = d2f_rn(v - f2d_exact(xh[g]));
       }
     } else {
       const float* nodes = static_cast<const float*>(a.nodes);

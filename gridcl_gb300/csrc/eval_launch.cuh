@@ -23,10 +23,27 @@ inline int persistent_grid(Kernel kern, size_t smem, int64_t work_items, int thr
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (sms <= 0) sms = 1;
   }
+  // Resident CTAs per SM, queried once per (kernel, shared memory, threads) on this thread.
+  struct Entry {
+    const void* kern;
+    size_t smem;
+    int threads, per_sm;
+  };
+  static thread_local Entry cache[64];
+  static thread_local int cached = 0;
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess ||
-      per_sm < 1)
-    per_sm = 1;
+  for (int i = 0; i < cached; ++i)
+    if (cache[i].kern == (const void*)kern && cache[i].smem == smem && cache[i].threads == threads) {
+      per_sm = cache[i].per_sm;
+      break;
+    }
+  if (per_sm == 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    cache[cached % 64] = {(const void*)kern, smem, threads, per_sm};
+    if (cached < 64) ++cached;
+  }
   const int64_t need = (work_items + threads - 1) / threads;
   const int64_t cap = (int64_t)sms * per_sm;
   return (int)(need < cap ? (need > 0 ? need : 1) : cap);

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/tlgeom.h"
+#include "convert.cuh"
 #include "status.h"
 
 namespace tlg {
@@ -249,3 +250,38 @@ tlg_status tlg_measure_static(const void* detj, int dtype, int64_t num_cells, in
 }
 
 }  // extern "C"
+
+// ----------------------------------------------------------------------------------------
+// Self-test of the integer conversions used by the split kernels.
+
+namespace {
+
+__global__ void conversions_kernel(const double* x, int64_t n, unsigned long long* mismatches) {
+  unsigned long long bad_round = 0, bad_widen = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float want = __double2float_rn(v);
+    const float got = tlg::d2f_rn(v);
+    const bool nan = want != want;
+    if (nan ? got == got : __float_as_uint(got) != __float_as_uint(want)) ++bad_round;
+    const double w = (double)want;
+    const double wg = tlg::f2d_exact(want);
+    if (nan ? wg == wg : __double_as_longlong(wg) != __double_as_longlong(w)) ++bad_widen;
+  }
+  if (bad_round) atomicAdd(mismatches, bad_round);
+  if (bad_widen) atomicAdd(mismatches + 1, bad_widen);
+}
+
+}  // namespace
+
+tlg_status tlg_selftest_conversions(const double* x, int64_t n, unsigned long long* mismatches, void* stream) {
+  if (n < 0 || !mismatches || (n > 0 && !x))
+    return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_selftest_conversions: bad arguments");
+  if (n == 0) return tlg::ok();
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  conversions_kernel<<<(unsigned)blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(x, n, mismatches);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return tlg::cuda_fail(e, "tlg_selftest_conversions launch");
+  return tlg::ok();
+}

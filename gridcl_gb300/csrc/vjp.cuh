@@ -157,7 +157,7 @@ __global__ void __launch_bounds__(kEvalThreads, vjp_min_blocks(SPLIT, D, K))
 #pragma unroll
       for (int g = 0; g < D; ++g) {
         const double v = __ldg(nodes + n * D + g);
-        if constexpr (SPLIT) xk[j][g] = own ? __double2float_rn(v - x0[g]) : 0.0f;
+        if constexpr (SPLIT) xk[j][g] = own ? d2f_rn(v - x0[g]) : 0.0f;
         else xk[j][g] = own ? v : 0.0;
       }
     }
@@ -166,8 +166,14 @@ __global__ void __launch_bounds__(kEvalThreads, vjp_min_blocks(SPLIT, D, K))
 #pragma unroll
     for (int g = 1; g < D; ++g)
       if (rl == g) xo = x0[g] + a.origin[g];
-    const S xh = (S)xo;
-    const S xl = SPLIT ? (S)(xo - (double)xh) : S(0);
+    S xh, xl;
+    if constexpr (SPLIT) {
+      xh = d2f_rn(xo);
+      xl = d2f_rn(xo - f2d_exact(xh));
+    } else {
+      xh = xo;
+      xl = 0.0;
+    }
 
     const int64_t o = a.out_first_cell + c;
     const int64_t tq = (o / TILE) * nq;
@@ -370,19 +376,6 @@ struct VjpRow<L, 1> {
   __device__ static T load(const L* p) { return __ldg(p); }
   __device__ static L get(const T& v, int) { return v; }
 };
-
-// f32 -> f64 by exponent rebias in integer operations: exact for zero and normal numbers, which
-// are what the FP64 pipe (2 lanes per clock per SM on this part) is spared; subnormal, infinite
-// and NaN values take the conversion instruction.
-__device__ __forceinline__ double f2d_exact(float f) {
-  const uint32_t b = __float_as_uint(f);
-  const uint32_t e = (b >> 23) & 0xFFu;
-  const uint64_t sign = (uint64_t)(b >> 31) << 63;
-  if ((b << 1) == 0u) return __longlong_as_double((long long)sign);
-  if (e == 0u || e == 0xFFu) return (double)f;
-  return __longlong_as_double(
-      (long long)(sign | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7FFFFFu) << 29)));
-}
 
 // A node's running sum of f32 contributions: f64 adds for f64 rows; for f32 rows an unevaluated
 // pair hi + lo kept by TwoSum (Knuth) in FP32, whose error per add is captured exactly, so the

@@ -275,6 +275,13 @@ tlg_status tlg_measure_static(const void* detj, int dtype, int64_t num_cells, in
                               int tile, const void* weights, void* result, void* stream);
 int64_t tlg_measure_static_max_cells(void);
 
+/* Self-test of the split kernels' integer f64 -> f32 rounding and f32 -> f64 widening against
+ * the conversion instructions: mismatches[0] += the number of x[0..n) (device f64 values) whose
+ * rounded f32 bits differ, mismatches[1] += those whose widened round trip differs (NaN
+ * payloads compared as NaN). No counterpart in the reference. */
+tlg_status tlg_selftest_conversions(const double* x, int64_t n, unsigned long long* mismatches,
+                                    void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -121,3 +121,28 @@ def test_split_rejects_f32_meshes(cuda):
     with pytest.raises(tg.GridError):
         tg.geometric_factors_block(g, 0, tg.PointSet("Tetrahedron", pts, np.ones(len(pts))),
                                    ("detj",), precision="split")
+
+
+def test_integer_conversions_match_the_instructions(cuda):
+    """The split kernels round f64 -> f32 and widen f32 -> f64 with integer operations; over
+    random bit patterns (NaN, infinities, subnormals), exact ties, and the edges of the f32
+    normal range, both match the conversion instructions bit for bit."""
+    from gridcl_gb300._lib import check, lib
+    from gridcl_gb300.geometry import current_stream_handle
+
+    rng = np.random.default_rng(17)
+    parts = [rng.integers(0, 2**63, 1 << 20, dtype=np.int64).view(np.float64)]
+    f = rng.standard_normal(1 << 18).astype(np.float32) * np.float32(2.0) ** rng.integers(-126, 127, 1 << 18)
+    nxt = np.nextafter(f, np.float32(np.inf), dtype=np.float32)
+    ties = 0.5 * (f.astype(np.float64) + nxt.astype(np.float64))  # exact halfway points
+    parts += [ties, np.nextafter(ties, np.inf), np.nextafter(ties, -np.inf), f.astype(np.float64)]
+    fmax = float(np.finfo(np.float32).max)
+    tiny = float(np.finfo(np.float32).tiny)
+    edges = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, fmax, -fmax, fmax * (1 + 2.0**-25),
+                      fmax * (1 + 2.0**-24), tiny, -tiny, tiny * (1 - 2.0**-30), tiny * 0.5,
+                      2.0**-149, 2.0**-150, 2.0**-151, 1.0, 1.0 + 2.0**-24, 1.0 + 3 * 2.0**-24])
+    parts.append(np.concatenate([edges, -edges]))
+    x = torch.from_numpy(np.concatenate(parts)).cuda()
+    bad = torch.zeros(2, dtype=torch.int64, device="cuda")
+    check(lib().tlg_selftest_conversions(x.data_ptr(), x.numel(), bad.data_ptr(), current_stream_handle()))
+    assert bad.tolist() == [0, 0]
