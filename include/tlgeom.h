@@ -147,8 +147,8 @@ typedef struct tlg_outputs {
   void* normals;          /* codimension 1: unit normals, GD */
   void* facet_normals;    /* codimension 0: K^T n_ref / |K^T n_ref|, GD (tables need ref_normals) */
   /* Split precision only (TLG_SPLIT32 tables): points whose condition estimate
-   * |J|_F |K|_F / TD exceeds cond_limit (or is not finite) get det J and K from FP64; 0 selects
-   * 1e3. `recomputed` (device u64, may be NULL) is incremented once per such point. */
+   * |J|_F |K|_F / TD exceeds cond_limit (or is not finite) get J, det J and K from FP64; 0
+   * selects 256. `recomputed` (device u64, may be NULL) is incremented once per such point. */
   double cond_limit;
   unsigned long long* recomputed;
 } tlg_outputs;
