@@ -34,7 +34,8 @@ struct tlg_tables {
   int64_t k, q;
   bool has_refn;
   unsigned char* dev = nullptr;  // phi [Q][K] | dphi [Q][K][TD] | refn [Q][TD] | error word
-  uint32_t bytes = 0;            // staged bytes (multiple of 16), error word excluded
+  uint32_t bytes = 0;            // table bytes (multiple of 16), error word excluded
+  bool staged = true;            // the tables fit the kernels' shared-memory budget
   uint32_t off_dphi = 0, off_refn = 0, off_phi2 = 0, off_dphi2 = 0, off_dphi64 = 0;
   // The adjoint's table after the error word (codimension 0, f64 or split tables; 0 bytes when
   // absent or too large to stage): per node of each point (f64) or point pair (split) the 32
@@ -107,10 +108,28 @@ void narrow_into(std::vector<unsigned char>& buf, size_t off, const double* src,
 
 // The paired-FP32 kernel: an f32 mesh (split = false) or split precision (split = true).
 // `found` is false when no paired kernel exists for the element (nothing launched).
+void fill_pair_args(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                    tlg::PairArgs* ap);
+
 tlg_status eval_pair(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
                      bool split, cudaStream_t stream, bool* found) {
   tlg::PairArgs a;
   std::memset(&a, 0, sizeof(a));
+  fill_pair_args(t, b, o, mask, &a);
+  if (!t->staged) {
+    *found = false;
+    return TLG_ERR_UNSUPPORTED;
+  }
+  cudaError_t e = tlg::launch_eval_pair(split, t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
+  if (!*found) return TLG_ERR_UNSUPPORTED;
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  return ok();
+}
+
+// The arguments of the paired and split-loops kernels.
+void fill_pair_args(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                    tlg::PairArgs* ap) {
+  tlg::PairArgs& a = *ap;
   a.nodes = b->nodes;
   a.dofmap = b->dofmap;
   a.flags = b->flags;
@@ -121,6 +140,7 @@ tlg_status eval_pair(const tlg_tables* t, const tlg_block* b, const tlg_outputs*
   a.recomputed = o->recomputed;
   a.first_cell = o->first_cell;
   a.padded = (o->num_cells + o->tile - 1) / o->tile * o->tile;
+  a.range_cells = o->num_cells;
   a.out_first_cell = o->out_first_cell;
   a.last_cell = b->num_cells - 1;
   const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
@@ -133,24 +153,27 @@ tlg_status eval_pair(const tlg_tables* t, const tlg_block* b, const tlg_outputs*
   a.off_phi2 = t->off_phi2;
   a.off_dphi2 = t->off_dphi2;
   a.off_dphi64 = t->off_dphi64;
+  a.off_dphi = t->off_dphi;
+  a.k_runtime = (int)t->k;
   a.mask = mask;
   a.num_points = (int)t->q;
-  cudaError_t e = tlg::launch_eval_pair(split, t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
-  if (!*found) return TLG_ERR_UNSUPPORTED;
-  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
-  return ok();
 }
 
 tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
                       cudaStream_t stream) {
+  if (o->tile != 16)
+    return fail(TLG_ERR_UNSUPPORTED, "tlg_eval_block: split precision runs with tile 16, not " +
+                                         std::to_string(o->tile));
   bool found = false;
-  tlg_status st = o->tile == 16 ? eval_pair(t, b, o, mask, true, stream, &found) : TLG_ERR_UNSUPPORTED;
-  if (!found)
-    return fail(TLG_ERR_UNSUPPORTED, "tlg_eval_block: no split-precision kernel for this element (tdim " +
-                                         std::to_string(t->td) + ", " + std::to_string(t->k) +
-                                         " nodes) and tile " + std::to_string(o->tile) +
-                                         " (split precision runs with tile 16)");
-  return st;
+  tlg_status st = eval_pair(t, b, o, mask, true, stream, &found);
+  if (found) return st;
+  // No paired kernel for this element, or tables beyond the shared-memory budget.
+  tlg::PairArgs a;
+  std::memset(&a, 0, sizeof(a));
+  fill_pair_args(t, b, o, mask, &a);
+  cudaError_t e = tlg::launch_split_loops(t->td, t->gd, !t->staged, a, t->bytes, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  return ok();
 }
 
 template <typename F>
@@ -181,6 +204,7 @@ tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs
   a.num_points = (int)t->q;
   a.tile_shift = shift;
   a.k_runtime = (int)t->k;
+  a.tab_global = t->staged ? 0 : 1;
   bool direct = false;
   cudaError_t e;
   if constexpr (sizeof(F) == 4) {
@@ -313,12 +337,14 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       t->off_dphi64 = (uint32_t)total;
       total = align16(total + std::max<size_t>(n_dphi, 1) * 8);
     }
-    if (total + 16 > (size_t)200 * 1024) {
+    // Tables beyond the shared-memory budget stay in global memory: the loops kernels read them
+    // there (L1/L2-cached) instead of staging them.
+    if (total > ((size_t)1 << 31)) {
       delete t;
       return fail(TLG_ERR_ALLOCATION_TOO_LARGE,
-                  "tlg_tables_create: the tabulation (" + std::to_string(total) +
-                      " bytes) exceeds the shared-memory budget of 200 KiB");
+                  "tlg_tables_create: the tabulation (" + std::to_string(total) + " bytes) exceeds 2 GiB");
     }
+    t->staged = total + 16 <= (size_t)200 * 1024;
     t->bytes = (uint32_t)total;
     t->off_vjp = (uint32_t)(total + 16);
     if (td == gdim && dtype != TLG_F32) {

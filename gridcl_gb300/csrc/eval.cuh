@@ -69,6 +69,7 @@ struct EvalArgs {
   int num_points;            // Q
   int tile_shift;            // log2(tile)
   int k_runtime;             // K for the loops kernel
+  int tab_global;            // loops kernel: tables read from global memory, not staged
 };
 
 // Arguments of the paired kernels (f32 arithmetic; nodes f32, or f64 with SPLIT).
@@ -80,11 +81,13 @@ struct PairArgs {
   float* out[6];
   int* err;
   unsigned long long* recomputed;  // may be null
-  int64_t first_cell, padded, out_first_cell, last_cell, last_flag;
+  int64_t first_cell, padded, range_cells, out_first_cell, last_cell, last_flag;
   double origin[3];
   float cond_limit;
   uint32_t last_node, tab_bytes, off_refn, off_phi2, off_dphi2, off_dphi64, mask;
   int num_points;
+  uint32_t off_dphi;  // the f32 derivative table [Q][K][TD] (split loops kernel; phi [Q][K] at 0)
+  int k_runtime;      // K (split loops kernel)
 };
 
 // ----------------------------------------------------------------------------------------
@@ -588,7 +591,7 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
             recompute_f64<TD, GD, K>(nodes, row, a.last_node, dphi64 + (2 * qp + h) * K * TD,
                                      pj ? pj + shift : nullptr, pd ? pd + h * TILE : nullptr,
                                      pk ? pk + shift : nullptr, TILE);
-            if (a.recomputed) atomicAdd(a.recomputed, 1ull);
+            if (a.recomputed && c < a.range_cells) atomicAdd(a.recomputed, 1ull);
           }
         }
       }
@@ -725,14 +728,13 @@ __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_
 // The loops kernel: any K and tile (run time), TD and GD at compile time; node coordinates
 // re-read through L1 at each point. The same operations as the kernels above.
 
+// The loops kernel's cells, tables at `tabs` (shared memory, or global memory when they exceed
+// the shared-memory budget).
 template <typename F, int TD, int GD>
-__global__ void __launch_bounds__(kEvalThreads) eval_loops_kernel(const __grid_constant__ EvalArgs<F> a) {
-  __shared__ uint64_t bar;
-  extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
-  const F* phi = reinterpret_cast<const F*>(smem);
-  const F* dphi = reinterpret_cast<const F*>(smem + a.off_dphi);
-  const F* refn = reinterpret_cast<const F*>(smem + a.off_refn);
+__device__ __forceinline__ void loops_cells(const EvalArgs<F>& a, const unsigned char* tabs) {
+  const F* phi = reinterpret_cast<const F*>(tabs);
+  const F* dphi = reinterpret_cast<const F*>(tabs + a.off_dphi);
+  const F* refn = reinterpret_cast<const F*>(tabs + a.off_refn);
   const int nq = a.num_points;
   const int K = a.k_runtime;
   const uint32_t mask = a.mask;
@@ -811,6 +813,172 @@ __global__ void __launch_bounds__(kEvalThreads) eval_loops_kernel(const __grid_c
         }
       }
     }
+  }
+}
+
+// GTAB: the tables are read from global memory (L1/L2-cached) instead of being staged.
+template <typename F, int TD, int GD, bool GTAB>
+__global__ void __launch_bounds__(kEvalThreads) eval_loops_kernel(const __grid_constant__ EvalArgs<F> a) {
+  if constexpr (GTAB) {
+    loops_cells<F, TD, GD>(a, a.tab);
+  } else {
+    __shared__ uint64_t bar;
+    extern __shared__ __align__(16) unsigned char smem[];
+    stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+    loops_cells<F, TD, GD>(a, smem);
+  }
+}
+
+// J, det J and K of one point in FP64 from the f64 nodes, K at run time (the split loops
+// kernel's recompute of near-degenerate points); outputs as recompute_f64.
+template <int TD, int GD>
+__device__ __noinline__ void recompute_f64_rt(const double* __restrict__ nodes, const uint32_t* row, int K,
+                                              uint32_t last_node, const double* d64, float* pj, float* pd,
+                                              float* pk, int stride) {
+  constexpr int LJ = TD * GD;
+  using M64 = Factors<double, TD, GD>;
+  double jd[LJ], kd[LJ], x0[GD];
+  const uint32_t n0 = min(__ldg(row), last_node);
+#pragma unroll
+  for (int g = 0; g < GD; ++g) x0[g] = __ldg(nodes + (int64_t)n0 * GD + g);
+#pragma unroll
+  for (int i = 0; i < LJ; ++i) jd[i] = 0.0;
+  for (int k = 1; k < K; ++k) {
+    const uint32_t nk = min(__ldg(row + k), last_node);
+#pragma unroll
+    for (int g = 0; g < GD; ++g) {
+      const double y = __ldg(nodes + (int64_t)nk * GD + g) - x0[g];
+#pragma unroll
+      for (int d = 0; d < TD; ++d) jd[d * GD + g] = __fma_rn(y, d64[k * TD + d], jd[d * GD + g]);
+    }
+  }
+  M64::pinv(jd, kd);
+#pragma unroll
+  for (int i = 0; i < LJ; ++i) {
+    if (pj) pj[i * stride] = (float)jd[i];
+    if (pk) pk[i * stride] = (float)kd[i];
+  }
+  if (pd) *pd = (float)M64::detj(jd);
+}
+
+// Split precision with K at run time (elements without a paired kernel, or tables beyond the
+// shared-memory budget with GTAB): one cell per thread, one point at a time, the same arithmetic
+// as the paired kernel (f64 shift by node 0, FP32 J and X, FP64 recompute above the condition
+// limit), tile 16.
+template <int TD, int GD>
+__device__ __forceinline__ void split_loops_cells(const PairArgs& a, const unsigned char* tabs) {
+  constexpr int TILE = 16;
+  constexpr int LJ = TD * GD;
+  using A = Ar<float>;
+  using M = Factors<float, TD, GD>;
+  const float* phi = reinterpret_cast<const float*>(tabs);
+  const float* dphi = reinterpret_cast<const float*>(tabs + a.off_dphi);
+  const float* refn = reinterpret_cast<const float*>(tabs + a.off_refn);
+  const double* dphi64 = reinterpret_cast<const double*>(tabs + a.off_dphi64);
+  const double* nodes = static_cast<const double*>(a.nodes);
+  const int nq = a.num_points;
+  const int K = a.k_runtime;
+  const uint32_t mask = a.mask;
+  const bool want_j = (mask & ~kOutPoints) != 0;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cell = min(a.first_cell + c, a.last_cell);
+    const uint32_t* row = a.dofmap + cell * K;
+    double x0[GD];
+    const uint32_t n0 = min(__ldg(row), a.last_node);
+    float xh[GD], xl[GD];
+#pragma unroll
+    for (int g = 0; g < GD; ++g) {
+      x0[g] = __ldg(nodes + (int64_t)n0 * GD + g);
+      const double v = x0[g] + a.origin[g];
+      xh[g] = d2f_rn(v);
+      xl[g] = d2f_rn(v - f2d_exact(xh[g]));
+    }
+    float sign = 1.0f;
+    if ((mask & kOutNormals) && a.flags != nullptr && a.last_flag >= 0) {
+      const uint32_t f = __ldg(a.flags + min(a.first_cell + c, a.last_flag));
+      sign = (f & 1u) ? -1.0f : 1.0f;
+    }
+    const int64_t o = a.out_first_cell + c;
+    const int64_t tile_idx = o / TILE;
+    const int lane = (int)(o % TILE);
+    for (int q = 0; q < nq; ++q) {
+      float xp[GD], j[LJ];
+#pragma unroll
+      for (int i = 0; i < GD; ++i) xp[i] = 0.0f;
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) j[i] = 0.0f;
+      for (int k = 1; k < K; ++k) {
+        const uint32_t n = min(__ldg(row + k), a.last_node);
+        float y[GD];
+#pragma unroll
+        for (int g = 0; g < GD; ++g) y[g] = d2f_rn(__ldg(nodes + (int64_t)n * GD + g) - x0[g]);
+        if (mask & kOutPoints) {
+          const float w = phi[q * K + k];
+#pragma unroll
+          for (int g = 0; g < GD; ++g) xp[g] = A::fma(y[g], w, xp[g]);
+        }
+        if (want_j) {
+#pragma unroll
+          for (int d = 0; d < TD; ++d) {
+            const float w = dphi[(q * K + k) * TD + d];
+#pragma unroll
+            for (int g = 0; g < GD; ++g) j[d * GD + g] = A::fma(y[g], w, j[d * GD + g]);
+          }
+        }
+      }
+      if (mask & kOutPoints) {
+#pragma unroll
+        for (int g = 0; g < GD; ++g) xp[g] = A::add(xh[g], A::add(xl[g], xp[g]));
+        store_point(a.out[0], tile_idx, q, nq, GD, lane, 4, xp, GD);
+      }
+      if (!want_j) continue;
+      float kk[LJ];
+      M::pinv(j, kk);
+      float dj = M::detj(j);
+      const float kap = M::condition(j, kk);
+      if (!(kap <= a.cond_limit) && (mask & (kOutJacobian | kOutDetJ | kOutPinv))) {
+        // Through separate arrays, so that j and kk keep living in registers.
+        float jr[LJ], kr[LJ], dr;
+        recompute_f64_rt<TD, GD>(nodes, row, K, a.last_node, dphi64 + (int64_t)q * K * TD, jr, &dr, kr, 1);
+#pragma unroll
+        for (int i = 0; i < LJ; ++i) {
+          j[i] = jr[i];
+          kk[i] = kr[i];
+        }
+        dj = dr;
+        if (a.recomputed && c < a.range_cells) atomicAdd(a.recomputed, 1ull);
+      }
+      if (mask & kOutJacobian) store_point(a.out[1], tile_idx, q, nq, LJ, lane, 4, j, LJ);
+      if (mask & kOutDetJ) store_point(a.out[2], tile_idx, q, nq, 1, lane, 4, &dj, 1);
+      if (mask & kOutPinv) store_point(a.out[3], tile_idx, q, nq, LJ, lane, 4, kk, LJ);
+      if constexpr (TD == GD) {
+        if (mask & kOutFacetNormals) {
+          float n[GD];
+          M::facet_normal(kk, refn + q * TD, n);
+          store_point(a.out[5], tile_idx, q, nq, GD, lane, 4, n, GD);
+        }
+      }
+      if constexpr (TD + 1 == GD) {
+        if (mask & kOutNormals) {
+          float n[GD];
+          M::normal(j, sign, n);
+          store_point(a.out[4], tile_idx, q, nq, GD, lane, 4, n, GD);
+        }
+      }
+    }
+  }
+}
+
+template <int TD, int GD, bool GTAB>
+__global__ void __launch_bounds__(kEvalThreads) split_loops_kernel(const __grid_constant__ PairArgs a) {
+  if constexpr (GTAB) {
+    split_loops_cells<TD, GD>(a, a.tab);
+  } else {
+    __shared__ uint64_t bar;
+    extern __shared__ __align__(16) unsigned char smem[];
+    stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+    split_loops_cells<TD, GD>(a, smem);
   }
 }
 

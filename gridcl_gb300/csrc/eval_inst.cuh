@@ -9,8 +9,8 @@ namespace tlg {
 cudaError_t TLG_LAUNCH(int td, int gd, int k, const EvalArgs<TLG_F>& a, size_t smem,
                        cudaStream_t s, bool* direct) {
 #ifdef TLG_WITH_DIRECT
-  // Unrolled kernels are compiled for f64 and the GPU tile of 16 cells.
-  *direct = a.tile_shift == 4;
+  // Unrolled kernels are compiled for f64 and the GPU tile of 16 cells, tables staged.
+  *direct = a.tile_shift == 4 && !a.tab_global;
 #define TLG_DIRECT(TD, GD, K) \
   if (*direct && td == TD && gd == GD && k == K) \
     return launch_persistent(eval_direct_kernel<TLG_F, TD, GD, K, 16>, a, a.padded, smem, s);
@@ -46,7 +46,9 @@ cudaError_t TLG_LAUNCH(int td, int gd, int k, const EvalArgs<TLG_F>& a, size_t s
 #endif
   *direct = false;
 #define TLG_LOOPS(TD, GD) \
-  if (td == TD && gd == GD) return launch_persistent(eval_loops_kernel<TLG_F, TD, GD>, a, a.padded, smem, s);
+  if (td == TD && gd == GD) \
+    return a.tab_global ? launch_persistent(eval_loops_kernel<TLG_F, TD, GD, true>, a, a.padded, 0, s) \
+                        : launch_persistent(eval_loops_kernel<TLG_F, TD, GD, false>, a, a.padded, smem, s);
   TLG_LOOPS(1, 1)
   TLG_LOOPS(1, 2)
   TLG_LOOPS(1, 3)

@@ -9,10 +9,12 @@
 //    fastest, with Gauss-Jacobi nodes by Newton's method on the Jacobi polynomial with
 //    deflation of the roots found so far (tetraloma-refcell/src/jacobi.rs);
 //  - the Lagrange basis (tetraloma-refcell/src/tabulation.rs:1-5): the reference expands it in
-//    an orthonormal set; here the expansion set is products of shifted Legendre polynomials
-//    truncated to the cell's space, and the generalised Vandermonde matrix is inverted by LU
-//    with partial pivoting. Both span the same space, so the Lagrange functions agree to
-//    rounding.
+//    an orthonormal set; here the expansion set is orthogonal but not normalised: products of
+//    shifted Legendre polynomials on intervals, quadrilaterals and hexahedra, Dubiner's
+//    collapsed-coordinate polynomials on triangles and tetrahedra (and triangle x Legendre on
+//    prisms), and the generalised Vandermonde matrix is inverted by LU with partial pivoting.
+//    Both span the same space, so the Lagrange functions agree to rounding; orthogonality keeps
+//    the Vandermonde matrix well conditioned at high degree.
 // Pyramids (a rational space) are not supported by this build.
 #include "refcell.h"
 
@@ -131,6 +133,86 @@ void legendre01(int n, double x, double* val, double* der) {
   for (int i = 0; i <= n; ++i) der[i] *= 2.0;
 }
 
+// Scaled Jacobi polynomials R_n = P_n^(alpha,0)(f / g) g^n, n = 0..m, with gradients dr[n * td + d]:
+// the three-term recurrence of P_n^(alpha,0) multiplied through by g^n, so that nothing is
+// divided by g (which vanishes at the collapsed vertex). With g = 1 these are the Jacobi
+// polynomials of f.
+//   R_0 = 1,  R_1 = ((alpha + 2) f + alpha g) / 2,
+//   R_n = (A_n f + B_n g) R_{n-1} - C_n g^2 R_{n-2}, with D = 2n (n + alpha) (2n + alpha - 2),
+//   A_n = (2n + alpha - 1)(2n + alpha)(2n + alpha - 2) / D, B_n = (2n + alpha - 1) alpha^2 / D,
+//   C_n = 2 (n + alpha - 1)(n - 1)(2n + alpha) / D.
+void scaled_jacobi(int m, double alpha, double f, const double* df, double g, const double* dg, int td,
+                   double* r, double* dr) {
+  r[0] = 1.0;
+  for (int d = 0; d < td; ++d) dr[d] = 0.0;
+  if (m < 1) return;
+  r[1] = 0.5 * ((alpha + 2.0) * f + alpha * g);
+  for (int d = 0; d < td; ++d) dr[td + d] = 0.5 * ((alpha + 2.0) * df[d] + alpha * dg[d]);
+  for (int n = 2; n <= m; ++n) {
+    const double D = 2.0 * n * (n + alpha) * (2.0 * n + alpha - 2.0);
+    const double A = (2.0 * n + alpha - 1.0) * (2.0 * n + alpha) * (2.0 * n + alpha - 2.0) / D;
+    const double B = (2.0 * n + alpha - 1.0) * alpha * alpha / D;
+    const double C = 2.0 * (n + alpha - 1.0) * (n - 1.0) * (2.0 * n + alpha) / D;
+    const double lin = A * f + B * g;
+    r[n] = lin * r[n - 1] - C * g * g * r[n - 2];
+    for (int d = 0; d < td; ++d)
+      dr[n * td + d] = (A * df[d] + B * dg[d]) * r[n - 1] + lin * dr[(n - 1) * td + d] -
+                       C * (2.0 * g * dg[d] * r[n - 2] + g * g * dr[(n - 2) * td + d]);
+  }
+}
+
+// Dubiner's orthogonal polynomials at one point of the reference triangle (td = 2), tetrahedron
+// (td = 3) or prism (triangle x Legendre, td = 3), for the exponent triples of `sp`:
+//   triangle:    Q_a(x, y) T_ab(y),        Q_a = P_a(f/g) g^a, f = 2x + y - 1, g = 1 - y,
+//                                          T_ab = P_b^(2a+1,0)(2y - 1);
+//   tetrahedron: Q_a(x, y, z) R_ab(y, z) S_abc(z), f = 2x + y + z - 1, g = 1 - y - z;
+//                R_ab = P_b^(2a+1,0)(f2/g2) g2^b, f2 = 2y + z - 1, g2 = 1 - z;
+//                S_abc = P_c^(2a+2b+2,0)(2z - 1);
+//   prism:       Q_a(x, y) T_ab(y) L_c(z), L_c = P_c(2z - 1).
+void dubiner_point(int cell, int p, const double* x, const std::vector<std::array<int, 3>>& sp, double* val,
+                   double* grad /* [j][td] */) {
+  const int td = cell == kTriangle ? 2 : 3;
+  const bool tet = cell == kTetrahedron;
+  const double X = x[0], Y = x[1], Z = td == 3 ? x[2] : 0.0;
+  const double zero[3] = {0.0, 0.0, 0.0};
+  // Q_a: the scaled Legendre polynomials of the first collapsed direction.
+  const double f1 = 2.0 * X + Y + (tet ? Z : 0.0) - 1.0, g1 = 1.0 - Y - (tet ? Z : 0.0);
+  const double df1[3] = {2.0, 1.0, tet ? 1.0 : 0.0}, dg1[3] = {0.0, -1.0, tet ? -1.0 : 0.0};
+  std::vector<double> q(p + 1), dq((p + 1) * 3);
+  scaled_jacobi(p, 0.0, f1, df1, g1, dg1, 3, q.data(), dq.data());
+  // Line factor of the prism.
+  std::vector<double> l(p + 1), dl((p + 1) * 3);
+  if (cell == kPrism) {
+    const double dfz[3] = {0.0, 0.0, 2.0};
+    scaled_jacobi(p, 0.0, 2.0 * Z - 1.0, dfz, 1.0, zero, 3, l.data(), dl.data());
+  }
+  std::vector<double> r(p + 1), dr((p + 1) * 3), t(p + 1), dt((p + 1) * 3);
+  for (size_t j = 0; j < sp.size(); ++j) {
+    const int a = sp[j][0], b = sp[j][1], c = sp[j][2];
+    double v = q[a], gv[3] = {dq[a * 3], dq[a * 3 + 1], dq[a * 3 + 2]};
+    auto times = [&](double w, const double* dw) {
+      for (int d = 0; d < 3; ++d) gv[d] = gv[d] * w + v * dw[d];
+      v *= w;
+    };
+    if (tet) {
+      const double f2 = 2.0 * Y + Z - 1.0, g2 = 1.0 - Z;
+      const double df2[3] = {0.0, 2.0, 1.0}, dg2[3] = {0.0, 0.0, -1.0};
+      scaled_jacobi(b, 2.0 * a + 1.0, f2, df2, g2, dg2, 3, r.data(), dr.data());
+      times(r[b], &dr[b * 3]);
+      const double dfz[3] = {0.0, 0.0, 2.0};
+      scaled_jacobi(c, 2.0 * a + 2.0 * b + 2.0, 2.0 * Z - 1.0, dfz, 1.0, zero, 3, t.data(), dt.data());
+      times(t[c], &dt[c * 3]);
+    } else {
+      const double dfy[3] = {0.0, 2.0, 0.0};
+      scaled_jacobi(b, 2.0 * a + 1.0, 2.0 * Y - 1.0, dfy, 1.0, zero, 3, t.data(), dt.data());
+      times(t[b], &dt[b * 3]);
+      if (cell == kPrism) times(l[c], &dl[c * 3]);
+    }
+    val[j] = v;
+    for (int d = 0; d < td; ++d) grad[j * td + d] = gv[d];
+  }
+}
+
 // Exponent triples of the expansion set of (cell, p).
 std::vector<std::array<int, 3>> space(int cell, int p) {
   std::vector<std::array<int, 3>> s;
@@ -160,7 +242,18 @@ std::vector<double> basis(int cell, int p, const double* pts, long npts, int nde
   const int rows = 1 + (nderivs ? td : 0);
   std::vector<double> out((size_t)rows * npts * nb);
   std::vector<double> val(3 * (p + 1)), der(3 * (p + 1));
+  const bool collapsed = cell == kTriangle || cell == kTetrahedron || cell == kPrism;
+  std::vector<double> v1(nb), g1((size_t)nb * 3);
   for (long q = 0; q < npts; ++q) {
+    if (collapsed) {
+      dubiner_point(cell, p, pts + q * td, sp, v1.data(), g1.data());
+      for (long j = 0; j < nb; ++j) {
+        out[q * nb + j] = v1[j];
+        if (nderivs)
+          for (int dd = 0; dd < td; ++dd) out[((size_t)(1 + dd) * npts + q) * nb + j] = g1[j * td + dd];
+      }
+      continue;
+    }
     for (int d = 0; d < td; ++d) legendre01(p, pts[q * td + d], &val[d * (p + 1)], &der[d * (p + 1)]);
     for (long j = 0; j < nb; ++j) {
       double v = 1.0;

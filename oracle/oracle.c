@@ -31,6 +31,9 @@
 
 #ifdef _OPENMP
 #include <omp.h>
+
+/* Nodes per cell the oracle accepts (a degree-7 hexahedron has 512). */
+#define ORC_MAX_K 512
 #endif
 
 #define ORC_OK 0
@@ -103,7 +106,7 @@ int orc_eval(int td, int gd, int k, int nq, int64_t ncells, const double* nodes,
              const uint32_t* dofmap, const double* tab, const uint32_t* flags,
              const double* ref_normals, double* x, double* jac, double* detj, double* kinv,
              double* normals, double* facet_normals, int nthreads) {
-  if (td < 1 || td > 3 || gd < td || gd > 3 || k < 1 || k > 64 || nq < 0 || ncells < 0 || nnodes < 1)
+  if (td < 1 || td > 3 || gd < td || gd > 3 || k < 1 || k > ORC_MAX_K || nq < 0 || ncells < 0 || nnodes < 1)
     return ORC_BAD_ARGS;
   if (normals && td + 1 != gd) return ORC_BAD_ARGS;
   if (facet_normals && (td != gd || !ref_normals)) return ORC_BAD_ARGS;
@@ -113,7 +116,7 @@ int orc_eval(int td, int gd, int k, int nq, int64_t ncells, const double* nodes,
 #pragma omp parallel for schedule(static)
 #endif
   for (int64_t c = 0; c < ncells; ++c) {
-    double xc[64 * 3];
+    double xc[ORC_MAX_K * 3];
     double jq[9], kq[9];
     const double* cx = xc;
     for (int i = 0; i < k; ++i) {
@@ -223,11 +226,11 @@ double orc_measure(const double* detj, const double* weights, int64_t ncells, in
 int orc_vjp(int d, int k, int nq, int64_t ncells, const double* nodes, int64_t nnodes,
             const uint32_t* dofmap, const double* tab, const double* xbar, const double* dbar,
             const double* kbar, double* grad) {
-  if (d < 1 || d > 3 || k < 1 || k > 64 || nq < 0 || ncells < 0 || nnodes < 1) return ORC_BAD_ARGS;
+  if (d < 1 || d > 3 || k < 1 || k > ORC_MAX_K || nq < 0 || ncells < 0 || nnodes < 1) return ORC_BAD_ARGS;
   for (int64_t i = 0; i < nnodes * d; ++i) grad[i] = 0.0;
-  double xc[64 * 3], gl[64 * 3];
+  double xc[ORC_MAX_K * 3], gl[ORC_MAX_K * 3];
   for (int64_t c = 0; c < ncells; ++c) {
-    uint32_t idx[64];
+    uint32_t idx[ORC_MAX_K];
     for (int i = 0; i < k; ++i) {
       uint32_t n = dofmap[c * k + i];
       if ((int64_t)n >= nnodes) n = (uint32_t)(nnodes - 1);

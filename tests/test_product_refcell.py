@@ -31,13 +31,14 @@ def test_rules_match_the_oracle(cell):
 
 @pytest.mark.parametrize("cell", CELLS)
 def test_tabulation_matches_the_oracle(cell):
-    # Degrees of the benchmark elements and below; the product's Vandermonde route loses
-    # accuracy on simplices above degree 4.
-    for p in range(1, 5):
+    # Degrees 1-8, as the reference's high-order acceptance tests; values and derivatives
+    # relative to their largest magnitude.
+    for p in range(1, 9):
         pts, _ = rc.gauss_rule(cell, 2 * p)
         for fam in (["Equispaced", "Gll"] if cell in ("Interval", "Quadrilateral", "Hexahedron") else ["Equispaced"]):
-            err = np.abs(pr.tabulate(cell, p, pts, 1, fam) - rc.tabulate(cell, p, pts, 1, fam)).max()
-            assert err < 5e-13, (cell, p, fam, err)
+            want = rc.tabulate(cell, p, pts, 1, fam)
+            err = np.abs(pr.tabulate(cell, p, pts, 1, fam) - want).max() / np.abs(want).max()
+            assert err < 5e-14, (cell, p, fam, err)
 
 
 @pytest.mark.parametrize("cell", CELLS)
