@@ -407,19 +407,23 @@ def facet_point_set(cell: str, degree: int) -> PointSet:
                     np.concatenate(rn).reshape(-1, td))
 
 
-def measure_block(g: Geometry, b: int, pts: PointSet, detj: QuadField | None = None) -> float:
+def measure_block(g: Geometry, b: int, pts: PointSet, detj: QuadField | None = None,
+                  sync: bool = True):
     """The measure of block b: sum over cells and points of det J * w, per cell then by a tree of
-    64-value sums, all on the device in F, read back once (tetraloma-geometry/src/measure.rs:
-    141-185). `detj` may pass an already computed det J field of the same point set."""
+    64-value sums, all on the device in the det J field's type, read back once
+    (tetraloma-geometry/src/measure.rs:141-185). `detj` may pass an already computed det J field
+    of the same point set (an f32 field of split precision sums in f32). With ``sync=False`` the
+    result stays on the device: a one-element tensor, ready when the current stream reaches it."""
     blk = g.blocks[b]
+    dev = g.nodes.device
     if blk.num_cells == 0 or len(pts) == 0:
-        return 0.0
+        return 0.0 if sync else torch.zeros(1, dtype=g.dtype, device=dev)
     if detj is None:
         detj = detj_block(g, b, pts)
-    es = _DTYPES[g.dtype]
-    dev = g.nodes.device
-    sums = torch.empty(blk.num_cells, dtype=g.dtype, device=dev)
-    w = pts.weights_device(g.dtype, dev)
+    dt = detj.chunks[0].data.dtype
+    es = _DTYPES[dt]
+    sums = torch.empty(blk.num_cells, dtype=dt, device=dev)
+    w = pts.weights_device(dt, dev)
     stream = current_stream_handle()
     for ch in detj.chunks:
         check(lib().tlg_measure_cell_sums(ch.data.data_ptr(), es, ch.num_cells, detj.num_points,
@@ -427,10 +431,10 @@ def measure_block(g: Geometry, b: int, pts: PointSet, detj: QuadField | None = N
                                           sums.data_ptr() + ch.first_cell * es, stream))
     nbytes = int(lib().tlg_sum_workspace_bytes(es, blk.num_cells))
     work = torch.empty(max(nbytes, es), dtype=torch.uint8, device=dev)
-    result = torch.empty(1, dtype=g.dtype, device=dev)
+    result = torch.empty(1, dtype=dt, device=dev)
     check(lib().tlg_sum(sums.data_ptr(), es, blk.num_cells, work.data_ptr(), nbytes,
                         result.data_ptr(), stream))
-    return float(result.item())
+    return float(result.item()) if sync else result
 
 
 @dataclasses.dataclass

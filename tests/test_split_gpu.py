@@ -146,3 +146,19 @@ def test_integer_conversions_match_the_instructions(cuda):
     bad = torch.zeros(2, dtype=torch.int64, device="cuda")
     check(lib().tlg_selftest_conversions(x.data_ptr(), x.numel(), bad.data_ptr(), current_stream_handle()))
     assert bad.tolist() == [0, 0]
+
+
+def test_measure_of_a_split_field(cuda):
+    """measure_block sums a split-precision (f32) det J field in f32, blocking or not."""
+    mesh = meshes.curved_box("Tetrahedron", 4, 2, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, w = tg.refcell.gauss_rule("Tetrahedron", 4)
+    ps = tg.PointSet("Tetrahedron", pts, w)
+    f = tg.geometric_factors_block(g, 0, ps, ("detj",), precision="split")
+    dev = tg.measure_block(g, 0, ps, detj=f["detj"], sync=False)
+    assert dev.dtype == torch.float32 and dev.is_cuda
+    blocking = tg.measure_block(g, 0, ps, detj=f["detj"])
+    assert float(dev.item()) == blocking
+    plain = tg.measure_block(g, 0, ps)  # the f64 path
+    assert abs(blocking - plain) < 1e-6 * abs(plain)
+    assert abs(plain - 1.0) < 1e-12  # the curved map keeps the unit cube's boundary
