@@ -30,6 +30,7 @@ from .geometry import (
     pseudo_inverse_block,
     vjp_block,
 )
+from .strategy import get_strategy, last_kernel_family, set_strategy, with_strategy
 from . import meshes, refcell
 
 __all__ = [
@@ -37,4 +38,5 @@ __all__ = [
     "QuadRule", "detj_block", "facet_normals_block", "facet_point_set", "fd_check",
     "geometric_factors_block", "jacobians_block", "lib", "measure_block", "meshes", "normals_block",
     "node_incidence", "physical_points_block", "pseudo_inverse_block", "refcell", "vjp_block",
+    "get_strategy", "last_kernel_family", "set_strategy", "with_strategy",
 ]

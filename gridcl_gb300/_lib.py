@@ -108,6 +108,9 @@ SIGNATURES = [
     ("tlg_measure_static", _I, [_P, _I, _L, _L, _I, _P, _P, _P]),
     ("tlg_measure_static_max_cells", _L, []),
     ("tlg_selftest_conversions", _I, [_P, _L, _P, _P]),
+    ("tlg_set_strategy", _I, [_I]),
+    ("tlg_get_strategy", _I, []),
+    ("tlg_last_kernel_family", _I, []),
 ]
 
 _lib = None

@@ -21,7 +21,7 @@ OUT_DIR = HERE / "_build"
 LIB = HERE / "libtlgeom.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "csr.cu", "eval_f32.cu", "eval_f64.cu", "eval_pair.cu", "measure.cu", "refcell.cpp",
-           "vjp_f64.cu", "vjp_split.cu"]
+           "sumfact.cu", "vjp_f64.cu", "vjp_split.cu"]
 
 
 def nvcc() -> str:

@@ -1,6 +1,9 @@
 // The C ABI of include/tlgeom.h: argument checks with the reference's error kinds, device
 // tables, and the launches of the evaluation and E-vector kernels.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstdint>
 #include <cstring>
@@ -16,6 +19,7 @@
 #include "eval_launch.cuh"
 #include "refcell.h"
 #include "status.h"
+#include "sumfact.cuh"
 #include "vjp.cuh"
 
 struct tlg_batch {
@@ -41,6 +45,13 @@ struct tlg_tables {
   // absent or too large to stage): per node of each point (f64) or point pair (split) the 32
   // bytes phi, dphi_0 .. dphi_{TD-1}, zero padding, as f64 values or f32 pairs.
   uint32_t off_vjp = 0, vjp_bytes = 0;
+  // Sum-factorisation section (quadrilaterals and hexahedra at a tensor-product point set), after
+  // the adjoint's: per direction d, B_d [m_d][N] = l_i(u_d[a]) and D_d [m_d][N] = l_i'(u_d[a]) in the
+  // arithmetic's type, then perm [K] u32 (lexicographic node index -> Lagrange node); offsets
+  // relative to the section.
+  bool sf_ok = false;
+  int sf_n = 0, sf_m[3] = {1, 1, 1};
+  uint32_t off_sf = 0, sf_bytes = 0, sf_offb[3] = {0, 0, 0}, sf_offd[3] = {0, 0, 0}, sf_offperm = 0;
   int* err = nullptr;
   std::vector<unsigned char> host;  // host copy of the device bytes
 };
@@ -108,6 +119,86 @@ void narrow_into(std::vector<unsigned char>& buf, size_t off, const double* src,
 
 // The paired-FP32 kernel: an f32 mesh (split = false) or split precision (split = true).
 // `found` is false when no paired kernel exists for the element (nothing launched).
+// Evaluation strategy: tlg_set_strategy's setting (-1: none), else TLG_GEOM_STRATEGY, else auto.
+std::atomic<int> g_strategy{-1};
+// The kernel family of the last launch of tlg_eval_block on this thread (TLG_STRATEGY_*, 0: none).
+thread_local int g_last_family = 0;
+
+int env_strategy() {
+  static const int v = [] {
+    const char* e = std::getenv("TLG_GEOM_STRATEGY");
+    if (!e) return (int)TLG_STRATEGY_AUTO;
+    const std::string s(e);
+    if (s == "direct") return (int)TLG_STRATEGY_DIRECT;
+    if (s == "loops") return (int)TLG_STRATEGY_LOOPS;
+    if (s == "sumfact") return (int)TLG_STRATEGY_SUMFACT;
+    return (int)TLG_STRATEGY_AUTO;
+  }();
+  return v;
+}
+
+int current_strategy() {
+  const int s = g_strategy.load(std::memory_order_relaxed);
+  return s >= 0 ? s : env_strategy();
+}
+
+// The policy of TLG_STRATEGY_AUTO for tables with sum-factorisation data, from GB300 timings of
+// curved hexahedra (ms per launch, 128^3 Q1/Q2, 64^3 Q3; paired-or-unrolled / loops / sumfact):
+// f64 Q1 4.19 / 5.00 / 3.14, Q2 34.6 / 45.3 / 13.1 (the FP64 pipe bounds, and sum factorisation
+// does a third of the multiply-adds); split Q1 0.33 / 1.21 / 0.35, Q2 1.37 / 21.9 / 1.53,
+// Q3 - / 11.5 / 0.62; f32 Q2 1.15 / 17.6 / 1.39, Q3 - / 16.7 / 0.55. So: sum factorisation
+// always in f64, and in f32 and split precision above the degrees with paired kernels
+// (quadrilaterals and hexahedra Q1-Q2).
+bool sumfact_preferred(const tlg_tables* t) { return t->sf_ok && (t->dtype == TLG_F64 || t->sf_n >= 4); }
+
+// The sum-factorised kernel; `found` is false when it does not apply (no tensor structure, facet
+// normals, split precision at a tile other than 16, or no instantiation): nothing is launched.
+tlg_status eval_sumfact(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                        cudaStream_t stream, bool* found) {
+  *found = false;
+  if (!t->sf_ok || (mask & tlg::kOutFacetNormals) || (t->dtype == TLG_SPLIT32 && o->tile != 16))
+    return TLG_ERR_UNSUPPORTED;
+  tlg::SfArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = b->nodes;
+  a.dofmap = b->dofmap;
+  a.flags = b->flags;
+  a.tab = t->dev + t->off_sf;
+  a.tab_bytes = t->sf_bytes;
+  a.dphi64 = t->dtype == TLG_SPLIT32 ? reinterpret_cast<const double*>(t->dev + t->off_dphi64) : nullptr;
+  void* outs[5] = {o->points, o->jacobian, o->detj, o->pinv, o->normals};
+  for (int i = 0; i < 5; ++i) a.out[i] = outs[i];
+  a.err = t->err;
+  a.recomputed = o->recomputed;
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + o->tile - 1) / o->tile * o->tile;
+  a.range_cells = o->num_cells;
+  a.out_first_cell = o->out_first_cell;
+  a.tile_shift = tile_shift(o->tile);
+  a.last_cell = b->num_cells - 1;
+  const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
+  a.last_flag = nflags - 1;
+  for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
+  a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 256.0f;
+  a.last_node = (uint32_t)(b->num_nodes - 1);
+  for (int d = 0; d < 3; ++d) {
+    a.off_b[d] = t->sf_offb[d];
+    a.off_d[d] = t->sf_offd[d];
+    a.m[d] = t->sf_m[d];
+  }
+  a.off_perm = t->sf_offperm;
+  a.mask = mask;
+  a.num_points = (int)t->q;
+  const size_t fbytes = t->dtype == TLG_F64 ? 8 : 4;
+  const size_t smem = (t->sf_bytes + 15) / 16 * 16 + tlg::sumfact_slot_bytes((int)t->k, t->gd, fbytes);
+  if (smem > (size_t)227 * 1024) return TLG_ERR_UNSUPPORTED;
+  cudaError_t e = tlg::launch_sumfact(t->dtype, t->td, t->gd, t->sf_n, a, smem, stream, found);
+  if (!*found) return TLG_ERR_UNSUPPORTED;
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  g_last_family = TLG_STRATEGY_SUMFACT;
+  return ok();
+}
+
 void fill_pair_args(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
                     tlg::PairArgs* ap);
 
@@ -123,6 +214,7 @@ tlg_status eval_pair(const tlg_tables* t, const tlg_block* b, const tlg_outputs*
   cudaError_t e = tlg::launch_eval_pair(split, t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
   if (!*found) return TLG_ERR_UNSUPPORTED;
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  g_last_family = TLG_STRATEGY_DIRECT;
   return ok();
 }
 
@@ -160,12 +252,12 @@ void fill_pair_args(const tlg_tables* t, const tlg_block* b, const tlg_outputs* 
 }
 
 tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
-                      cudaStream_t stream) {
+                      cudaStream_t stream, bool loops_only) {
   if (o->tile != 16)
     return fail(TLG_ERR_UNSUPPORTED, "tlg_eval_block: split precision runs with tile 16, not " +
                                          std::to_string(o->tile));
   bool found = false;
-  tlg_status st = eval_pair(t, b, o, mask, true, stream, &found);
+  tlg_status st = loops_only ? TLG_ERR_UNSUPPORTED : eval_pair(t, b, o, mask, true, stream, &found);
   if (found) return st;
   // No paired kernel for this element, or tables beyond the shared-memory budget.
   tlg::PairArgs a;
@@ -173,12 +265,13 @@ tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs
   fill_pair_args(t, b, o, mask, &a);
   cudaError_t e = tlg::launch_split_loops(t->td, t->gd, !t->staged, a, t->bytes, stream);
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  g_last_family = TLG_STRATEGY_LOOPS;
   return ok();
 }
 
 template <typename F>
 tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
-                      cudaStream_t stream) {
+                      cudaStream_t stream, bool loops_only) {
   tlg::EvalArgs<F> a;
   std::memset(&a, 0, sizeof(a));
   a.nodes = static_cast<const F*>(b->nodes);
@@ -205,10 +298,11 @@ tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs
   a.tile_shift = shift;
   a.k_runtime = (int)t->k;
   a.tab_global = t->staged ? 0 : 1;
+  a.loops_only = loops_only ? 1 : 0;
   bool direct = false;
   cudaError_t e;
   if constexpr (sizeof(F) == 4) {
-    if (shift == 4) {  // the GPU tile: the paired-FP32 kernel, when one is compiled for the element
+    if (shift == 4 && !loops_only) {  // the GPU tile: the paired-FP32 kernel, when compiled
       tlg_status st = eval_pair(t, b, o, mask, false, stream, &direct);
       if (direct) return st;
     }
@@ -217,6 +311,7 @@ tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs
     e = tlg::launch_eval_f64(t->td, t->gd, (int)t->k, a, t->bytes, stream, &direct);
   }
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  g_last_family = direct ? TLG_STRATEGY_DIRECT : TLG_STRATEGY_LOOPS;
   return ok();
 }
 
@@ -287,6 +382,90 @@ tlg_status tlg_reference_facet_normals(int cell, double* out, int64_t cap) {
   });
 }
 
+namespace {
+
+// 1D Lagrange basis at the sorted nodes s: l_i(x) and l_i'(x).
+void lagrange_1d(const std::vector<double>& s, double x, double* val, double* der) {
+  const int n = (int)s.size();
+  for (int i = 0; i < n; ++i) {
+    double v = 1.0, d = 0.0;
+    for (int r = 0; r < n; ++r) {
+      if (r == i) continue;
+      const double w = 1.0 / (s[i] - s[r]);
+      d = d * (x - s[r]) * w + v * w;
+      v *= (x - s[r]) * w;
+    }
+    val[i] = v;
+    der[i] = d;
+  }
+}
+
+// The sum-factorisation tables of a quadrilateral or hexahedron at `points`, when the points are
+// a tensor product (direction 0 fastest, as the collapsed rules order them) and the Lagrange
+// nodes a tensor lattice: per direction the 1D rule u_d, B_d = l(u_d), D_d = l'(u_d), and the
+// lexicographic-to-Lagrange node permutation. Returns false when the structure is absent.
+bool tensor_tables(int cell, int degree, int family, const double* pts, int64_t nq, int* m,
+                   std::vector<double>* B, std::vector<double>* D, std::vector<uint32_t>& perm) {
+  const int td = tlg::tdim(cell);
+  const int n = degree + 1;
+  if (nq < 1) return false;
+  // Points per direction.
+  int64_t m0 = 1;
+  while (m0 < nq) {
+    bool same = true;
+    for (int d = 1; d < td; ++d) same = same && pts[m0 * td + d] == pts[d];
+    if (!same) break;
+    ++m0;
+  }
+  int64_t m1 = nq / m0, m2 = 1;
+  if (td == 3) {
+    m1 = 1;
+    while (m1 * m0 < nq && pts[m1 * m0 * td + 2] == pts[2] && pts[m1 * m0 * td] == pts[0]) ++m1;
+    m2 = nq / (m0 * m1);
+  }
+  if (m0 * m1 * m2 != nq) return false;
+  m[0] = (int)m0;
+  m[1] = (int)m1;
+  m[2] = (int)m2;
+  std::vector<double> u[3];
+  for (int64_t a0 = 0; a0 < m0; ++a0) u[0].push_back(pts[a0 * td]);
+  for (int64_t a1 = 0; a1 < m1; ++a1) u[1].push_back(pts[a1 * m0 * td + 1]);
+  if (td == 3)
+    for (int64_t a2 = 0; a2 < m2; ++a2) u[2].push_back(pts[a2 * m0 * m1 * td + 2]);
+  for (int64_t q = 0; q < nq; ++q) {
+    const int64_t idx[3] = {q % m0, (q / m0) % m1, q / (m0 * m1)};
+    for (int d = 0; d < td; ++d)
+      if (pts[q * td + d] != u[d][idx[d]]) return false;
+  }
+  // 1D nodes and the node permutation.
+  std::vector<double> s1 = tlg::lagrange_points(tlg::kInterval, degree, family);
+  std::sort(s1.begin(), s1.end());
+  const std::vector<double> lp = tlg::lagrange_points(cell, degree, family);
+  const int64_t k = tlg::num_lagrange_nodes(cell, degree);
+  perm.assign((size_t)k, 0xFFFFFFFFu);
+  for (int64_t kk = 0; kk < k; ++kk) {
+    int64_t l = 0, scale = 1;
+    for (int d = 0; d < td; ++d) {
+      int found = -1;
+      for (int i = 0; i < n; ++i)
+        if (std::fabs(lp[kk * td + d] - s1[i]) < 1e-12) found = i;
+      if (found < 0) return false;
+      l += found * scale;
+      scale *= n;
+    }
+    if (perm[(size_t)l] != 0xFFFFFFFFu) return false;
+    perm[(size_t)l] = (uint32_t)kk;
+  }
+  for (int d = 0; d < td; ++d) {
+    B[d].assign(u[d].size() * n, 0.0);
+    D[d].assign(u[d].size() * n, 0.0);
+    for (size_t a = 0; a < u[d].size(); ++a) lagrange_1d(s1, u[d][a], &B[d][a * n], &D[d][a * n]);
+  }
+  return true;
+}
+
+}  // namespace
+
 tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dtype,
                              const double* points, int64_t npoints, const double* ref_normals,
                              tlg_tables** out) {
@@ -351,7 +530,36 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       const size_t vb = (size_t)(dtype == TLG_SPLIT32 ? qp : npoints) * k * 32;
       if (vb > 0 && vb <= (size_t)160 * 1024) t->vjp_bytes = (uint32_t)vb;
     }
-    t->host.assign(t->off_vjp + t->vjp_bytes, 0);
+    std::vector<double> sf_b[3], sf_d[3];
+    std::vector<uint32_t> sf_perm;
+    if ((cell == tlg::kQuadrilateral || cell == tlg::kHexahedron) && degree + 1 <= 6)
+      t->sf_ok = tensor_tables(cell, degree, family, points, npoints, t->sf_m, sf_b, sf_d, sf_perm);
+    t->off_sf = (uint32_t)align16(t->off_vjp + t->vjp_bytes);
+    if (t->sf_ok) {
+      t->sf_n = degree + 1;
+      size_t off = 0;
+      for (int d = 0; d < td; ++d) {
+        t->sf_offb[d] = (uint32_t)off;
+        off = align16(off + sf_b[d].size() * es);
+        t->sf_offd[d] = (uint32_t)off;
+        off = align16(off + sf_d[d].size() * es);
+      }
+      t->sf_offperm = (uint32_t)off;
+      t->sf_bytes = (uint32_t)align16(off + sf_perm.size() * 4);
+    }
+    t->host.assign(t->off_sf + t->sf_bytes, 0);
+    if (t->sf_ok) {
+      for (int d = 0; d < td; ++d) {
+        if (dtype == TLG_F64) {
+          narrow_into<double>(t->host, t->off_sf + t->sf_offb[d], sf_b[d].data(), sf_b[d].size());
+          narrow_into<double>(t->host, t->off_sf + t->sf_offd[d], sf_d[d].data(), sf_d[d].size());
+        } else {
+          narrow_into<float>(t->host, t->off_sf + t->sf_offb[d], sf_b[d].data(), sf_b[d].size());
+          narrow_into<float>(t->host, t->off_sf + t->sf_offd[d], sf_d[d].data(), sf_d[d].size());
+        }
+      }
+      std::memcpy(t->host.data() + t->off_sf + t->sf_offperm, sf_perm.data(), sf_perm.size() * 4);
+    }
     // Reorder [deriv][q][k] into phi [q][k] and dphi [q][k][d].
     std::vector<double> phi(n_phi), dphi(n_dphi), refn(n_refn, 0.0);
     for (int64_t q = 0; q < npoints; ++q)
@@ -477,10 +685,29 @@ tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_out
     return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_eval_block: cells but no nodes");
   if (b->num_nodes > (int64_t)UINT32_MAX + 1 || b->num_cells > (int64_t)UINT32_MAX)
     return fail(TLG_ERR_TOO_LARGE, "tlg_eval_block: node or cell count does not fit u32");
-  if (t->dtype == TLG_SPLIT32) return eval_split(t, b, o, mask, static_cast<cudaStream_t>(stream));
-  if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, static_cast<cudaStream_t>(stream));
-  return eval_typed<double>(t, b, o, mask, static_cast<cudaStream_t>(stream));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int strategy = current_strategy();
+  if (strategy == TLG_STRATEGY_SUMFACT || (strategy == TLG_STRATEGY_AUTO && sumfact_preferred(t))) {
+    bool found = false;
+    tlg_status st = eval_sumfact(t, b, o, mask, s, &found);
+    if (found) return st;
+  }
+  const bool loops_only = strategy == TLG_STRATEGY_LOOPS;
+  if (t->dtype == TLG_SPLIT32) return eval_split(t, b, o, mask, s, loops_only);
+  if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, s, loops_only);
+  return eval_typed<double>(t, b, o, mask, s, loops_only);
 }
+
+tlg_status tlg_set_strategy(int strategy) {
+  if (strategy < -1 || strategy > TLG_STRATEGY_SUMFACT)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_strategy: strategy must be -1 .. 3");
+  g_strategy.store(strategy, std::memory_order_relaxed);
+  return ok();
+}
+
+int tlg_get_strategy(void) { return current_strategy(); }
+
+int tlg_last_kernel_family(void) { return g_last_family; }
 
 tlg_status tlg_evector(const tlg_block* b, int nodes_per_cell, int64_t first_cell, int64_t chunk_cells,
                        int64_t stride, void* out, void* stream) {

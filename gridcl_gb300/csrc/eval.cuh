@@ -70,6 +70,7 @@ struct EvalArgs {
   int tile_shift;            // log2(tile)
   int k_runtime;             // K for the loops kernel
   int tab_global;            // loops kernel: tables read from global memory, not staged
+  int loops_only;            // the loops kernel even where an unrolled kernel is compiled
 };
 
 // Arguments of the paired kernels (f32 arithmetic; nodes f32, or f64 with SPLIT).

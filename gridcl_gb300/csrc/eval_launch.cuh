@@ -74,6 +74,12 @@ cudaError_t launch_eval_pair(bool split, int td, int gd, int k, const PairArgs& 
 // shared memory or (tab_global) read from global memory.
 cudaError_t launch_split_loops(int td, int gd, bool tab_global, const PairArgs& a, size_t smem, cudaStream_t s);
 
+struct SfArgs;
+// Defined in sumfact.cu: the sum-factorised kernel for precision 4 (f32), 8 (f64) or 12 (split),
+// N nodes per direction; `found` is false when none is compiled for (td, gd, n).
+cudaError_t launch_sumfact(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
+                           bool* found);
+
 struct VjpArgs;
 // Defined in vjp_f64.cu / vjp_split.cu; `found` is false when no kernel exists for (d, k). `smem`
 // is the dynamic shared memory: the staged tables (rounded up to 16 bytes) and the staging slots.

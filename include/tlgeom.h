@@ -236,6 +236,28 @@ tlg_status tlg_vjp_block(const tlg_tables* tables, const tlg_block* block, const
 tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes,
                           int gdim, const void* local, int local_dtype, double* grad, void* stream);
 
+/* Evaluation strategy (the reference's strategy::choose, tetraloma-geometry/src/strategy.rs:
+ * 373-407, with its precedence: a scoped setting, then the environment, then the built-in
+ * policy). AUTO picks per element: for quadrilaterals and hexahedra at tensor-product point sets,
+ * sum factorisation in f64 and above the degrees with paired kernels (Q1-Q2) in f32 and split
+ * precision; otherwise the paired / unrolled kernels where compiled, the loops kernels else. DIRECT, LOOPS and SUMFACT force a kernel family where it
+ * applies (sum factorisation needs a quadrilateral or hexahedron at a tensor-product point set,
+ * no facet normals, and tile 16 in split precision; elsewhere the AUTO choice runs). The environment variable TLG_GEOM_STRATEGY (auto, direct, loops, sumfact) is read once;
+ * tlg_set_strategy overrides it for the process until called with -1. */
+typedef enum tlg_strategy {
+  TLG_STRATEGY_AUTO = 0,
+  TLG_STRATEGY_DIRECT = 1,
+  TLG_STRATEGY_LOOPS = 2,
+  TLG_STRATEGY_SUMFACT = 3
+} tlg_strategy;
+tlg_status tlg_set_strategy(int strategy);
+/* The strategy in effect (TLG_STRATEGY_*). */
+int tlg_get_strategy(void);
+/* The kernel family that ran in this thread's last launching tlg_eval_block: DIRECT (paired or
+ * unrolled), LOOPS or SUMFACT; 0 before any (the reference's record_strategies test hook,
+ * tetraloma-geometry/src/testing.rs:34-43). */
+int tlg_last_kernel_family(void);
+
 /* ---------------------------------------------------------------------------------------
  * Measure (tetraloma-geometry/src/measure.rs:15-185): per-cell sums of det J * w over the
  * points of a det J QuadField chunk, then a sum tree of 64-value blocks, all in F and in a

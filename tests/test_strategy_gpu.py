@@ -1,0 +1,131 @@
+"""Evaluation strategies (GPU): the paired/unrolled, loops and sum-factorised kernels against the
+oracle for quadrilaterals and hexahedra at tensor-product rules, in f64, f32 and split
+precision, with the kernel family that ran recorded per launch (the reference's strategy tests,
+tetraloma-geometry/tests/strategy.rs)."""
+
+import numpy as np
+import pytest
+import torch
+
+import gridcl_gb300 as tg
+from gridcl_gb300 import meshes
+from oracle import oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+F64, F32 = torch.float64, torch.float32
+KEYS = {"points": "x", "jacobian": "j", "detj": "detj", "pinv": "k", "normals": "normals"}
+
+
+def quad_box(n, degree, gd):
+    """The unit square of n^2 quadrilaterals, interior nodes jittered; with gd = 3 lifted to the
+    surface z = 0.1 sin(2 pi x) sin(2 pi y)."""
+    m = meshes.square_box("Quadrilateral", n, degree)
+    x = meshes.jitter_interior(m.nodes, m.nodes, 0.02 / n, 2026)
+    if gd == 3:
+        z = 0.1 * np.sin(2 * np.pi * x[:, 0]) * np.sin(2 * np.pi * x[:, 1])
+        x = np.column_stack([x, z])
+        m = meshes.HostMesh(3, x, m.blocks)
+    else:
+        m.nodes = x
+    return m
+
+
+CASES = [
+    # (cell, n, degree, rule degree, gdim)
+    ("Hexahedron", 3, 1, 2, 3),
+    ("Hexahedron", 3, 2, 4, 3),
+    ("Hexahedron", 2, 3, 6, 3),
+    ("Quadrilateral", 4, 1, 2, 2),
+    ("Quadrilateral", 4, 2, 4, 2),
+    ("Quadrilateral", 3, 3, 6, 2),
+    ("Quadrilateral", 3, 4, 8, 2),
+    ("Quadrilateral", 2, 5, 10, 2),
+    ("Quadrilateral", 4, 2, 4, 3),
+    ("Quadrilateral", 3, 4, 8, 3),
+]
+
+
+def mesh_for(cell, n, degree, gd):
+    return meshes.curved_box(cell, n, degree, jitter=0.02) if cell == "Hexahedron" else quad_box(n, degree, gd)
+
+
+def factors_for(gd, td):
+    return ("points", "jacobian", "detj", "pinv") + (("normals",) if td + 1 == gd else ())
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "split"])
+@pytest.mark.parametrize("strategy", ["direct", "loops", "sumfact"])
+@pytest.mark.parametrize("cell,n,degree,rdeg,gd", CASES)
+def test_strategies_match_the_oracle(cuda, cell, n, degree, rdeg, gd, strategy, precision):
+    mesh = mesh_for(cell, n, degree, gd)
+    td = 3 if cell == "Hexahedron" else 2
+    g = tg.Geometry.from_host(mesh, dtype=F32 if precision == "f32" else F64)
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    names = factors_for(gd, td)
+    with tg.with_strategy(strategy):
+        got = tg.geometric_factors_block(g, 0, ps, names, precision="split" if precision == "split" else "native")
+        family = tg.last_kernel_family()
+    if strategy == "sumfact":
+        assert family == "sumfact"
+    elif strategy == "loops":
+        assert family == "loops"
+    else:
+        assert family in ("direct", "loops")
+    absx = g.nodes.double().cpu().numpy() + np.array(g.origin[:gd])
+    want = orc.eval_block(cell, degree, absx, mesh.blocks[0].cells, pts, factors=[KEYS[f] for f in names])
+    base = orc.TOL_F64 if precision == "f64" else orc.TOL_F32
+    nodes = orc.node_ratio(cell, degree)
+    s_val = orc.tolerance_scale(cell, degree, "Equispaced", pts, "values") * nodes
+    s_der = orc.tolerance_scale(cell, degree, "Equispaced", pts) * nodes
+    if precision == "f32":  # coordinates rounded relative to the origin
+        ratio = orc.origin_ratio(absx, np.array(g.origin[:gd]), want["j"])
+        s_val, s_der = s_val * ratio, s_der * ratio
+    cond = orc.condition_scale(want["j"], td, gd)
+    scale = {"points": s_val, "jacobian": s_der, "detj": s_der, "pinv": s_der * cond, "normals": s_der * cond}
+    for f in names:
+        err = orc.rel_err(got[f].to_host_cell_major(), want[KEYS[f]])
+        assert err < base * scale[f], (f, err, base * scale[f])
+
+
+def test_sumfact_needs_a_tensor_rule(cuda):
+    """A point set that is not a tensor product (a shuffled Gauss rule) runs another family under
+    the sumfact strategy, with the same values."""
+    mesh = meshes.curved_box("Hexahedron", 2, 2, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=F64)
+    pts, _ = tg.refcell.gauss_rule("Hexahedron", 4)
+    perm = np.random.default_rng(3).permutation(len(pts))
+    shuffled = tg.PointSet("Hexahedron", pts[perm], np.ones(len(pts)))
+    with tg.with_strategy("sumfact"):
+        got = tg.geometric_factors_block(g, 0, shuffled, ("jacobian",))
+        assert tg.last_kernel_family() != "sumfact"
+    with tg.with_strategy("sumfact"):
+        tensor = tg.geometric_factors_block(g, 0, tg.PointSet("Hexahedron", pts, np.ones(len(pts))), ("jacobian",))
+        assert tg.last_kernel_family() == "sumfact"
+    a = got["jacobian"].to_host_cell_major()
+    b = tensor["jacobian"].to_host_cell_major()[:, perm]
+    assert orc.rel_err(a, b) < 1e-13
+
+
+@pytest.mark.parametrize("precision,degree,family", [("f64", 2, "sumfact"), ("f64", 1, "sumfact"),
+                                                     ("split", 2, "direct"), ("split", 3, "sumfact"),
+                                                     ("f32", 2, "direct"), ("f32", 3, "sumfact")])
+def test_auto_policy(cuda, precision, degree, family):
+    mesh = meshes.curved_box("Hexahedron", 2, degree, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=F32 if precision == "f32" else F64)
+    pts, _ = tg.refcell.gauss_rule("Hexahedron", 2 * degree)
+    ps = tg.PointSet("Hexahedron", pts, np.ones(len(pts)))
+    with tg.with_strategy("auto"):
+        tg.geometric_factors_block(g, 0, ps, ("detj",), precision="split" if precision == "split" else "native")
+        assert tg.last_kernel_family() == family
+
+
+def test_strategy_scopes_nest_and_restore(cuda):
+    before = tg.get_strategy()
+    with tg.with_strategy("loops"):
+        assert tg.get_strategy() == "loops"
+        with tg.with_strategy("sumfact"):
+            assert tg.get_strategy() == "sumfact"
+        assert tg.get_strategy() == "loops"
+    assert tg.get_strategy() == before
