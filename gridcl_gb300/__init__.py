@@ -28,6 +28,7 @@ from .geometry import (
     normals_block,
     physical_points_block,
     pseudo_inverse_block,
+    pull_back_block,
     vjp_block,
 )
 from .strategy import get_strategy, last_kernel_family, set_strategy, with_strategy
@@ -37,6 +38,6 @@ __all__ = [
     "Batch", "CoordinateElement", "Geometry", "GeometryBlock", "GridError", "PointSet", "QuadField",
     "QuadRule", "detj_block", "facet_normals_block", "facet_point_set", "fd_check",
     "geometric_factors_block", "jacobians_block", "lib", "measure_block", "meshes", "normals_block",
-    "node_incidence", "physical_points_block", "pseudo_inverse_block", "refcell", "vjp_block",
+    "node_incidence", "physical_points_block", "pseudo_inverse_block", "pull_back_block", "refcell", "vjp_block",
     "get_strategy", "last_kernel_family", "set_strategy", "with_strategy",
 ]

@@ -437,6 +437,62 @@ def measure_block(g: Geometry, b: int, pts: PointSet, detj: QuadField | None = N
     return float(result.item()) if sync else result
 
 
+_BASES: dict = {}
+
+
+def _basis(el: CoordinateElement):
+    """The device Lagrange basis at arbitrary points of a coordinate element (cached)."""
+    key = (el.cell, el.degree, el.family)
+    h = _BASES.get(key)
+    if h is None:
+        h = ctypes.c_void_p()
+        check(lib().tlg_basis_create(CELL_IDS[el.cell], el.degree, FAMILY_IDS[el.family], ctypes.byref(h)))
+        _BASES[key] = h
+    return h
+
+
+def pull_back_block(g: Geometry, b: int, x: QuadField, tolerance: float | None = None,
+                    max_iterations: int = 16):
+    """Reference points of the physical points `x` (a QuadField of block b, GD components) by
+    Newton's method (tetraloma-geometry/src/pull_back.rs:566): returns ``(xi, step)``, xi with
+    TD components and step = |delta xi|_inf of each point's last iteration, tiled and chunked as
+    `x`. Every point starts at the reference cell's vertex centroid and runs `max_iterations`
+    steps (no early exit), clamped to [-0.1, 1.1]^TD and frozen once its step is at most the
+    tolerance (None: 1e-13 in f64, 1e-5 in f32); a point has converged when its step is at most
+    the tolerance."""
+    blk = g.blocks[b]
+    td = blk.element.tdim
+    if x.num_cells != blk.num_cells:
+        raise GridError(2, f"LengthMismatch {{ expected: {blk.num_cells}, found: {x.num_cells} }}")
+    if x.length != g.gdim:
+        raise GridError(1, f"pull_back_block: points of {x.length} components on a grid of dimension {g.gdim}")
+    if max_iterations < 0:
+        raise GridError(1, "pull_back_block: max_iterations must be >= 0")
+    nq, tile = x.num_points, x.tile
+    xi_chunks, step_chunks = [], []
+    for ch in x.chunks:
+        if ch.data.dtype != g.dtype:
+            raise GridError(1, f"pull_back_block: points of {ch.data.dtype} on a {g.dtype} grid")
+        padded = -(-ch.num_cells // tile) * tile
+        xi_chunks.append(QuadChunk(ch.first_cell, ch.num_cells,
+                                   torch.empty(padded * nq * td, dtype=g.dtype, device=g.nodes.device)))
+        step_chunks.append(QuadChunk(ch.first_cell, ch.num_cells,
+                                     torch.empty(padded * nq, dtype=g.dtype, device=g.nodes.device)))
+    xi = QuadField(xi_chunks, blk.num_cells, nq, td, tile)
+    step = QuadField(step_chunks, blk.num_cells, nq, 1, tile)
+    if blk.num_cells == 0 or nq == 0:
+        return xi, step
+    h = _basis(blk.element)
+    desc = g.block_desc(b)
+    stream = current_stream_handle()
+    tol = 0.0 if tolerance is None else float(tolerance)
+    for ch, cxi, cst in zip(x.chunks, xi_chunks, step_chunks):
+        check(lib().tlg_pull_back_block(h, ctypes.byref(desc), ch.data.data_ptr(), 0, ch.first_cell,
+                                        ch.num_cells, 0, nq, tile, tol, max_iterations,
+                                        cxi.data.data_ptr(), cst.data.data_ptr(), stream))
+    return xi, step
+
+
 @dataclasses.dataclass
 class NodeIncidence:
     """Node-to-(cell, local node) CSR of one block: node n's dofmap entries e = cell * K + k

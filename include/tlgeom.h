@@ -236,6 +236,27 @@ tlg_status tlg_vjp_block(const tlg_tables* tables, const tlg_block* block, const
 tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes,
                           int gdim, const void* local, int local_dtype, double* grad, void* stream);
 
+/* ---------------------------------------------------------------------------------------
+ * Pull-back (tetraloma-geometry/src/pull_back.rs:94-330, 566): the reference point xi of each
+ * physical point of a block by Newton's method on the cell's Lagrange map. Every point starts
+ * at the reference cell's vertex centroid (rounded to f32) and runs exactly max_iterations
+ * steps delta = K(xi) (y - X(xi)) (K the pseudo-inverse when TD < GD: Gauss-Newton); a point
+ * not yet frozen moves to xi + delta clamped to [-0.1, 1.1]^TD, records |delta|_inf (the
+ * largest finite value when a component is not finite) and freezes once that is at most the
+ * tolerance (<= 0 selects 1e-13 in f64, 1e-5 in f32); frozen points keep xi and their step.
+ * A point has converged when its step is at most the tolerance. */
+typedef struct tlg_basis tlg_basis;
+/* The Lagrange basis of (cell, degree, family) at arbitrary reference points (device). */
+tlg_status tlg_basis_create(int cell, int degree, int family, tlg_basis** out);
+tlg_status tlg_basis_destroy(tlg_basis* basis);
+/* Points x: a QuadField chunk of GD components (absolute coordinates), x_first_cell the range's
+ * first cell in it; outputs xi (TD components) and step (1) chunks at out_first_cell; the same
+ * tile and num_points for all three. Replaces pull_back_block's kernels. */
+tlg_status tlg_pull_back_block(const tlg_basis* basis, const tlg_block* block, const void* x,
+                               int64_t x_first_cell, int64_t first_cell, int64_t num_cells,
+                               int64_t out_first_cell, int num_points, int tile, double tolerance,
+                               int max_iterations, void* xi, void* step, void* stream);
+
 /* Evaluation strategy (the reference's strategy::choose, tetraloma-geometry/src/strategy.rs:
  * 373-407, with its precedence: a scoped setting, then the environment, then the built-in
  * policy). AUTO picks per element: for quadrilaterals and hexahedra at tensor-product point sets,

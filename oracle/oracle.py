@@ -10,6 +10,7 @@ calls it.
   widened to f64 plus the origin, gathered through the dofmap, contracted with the f64
   tabulation.
 - :func:`evector` is the E-vector gather of ``tetraloma-geometry/src/evector.rs:195-236``.
+- :func:`pull_back` is the Newton pull-back of ``tetraloma-geometry/src/pull_back.rs:102-194``.
 - :func:`untile` is ``QuadField::to_host_cell_major`` (``tetraloma-geometry/src/field.rs:380-408``).
 - :func:`rel_err` and the tolerance scales restate ``reference.rs:579-817``.
 """
@@ -130,6 +131,53 @@ def vjp(cell: str, degree: int, nodes_abs: np.ndarray, dofmap: np.ndarray, point
     if rc != 0:
         raise ValueError(f"orc_vjp rejected its arguments ({rc})")
     return grad
+
+
+CENTROID = {"Interval": (0.5,), "Triangle": (1 / 3, 1 / 3), "Quadrilateral": (0.5, 0.5),
+            "Tetrahedron": (0.25, 0.25, 0.25), "Hexahedron": (0.5, 0.5, 0.5), "Prism": (1 / 3, 1 / 3, 0.5)}
+
+
+def pull_back(cell: str, degree: int, nodes_abs: np.ndarray, dofmap: np.ndarray, x_abs: np.ndarray,
+              tolerance: float = 1e-13, max_iterations: int = 16, family: str = "Equispaced"):
+    """Reference points ``[cell][q][TD]`` and last steps ``[cell][q]`` of the physical points
+    ``x_abs [cell][q][GD]`` (tetraloma-geometry/src/pull_back.rs:102-194, 566): from the vertex
+    centroid rounded to f32, `max_iterations` Newton steps delta = K (y - X) with K the
+    pseudo-inverse of J, iterates clamped to [-0.1, 1.1] (bounds rounded to f32), |delta|_inf
+    recorded (the largest finite value when not finite), points frozen once it is at most the
+    tolerance. f64, the basis from the restated tabulation at the iterates."""
+    td = refcell.tdim(cell)
+    nodes_abs = np.asarray(nodes_abs, dtype=np.float64)
+    dofmap = np.asarray(dofmap, dtype=np.int64)
+    xc = nodes_abs[np.minimum(dofmap, nodes_abs.shape[0] - 1)]  # [cell][K][GD]
+    y = np.asarray(x_abs, dtype=np.float64)
+    nc, nq, gd = y.shape
+    big = np.finfo(np.float64).max
+    lo, hi = float(np.float32(-0.1)), float(np.float32(1.1))
+    start = np.array([float(np.float32(c)) for c in CENTROID[cell]])
+    p = np.broadcast_to(start, (nc, nq, td)).copy()
+    last = np.full((nc, nq), big)
+    frozen = np.zeros((nc, nq), dtype=bool)
+    for _ in range(max_iterations):
+        tab = refcell.tabulate(cell, degree, p.reshape(-1, td), 1, family)
+        k = tab.shape[2]
+        phi = tab[0].reshape(nc, nq, k)
+        dphi = tab[1:].reshape(td, nc, nq, k)
+        X = np.einsum("cqk,ckg->cqg", phi, xc)
+        J = np.einsum("dcqk,ckg->cqgd", dphi, xc)  # J[g][d]
+        with np.errstate(all="ignore"):
+            K = np.linalg.pinv(J)  # [c][q][d][g]
+            delta = np.einsum("cqdg,cqg->cqd", K, y - X)
+            m = np.abs(delta)
+            bad = ~np.all(m <= big, axis=2)
+            s_ = np.where(bad, big, np.max(np.where(np.isfinite(m), m, 0.0), axis=2))
+            q_ = p + delta
+            q_ = np.where(q_ < lo, lo, q_)
+            q_ = np.where(q_ > hi, hi, q_)
+        move = ~frozen
+        p = np.where(move[..., None], q_, p)
+        last = np.where(move, s_, last)
+        frozen = frozen | (move & (s_ <= tolerance))
+    return p, last
 
 
 def evector(nodes_stored: np.ndarray, dofmap: np.ndarray, num_cells: int, k: int, gd: int,

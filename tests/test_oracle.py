@@ -171,3 +171,30 @@ def test_rel_err_semantics():
     assert abs(orc.rel_err([1.0, 1.1e-3, 1e-3, 2.0], [1.0, 1e-3, 1e-3, 2.0]) - 5e-5) < 1e-15
     assert orc.rel_err([1e-3], [0.0]) == 1e-3
     assert orc.rel_err([1.0, float("nan")], [1.0, 1.0]) == float("inf")
+
+
+@pytest.mark.parametrize("cell,degree", [("Tetrahedron", 2), ("Hexahedron", 2), ("Prism", 2), ("Tetrahedron", 1)])
+def test_oracle_pull_back_round_trip(cell, degree):
+    """The oracle's Newton pull-back returns the Gauss points of curved cells from their images
+    (pull_back.rs's documented property), every point converged."""
+    from gridcl_gb300 import meshes
+    m = meshes.curved_box(cell, 2, degree, jitter=0.02)
+    pts, _ = rc.gauss_rule(cell, 4)
+    x = orc.eval_block(cell, degree, m.nodes, m.blocks[0].cells, pts, factors=("x",))["x"]
+    xi, step = orc.pull_back(cell, degree, m.nodes, m.blocks[0].cells, x)
+    assert np.abs(xi - pts[None]).max() < 1e-13
+    assert step.max() <= 1e-13
+
+
+def test_oracle_pull_back_centres_and_outside_points():
+    """Cell centres of an affine square pull back to the reference centre (pull_back.rs's
+    example); a point outside its cell stays in the clamp box and does not converge."""
+    from gridcl_gb300 import meshes
+    m = meshes.square_box("Quadrilateral", 2, 1)
+    cells = m.blocks[0].cells
+    centres = m.nodes[cells].mean(axis=1)[:, None, :]
+    xi, step = orc.pull_back("Quadrilateral", 1, m.nodes, cells, centres, tolerance=1e-5)
+    assert np.allclose(xi, 0.5, atol=1e-12) and step.max() <= 1e-5
+    far = centres + np.array([0.0, 2.0])  # two cell widths away
+    xi, step = orc.pull_back("Quadrilateral", 1, m.nodes, cells, far, tolerance=1e-5)
+    assert np.all(xi <= float(np.float32(1.1))) and np.all(step > 1e-5)
