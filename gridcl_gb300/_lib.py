@@ -114,7 +114,7 @@ SIGNATURES = [
     ("tlg_basis_create", _I, [_I, _I, _I, _P]),
     ("tlg_basis_destroy", _I, [_P]),
     ("tlg_pull_back_block", _I, [_P, ctypes.POINTER(TlgBlock), _P, _L, _L, _L, _L, _I, _I,
-                                 ctypes.c_double, _I, _P, _P, _P]),
+                                 ctypes.c_double, _I, _I, _P, _P, _P]),
 ]
 
 _lib = None

@@ -30,6 +30,7 @@
 
 #include <cuda_runtime.h>
 
+#include "convert.cuh"
 #include "eval.cuh"
 #include "refcell.h"
 #include "status.h"
@@ -65,6 +66,7 @@ struct PullBackArgs {
   double tolerance;
   uint32_t last_node;
   int num_points, max_iterations, tile_shift, threads;
+  int refinements;  // mixed precision: FP64-residual steps after the FP32 iteration (0: native)
 };
 
 template <typename F>
@@ -104,8 +106,9 @@ __device__ void simplex_factors(int p, F lam, F* f, F* df) {
   }
 }
 
-// X (GD) and J (J(g, d) at d * GD + g) at xi from the node coordinates in the thread's slots.
-template <typename F, int TD, int GD>
+// X (GD) and, with WANT_J, J (J(g, d) at d * GD + g) at xi from the node coordinates in the
+// thread's slots.
+template <typename F, int TD, int GD, bool WANT_J = true>
 __device__ void map_at(const BasisData& b, const F* xs, int T, const F* xi, F* X, F* J) {
   constexpr int MAXN = kBasisMaxN;
   F v[3][MAXN], dv[3][MAXN];
@@ -132,8 +135,9 @@ __device__ void map_at(const BasisData& b, const F* xs, int T, const F* xi, F* X
   }
 #pragma unroll
   for (int g = 0; g < GD; ++g) X[g] = F(0);
+  if constexpr (WANT_J)
 #pragma unroll
-  for (int i = 0; i < TD * GD; ++i) J[i] = F(0);
+    for (int i = 0; i < TD * GD; ++i) J[i] = F(0);
   for (int k = 0; k < b.k; ++k) {
     const uint8_t* id = b.idx[k];
     F phi, grad[3];
@@ -186,10 +190,55 @@ __device__ void map_at(const BasisData& b, const F* xs, int T, const F* xi, F* X
     for (int g = 0; g < GD; ++g) {
       const F xk = xs[(k * GD + g) * T];
       X[g] = fma(xk, phi, X[g]);
+      if constexpr (WANT_J)
 #pragma unroll
-      for (int d = 0; d < TD; ++d) J[d * GD + g] = fma(xk, grad[d], J[d * GD + g]);
+        for (int d = 0; d < TD; ++d) J[d * GD + g] = fma(xk, grad[d], J[d * GD + g]);
     }
   }
+}
+
+// One step of a point: delta = K r, s = |delta|_inf (the largest finite value when a component
+// is not finite); a point not yet frozen moves to p + delta clamped to [lo, hi], records s and
+// freezes once s <= tol. K(t, g) at g * TD + t (in KT's precision), r and p in P's.
+template <typename P, typename KT, int TD, int GD>
+__device__ __forceinline__ void newton_update(P* p, const KT* K, const P* r, P& last, bool& frozen, P tol, P lo,
+                                              P hi, P big) {
+  P delta[TD];
+  P s = big;
+  bool bad = false;
+#pragma unroll
+  for (int t = 0; t < TD; ++t) {
+    P acc = P(K[t]) * r[0];
+#pragma unroll
+    for (int g = 1; g < GD; ++g) acc = fma(P(K[g * TD + t]), r[g], acc);
+    delta[t] = acc;
+    const P m = fabs(acc);
+    s = t == 0 ? m : (m > s ? m : s);
+    bad = bad || !(m <= big);
+  }
+  if (bad) s = big;
+  if (!frozen) {
+#pragma unroll
+    for (int d = 0; d < TD; ++d) {
+      P qd = p[d] + delta[d];
+      qd = qd < lo ? lo : qd;
+      qd = qd > hi ? hi : qd;
+      p[d] = qd;
+    }
+    last = s;
+    frozen = s <= tol;
+  }
+}
+
+// The vertex centroid of the reference cell, rounded to f32.
+__device__ __forceinline__ void centroid_f32(int cell, float* start) {
+  const float third = 1.0f / 3.0f;
+  if (cell == kTriangle) start[0] = start[1] = third;
+  else if (cell == kTetrahedron) start[0] = start[1] = start[2] = 0.25f;
+  else if (cell == kPrism) {
+    start[0] = start[1] = third;
+    start[2] = 0.5f;
+  } else start[0] = start[1] = start[2] = 0.5f;
 }
 
 template <typename F, int TD, int GD>
@@ -217,18 +266,8 @@ __global__ void pull_back_kernel(const __grid_constant__ PullBackArgs a) {
   const F big = fmax_finite<F>();
   const F lo = F(-0.1f), hi = F(1.1f);
   const F tol = F(a.tolerance);
-  // The vertex centroid of the reference cell, rounded to f32.
-  F start[3];
-  {
-    const int cell = basis.cell;
-    const float third = 1.0f / 3.0f;
-    if (cell == kTriangle) start[0] = start[1] = F(third);
-    else if (cell == kTetrahedron) start[0] = start[1] = start[2] = F(0.25f);
-    else if (cell == kPrism) {
-      start[0] = start[1] = F(third);
-      start[2] = F(0.5f);
-    } else start[0] = start[1] = start[2] = F(0.5f);
-  }
+  float start[3];
+  centroid_f32(basis.cell, start);
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
        c += (int64_t)gridDim.x * blockDim.x) {
     const int64_t cell = min(a.first_cell + c, a.last_cell);
@@ -258,31 +297,110 @@ __global__ void pull_back_kernel(const __grid_constant__ PullBackArgs a) {
         F r[GD];
 #pragma unroll
         for (int g = 0; g < GD; ++g) r[g] = y[g] - X[g];
-        F delta[TD];
-        F s = big;
-        bool bad = false;
+        newton_update<F, F, TD, GD>(p, K_, r, last, frozen, tol, lo, hi, big);
+      }
 #pragma unroll
-        for (int t = 0; t < TD; ++t) {
-          F acc = K_[t] * r[0];  // K(t, g) at g * TD + t
+      for (int d = 0; d < TD; ++d) xi_out[(((to * nq + q) * TD + d) << a.tile_shift) + lo_] = p[d];
+      step_out[((to * nq + q) << a.tile_shift) + lo_] = last;
+    }
+  }
+}
+
+// Mixed precision for f64 meshes: the native iteration in FP32 on coordinates shifted by the
+// cell's first node (rounding relative to the cell size, as the split evaluation), then
+// `refinements` steps with the residual y - X(xi) in FP64 and the correction K r through the
+// FP32 inverse Jacobian at xi: an iteration with an approximate Jacobian, converging linearly
+// at a rate of the FP32 rounding of K times the condition of J, so that a few steps reach the
+// FP64 tolerance. xi and the step (of the last refinement) are f64; a point whose FP32 phase
+// left its cell does not converge in the refinement either.
+template <int TD, int GD>
+__global__ void pull_back_split_kernel(const __grid_constant__ PullBackArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ BasisData basis;
+  {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(a.basis);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(&basis);
+    for (int i = threadIdx.x; i < (int)(sizeof(BasisData) / 4); i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  using M = Factors<float, TD, GD>;
+  constexpr int LJ = TD * GD;
+  const int T = a.threads;
+  const int K = basis.k;
+  // Slots: the f64 shifted coordinates, then their f32 roundings.
+  double* xs64 = reinterpret_cast<double*>(smem) + threadIdx.x;
+  float* xs32 = reinterpret_cast<float*>(smem + (size_t)K * GD * T * sizeof(double)) + threadIdx.x;
+  const double* nodes = static_cast<const double*>(a.nodes);
+  const double* xin = static_cast<const double*>(a.x);
+  double* xi_out = static_cast<double*>(a.xi);
+  double* step_out = static_cast<double*>(a.step);
+  const int nq = a.num_points;
+  const int tmask = (1 << a.tile_shift) - 1;
+  const float big32 = fmax_finite<float>();
+  const double big = fmax_finite<double>();
+  const float tol32 = 1e-5f;
+  const double tol = a.tolerance;
+  float start[3];
+  centroid_f32(basis.cell, start);
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cell = min(a.first_cell + c, a.last_cell);
+    const uint32_t* row = a.dofmap + cell * K;
+    double x0[GD];
+    const uint32_t n0 = min(__ldg(row), a.last_node);
 #pragma unroll
-          for (int g = 1; g < GD; ++g) acc = fma(K_[g * TD + t], r[g], acc);
-          delta[t] = acc;
-          const F m = fabs(acc);
-          s = t == 0 ? m : (m > s ? m : s);
-          bad = bad || !(m <= big);
-        }
-        if (bad) s = big;
-        if (!frozen) {
+    for (int g = 0; g < GD; ++g) x0[g] = __ldg(nodes + (int64_t)n0 * GD + g);
+    for (int k = 0; k < K; ++k) {
+      const uint32_t n = min(__ldg(row + k), a.last_node);
 #pragma unroll
-          for (int d = 0; d < TD; ++d) {
-            F qd = p[d] + delta[d];
-            qd = qd < lo ? lo : qd;
-            qd = qd > hi ? hi : qd;
-            p[d] = qd;
-          }
-          last = s;
-          frozen = s <= tol;
-        }
+      for (int g = 0; g < GD; ++g) {
+        const double v = __ldg(nodes + (int64_t)n * GD + g) - x0[g];
+        xs64[(k * GD + g) * T] = v;
+        xs32[(k * GD + g) * T] = d2f_rn(v);
+      }
+    }
+    const int64_t ox = a.x_first_cell + c, oo = a.out_first_cell + c;
+    const int64_t tx = ox >> a.tile_shift, to = oo >> a.tile_shift;
+    const int lx = (int)(ox & tmask), lo_ = (int)(oo & tmask);
+    for (int q = 0; q < nq; ++q) {
+      double y[GD];
+      float y32[GD];
+#pragma unroll
+      for (int g = 0; g < GD; ++g) {
+        y[g] = (xin[(((tx * nq + q) * GD + g) << a.tile_shift) + lx] - a.origin[g]) - x0[g];
+        y32[g] = d2f_rn(y[g]);
+      }
+      float p32[TD];
+#pragma unroll
+      for (int d = 0; d < TD; ++d) p32[d] = start[d];
+      float last32 = big32;
+      bool frozen32 = false;
+      for (int it = 0; it < a.max_iterations; ++it) {
+        float X[GD], J[LJ], K_[LJ];
+        map_at<float, TD, GD>(basis, xs32, T, p32, X, J);
+        M::pinv(J, K_);
+        float r[GD];
+#pragma unroll
+        for (int g = 0; g < GD; ++g) r[g] = y32[g] - X[g];
+        newton_update<float, float, TD, GD>(p32, K_, r, last32, frozen32, tol32, -0.1f, 1.1f, big32);
+      }
+      double p[TD];
+#pragma unroll
+      for (int d = 0; d < TD; ++d) p[d] = f2d_exact(p32[d]);
+      double last = big;
+      bool frozen = false;
+      for (int it = 0; it < a.refinements; ++it) {
+        double X[GD], Jd[1];
+        map_at<double, TD, GD, false>(basis, xs64, T, p, X, Jd);
+        float pf[TD], X32[GD], J[LJ], K_[LJ];
+#pragma unroll
+        for (int d = 0; d < TD; ++d) pf[d] = d2f_rn(p[d]);
+        map_at<float, TD, GD>(basis, xs32, T, pf, X32, J);
+        M::pinv(J, K_);
+        double r[GD];
+#pragma unroll
+        for (int g = 0; g < GD; ++g) r[g] = y[g] - X[g];
+        newton_update<double, float, TD, GD>(p, K_, r, last, frozen, tol, double(-0.1f), double(1.1f), big);
       }
 #pragma unroll
       for (int d = 0; d < TD; ++d) xi_out[(((to * nq + q) * TD + d) << a.tile_shift) + lo_] = p[d];
@@ -380,8 +498,8 @@ tlg_status tlg_basis_destroy(tlg_basis* b) {
 
 tlg_status tlg_pull_back_block(const tlg_basis* basis, const tlg_block* b, const void* x, int64_t x_first_cell,
                                int64_t first_cell, int64_t num_cells, int64_t out_first_cell, int num_points,
-                               int tile, double tolerance, int max_iterations, void* xi, void* step,
-                               void* stream) {
+                               int tile, double tolerance, int max_iterations, int refinements, void* xi,
+                               void* step, void* stream) {
   if (!basis || !b) return basis_fail(TLG_ERR_INVALID_ARGUMENT, "tlg_pull_back_block: NULL argument");
   if (b->dtype != TLG_F32 && b->dtype != TLG_F64)
     return basis_fail(TLG_ERR_INVALID_ARGUMENT, "tlg_pull_back_block: dtype must be 4 or 8");
@@ -392,8 +510,11 @@ tlg_status tlg_pull_back_block(const tlg_basis* basis, const tlg_block* b, const
     if (tile == (1 << s)) shift = s;
   if (shift < 0) return basis_fail(TLG_ERR_INVALID_ARGUMENT, "tlg_pull_back_block: tile is not 1, 2, 4, 8 or 16");
   if (first_cell < 0 || num_cells < 0 || first_cell + num_cells > b->num_cells || x_first_cell < 0 ||
-      out_first_cell < 0 || x_first_cell % tile || out_first_cell % tile || num_points < 0 || max_iterations < 0)
+      out_first_cell < 0 || x_first_cell % tile || out_first_cell % tile || num_points < 0 || max_iterations < 0 ||
+      refinements < 0)
     return basis_fail(TLG_ERR_INVALID_ARGUMENT, "tlg_pull_back_block: bad range, points or iterations");
+  if (refinements > 0 && b->dtype != TLG_F64)
+    return basis_fail(TLG_ERR_INVALID_ARGUMENT, "tlg_pull_back_block: mixed precision refines f64 meshes");
   if (num_cells == 0 || num_points == 0) return tlg::ok();
   if (!x || !xi || !step || !b->nodes || !b->dofmap)
     return basis_fail(TLG_ERR_INVALID_ARGUMENT, "tlg_pull_back_block: NULL points, outputs, nodes or dofmap");
@@ -417,8 +538,11 @@ tlg_status tlg_pull_back_block(const tlg_basis* basis, const tlg_block* b, const
   a.num_points = num_points;
   a.max_iterations = max_iterations;
   a.tile_shift = shift;
-  // Threads per CTA: the node slots of 128 threads, or fewer, within 96 KiB.
-  const size_t per_thread = (size_t)basis->k * b->gdim * (size_t)b->dtype;
+  a.refinements = refinements;
+  // Threads per CTA: the node slots of 128 threads, or fewer, within 96 KiB (mixed precision
+  // keeps f64 and f32 copies); the basis description adds a static 4 KiB. The dynamic size is
+  // always declared, as static and dynamic shared memory together may pass the default 48 KiB.
+  const size_t per_thread = (size_t)basis->k * b->gdim * (refinements > 0 ? 12 : (size_t)b->dtype);
   int threads = 128;
   while (threads > 32 && per_thread * threads > (size_t)96 * 1024) threads /= 2;
   const size_t smem = per_thread * threads;
@@ -436,13 +560,24 @@ tlg_status tlg_pull_back_block(const tlg_basis* basis, const tlg_block* b, const
 #define TLG_PB(F, TD, GD) \
   if (basis->td == TD && b->gdim == GD) { \
     auto kern = tlg::pull_back_kernel<F, TD, GD>; \
-    if (smem > 48 * 1024) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
     if (e == cudaSuccess) { \
       kern<<<grid, threads, smem, s>>>(a); \
       e = cudaGetLastError(); \
     } \
   }
-  if (b->dtype == TLG_F64) {
+#define TLG_PBS(TD, GD) \
+  if (basis->td == TD && b->gdim == GD) { \
+    auto kern = tlg::pull_back_split_kernel<TD, GD>; \
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e == cudaSuccess) { \
+      kern<<<grid, threads, smem, s>>>(a); \
+      e = cudaGetLastError(); \
+    } \
+  }
+  if (refinements > 0) {
+    TLG_PBS(1, 1) TLG_PBS(1, 2) TLG_PBS(1, 3) TLG_PBS(2, 2) TLG_PBS(2, 3) TLG_PBS(3, 3)
+  } else if (b->dtype == TLG_F64) {
     TLG_PB(double, 1, 1) TLG_PB(double, 1, 2) TLG_PB(double, 1, 3) TLG_PB(double, 2, 2) TLG_PB(double, 2, 3)
     TLG_PB(double, 3, 3)
   } else {
@@ -450,6 +585,7 @@ tlg_status tlg_pull_back_block(const tlg_basis* basis, const tlg_block* b, const
     TLG_PB(float, 3, 3)
   }
 #undef TLG_PB
+#undef TLG_PBS
   if (e != cudaSuccess) return tlg::cuda_fail(e, "tlg_pull_back_block launch");
   return tlg::ok();
 }

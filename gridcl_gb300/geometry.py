@@ -452,14 +452,18 @@ def _basis(el: CoordinateElement):
 
 
 def pull_back_block(g: Geometry, b: int, x: QuadField, tolerance: float | None = None,
-                    max_iterations: int = 16):
+                    max_iterations: int = 16, precision: str = "native", refinements: int = 3):
     """Reference points of the physical points `x` (a QuadField of block b, GD components) by
     Newton's method (tetraloma-geometry/src/pull_back.rs:566): returns ``(xi, step)``, xi with
     TD components and step = |delta xi|_inf of each point's last iteration, tiled and chunked as
     `x`. Every point starts at the reference cell's vertex centroid and runs `max_iterations`
     steps (no early exit), clamped to [-0.1, 1.1]^TD and frozen once its step is at most the
     tolerance (None: 1e-13 in f64, 1e-5 in f32); a point has converged when its step is at most
-    the tolerance."""
+    the tolerance.
+
+    ``precision="split"`` (f64 meshes): the iteration in FP32 on cell-shifted coordinates, then
+    `refinements` steps with the residual in FP64 and the correction through the FP32 inverse
+    Jacobian; xi and step are f64, step that of the last refinement."""
     blk = g.blocks[b]
     td = blk.element.tdim
     if x.num_cells != blk.num_cells:
@@ -468,6 +472,11 @@ def pull_back_block(g: Geometry, b: int, x: QuadField, tolerance: float | None =
         raise GridError(1, f"pull_back_block: points of {x.length} components on a grid of dimension {g.gdim}")
     if max_iterations < 0:
         raise GridError(1, "pull_back_block: max_iterations must be >= 0")
+    if precision not in ("native", "split"):
+        raise GridError(1, f"unknown precision {precision!r}")
+    if precision == "split" and (g.dtype != torch.float64 or refinements < 1):
+        raise GridError(1, "pull_back_block: split precision refines f64 meshes (refinements >= 1)")
+    nref = refinements if precision == "split" else 0
     nq, tile = x.num_points, x.tile
     xi_chunks, step_chunks = [], []
     for ch in x.chunks:
@@ -488,7 +497,7 @@ def pull_back_block(g: Geometry, b: int, x: QuadField, tolerance: float | None =
     tol = 0.0 if tolerance is None else float(tolerance)
     for ch, cxi, cst in zip(x.chunks, xi_chunks, step_chunks):
         check(lib().tlg_pull_back_block(h, ctypes.byref(desc), ch.data.data_ptr(), 0, ch.first_cell,
-                                        ch.num_cells, 0, nq, tile, tol, max_iterations,
+                                        ch.num_cells, 0, nq, tile, tol, max_iterations, nref,
                                         cxi.data.data_ptr(), cst.data.data_ptr(), stream))
     return xi, step
 

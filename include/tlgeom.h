@@ -251,11 +251,16 @@ tlg_status tlg_basis_create(int cell, int degree, int family, tlg_basis** out);
 tlg_status tlg_basis_destroy(tlg_basis* basis);
 /* Points x: a QuadField chunk of GD components (absolute coordinates), x_first_cell the range's
  * first cell in it; outputs xi (TD components) and step (1) chunks at out_first_cell; the same
- * tile and num_points for all three. Replaces pull_back_block's kernels. */
+ * tile and num_points for all three. Replaces pull_back_block's kernels. refinements = 0: the
+ * iteration in the block's scalar type. refinements > 0 (f64 blocks): mixed precision, the
+ * iteration in FP32 on coordinates shifted by the cell's first node (frozen at 1e-5), then that
+ * many steps with the residual in FP64 and the correction through the FP32 inverse Jacobian
+ * (frozen at the tolerance); xi and step are f64, step that of the last refinement. */
 tlg_status tlg_pull_back_block(const tlg_basis* basis, const tlg_block* block, const void* x,
                                int64_t x_first_cell, int64_t first_cell, int64_t num_cells,
                                int64_t out_first_cell, int num_points, int tile, double tolerance,
-                               int max_iterations, void* xi, void* step, void* stream);
+                               int max_iterations, int refinements, void* xi, void* step,
+                               void* stream);
 
 /* Evaluation strategy (the reference's strategy::choose, tetraloma-geometry/src/strategy.rs:
  * 373-407, with its precedence: a scoped setting, then the environment, then the built-in

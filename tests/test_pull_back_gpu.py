@@ -133,3 +133,37 @@ def test_pull_back_errors(cuda):
     wrong = tg.QuadField(x.chunks, x.num_cells + 1, x.num_points, x.length, x.tile)
     with pytest.raises(tg.GridError):
         tg.pull_back_block(g, 0, wrong)
+
+
+@pytest.mark.parametrize("cell,degree", CELLS)
+def test_split_pull_back_matches_f64(cuda, cell, degree):
+    """Mixed precision (FP32 iteration, FP64-residual refinement): on Gauss points and on seeded
+    points inside and beyond the cells, the points that converge in f64 converge here too, to
+    the same reference point within 1e-12, with steps of at most the f64 tolerance."""
+    mesh = mesh_for(cell, degree)
+    g = tg.Geometry.from_host(mesh, dtype=F64)
+    td = tg.refcell.tdim(cell)
+    pts, _ = tg.refcell.gauss_rule(cell, 2 * degree)
+    ref = np.concatenate([pts, np.random.default_rng(8).uniform(-0.3, 1.3, size=(8, td))])
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[: g.gdim])
+    x = orc.eval_block(cell, degree, absx, mesh.blocks[0].cells, ref, factors=("x",))["x"]
+    field = field_of(x, 16, F64)
+    xi64, st64 = tg.pull_back_block(g, 0, field)
+    xis, sts = tg.pull_back_block(g, 0, field, precision="split")
+    xi64, st64 = xi64.to_host_cell_major(), st64.to_host_cell_major()[..., 0]
+    xis, sts = xis.to_host_cell_major(), sts.to_host_cell_major()[..., 0]
+    both = (st64 <= 1e-13) & (sts <= 1e-13)
+    assert both.any()
+    assert np.abs(xis[both] - xi64[both]).max() < 1e-12
+    # Points converged in f64 well inside the box converge in mixed precision too.
+    inside = (st64 <= 1e-13) & np.all((xi64 > 0.0) & (xi64 < 1.0), axis=2)
+    assert np.all(sts[inside] <= 1e-13)
+
+
+def test_split_pull_back_needs_f64(cuda):
+    mesh = meshes.curved_box("Tetrahedron", 1, 2, jitter=0.0)
+    g = tg.Geometry.from_host(mesh, dtype=F32)
+    pts, _ = tg.refcell.gauss_rule("Tetrahedron", 2)
+    x = tg.physical_points_block(g, 0, tg.PointSet("Tetrahedron", pts, np.ones(len(pts))))
+    with pytest.raises(tg.GridError):
+        tg.pull_back_block(g, 0, x, precision="split")
