@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--n", type=int, default=64, help="subcells per direction")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
-                   help="skip the other workloads (hybrid batch, sphere surface, Q2 adjoint, P1 box)")
+                   help="skip the other workloads (hybrid batch, sphere surface, Q2 adjoint, pull-back, P1 box)")
     p.add_argument("--workload", choices=["main", *EXTRAS], default="main",
                    help="run one of the other workloads alone and print its JSON object")
     p.add_argument("--adjoint-n", type=int, default=128, help="Q2 hexahedra per direction (adjoint)")
@@ -399,6 +399,42 @@ def extra_adjoint(n: int = 128):
             "fd_check_fp64": fd}
 
 
+def extra_pull_back():
+    """Pull-back of the 24 quadrature points' images of the 32^3 x 6 curved P2 tetrahedra
+    (4.7 M points): the f64 iteration, the FP32 iteration of an f32 mesh, and mixed precision
+    (FP32 iteration, three FP64-residual refinements) on the f64 mesh, 16 iterations each."""
+    import numpy as np
+    import torch
+
+    import gridcl_gb300 as tg
+
+    mesh = build_mesh(32)
+    pts, w = rule()
+    ps = tg.PointSet("Tetrahedron", pts, w)
+    npts = mesh.blocks[0].num_cells * len(pts)
+    out = {"workload": "pull-back of the images of 24 points in 32^3x6 curved P2 tetrahedra, 16 iterations",
+           "points": int(npts)}
+    g64 = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    x64 = tg.physical_points_block(g64, 0, ps)
+    xi64, st64 = tg.pull_back_block(g64, 0, x64)
+    ms = event_ms(lambda: tg.pull_back_block(g64, 0, x64), reps=2, warm=1)
+    out["f64"] = {"ms": ms, "value": npts / (ms * 1e-3),
+                  "converged": float((st64.to_host_cell_major() <= 1e-13).mean())}
+    xs, sts = tg.pull_back_block(g64, 0, x64, precision="split")
+    ms_s = event_ms(lambda: tg.pull_back_block(g64, 0, x64, precision="split"))
+    d = np.abs(xs.to_host_cell_major() - xi64.to_host_cell_major()).max()
+    out["split"] = {"ms": ms_s, "value": npts / (ms_s * 1e-3), "speedup_vs_f64": ms / ms_s,
+                    "converged": float((sts.to_host_cell_major() <= 1e-13).mean()),
+                    "max_abs_diff_vs_f64": float(d)}
+    g32 = tg.Geometry.from_host(mesh, dtype=torch.float32)
+    x32 = tg.physical_points_block(g32, 0, ps)
+    _, st32 = tg.pull_back_block(g32, 0, x32)
+    ms32 = event_ms(lambda: tg.pull_back_block(g32, 0, x32))
+    out["f32"] = {"ms": ms32, "value": npts / (ms32 * 1e-3),
+                  "converged": float((st32.to_host_cell_major() <= 1e-5).mean())}
+    return out
+
+
 def extra_p1_box():
     """BASELINE's CPU-runtime case: 8^3 x 6 = 3,072 P1 tetrahedra, interior nodes jittered by
     +-0.1 h, 14 points (collapsed 7 x 2 x 1), f64; GPU against the oracle on the host cores."""
@@ -582,7 +618,7 @@ def run_ours(args):
             workloads = {}
             for name, fn in (("hybrid_batched", extra_hybrid), ("sphere_surface", extra_sphere),
                              ("q2_forward_adjoint", lambda: extra_adjoint(args.adjoint_n)),
-                             ("p1_box", extra_p1_box)):
+                             ("pull_back", extra_pull_back), ("p1_box", extra_p1_box)):
                 try:
                     workloads[name] = fn()
                 except Exception as exc:  # reported, not fatal: the main line stands
@@ -598,7 +634,7 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "p1_box")
+EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "pull_back", "p1_box")
 
 
 def run_extra(args):
@@ -607,7 +643,8 @@ def run_extra(args):
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     fn = {"hybrid_batched": extra_hybrid, "sphere_surface": extra_sphere,
-          "q2_forward_adjoint": lambda: extra_adjoint(args.adjoint_n), "p1_box": extra_p1_box}[args.workload]
+          "q2_forward_adjoint": lambda: extra_adjoint(args.adjoint_n), "pull_back": extra_pull_back,
+          "p1_box": extra_p1_box}[args.workload]
     print(json.dumps(fn()), flush=True)
 
 
