@@ -435,6 +435,35 @@ def extra_pull_back():
     return out
 
 
+def extra_ordering():
+    """Gather locality: the 64^3 x 6 curved P2 tetrahedra with cells and nodes in a seeded random
+    order, then reordered along the Hilbert curve of the vertex centroids with nodes numbered by
+    first use (host, native); split-precision evaluation of each against the generator's order."""
+    import numpy as np
+    import torch
+
+    import gridcl_gb300 as tg
+    from gridcl_gb300 import meshes
+
+    mesh = build_mesh(64)
+    pts, w = rule()
+    ps = tg.PointSet("Tetrahedron", pts, w)
+    names = ("points", "jacobian", "detj", "pinv")
+    mix = meshes.shuffled(mesh, seed=7)
+    t0 = time.perf_counter()
+    hil, _, _ = meshes.reorder(mix, "hilbert")
+    host_s = time.perf_counter() - t0
+    out = {"workload": "P2 tet 64^3x6 split evaluation: generator order, shuffled, Hilbert-reordered",
+           "hilbert_host_s": host_s}
+    for name, m in (("generator", mesh), ("shuffled", mix), ("hilbert", hil)):
+        g = tg.Geometry.from_host(m, dtype=torch.float64)
+        f = tg.geometric_factors_block(g, 0, ps, names, precision="split")
+        out[name + "_ms"] = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, names, out=f, precision="split"))
+        del g, f
+        torch.cuda.empty_cache()
+    return out
+
+
 def extra_p1_box():
     """BASELINE's CPU-runtime case: 8^3 x 6 = 3,072 P1 tetrahedra, interior nodes jittered by
     +-0.1 h, 14 points (collapsed 7 x 2 x 1), f64; GPU against the oracle on the host cores."""
@@ -618,7 +647,8 @@ def run_ours(args):
             workloads = {}
             for name, fn in (("hybrid_batched", extra_hybrid), ("sphere_surface", extra_sphere),
                              ("q2_forward_adjoint", lambda: extra_adjoint(args.adjoint_n)),
-                             ("pull_back", extra_pull_back), ("p1_box", extra_p1_box)):
+                             ("pull_back", extra_pull_back), ("ordering", extra_ordering),
+                             ("p1_box", extra_p1_box)):
                 try:
                     workloads[name] = fn()
                 except Exception as exc:  # reported, not fatal: the main line stands
@@ -634,7 +664,7 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "pull_back", "p1_box")
+EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "pull_back", "ordering", "p1_box")
 
 
 def run_extra(args):
@@ -644,7 +674,7 @@ def run_extra(args):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     fn = {"hybrid_batched": extra_hybrid, "sphere_surface": extra_sphere,
           "q2_forward_adjoint": lambda: extra_adjoint(args.adjoint_n), "pull_back": extra_pull_back,
-          "p1_box": extra_p1_box}[args.workload]
+          "ordering": extra_ordering, "p1_box": extra_p1_box}[args.workload]
     print(json.dumps(fn()), flush=True)
 
 

@@ -111,6 +111,10 @@ SIGNATURES = [
     ("tlg_set_strategy", _I, [_I]),
     ("tlg_get_strategy", _I, []),
     ("tlg_last_kernel_family", _I, []),
+    ("tlg_order_cells", _I, [_I, _I, _P, _L, _I, _P, _L, _I, _P]),
+    ("tlg_number_nodes", _I, [_P, _L, _I, _L, _P, _P]),
+    ("tlg_hilbert_key", ctypes.c_uint64, [_P, _I, _I]),
+    ("tlg_quantise", ctypes.c_uint32, [ctypes.c_double, ctypes.c_double, ctypes.c_double]),
     ("tlg_basis_create", _I, [_I, _I, _I, _P]),
     ("tlg_basis_destroy", _I, [_P]),
     ("tlg_pull_back_block", _I, [_P, ctypes.POINTER(TlgBlock), _P, _L, _L, _L, _L, _I, _I,

@@ -20,8 +20,8 @@ CSRC = HERE / "csrc"
 OUT_DIR = HERE / "_build"
 LIB = HERE / "libtlgeom.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "csr.cu", "eval_f32.cu", "eval_f64.cu", "eval_pair.cu", "measure.cu", "pullback.cu",
-           "refcell.cpp", "sumfact.cu", "vjp_f64.cu", "vjp_split.cu"]
+SOURCES = ["api.cu", "csr.cu", "eval_f32.cu", "eval_f64.cu", "eval_pair.cu", "measure.cu", "order.cpp",
+           "pullback.cu", "refcell.cpp", "sumfact.cu", "vjp_f64.cu", "vjp_split.cu"]
 
 
 def nvcc() -> str:

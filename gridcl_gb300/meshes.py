@@ -328,3 +328,58 @@ def hybrid_box(hexes: int, prisms: int, tets: int, jitter: float = 0.02, seed: i
         m = curved_box(cell, n, p, jitter=jitter, seed=seed)
         parts.append(m.first_cells(count))
     return combine(parts, [(0.0, 0.0, 0.0), (1.5, 0.0, 0.0), (3.0, 0.0, 0.0)])
+
+
+# ------------------------------------------------------------------------------------------
+# Cell orderings before upload (tetraloma/src/pipeline/order.rs:24-192, builder.rs:95-113),
+# computed by the native library.
+
+ORDERINGS = {"input": 0, "hilbert": 1, "rcm": 2}
+
+
+def reorder(mesh: HostMesh, ordering: str = "hilbert"):
+    """The mesh with each block's cells in `ordering` ("input", "hilbert": by the Hilbert key of
+    the vertex centroid; "rcm": reverse Cuthill-McKee on the facet graph) and the nodes numbered
+    by first use (blocks in order, each cell's nodes in Lagrange order; unused nodes last).
+    Returns ``(mesh, cell_orders, node_order)``: per block the old index of each new cell, and the
+    old index of each new node."""
+    import ctypes
+
+    from ._lib import CELL_IDS, check, lib
+
+    if ordering not in ORDERINGS:
+        raise ValueError(f"unknown ordering {ordering!r}")
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    nodes = np.ascontiguousarray(mesh.nodes, dtype=np.float64)
+    orders, ordered = [], []
+    for blk in mesh.blocks:
+        cells = np.ascontiguousarray(blk.cells, dtype=np.uint32)
+        order = np.empty(cells.shape[0], dtype=np.int64)
+        check(lib().tlg_order_cells(ORDERINGS[ordering], CELL_IDS[blk.cell], ptr(cells), cells.shape[0],
+                                    cells.shape[1], ptr(nodes), nodes.shape[0], mesh.gdim, ptr(order)))
+        orders.append(order)
+        ordered.append(np.ascontiguousarray(cells[order]))
+    flat = np.concatenate([c.ravel() for c in ordered]) if ordered else np.zeros(0, dtype=np.uint32)
+    flat = np.ascontiguousarray(flat, dtype=np.uint32)
+    renumbered = np.empty_like(flat)
+    node_order = np.empty(nodes.shape[0], dtype=np.int64)
+    check(lib().tlg_number_nodes(ptr(flat), flat.size, 1, nodes.shape[0], ptr(renumbered), ptr(node_order)))
+    blocks, at = [], 0
+    for blk, c in zip(mesh.blocks, ordered):
+        blocks.append(HostBlock(blk.cell, blk.degree, renumbered[at: at + c.size].reshape(c.shape), blk.family))
+        at += c.size
+    return HostMesh(mesh.gdim, nodes[node_order], blocks), orders, node_order
+
+
+def shuffled(mesh: HostMesh, seed: int = 2026) -> HostMesh:
+    """The mesh with the cells of each block and the nodes in a seeded random order (a mesh as an
+    unordered generator or file would deliver it)."""
+    rng = np.random.default_rng(seed)
+    node_perm = rng.permutation(mesh.num_nodes)  # new index -> old index
+    new_of_old = np.empty_like(node_perm)
+    new_of_old[node_perm] = np.arange(mesh.num_nodes)
+    blocks = []
+    for blk in mesh.blocks:
+        cells = blk.cells[rng.permutation(blk.num_cells)]
+        blocks.append(HostBlock(blk.cell, blk.degree, new_of_old[cells].astype(np.uint32), blk.family))
+    return HostMesh(mesh.gdim, mesh.nodes[node_perm], blocks)

@@ -262,6 +262,26 @@ tlg_status tlg_pull_back_block(const tlg_basis* basis, const tlg_block* block, c
                                int max_iterations, int refinements, void* xi, void* step,
                                void* stream);
 
+/* ---------------------------------------------------------------------------------------
+ * Cell orderings before upload (tetraloma/src/pipeline/order.rs:24-192, builder.rs:95-113):
+ * the order in which the kernels visit cells. Host functions (no device). INPUT keeps the
+ * order; HILBERT sorts by the Hilbert key of each cell's vertex centroid quantised to 2^21 steps
+ * per axis in the node bounding box, then by position; RCM is reverse Cuthill-McKee on the facet
+ * graph (components from their least (degree, position) cell, neighbours by (degree,
+ * position)). order receives num_cells old cell indices. tlg_number_nodes numbers nodes by
+ * first use in `cells` (already in the new order): new_cells receives the renumbered cells and
+ * node_order the old node index of each new index (unused nodes last). */
+typedef enum tlg_ordering { TLG_ORDER_INPUT = 0, TLG_ORDER_HILBERT = 1, TLG_ORDER_RCM = 2 } tlg_ordering;
+tlg_status tlg_order_cells(int ordering, int cell, const uint32_t* cells, int64_t num_cells,
+                           int nodes_per_cell, const double* nodes, int64_t num_nodes, int gdim,
+                           int64_t* order);
+tlg_status tlg_number_nodes(const uint32_t* cells, int64_t num_cells, int nodes_per_cell,
+                            int64_t num_nodes, uint32_t* new_cells, int64_t* node_order);
+/* The Hilbert index of a point of a grid of 2^bits points per axis (d axes, d * bits <= 64), and
+ * the quantisation of a coordinate to [0, 2^21) in [lo, hi]. */
+uint64_t tlg_hilbert_key(const uint32_t* x, int d, int bits);
+uint32_t tlg_quantise(double x, double lo, double hi);
+
 /* Evaluation strategy (the reference's strategy::choose, tetraloma-geometry/src/strategy.rs:
  * 373-407, with its precedence: a scoped setting, then the environment, then the built-in
  * policy). AUTO picks per element: for quadrilaterals and hexahedra at tensor-product point sets,
