@@ -27,6 +27,7 @@ struct tlg_batch {
   std::vector<tlg_block> blocks;
   std::vector<tlg_outputs> outputs;
   std::vector<int> grid;  // launch grid per block (0: the kernel's persistent default)
+  bool serial = false;    // the blocks one after another instead of parallel graph branches
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> events;  // fork, then one join per block
   cudaStream_t capture = nullptr;
@@ -819,6 +820,8 @@ namespace {
 
 std::mutex g_tune_mutex;
 std::map<std::string, int> g_tune_cache;  // launch-shape key -> grid multiplier
+std::map<std::string, std::vector<int>> g_joint_cache;  // batch key -> grids after the joint pass,
+                                                        // then 1 for a serial chain, 0 for branches
 
 std::string tune_key(const tlg_tables* t, const tlg_outputs* o, int64_t cells) {
   int bucket = 0;
@@ -934,8 +937,75 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
       g_tune_cache[key] = mult;
     }
     b->grid[i] = mult == 0 ? 0 : mult * sms;
-    if (grids) grids[i] = b->grid[i];
   }
+  // Joint pass: the graph runs the blocks concurrently, so each block's best grid alone is only
+  // the start. One round of coordinate descent over each block's candidates, timing the whole
+  // graph (one warm launch, then three), keeps a change only when the graph gets faster.
+  std::string batch_key;
+  for (size_t i = 0; i < b->tables.size(); ++i)
+    batch_key += tune_key(b->tables[i], &b->outputs[i], b->outputs[i].num_cells) + ";";
+  std::vector<int> joint;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_joint_cache.find(batch_key);
+    if (it != g_joint_cache.end()) joint = it->second;
+  }
+  if (joint.size() == b->tables.size() + 1) {
+    for (size_t i = 0; i < b->tables.size(); ++i) b->grid[i] = joint[i];
+    b->serial = joint.back() != 0;
+  } else if (b->tables.size() > 1) {
+    auto time_graph = [&](float* ms) -> tlg_status {
+      destroy_graph(b);
+      tlg_status st = tlg_batch_launch(b, s);
+      if (st != TLG_OK) return st;
+      cudaEventRecord(t0, s);
+      for (int r = 0; r < 3 && st == TLG_OK; ++r) st = tlg_batch_launch(b, s);
+      cudaEventRecord(t1, s);
+      cudaEventSynchronize(t1);
+      cudaEventElapsedTime(ms, t0, t1);
+      return st;
+    };
+    // Parallel branches or a serial chain: the concurrent branches of persistent kernels share
+    // the SMs in an order the hardware picks, which can cost more than running them in turn.
+    float best = 0.0f, serial_ms = 0.0f;
+    b->serial = false;
+    tlg_status st = time_graph(&best);
+    if (st == TLG_OK) {
+      b->serial = true;
+      st = time_graph(&serial_ms);
+      if (serial_ms < best) best = serial_ms;
+      else b->serial = false;
+    }
+    const int cands[] = {0, 1, 2, 3, 4, 6, 8};
+    for (size_t i = 0; i < b->tables.size() && st == TLG_OK; ++i) {
+      const int keep = b->grid[i];
+      int chosen = keep;
+      for (int c : cands) {
+        const int grid = c == 0 ? 0 : c * sms;
+        if (grid == keep) continue;
+        b->grid[i] = grid;
+        float ms = 0.0f;
+        st = time_graph(&ms);
+        if (st != TLG_OK) break;
+        if (ms < best) {
+          best = ms;
+          chosen = grid;
+        }
+      }
+      b->grid[i] = chosen;
+    }
+    if (st != TLG_OK) {
+      cudaEventDestroy(t0);
+      cudaEventDestroy(t1);
+      return st;
+    }
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    std::vector<int> rec = b->grid;
+    rec.push_back(b->serial ? 1 : 0);
+    g_joint_cache[batch_key] = rec;
+  }
+  if (grids)
+    for (size_t i = 0; i < b->tables.size(); ++i) grids[i] = b->grid[i];
   cudaEventDestroy(t0);
   cudaEventDestroy(t1);
   destroy_graph(b);
@@ -953,12 +1023,17 @@ tlg_status tlg_batch_launch(tlg_batch* b, void* stream) {
     cudaError_t e = cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_fail(e, "tlg_batch_launch: begin capture");
     tlg_status st = TLG_OK;
-    cudaEventRecord(b->events[0], b->capture);
-    for (size_t i = 0; i < b->tables.size() && st == TLG_OK; ++i) {
-      cudaStreamWaitEvent(b->streams[i], b->events[0], 0);
-      st = eval_with_grid(b, i, b->streams[i], b->grid[i]);
-      cudaEventRecord(b->events[i + 1], b->streams[i]);
-      cudaStreamWaitEvent(b->capture, b->events[i + 1], 0);
+    if (b->serial) {
+      for (size_t i = 0; i < b->tables.size() && st == TLG_OK; ++i)
+        st = eval_with_grid(b, i, b->capture, b->grid[i]);
+    } else {
+      cudaEventRecord(b->events[0], b->capture);
+      for (size_t i = 0; i < b->tables.size() && st == TLG_OK; ++i) {
+        cudaStreamWaitEvent(b->streams[i], b->events[0], 0);
+        st = eval_with_grid(b, i, b->streams[i], b->grid[i]);
+        cudaEventRecord(b->events[i + 1], b->streams[i]);
+        cudaStreamWaitEvent(b->capture, b->events[i + 1], 0);
+      }
     }
     cudaGraph_t graph = nullptr;
     e = cudaStreamEndCapture(b->capture, &graph);

@@ -176,9 +176,12 @@ tlg_status tlg_batch_create(const tlg_tables* const* tables, const tlg_block* bl
 tlg_status tlg_batch_destroy(tlg_batch* batch);
 
 /* Times candidate persistent grids (0 and 1..8 CTAs per SM) for each block on `stream`, keeps the
- * fastest, and caches the choice per launch shape for the process; grids[i] (may be NULL) receives
- * block i's grid (0: the occupancy limit). Runs the blocks' kernels; call it outside stream
- * capture. Rebuilds the graph on the next launch. */
+ * fastest, and caches the choice per launch shape for the process; then times the whole graph
+ * with the blocks as parallel branches and as a serial chain, keeps the faster, and runs one
+ * round of coordinate descent over each block's candidates timing the whole graph (cached per
+ * batch shape). grids[i] (may be NULL) receives block i's grid (0: the
+ * occupancy limit). Runs the blocks' kernels; call it outside stream capture. Rebuilds the graph
+ * on the next launch. */
 tlg_status tlg_batch_tune(tlg_batch* batch, void* stream, int* grids);
 
 /* Evaluates every block: one launch of a CUDA graph (captured on the first call). */
