@@ -64,6 +64,7 @@ def parse():
     p.add_argument("--workload", choices=["main", *EXTRAS], default="main",
                    help="run one of the other workloads alone and print its JSON object")
     p.add_argument("--adjoint-n", type=int, default=128, help="Q2 hexahedra per direction (adjoint)")
+    p.add_argument("--hex-n", type=int, default=64, help="hexahedra per direction (hex_strategies)")
     return p.parse_args()
 
 
@@ -464,6 +465,40 @@ def extra_ordering():
     return out
 
 
+def extra_hex_strategies(n: int = 64):
+    """Curved hexahedra Q1-Q3 (n^3 cells, Gauss rules of 2, 3, 4 points per direction) evaluated
+    (x/J/detJ/K) under each strategy and precision: ms per launch and the kernel family that ran.
+    Run with --workload hex_strategies (not part of the default run)."""
+    import numpy as np
+    import torch
+
+    import gridcl_gb300 as tg
+    from gridcl_gb300 import meshes
+
+    names = ("points", "jacobian", "detj", "pinv")
+    out = {"workload": f"curved hexahedra Q1-Q3, {n}^3 cells, tensor Gauss rules, x/J/detJ/K"}
+    for degree in (1, 2, 3):
+        mesh = meshes.curved_box("Hexahedron", n, degree, jitter=0.02)
+        pts, w = tg.refcell.gauss_rule("Hexahedron", 2 * degree)
+        ps = tg.PointSet("Hexahedron", pts, w)
+        for prec, dt in (("split", torch.float64), ("native", torch.float64), ("native", torch.float32)):
+            g = tg.Geometry.from_host(mesh, dtype=dt)
+            row = {}
+            for strat in ("direct", "loops", "sumfact"):
+                with tg.with_strategy(strat):
+                    f = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+                    fam = tg.last_kernel_family()
+                    ms = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, names, out=f, precision=prec),
+                                  reps=3, warm=1)
+                row[strat] = {"family": fam, "ms": ms}
+                del f
+            label = "split" if prec == "split" else ("f64" if dt == torch.float64 else "f32")
+            out[f"Q{degree}_{label}"] = row
+            del g
+            torch.cuda.empty_cache()
+    return out
+
+
 def extra_p1_box():
     """BASELINE's CPU-runtime case: 8^3 x 6 = 3,072 P1 tetrahedra, interior nodes jittered by
     +-0.1 h, 14 points (collapsed 7 x 2 x 1), f64; GPU against the oracle on the host cores."""
@@ -664,7 +699,8 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
-EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "pull_back", "ordering", "p1_box")
+EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "pull_back", "ordering", "p1_box",
+          "hex_strategies")
 
 
 def run_extra(args):
@@ -674,7 +710,8 @@ def run_extra(args):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     fn = {"hybrid_batched": extra_hybrid, "sphere_surface": extra_sphere,
           "q2_forward_adjoint": lambda: extra_adjoint(args.adjoint_n), "pull_back": extra_pull_back,
-          "ordering": extra_ordering, "p1_box": extra_p1_box}[args.workload]
+          "ordering": extra_ordering, "p1_box": extra_p1_box,
+          "hex_strategies": lambda: extra_hex_strategies(args.hex_n)}[args.workload]
     print(json.dumps(fn()), flush=True)
 
 
