@@ -64,6 +64,7 @@ def parse():
     p.add_argument("--workload", choices=["main", *EXTRAS], default="main",
                    help="run one of the other workloads alone and print its JSON object")
     p.add_argument("--adjoint-n", type=int, default=128, help="Q2 hexahedra per direction (adjoint)")
+    p.add_argument("--fd-nodes", type=int, default=1000, help="nodes of the adjoint's central-difference check")
     p.add_argument("--hex-n", type=int, default=64, help="hexahedra per direction (hex_strategies)")
     return p.parse_args()
 
@@ -339,10 +340,10 @@ def extra_sphere():
                       "rel_err_vs_fp64": rel_err_fields(split, f64)}}
 
 
-def extra_adjoint(n: int = 128):
+def extra_adjoint(n: int = 128, fd_nodes: int = 1000):
     """Forward + adjoint: n^3 Q2 hexahedra, 27-point Gauss, seeded standard-normal cotangents on
     det J and K; the fused split-precision forward + vjp (+ node sums) against the plain FP64
-    forward followed by the FP64 vjp; central differences (step 1e-6) at 1,000 seeded nodes."""
+    forward followed by the FP64 vjp; central differences (step 1e-6) at `fd_nodes` seeded nodes (1,000)."""
     import numpy as np
     import torch
 
@@ -379,11 +380,25 @@ def extra_adjoint(n: int = 128):
 
     plain_ms = event_ms(plain, reps=2, warm=1)
     fused_ms = event_ms(fused_step)
+    # The two adjoint kernel families on the same step: node rows (four lanes per cell) and sum
+    # factorisation (one cell per thread); AUTO picks the latter for Q2 hexahedra.
+    families = {}
+    for strat in ("direct", "sumfact"):
+        with tg.with_strategy(strat):
+            ms = event_ms(fused_step)
+            ms64 = event_ms(lambda: tg.vjp_block(g, 0, ps, ct64, local=local64), reps=2, warm=1)
+            g32, _ = tg.vjp_block(g, 0, ps, ct32, precision="split", forward=factors, local=local32)
+            g64, _ = tg.vjp_block(g, 0, ps, ct64, local=local64)
+            families[strat] = {"fused_split_ms": ms, "vjp_fp64_ms": ms64,
+                               "split_grad_rel_err_vs_fp64": float((g32 - grad64).abs().max() / grad64.abs().max()),
+                               "fp64_grad_rel_err": float((g64 - grad64).abs().max() / grad64.abs().max())}
     # Central differences of the FP64 functional at 1,000 seeded nodes against the FP64 adjoint.
-    sample = np.random.default_rng(2026).choice(mesh.num_nodes, 1000, replace=False)
-    host = {k: v.to_host_cell_major() for k, v in ct64.items()}
-    fd = tg.fd_check(g, 0, ps, {"detj": host["detj"][..., 0], "pinv": host["pinv"]},
-                     grad64.cpu().numpy(), sample)
+    fd = None
+    if fd_nodes > 0:
+        sample = np.random.default_rng(2026).choice(mesh.num_nodes, fd_nodes, replace=False)
+        host = {k: v.to_host_cell_major() for k, v in ct64.items()}
+        fd = tg.fd_check(g, 0, ps, {"detj": host["detj"][..., 0], "pinv": host["pinv"]},
+                         grad64.cpu().numpy(), sample)
     gerr = float((grad32 - grad64).abs().max() / grad64.abs().max())
     # Compulsory traffic of the fused step: cotangents in, forward fields out, nodes and dofmap
     # in, contributions out and back in through the CSR, node cotangents out.
@@ -397,6 +412,7 @@ def extra_adjoint(n: int = 128):
                                     "hbm_gbs": alg / (fused_ms * 1e-3) / 1e9,
                                     "grad_rel_err_vs_fp64": gerr,
                                     "forward_rel_err_vs_fp64": rel_err_fields(fused, fwd64)},
+            "families": families,
             "fd_check_fp64": fd}
 
 
@@ -681,7 +697,7 @@ def run_ours(args):
         if not args.no_extras and world == 1:
             workloads = {}
             for name, fn in (("hybrid_batched", extra_hybrid), ("sphere_surface", extra_sphere),
-                             ("q2_forward_adjoint", lambda: extra_adjoint(args.adjoint_n)),
+                             ("q2_forward_adjoint", lambda: extra_adjoint(args.adjoint_n, args.fd_nodes)),
                              ("pull_back", extra_pull_back), ("ordering", extra_ordering),
                              ("p1_box", extra_p1_box)):
                 try:
@@ -709,7 +725,7 @@ def run_extra(args):
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     fn = {"hybrid_batched": extra_hybrid, "sphere_surface": extra_sphere,
-          "q2_forward_adjoint": lambda: extra_adjoint(args.adjoint_n), "pull_back": extra_pull_back,
+          "q2_forward_adjoint": lambda: extra_adjoint(args.adjoint_n, args.fd_nodes), "pull_back": extra_pull_back,
           "ordering": extra_ordering, "p1_box": extra_p1_box,
           "hex_strategies": lambda: extra_hex_strategies(args.hex_n)}[args.workload]
     print(json.dumps(fn()), flush=True)

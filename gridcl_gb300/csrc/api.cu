@@ -744,6 +744,55 @@ tlg_status tlg_evector(const tlg_block* b, int nodes_per_cell, int64_t first_cel
   return ok();
 }
 
+namespace {
+
+// Hexahedra with a tensor-product rule and 2 or 3 nodes per direction have the sum-factorised
+// adjoint.
+bool vjp_sumfact_preferred(const tlg_tables* t) { return t->sf_ok && t->td == 3 && (t->sf_n == 2 || t->sf_n == 3); }
+
+// The sum-factorised adjoint from the arguments of the node-row kernel; `found` is false when
+// the element has none (then the node-row kernel runs).
+tlg_status vjp_sumfact(const tlg_tables* t, const tlg::VjpArgs& v, cudaStream_t s, bool* found) {
+  *found = false;
+  if (!vjp_sumfact_preferred(t)) return TLG_ERR_UNSUPPORTED;
+  const bool split = t->dtype == TLG_SPLIT32;
+  const size_t fbytes = split ? 4 : 8;
+  const int threads = tlg::kEvalThreads;
+  const size_t smem = (t->sf_bytes + 15) / 16 * 16 + tlg::vjp_sumfact_extra_bytes(t->sf_n, threads, fbytes);
+  if (smem > (size_t)227 * 1024) return TLG_ERR_UNSUPPORTED;
+  tlg::VjpSfArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = v.nodes;
+  a.dofmap = v.dofmap;
+  a.tab = t->dev + t->off_sf;
+  for (int i = 0; i < 3; ++i) a.ct[i] = v.ct[i];
+  for (int i = 0; i < 4; ++i) a.out[i] = v.out[i];
+  a.local = v.local;
+  a.err = v.err;
+  a.first_cell = v.first_cell;
+  a.padded = v.padded;
+  a.out_first_cell = v.out_first_cell;
+  a.last_cell = v.last_cell;
+  a.range_end = v.range_end;
+  for (int g = 0; g < 3; ++g) a.origin[g] = v.origin[g];
+  a.last_node = v.last_node;
+  a.tab_bytes = t->sf_bytes;
+  for (int d = 0; d < 3; ++d) {
+    a.off_b[d] = t->sf_offb[d];
+    a.off_d[d] = t->sf_offd[d];
+    a.m[d] = t->sf_m[d];
+  }
+  a.off_perm = t->sf_offperm;
+  a.num_points = v.num_points;
+  cudaError_t e = tlg::launch_vjp_sumfact(split, t->sf_n, a, smem, threads, s, found);
+  if (!*found) return TLG_ERR_UNSUPPORTED;
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_block launch");
+  g_last_family = TLG_STRATEGY_SUMFACT;
+  return ok();
+}
+
+}  // namespace
+
 tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o,
                          const tlg_cotangents* ct, void* local, int64_t local_cells, void* stream) {
   if (!t || !b || !o || !ct) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: NULL argument");
@@ -795,10 +844,16 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
                                                   " bytes) exceed 227 KiB of shared memory");
   bool found = false;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int strategy = current_strategy();
+  if (strategy == TLG_STRATEGY_SUMFACT || (strategy == TLG_STRATEGY_AUTO && vjp_sumfact_preferred(t))) {
+    tlg_status st = vjp_sumfact(t, a, s, &found);
+    if (found) return st;
+  }
   cudaError_t e = split ? tlg::launch_vjp_split(t->td, (int)t->k, a, smem, s, &found)
                         : tlg::launch_vjp_f64(t->td, (int)t->k, a, smem, s, &found);
   if (!found) return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: no adjoint kernel for this element");
   if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_block launch");
+  g_last_family = TLG_STRATEGY_DIRECT;
   return ok();
 }
 

@@ -75,6 +75,11 @@ cudaError_t launch_eval_pair(bool split, int td, int gd, int k, const PairArgs& 
 cudaError_t launch_split_loops(int td, int gd, bool tab_global, const PairArgs& a, size_t smem, cudaStream_t s);
 
 struct SfArgs;
+struct VjpSfArgs;
+// Defined in sumfact.cu: the sum-factorised adjoint of hexahedra (split: f32 arithmetic, else f64),
+// N nodes per direction, `threads` per CTA; `found` is false when none is compiled for n.
+cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t smem, int threads, cudaStream_t s,
+                               bool* found);
 // Defined in sumfact.cu: the sum-factorised kernel for precision 4 (f32), 8 (f64) or 12 (split),
 // N nodes per direction; `found` is false when none is compiled for (td, gd, n).
 cudaError_t launch_sumfact(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,

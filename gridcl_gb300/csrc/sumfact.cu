@@ -1,5 +1,7 @@
 // Instantiations of the sum-factorised kernel (sumfact.cuh): hexahedra Q1-Q3 and quadrilaterals
 // Q1-Q5, planar and embedded in 3D.
+#include <algorithm>
+
 #include "eval_launch.cuh"
 #include "sumfact.cuh"
 
@@ -32,6 +34,36 @@ cudaError_t launch_sf(int td, int gd, int n, const SfArgs& a, size_t smem, cudaS
 }
 
 }  // namespace
+
+cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t smem, int threads, cudaStream_t s,
+                               bool* found) {
+  *found = true;
+#define TLG_VSF(F, SPLIT, NN) \
+  if (n == NN) { \
+    auto kern = vjp_sumfact_kernel<F, SPLIT, NN>; \
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e != cudaSuccess) return e; \
+    int per_sm = 0, sms = 1, dev = 0; \
+    cudaGetDevice(&dev); \
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev); \
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess || per_sm < 1) \
+      per_sm = 1; \
+    const int64_t need = (a.padded + threads - 1) / threads; \
+    const int grid = (int)std::min<int64_t>(need, (int64_t)sms * per_sm); \
+    kern<<<grid > 0 ? grid : 1, threads, smem, s>>>(a); \
+    return cudaGetLastError(); \
+  }
+  if (split) {
+    TLG_VSF(float, true, 2)
+    TLG_VSF(float, true, 3)
+  } else {
+    TLG_VSF(double, false, 2)
+    TLG_VSF(double, false, 3)
+  }
+#undef TLG_VSF
+  *found = false;
+  return cudaSuccess;
+}
 
 cudaError_t launch_sumfact(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
                            bool* found) {

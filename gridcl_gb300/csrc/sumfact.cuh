@@ -267,3 +267,306 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_kernel(const __grid_cons
 }
 
 }  // namespace tlg
+
+namespace tlg {
+
+// ----------------------------------------------------------------------------------------
+// The sum-factorised adjoint of hexahedra (TD = GD = 3) at tensor-product rules.
+//
+// Per cell (one thread): the forward contraction as sumfact_kernel, plane by plane and row by
+// row; at every point K, det J, the fused forward outputs when asked, and from the cotangents
+// xbar, Jbar = dbar det J K^T - K^T Kbar K^T. The node contributions
+//   L_g(i, j, k) = sum_{a,b,c} [B0 B1 B2 xbar_g + D0 B1 B2 Jbar(g, 0) + B0 D1 B2 Jbar(g, 1)
+//                               + B0 B1 D2 Jbar(g, 2)]
+// are the transposed contraction, accumulated in the reverse order: over a row's points into
+// RU = sum_a (B0 xbar + D0 Jbar0), RD1 = sum_a B0 Jbar1, RD2 = sum_a B0 Jbar2 (registers), over a
+// plane's rows into PU += B1 RU + D1 RD1, PV += B1 RD2 (shared-memory slots), over the planes
+// into L += B2 PU + D2 PV (shared-memory slots). The 32 cells of a warp then write their rows
+// (Lagrange node order, R = 4 values, the fourth zero) as one contiguous run.
+
+struct VjpSfArgs {
+  const void* nodes;
+  const uint32_t* dofmap;
+  const unsigned char* tab;  // the sum-factorisation section: B_d, D_d, perm
+  const void* ct[3];         // cotangents: points, detj, pinv (tile 16 chunks) or null
+  void* out[4];              // fused forward fields: points, jacobian, detj, pinv, or null
+  void* local;               // contributions [cell][K][4]
+  int* err;
+  int64_t first_cell, padded, out_first_cell, last_cell, range_end;
+  double origin[3];
+  uint32_t last_node, tab_bytes, off_b[3], off_d[3], off_perm;
+  int m[3];
+  int num_points;
+};
+
+// Shared memory past the tables: the inverse permutation (K u32, rounded to 16 bytes), then per
+// thread the coordinate slots (K * 3, stride `threads`), the plane accumulators (2 * 3 * N^2,
+// stride `threads`) and the contribution slots (K * 3, stride threads + 1, so that the final
+// write-out, whose lanes read one cell's slots, spreads over the banks), of F.
+inline size_t vjp_sumfact_extra_bytes(int n, int threads, size_t f_bytes) {
+  const size_t k = (size_t)n * n * n;
+  return (k * 4 + 15) / 16 * 16 +
+         f_bytes * ((size_t)threads * (k * 3 + 2 * 3 * (size_t)n * n) + (size_t)(threads + 1) * k * 3);
+}
+
+template <typename F, bool SPLIT, int N>
+__global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_constant__ VjpSfArgs a) {
+  using NT = typename std::conditional<SPLIT, double, F>::type;
+  using A = Ar<F>;
+  using M = Factors<F, 3, 3>;
+  constexpr int D = 3, K = N * N * N, LJ = 9, R = 4, TILE = 16;
+  constexpr int T = kEvalThreads;  // compile-time slot strides: shared-memory offsets are immediates
+  __shared__ uint64_t bar;
+  extern __shared__ __align__(16) unsigned char smem[];
+  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
+  uint32_t* invperm = reinterpret_cast<uint32_t*>(smem + (a.tab_bytes + 15) / 16 * 16);
+  for (int i = threadIdx.x; i < K; i += T) invperm[perm[i]] = i;
+  __syncthreads();
+  F* slots = reinterpret_cast<F*>(reinterpret_cast<unsigned char*>(invperm) + (K * 4 + 15) / 16 * 16);
+  constexpr int S = T + 1;                                        // stride of the contribution slots
+  F* xs = slots + threadIdx.x;                                    // [K][3] coordinates
+  F* Ps = slots + (size_t)K * D * T + threadIdx.x;                // [2][3][N][N] plane accumulators
+  F* Lw = slots + (size_t)K * D * T + (size_t)2 * D * N * N * T;  // [K][3] contributions
+  F* Ls = Lw + threadIdx.x;
+  const F* B0 = reinterpret_cast<const F*>(smem + a.off_b[0]);
+  const F* D0 = reinterpret_cast<const F*>(smem + a.off_d[0]);
+  const F* B1 = reinterpret_cast<const F*>(smem + a.off_b[1]);
+  const F* D1 = reinterpret_cast<const F*>(smem + a.off_d[1]);
+  const F* B2 = reinterpret_cast<const F*>(smem + a.off_b[2]);
+  const F* D2 = reinterpret_cast<const F*>(smem + a.off_d[2]);
+  const NT* nodes = static_cast<const NT*>(a.nodes);
+  const F* ctx = static_cast<const F*>(a.ct[0]);
+  const F* ctd = static_cast<const F*>(a.ct[1]);
+  const F* ctk = static_cast<const F*>(a.ct[2]);
+  const int m0 = a.m[0], m1 = a.m[1], m2 = a.m[2];
+  const int nq = a.num_points;
+  const int lane = threadIdx.x % 32;
+  const int64_t step = (int64_t)gridDim.x * T;
+
+  // A warp walks 32 consecutive cells; lanes past the padded range repeat the last cell and
+  // store nothing.
+  for (int64_t cw = (int64_t)blockIdx.x * T + (threadIdx.x & ~31); cw < a.padded; cw += step) {
+    const int64_t c = cw + lane;
+    const bool live = c < a.padded;
+    const int64_t cell = min(a.first_cell + c, a.last_cell);
+    const uint32_t* row = a.dofmap + cell * K;
+    F xh[D], xl[D];
+    double x0[D];
+    if constexpr (SPLIT) {
+      const uint32_t n0 = min(__ldg(row), a.last_node);
+#pragma unroll
+      for (int g = 0; g < D; ++g) {
+        x0[g] = __ldg(nodes + (int64_t)n0 * D + g);
+        const double v = x0[g] + a.origin[g];
+        xh[g] = d2f_rn(v);
+        xl[g] = d2f_rn(v - f2d_exact(xh[g]));
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < D; ++g) {
+        x0[g] = 0.0;
+        xh[g] = (F)a.origin[g];
+        xl[g] = F(0);
+      }
+    }
+#pragma unroll 4
+    for (int l = 0; l < K; ++l) {
+      const uint32_t n = min(__ldg(row + perm[l]), a.last_node);
+#pragma unroll
+      for (int g = 0; g < D; ++g) {
+        const NT v = __ldg(nodes + (int64_t)n * D + g);
+        F y;
+        if constexpr (SPLIT) y = d2f_rn(v - x0[g]);
+        else y = v;
+        xs[(l * D + g) * T] = y;
+        Ls[(l * D + g) * S] = F(0);
+      }
+    }
+    // Lanes past the padded range read the cotangents of the last padded cell.
+    const int64_t o = a.out_first_cell + (live ? c : a.padded - 1);
+    const int64_t tq = (o / TILE) * nq;
+    const int l16 = (int)(o % TILE);
+#define TLG_AT(q, len, comp) (((tq + (q)) * (len) + (comp)) * TILE + l16)
+    // The cotangents of a point (xbar, dbar, Kbar; zero where absent), loaded one point ahead
+    // (points run in rule order) so that their latency overlaps the current point's work.
+    auto load_ct = [&](int q, F* v) {
+#pragma unroll
+      for (int g = 0; g < D; ++g) v[g] = ctx ? __ldg(ctx + TLG_AT(q, D, g)) : F(0);
+      v[D] = ctd ? __ldg(ctd + TLG_AT(q, 1, 0)) : F(0);
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) v[D + 1 + i] = ctk ? __ldg(ctk + TLG_AT(q, LJ, i)) : F(0);
+    };
+    F cur[D + 1 + LJ];
+    load_ct(0, cur);
+
+    for (int c2 = 0; c2 < m2; ++c2) {
+      F U[D][N][N], V[D][N][N];
+#pragma unroll
+      for (int g = 0; g < D; ++g)
+#pragma unroll
+        for (int jj = 0; jj < N; ++jj)
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            U[g][jj][i] = V[g][jj][i] = F(0);
+            Ps[((0 * D + g) * N * N + jj * N + i) * T] = F(0);
+            Ps[((1 * D + g) * N * N + jj * N + i) * T] = F(0);
+          }
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const F bk = B2[c2 * N + k], dk = D2[c2 * N + k];
+#pragma unroll
+        for (int jj = 0; jj < N; ++jj)
+#pragma unroll
+          for (int i = 0; i < N; ++i)
+#pragma unroll
+            for (int g = 0; g < D; ++g) {
+              const F xv = xs[((i + N * (jj + N * k)) * D + g) * T];
+              U[g][jj][i] = A::fma(xv, bk, U[g][jj][i]);
+              V[g][jj][i] = A::fma(xv, dk, V[g][jj][i]);
+            }
+      }
+      for (int b1 = 0; b1 < m1; ++b1) {
+        F UU[D][N], UD[D][N], VU[D][N], RU[D][N], RD1[D][N], RD2[D][N];
+#pragma unroll
+        for (int g = 0; g < D; ++g)
+#pragma unroll
+          for (int i = 0; i < N; ++i) UU[g][i] = UD[g][i] = VU[g][i] = RU[g][i] = RD1[g][i] = RD2[g][i] = F(0);
+#pragma unroll
+        for (int jj = 0; jj < N; ++jj) {
+          const F bj = B1[b1 * N + jj], dj = D1[b1 * N + jj];
+#pragma unroll
+          for (int g = 0; g < D; ++g)
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              UU[g][i] = A::fma(U[g][jj][i], bj, UU[g][i]);
+              UD[g][i] = A::fma(U[g][jj][i], dj, UD[g][i]);
+              VU[g][i] = A::fma(V[g][jj][i], bj, VU[g][i]);
+            }
+        }
+        for (int a0 = 0; a0 < m0; ++a0) {
+          const int q = a0 + m0 * (b1 + m1 * c2);
+          F nxt[D + 1 + LJ];
+          load_ct(min(q + 1, nq - 1), nxt);
+          F x[D], j[LJ];
+#pragma unroll
+          for (int g = 0; g < D; ++g) {
+            F s = F(0), j0 = F(0), j1 = F(0), j2 = F(0);
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              const F bi = B0[a0 * N + i], di = D0[a0 * N + i];
+              s = A::fma(UU[g][i], bi, s);
+              j0 = A::fma(UU[g][i], di, j0);
+              j1 = A::fma(UD[g][i], bi, j1);
+              j2 = A::fma(VU[g][i], bi, j2);
+            }
+            x[g] = s;
+            j[0 * D + g] = j0;
+            j[1 * D + g] = j1;
+            j[2 * D + g] = j2;
+          }
+          F kinv[LJ];
+          M::pinv(j, kinv);
+          const F det = M::detj(j);
+          if (live) {
+            if (a.out[0]) {
+#pragma unroll
+              for (int g = 0; g < D; ++g) {
+                const F v = SPLIT ? A::add(xh[g], A::add(xl[g], x[g])) : A::add(x[g], xh[g]);
+                static_cast<F*>(a.out[0])[TLG_AT(q, D, g)] = v;
+              }
+            }
+            if (a.out[1])
+#pragma unroll
+              for (int i = 0; i < LJ; ++i) static_cast<F*>(a.out[1])[TLG_AT(q, LJ, i)] = j[i];
+            if (a.out[2]) static_cast<F*>(a.out[2])[TLG_AT(q, 1, 0)] = det;
+            if (a.out[3])
+#pragma unroll
+              for (int i = 0; i < LJ; ++i) static_cast<F*>(a.out[3])[TLG_AT(q, LJ, i)] = kinv[i];
+          }
+          // Jbar(g, d) at g * D + d; K(t, h) and Kbar(t, h) at h * D + t.
+          F jb[LJ];
+          const F s = A::mul(cur[D], det);
+#pragma unroll
+          for (int g = 0; g < D; ++g)
+#pragma unroll
+            for (int d = 0; d < D; ++d) jb[g * D + d] = A::mul(s, kinv[g * D + d]);
+          if (ctk) {
+            const F* kb = cur + D + 1;
+#pragma unroll
+            for (int t = 0; t < D; ++t)
+#pragma unroll
+              for (int d = 0; d < D; ++d) {
+                F mt = A::mul(kb[t], kinv[d]);
+#pragma unroll
+                for (int h = 1; h < D; ++h) mt = A::fma(kb[h * D + t], kinv[h * D + d], mt);
+#pragma unroll
+                for (int g = 0; g < D; ++g) jb[g * D + d] = A::fma(A::neg(kinv[g * D + t]), mt, jb[g * D + d]);
+              }
+          }
+          const F* xb = cur;
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            const F bi = B0[a0 * N + i], di = D0[a0 * N + i];
+#pragma unroll
+            for (int g = 0; g < D; ++g) {
+              RU[g][i] = A::fma(bi, xb[g], A::fma(di, jb[g * D + 0], RU[g][i]));
+              RD1[g][i] = A::fma(bi, jb[g * D + 1], RD1[g][i]);
+              RD2[g][i] = A::fma(bi, jb[g * D + 2], RD2[g][i]);
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < D + 1 + LJ; ++i) cur[i] = nxt[i];
+        }
+        // The row into the plane accumulators.
+#pragma unroll
+        for (int jj = 0; jj < N; ++jj) {
+          const F bj = B1[b1 * N + jj], dj = D1[b1 * N + jj];
+#pragma unroll
+          for (int g = 0; g < D; ++g)
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              F* pu = Ps + ((0 * D + g) * N * N + jj * N + i) * T;
+              F* pv = Ps + ((1 * D + g) * N * N + jj * N + i) * T;
+              *pu = A::fma(bj, RU[g][i], A::fma(dj, RD1[g][i], *pu));
+              *pv = A::fma(bj, RD2[g][i], *pv);
+            }
+        }
+      }
+      // The plane into the contributions.
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const F bk = B2[c2 * N + k], dk = D2[c2 * N + k];
+#pragma unroll
+        for (int jj = 0; jj < N; ++jj)
+#pragma unroll
+          for (int i = 0; i < N; ++i)
+#pragma unroll
+            for (int g = 0; g < D; ++g) {
+              F* lp = Ls + ((i + N * (jj + N * k)) * D + g) * S;
+              const F pu = Ps[((0 * D + g) * N * N + jj * N + i) * T];
+              const F pv = Ps[((1 * D + g) * N * N + jj * N + i) * T];
+              *lp = A::fma(bk, pu, A::fma(dk, pv, *lp));
+            }
+      }
+    }
+#undef TLG_AT
+    // The warp's cells' rows, Lagrange node order, as one run.
+    __syncwarp();
+    const int64_t cell0 = a.first_cell + cw;
+    const int64_t nreal = min((int64_t)32, a.range_end - cell0);
+    if (nreal > 0) {
+      F* dst = static_cast<F*>(a.local) + cell0 * (K * R);
+      const F* lw = Lw + (threadIdx.x & ~31);  // the warp's contribution slots
+      for (int e = lane; e < nreal * (K * R); e += 32) {
+        const int cl = e / (K * R);
+        const int rem = e - cl * (K * R);
+        const int kk = rem / R, g = rem - kk * R;
+        dst[e] = g < D ? lw[(invperm[kk] * D + g) * S + cl] : F(0);
+      }
+    }
+    __syncwarp();
+  }
+}
+
+}  // namespace tlg

@@ -193,3 +193,67 @@ def test_gather_sums_rows_in_f64(cuda, dtype):
     np.add.at(want, cells.ravel(), v64)
     np.add.at(mag, cells.ravel(), np.abs(v64))
     assert np.all(np.abs(got - want) <= 8 * 2.0 ** -46 * mag)
+
+
+@pytest.mark.parametrize("precision", ["native", "split"])
+@pytest.mark.parametrize("n,degree,rdeg", [(3, 2, 4), (5, 2, 5), (4, 1, 2), (3, 1, 4), (2, 2, 3)])
+def test_sumfact_adjoint_matches_node_rows(cuda, n, degree, rdeg, precision):
+    """Hexahedra at tensor rules: the sum-factorised adjoint (one cell per thread, transposed
+    contraction row by row and plane by plane) against the node-row kernel and the oracle, with the
+    fused forward; cell counts that are not multiples of the 32-cell warp runs."""
+    mesh = meshes.curved_box("Hexahedron", n, degree, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, _ = tg.refcell.gauss_rule("Hexahedron", rdeg)
+    ps = tg.PointSet("Hexahedron", pts, np.ones(len(pts)))
+    ncells = mesh.blocks[0].num_cells
+    dt = torch.float64 if precision == "native" else torch.float32
+    ct, host = cotangent_fields(np.random.default_rng(13), ncells, len(pts), dt)
+    names = ("points", "jacobian", "detj", "pinv")
+    with tg.with_strategy("sumfact"):
+        got, fused = tg.vjp_block(g, 0, ps, ct, precision=precision, forward=names)
+        assert tg.last_kernel_family() == "sumfact"
+    with tg.with_strategy("direct"):
+        rows, plain = tg.vjp_block(g, 0, ps, ct, precision=precision, forward=names)
+        assert tg.last_kernel_family() == "direct"
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
+    want = orc.vjp("Hexahedron", degree, absx, mesh.blocks[0].cells, pts, host["points"],
+                   host["detj"][..., 0], host["pinv"])
+    tol = 1e-11 if precision == "native" else 2e-5
+    assert orc.rel_err(got.cpu().numpy(), want) < tol
+    assert orc.rel_err(got.cpu().numpy(), rows.cpu().numpy()) < tol
+    fwd = orc.eval_block("Hexahedron", degree, absx, mesh.blocks[0].cells, pts)
+    for k, o in zip(names, ("x", "j", "detj", "k")):
+        f = fused[k].to_host_cell_major()
+        assert orc.rel_err(f, plain[k].to_host_cell_major()) < (1e-13 if precision == "native" else 2e-6), k
+        assert orc.rel_err(f, fwd[o]) < (1e-12 if precision == "native" else 1e-5), k
+
+
+@pytest.mark.parametrize("missing", ["points", "detj", "pinv"])
+def test_sumfact_adjoint_with_missing_cotangents(cuda, missing):
+    """A missing cotangent field counts as zero, in both kernel families."""
+    mesh = meshes.curved_box("Hexahedron", 3, 2, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, _ = tg.refcell.gauss_rule("Hexahedron", 4)
+    ps = tg.PointSet("Hexahedron", pts, np.ones(len(pts)))
+    ct, host = cotangent_fields(np.random.default_rng(17), mesh.blocks[0].num_cells, len(pts), torch.float64)
+    del ct[missing]
+    host[missing] = np.zeros_like(host[missing])
+    with tg.with_strategy("sumfact"):
+        got, _ = tg.vjp_block(g, 0, ps, ct)
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
+    want = orc.vjp("Hexahedron", 2, absx, mesh.blocks[0].cells, pts, host["points"],
+                   host["detj"][..., 0], host["pinv"])
+    assert orc.rel_err(got.cpu().numpy(), want) < 1e-11
+
+
+@pytest.mark.parametrize("cell,degree,rdeg,family", [("Hexahedron", 2, 4, "sumfact"), ("Hexahedron", 1, 2, "sumfact"),
+                                                     ("Prism", 2, 4, "direct"), ("Tetrahedron", 2, 4, "direct")])
+def test_adjoint_auto_policy(cuda, cell, degree, rdeg, family):
+    mesh = meshes.curved_box(cell, 2, degree, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    ct, _ = cotangent_fields(np.random.default_rng(1), mesh.blocks[0].num_cells, len(pts), torch.float32)
+    with tg.with_strategy("auto"):
+        tg.vjp_block(g, 0, ps, ct, precision="split")
+        assert tg.last_kernel_family() == family
