@@ -481,10 +481,11 @@ def extra_ordering():
     return out
 
 
-def extra_hex_strategies(n: int = 64):
-    """Curved hexahedra Q1-Q3 (n^3 cells, Gauss rules of 2, 3, 4 points per direction) evaluated
-    (x/J/detJ/K) under each strategy and precision: ms per launch and the kernel family that ran.
-    Run with --workload hex_strategies (not part of the default run)."""
+def extra_hex_strategies(n: int = 64, cell: str = "Hexahedron"):
+    """Curved hexahedra Q1-Q3 (n^3 cells) or prisms P1-P3 (2 n^3 cells) at Gauss rules of 2, 3, 4
+    points per direction, evaluated (x/J/detJ/K) under each strategy and precision: ms per launch
+    and the kernel family that ran. Run with --workload hex_strategies / prism_strategies (not
+    part of the default run)."""
     import numpy as np
     import torch
 
@@ -492,11 +493,12 @@ def extra_hex_strategies(n: int = 64):
     from gridcl_gb300 import meshes
 
     names = ("points", "jacobian", "detj", "pinv")
-    out = {"workload": f"curved hexahedra Q1-Q3, {n}^3 cells, tensor Gauss rules, x/J/detJ/K"}
+    label_cells = f"{n}^3 hexahedra" if cell == "Hexahedron" else f"2x{n}^3 prisms"
+    out = {"workload": f"curved {label_cells}, degrees 1-3, Gauss rules, x/J/detJ/K"}
     for degree in (1, 2, 3):
-        mesh = meshes.curved_box("Hexahedron", n, degree, jitter=0.02)
-        pts, w = tg.refcell.gauss_rule("Hexahedron", 2 * degree)
-        ps = tg.PointSet("Hexahedron", pts, w)
+        mesh = meshes.curved_box(cell, n, degree, jitter=0.02)
+        pts, w = tg.refcell.gauss_rule(cell, 2 * degree)
+        ps = tg.PointSet(cell, pts, w)
         for prec, dt in (("split", torch.float64), ("native", torch.float64), ("native", torch.float32)):
             g = tg.Geometry.from_host(mesh, dtype=dt)
             row = {}
@@ -509,7 +511,7 @@ def extra_hex_strategies(n: int = 64):
                 row[strat] = {"family": fam, "ms": ms}
                 del f
             label = "split" if prec == "split" else ("f64" if dt == torch.float64 else "f32")
-            out[f"Q{degree}_{label}"] = row
+            out[f"{'Q' if cell == 'Hexahedron' else 'P'}{degree}_{label}"] = row
             del g
             torch.cuda.empty_cache()
     return out
@@ -716,7 +718,7 @@ def run_ours(args):
 
 
 EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "pull_back", "ordering", "p1_box",
-          "hex_strategies")
+          "hex_strategies", "prism_strategies")
 
 
 def run_extra(args):
@@ -727,7 +729,8 @@ def run_extra(args):
     fn = {"hybrid_batched": extra_hybrid, "sphere_surface": extra_sphere,
           "q2_forward_adjoint": lambda: extra_adjoint(args.adjoint_n, args.fd_nodes), "pull_back": extra_pull_back,
           "ordering": extra_ordering, "p1_box": extra_p1_box,
-          "hex_strategies": lambda: extra_hex_strategies(args.hex_n)}[args.workload]
+          "hex_strategies": lambda: extra_hex_strategies(args.hex_n),
+          "prism_strategies": lambda: extra_hex_strategies(args.hex_n, "Prism")}[args.workload]
     print(json.dumps(fn()), flush=True)
 
 

@@ -50,8 +50,11 @@ struct tlg_tables {
   // the adjoint's: per direction d, B_d [m_d][N] = l_i(u_d[a]) and D_d [m_d][N] = l_i'(u_d[a]) in the
   // arithmetic's type, then perm [K] u32 (lexicographic node index -> Lagrange node); offsets
   // relative to the section.
-  bool sf_ok = false;
-  int sf_n = 0, sf_m[3] = {1, 1, 1};
+  // Prisms: psi, d_x psi, d_y psi [m_t][NT] of the triangle rule in B_0, D_0, D_1 (B_1 empty), the
+  // interval's l, l' [m_z][N] in B_2, D_2, perm [N * NT] (index c NT + t -> Lagrange node); point
+  // q = i sf_qs[0] + j sf_qs[1].
+  bool sf_ok = false, sf_prism = false;
+  int sf_n = 0, sf_m[3] = {1, 1, 1}, sf_qs[2] = {0, 0};
   uint32_t off_sf = 0, sf_bytes = 0, sf_offb[3] = {0, 0, 0}, sf_offd[3] = {0, 0, 0}, sf_offperm = 0;
   int* err = nullptr;
   std::vector<unsigned char> host;  // host copy of the device bytes
@@ -188,6 +191,9 @@ tlg_status eval_sumfact(const tlg_tables* t, const tlg_block* b, const tlg_outpu
     a.m[d] = t->sf_m[d];
   }
   a.off_perm = t->sf_offperm;
+  a.prism = t->sf_prism;
+  a.qs[0] = t->sf_qs[0];
+  a.qs[1] = t->sf_qs[1];
   a.mask = mask;
   a.num_points = (int)t->q;
   const size_t fbytes = t->dtype == TLG_F64 ? 8 : 4;
@@ -465,6 +471,97 @@ bool tensor_tables(int cell, int degree, int family, const double* pts, int64_t 
   return true;
 }
 
+// The prism tables when the points are a triangle rule times points in z (either index order)
+// and the prism basis is the product of the triangle's and the interval's: the product of the
+// factor tables equals the full tabulation `tab` ([deriv][q][k]) to 1e-10 at every point and node.
+bool prism_tables(int degree, int family, const double* pts, int64_t nq, const std::vector<double>& tab, int* m,
+                  int* qs, std::vector<double>* B, std::vector<double>* D, std::vector<uint32_t>& perm) {
+  const int n = degree + 1, nt = n * (n + 1) / 2;
+  const int64_t k = (int64_t)nt * n;
+  if (nq < 1 || tlg::num_lagrange_nodes(tlg::kPrism, degree) != k) return false;
+  int64_t mt = 0, mz = 0, st = 0, sz = 0, run = 1;
+  while (run < nq && pts[run * 3 + 2] == pts[2]) ++run;
+  if (run > 1 || nq == 1) {  // z slowest: q = i + mt j
+    mt = run;
+    mz = nq / mt;
+    st = 1;
+    sz = mt;
+  } else {  // z fastest: q = j + mz i
+    run = 1;
+    while (run < nq && pts[run * 3] == pts[0] && pts[run * 3 + 1] == pts[1]) ++run;
+    mz = run;
+    mt = nq / mz;
+    sz = 1;
+    st = mz;
+  }
+  if (mt * mz != nq) return false;
+  std::vector<double> tri((size_t)mt * 2), zs((size_t)mz);
+  for (int64_t i = 0; i < mt; ++i)
+    for (int d = 0; d < 2; ++d) tri[(size_t)(i * 2 + d)] = pts[i * st * 3 + d];
+  for (int64_t j = 0; j < mz; ++j) zs[(size_t)j] = pts[j * sz * 3 + 2];
+  for (int64_t i = 0; i < mt; ++i)
+    for (int64_t j = 0; j < mz; ++j) {
+      const double* x = pts + (i * st + j * sz) * 3;
+      if (x[0] != tri[(size_t)(i * 2)] || x[1] != tri[(size_t)(i * 2 + 1)] || x[2] != zs[(size_t)j]) return false;
+    }
+  std::vector<double> tt, lt, s1, lp;
+  try {
+    tt = tlg::tabulate(tlg::kTriangle, degree, family, tri.data(), (long)mt, 1);
+    lt = tlg::lagrange_points(tlg::kTriangle, degree, family);
+    s1 = tlg::lagrange_points(tlg::kInterval, degree, family);
+    lp = tlg::lagrange_points(tlg::kPrism, degree, family);
+  } catch (const std::exception&) {
+    return false;
+  }
+  std::sort(s1.begin(), s1.end());
+  if ((int64_t)lt.size() != (int64_t)nt * 2 || (int)s1.size() != n || (int64_t)lp.size() != k * 3) return false;
+  perm.assign((size_t)k, 0xFFFFFFFFu);
+  for (int64_t kk = 0; kk < k; ++kk) {
+    int ft = -1, fc = -1;
+    for (int t = 0; t < nt; ++t)
+      if (std::fabs(lp[kk * 3] - lt[t * 2]) < 1e-12 && std::fabs(lp[kk * 3 + 1] - lt[t * 2 + 1]) < 1e-12) ft = t;
+    for (int c = 0; c < n; ++c)
+      if (std::fabs(lp[kk * 3 + 2] - s1[c]) < 1e-12) fc = c;
+    if (ft < 0 || fc < 0 || perm[(size_t)(fc * nt + ft)] != 0xFFFFFFFFu) return false;
+    perm[(size_t)(fc * nt + ft)] = (uint32_t)kk;
+  }
+  B[0].assign((size_t)(mt * nt), 0.0);
+  D[0].assign((size_t)(mt * nt), 0.0);
+  B[1].clear();
+  D[1].assign((size_t)(mt * nt), 0.0);
+  for (int64_t i = 0; i < mt; ++i)
+    for (int t = 0; t < nt; ++t) {
+      B[0][(size_t)(i * nt + t)] = tt[(size_t)(i * nt + t)];
+      D[0][(size_t)(i * nt + t)] = tt[(size_t)((mt + i) * nt + t)];
+      D[1][(size_t)(i * nt + t)] = tt[(size_t)((2 * mt + i) * nt + t)];
+    }
+  B[2].assign((size_t)(mz * n), 0.0);
+  D[2].assign((size_t)(mz * n), 0.0);
+  for (int64_t j = 0; j < mz; ++j) lagrange_1d(s1, zs[(size_t)j], &B[2][(size_t)(j * n)], &D[2][(size_t)(j * n)]);
+  // The product identity against the prism's own tabulation.
+  for (int64_t i = 0; i < mt; ++i)
+    for (int64_t j = 0; j < mz; ++j) {
+      const int64_t q = i * st + j * sz;
+      for (int c = 0; c < n; ++c)
+        for (int t = 0; t < nt; ++t) {
+          const int64_t kk = perm[(size_t)(c * nt + t)];
+          const double l = B[2][(size_t)(j * n + c)], ld = D[2][(size_t)(j * n + c)];
+          const double want[4] = {B[0][(size_t)(i * nt + t)] * l, D[0][(size_t)(i * nt + t)] * l,
+                                  D[1][(size_t)(i * nt + t)] * l, B[0][(size_t)(i * nt + t)] * ld};
+          for (int r = 0; r < 4; ++r) {
+            const double got = tab[(size_t)((r * nq + q) * k + kk)];
+            if (!(std::fabs(got - want[r]) <= 1e-10 * std::max(1.0, std::fabs(got)))) return false;
+          }
+        }
+    }
+  m[0] = (int)mt;
+  m[1] = 1;
+  m[2] = (int)mz;
+  qs[0] = (int)st;
+  qs[1] = (int)sz;
+  return true;
+}
+
 }  // namespace
 
 tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dtype,
@@ -535,6 +632,10 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
     std::vector<uint32_t> sf_perm;
     if ((cell == tlg::kQuadrilateral || cell == tlg::kHexahedron) && degree + 1 <= 6)
       t->sf_ok = tensor_tables(cell, degree, family, points, npoints, t->sf_m, sf_b, sf_d, sf_perm);
+    if (cell == tlg::kPrism && degree <= 3 && gdim == 3) {
+      t->sf_ok = prism_tables(degree, family, points, npoints, tab, t->sf_m, t->sf_qs, sf_b, sf_d, sf_perm);
+      t->sf_prism = t->sf_ok;
+    }
     t->off_sf = (uint32_t)align16(t->off_vjp + t->vjp_bytes);
     if (t->sf_ok) {
       t->sf_n = degree + 1;
@@ -748,7 +849,9 @@ namespace {
 
 // Hexahedra with a tensor-product rule and 2 or 3 nodes per direction have the sum-factorised
 // adjoint.
-bool vjp_sumfact_preferred(const tlg_tables* t) { return t->sf_ok && t->td == 3 && (t->sf_n == 2 || t->sf_n == 3); }
+bool vjp_sumfact_preferred(const tlg_tables* t) {
+  return t->sf_ok && t->cell == tlg::kHexahedron && (t->sf_n == 2 || t->sf_n == 3);
+}
 
 // The sum-factorised adjoint from the arguments of the node-row kernel; `found` is false when
 // the element has none (then the node-row kernel runs).

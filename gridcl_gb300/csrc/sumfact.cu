@@ -1,5 +1,5 @@
-// Instantiations of the sum-factorised kernel (sumfact.cuh): hexahedra Q1-Q3 and quadrilaterals
-// Q1-Q5, planar and embedded in 3D.
+// Instantiations of the sum-factorised kernels (sumfact.cuh): hexahedra Q1-Q3, quadrilaterals
+// Q1-Q5 (planar and embedded in 3D), prisms P1-P3, and the hexahedral adjoint.
 #include <algorithm>
 
 #include "eval_launch.cuh"
@@ -12,6 +12,13 @@ namespace {
 template <typename F, bool SPLIT>
 cudaError_t launch_sf(int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s, bool* found) {
   *found = true;
+  if (a.prism) {
+    if (n == 2) return launch_persistent(sumfact_prism_kernel<F, SPLIT, 2>, a, a.padded, smem, s);
+    if (n == 3) return launch_persistent(sumfact_prism_kernel<F, SPLIT, 3>, a, a.padded, smem, s);
+    if (n == 4) return launch_persistent(sumfact_prism_kernel<F, SPLIT, 4>, a, a.padded, smem, s);
+    *found = false;
+    return cudaSuccess;
+  }
 #define TLG_SF(TD, GD, NN) \
   if (td == TD && gd == GD && n == NN) \
     return launch_persistent(sumfact_kernel<F, SPLIT, TD, GD, NN>, a, a.padded, smem, s);

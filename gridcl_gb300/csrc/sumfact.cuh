@@ -40,7 +40,9 @@ struct SfArgs {
   double origin[3];
   float cond_limit;
   uint32_t last_node, tab_bytes, off_b[3], off_d[3], off_perm, mask;
-  int m[3];  // points per direction
+  int m[3];  // points per direction (prisms: triangle points, 1, z points)
+  int qs[2];  // prisms: the point index strides of the triangle point and of the z point
+  int prism;  // the table is a prism's
   int num_points;
   int tile_shift;  // log2 of the output tile
 };
@@ -266,7 +268,121 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_kernel(const __grid_cons
   }
 }
 
+// Prisms (the reference's prism blocks, tetraloma-geometry/src/sumfact/prism.rs:23-136). The
+// prism's Lagrange basis is the product of the triangle's (NT = N (N + 1) / 2 nodes) and the
+// interval's (N nodes), and a tensor rule is a triangle rule times points in z. Per triangle point
+// i the cell's coordinates are contracted with the triangle basis and its two derivatives,
+//   BV_g[c] = sum_t x_{(c, t), g} psi_t(i),  BX_g[c] = ... d_x psi_t(i),  BY_g[c] = ... d_y psi_t(i),
+// then per z point j with the interval basis:
+//   X_g = sum_c BV_g[c] l_c(z_j), J(g, 0) = sum_c BX_g[c] l_c(z_j), J(g, 1) = sum_c BY_g[c] l_c(z_j),
+//   J(g, 2) = sum_c BV_g[c] l_c'(z_j):
+// 3 NT N per triangle point and 4 N per point and coordinate instead of 4 NT N per point. Table:
+// psi [m_t][NT] at off_b[0], d_x psi at off_d[0], d_y psi at off_d[1], l [m_z][N] at off_b[2], l' at
+// off_d[2]; perm maps the index c NT + t to the Lagrange node; point q = i qs[0] + j qs[1].
+template <typename F, bool SPLIT, int N>
+__global__ void __launch_bounds__(kEvalThreads) sumfact_prism_kernel(const __grid_constant__ SfArgs a) {
+  using NT_ = typename std::conditional<SPLIT, double, F>::type;  // node type
+  using A = Ar<F>;
+  constexpr int TD = 3, GD = 3, NT = N * (N + 1) / 2, K = NT * N, LJ = TD * GD;
+  constexpr int T = kEvalThreads;
+  __shared__ uint64_t bar;
+  extern __shared__ __align__(16) unsigned char smem[];
+  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  F* xs = reinterpret_cast<F*>(smem + (a.tab_bytes + 15) / 16 * 16) + threadIdx.x;
+  const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
+  const F* PV = reinterpret_cast<const F*>(smem + a.off_b[0]);
+  const F* PX = reinterpret_cast<const F*>(smem + a.off_d[0]);
+  const F* PY = reinterpret_cast<const F*>(smem + a.off_d[1]);
+  const F* LV = reinterpret_cast<const F*>(smem + a.off_b[2]);
+  const F* LD = reinterpret_cast<const F*>(smem + a.off_d[2]);
+  const NT_* nodes = static_cast<const NT_*>(a.nodes);
+  const int mt = a.m[0], mz = a.m[2], st = a.qs[0], sz = a.qs[1];
+
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t cell = min(a.first_cell + c, a.last_cell);
+    const uint32_t* row = a.dofmap + cell * K;
+    F xh[GD], xl[GD];
+    double x0[GD];
+    if constexpr (SPLIT) {
+      const uint32_t n0 = min(__ldg(row), a.last_node);
+#pragma unroll
+      for (int g = 0; g < GD; ++g) {
+        x0[g] = __ldg(nodes + (int64_t)n0 * GD + g);
+        const double v = x0[g] + a.origin[g];
+        xh[g] = d2f_rn(v);
+        xl[g] = d2f_rn(v - f2d_exact(xh[g]));
+      }
+    } else {
+#pragma unroll
+      for (int g = 0; g < GD; ++g) {
+        x0[g] = 0.0;
+        xh[g] = (F)a.origin[g];
+        xl[g] = F(0);
+      }
+    }
+#pragma unroll 4
+    for (int l = 0; l < K; ++l) {
+      const uint32_t n = min(__ldg(row + perm[l]), a.last_node);
+#pragma unroll
+      for (int g = 0; g < GD; ++g) {
+        const NT_ v = __ldg(nodes + (int64_t)n * GD + g);
+        F y;
+        if constexpr (SPLIT) y = d2f_rn(v - x0[g]);
+        else y = v;
+        xs[(l * GD + g) * T] = y;
+      }
+    }
+    const int64_t o = a.out_first_cell + c;
+    const int64_t tile_idx = o >> a.tile_shift;
+    const int lane = (int)(o & ((1 << a.tile_shift) - 1));
+
+    for (int i = 0; i < mt; ++i) {
+      F bv[GD][N], bx[GD][N], by[GD][N];
+#pragma unroll
+      for (int g = 0; g < GD; ++g)
+#pragma unroll
+        for (int cc = 0; cc < N; ++cc) bv[g][cc] = bx[g][cc] = by[g][cc] = F(0);
+      // (f64 P3: a rolled loop, the unrolled one spills.)
+#pragma unroll(sizeof(F) == 8 && N >= 4 ? 1 : NT)
+      for (int t = 0; t < NT; ++t) {
+        const F w = PV[i * NT + t], wx = PX[i * NT + t], wy = PY[i * NT + t];
+#pragma unroll
+        for (int cc = 0; cc < N; ++cc)
+#pragma unroll
+          for (int g = 0; g < GD; ++g) {
+            const F xv = xs[((cc * NT + t) * GD + g) * T];
+            bv[g][cc] = A::fma(xv, w, bv[g][cc]);
+            bx[g][cc] = A::fma(xv, wx, bx[g][cc]);
+            by[g][cc] = A::fma(xv, wy, by[g][cc]);
+          }
+      }
+      for (int jz = 0; jz < mz; ++jz) {
+        F x[GD], j[LJ];
+#pragma unroll
+        for (int g = 0; g < GD; ++g) {
+          F s0 = F(0), j0 = F(0), j1 = F(0), j2 = F(0);
+#pragma unroll
+          for (int cc = 0; cc < N; ++cc) {
+            const F l = LV[jz * N + cc], ld = LD[jz * N + cc];
+            s0 = A::fma(bv[g][cc], l, s0);
+            j0 = A::fma(bx[g][cc], l, j0);
+            j1 = A::fma(by[g][cc], l, j1);
+            j2 = A::fma(bv[g][cc], ld, j2);
+          }
+          x[g] = s0;
+          j[0 * GD + g] = j0;
+          j[1 * GD + g] = j1;
+          j[2 * GD + g] = j2;
+        }
+        sf_point<F, SPLIT, TD, GD>(a, i * st + jz * sz, tile_idx, lane, x, j, F(1), xh, xl, row, K, c);
+      }
+    }
+  }
+}
+
 }  // namespace tlg
+
 
 namespace tlg {
 

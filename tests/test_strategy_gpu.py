@@ -43,11 +43,14 @@ CASES = [
     ("Quadrilateral", 2, 5, 10, 2),
     ("Quadrilateral", 4, 2, 4, 3),
     ("Quadrilateral", 3, 4, 8, 3),
+    ("Prism", 3, 1, 2, 3),
+    ("Prism", 3, 2, 4, 3),
+    ("Prism", 2, 3, 6, 3),
 ]
 
 
 def mesh_for(cell, n, degree, gd):
-    return meshes.curved_box(cell, n, degree, jitter=0.02) if cell == "Hexahedron" else quad_box(n, degree, gd)
+    return meshes.curved_box(cell, n, degree, jitter=0.02) if cell != "Quadrilateral" else quad_box(n, degree, gd)
 
 
 def factors_for(gd, td):
@@ -59,7 +62,7 @@ def factors_for(gd, td):
 @pytest.mark.parametrize("cell,n,degree,rdeg,gd", CASES)
 def test_strategies_match_the_oracle(cuda, cell, n, degree, rdeg, gd, strategy, precision):
     mesh = mesh_for(cell, n, degree, gd)
-    td = 3 if cell == "Hexahedron" else 2
+    td = 2 if cell == "Quadrilateral" else 3
     g = tg.Geometry.from_host(mesh, dtype=F32 if precision == "f32" else F64)
     pts, _ = tg.refcell.gauss_rule(cell, rdeg)
     ps = tg.PointSet(cell, pts, np.ones(len(pts)))
@@ -129,3 +132,41 @@ def test_strategy_scopes_nest_and_restore(cuda):
             assert tg.get_strategy() == "sumfact"
         assert tg.get_strategy() == "loops"
     assert tg.get_strategy() == before
+
+
+@pytest.mark.parametrize("order", ["z_slowest", "z_fastest"])
+@pytest.mark.parametrize("precision", ["f64", "split"])
+def test_prism_rules_in_both_orders(cuda, order, precision):
+    """A prism rule as triangle points times z points runs sum factorisation with z the slowest
+    or the fastest index; the values match those of the same rule under the direct strategy."""
+    mesh = meshes.curved_box("Prism", 2, 2, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=F64)
+    tri, _ = tg.refcell.gauss_rule("Triangle", 4)
+    z = np.array([0.1, 0.45, 0.8, 0.95])
+    if order == "z_slowest":
+        pts = np.array([[a, b, c] for c in z for a, b in tri])
+    else:
+        pts = np.array([[a, b, c] for a, b in tri for c in z])
+    ps = tg.PointSet("Prism", pts, np.ones(len(pts)))
+    names = ("points", "jacobian", "detj", "pinv")
+    prec = "split" if precision == "split" else "native"
+    with tg.with_strategy("sumfact"):
+        got = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+        assert tg.last_kernel_family() == "sumfact"
+    with tg.with_strategy("direct"):
+        want = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+    tol = 1e-13 if precision == "f64" else 2e-6
+    for f in names:
+        assert orc.rel_err(got[f].to_host_cell_major(), want[f].to_host_cell_major()) < tol, f
+
+
+def test_prism_without_a_product_rule(cuda):
+    """Points that are not a triangle rule times z points run another family under sumfact."""
+    mesh = meshes.curved_box("Prism", 2, 2, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=F64)
+    pts, _ = tg.refcell.gauss_rule("Prism", 4)
+    pts = pts.copy()
+    pts[0, 2] += 1e-3
+    with tg.with_strategy("sumfact"):
+        tg.geometric_factors_block(g, 0, tg.PointSet("Prism", pts, np.ones(len(pts))), ("detj",))
+        assert tg.last_kernel_family() != "sumfact"
