@@ -517,6 +517,41 @@ def extra_hex_strategies(n: int = 64, cell: str = "Hexahedron"):
     return out
 
 
+def extra_high_order(n: int = 16):
+    """Curved tetrahedra P4-P6 (6 n^3 cells, 35 / 56 / 84 nodes) at the collapsed Gauss rules of
+    degree 2p, x/J/detJ/K, under the loops (global tables), shared (staged tables) and
+    cooperative kernels and AUTO, in split precision, f64 and f32: ms per launch and the family.
+    Run with --workload high_order (not part of the default run)."""
+    import torch
+
+    import gridcl_gb300 as tg
+    from gridcl_gb300 import meshes
+
+    names = ("points", "jacobian", "detj", "pinv")
+    out = {"workload": f"curved tetrahedra P4-P6, 6x{n}^3 cells, Gauss rules of degree 2p, x/J/detJ/K"}
+    for degree in (4, 5, 6):
+        mesh = meshes.curved_box("Tetrahedron", n, degree, jitter=0.02)
+        pts, w = tg.refcell.gauss_rule("Tetrahedron", 2 * degree)
+        ps = tg.PointSet("Tetrahedron", pts, w)
+        qpts = mesh.blocks[0].num_cells * len(ps)
+        for prec, dt in (("split", torch.float64), ("native", torch.float64), ("native", torch.float32)):
+            g = tg.Geometry.from_host(mesh, dtype=dt)
+            row = {"qpoints": int(qpts)}
+            for strat in ("loops", "shared", "cooperative", "auto"):
+                with tg.with_strategy(strat):
+                    f = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+                    fam = tg.last_kernel_family()
+                    ms = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, names, out=f, precision=prec),
+                                  reps=3, warm=1)
+                row[strat] = {"family": fam, "ms": ms, "gpts_per_s": qpts / (ms * 1e-3) / 1e9}
+                del f
+            label = "split" if prec == "split" else ("f64" if dt == torch.float64 else "f32")
+            out[f"P{degree}_{label}"] = row
+            del g
+            torch.cuda.empty_cache()
+    return out
+
+
 def extra_p1_box():
     """BASELINE's CPU-runtime case: 8^3 x 6 = 3,072 P1 tetrahedra, interior nodes jittered by
     +-0.1 h, 14 points (collapsed 7 x 2 x 1), f64; GPU against the oracle on the host cores."""
@@ -718,7 +753,7 @@ def run_ours(args):
 
 
 EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "pull_back", "ordering", "p1_box",
-          "hex_strategies", "prism_strategies")
+          "hex_strategies", "prism_strategies", "high_order")
 
 
 def run_extra(args):
@@ -730,7 +765,8 @@ def run_extra(args):
           "q2_forward_adjoint": lambda: extra_adjoint(args.adjoint_n, args.fd_nodes), "pull_back": extra_pull_back,
           "ordering": extra_ordering, "p1_box": extra_p1_box,
           "hex_strategies": lambda: extra_hex_strategies(args.hex_n),
-          "prism_strategies": lambda: extra_hex_strategies(args.hex_n, "Prism")}[args.workload]
+          "prism_strategies": lambda: extra_hex_strategies(args.hex_n, "Prism"),
+          "high_order": extra_high_order}[args.workload]
     print(json.dumps(fn()), flush=True)
 
 

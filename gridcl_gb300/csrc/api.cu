@@ -19,6 +19,7 @@
 #include "eval_launch.cuh"
 #include "refcell.h"
 #include "status.h"
+#include "coop.cuh"
 #include "sumfact.cuh"
 #include "vjp.cuh"
 
@@ -136,6 +137,8 @@ int env_strategy() {
     if (s == "direct") return (int)TLG_STRATEGY_DIRECT;
     if (s == "loops") return (int)TLG_STRATEGY_LOOPS;
     if (s == "sumfact") return (int)TLG_STRATEGY_SUMFACT;
+    if (s == "shared") return (int)TLG_STRATEGY_SHARED;
+    if (s == "cooperative") return (int)TLG_STRATEGY_COOPERATIVE;
     return (int)TLG_STRATEGY_AUTO;
   }();
   return v;
@@ -154,6 +157,10 @@ int current_strategy() {
 // always in f64, and in f32 and split precision above the degrees with paired kernels
 // (quadrilaterals and hexahedra Q1-Q2).
 bool sumfact_preferred(const tlg_tables* t) { return t->sf_ok && (t->dtype == TLG_F64 || t->sf_n >= 4); }
+
+// The policy of TLG_STRATEGY_AUTO beyond the compiled unrolled kernels (more than 27 nodes per
+// cell): the cooperative kernel instead of the loops kernel.
+bool coop_preferred(const tlg_tables* t) { return t->k > 27; }
 
 // The sum-factorised kernel; `found` is false when it does not apply (no tensor structure, facet
 // normals, split precision at a tile other than 16, or no instantiation): nothing is launched.
@@ -259,7 +266,7 @@ void fill_pair_args(const tlg_tables* t, const tlg_block* b, const tlg_outputs* 
 }
 
 tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
-                      cudaStream_t stream, bool loops_only) {
+                      cudaStream_t stream, bool loops_only, bool global_tables) {
   if (o->tile != 16)
     return fail(TLG_ERR_UNSUPPORTED, "tlg_eval_block: split precision runs with tile 16, not " +
                                          std::to_string(o->tile));
@@ -270,15 +277,16 @@ tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs
   tlg::PairArgs a;
   std::memset(&a, 0, sizeof(a));
   fill_pair_args(t, b, o, mask, &a);
-  cudaError_t e = tlg::launch_split_loops(t->td, t->gd, !t->staged, a, t->bytes, stream);
+  const bool global = global_tables || !t->staged;
+  cudaError_t e = tlg::launch_split_loops(t->td, t->gd, global, a, t->bytes, stream);
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
-  g_last_family = TLG_STRATEGY_LOOPS;
+  g_last_family = global ? TLG_STRATEGY_LOOPS : TLG_STRATEGY_SHARED;
   return ok();
 }
 
 template <typename F>
 tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
-                      cudaStream_t stream, bool loops_only) {
+                      cudaStream_t stream, bool loops_only, bool global_tables) {
   tlg::EvalArgs<F> a;
   std::memset(&a, 0, sizeof(a));
   a.nodes = static_cast<const F*>(b->nodes);
@@ -304,7 +312,7 @@ tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs
   a.num_points = (int)t->q;
   a.tile_shift = shift;
   a.k_runtime = (int)t->k;
-  a.tab_global = t->staged ? 0 : 1;
+  a.tab_global = t->staged && !global_tables ? 0 : 1;
   a.loops_only = loops_only ? 1 : 0;
   bool direct = false;
   cudaError_t e;
@@ -318,7 +326,48 @@ tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs
     e = tlg::launch_eval_f64(t->td, t->gd, (int)t->k, a, t->bytes, stream, &direct);
   }
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
-  g_last_family = direct ? TLG_STRATEGY_DIRECT : TLG_STRATEGY_LOOPS;
+  g_last_family = direct ? TLG_STRATEGY_DIRECT : a.tab_global ? TLG_STRATEGY_LOOPS : TLG_STRATEGY_SHARED;
+  return ok();
+}
+
+// The cooperative kernel; `found` is false where it does not apply (nothing launched).
+tlg_status eval_coop(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                     cudaStream_t stream, bool* found) {
+  *found = false;
+  if (t->td < 2 || t->k > 128 || (t->dtype == TLG_F64 && t->k > 64)) return TLG_ERR_UNSUPPORTED;
+  tlg::CoopArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = b->nodes;
+  a.dofmap = b->dofmap;
+  a.flags = b->flags;
+  a.tab = t->dev;
+  void* outs[6] = {o->points, o->jacobian, o->detj, o->pinv, o->normals, o->facet_normals};
+  for (int i = 0; i < 6; ++i) a.out[i] = outs[i];
+  a.err = t->err;
+  a.recomputed = t->dtype == TLG_SPLIT32 ? o->recomputed : nullptr;
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + o->tile - 1) / o->tile * o->tile;
+  a.range_cells = o->num_cells;
+  a.out_first_cell = o->out_first_cell;
+  a.last_cell = b->num_cells - 1;
+  const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
+  a.last_flag = nflags - 1;
+  for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
+  a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 256.0f;
+  a.last_node = (uint32_t)(b->num_nodes - 1);
+  a.tab_bytes = t->bytes;
+  a.off_dphi = t->off_dphi;
+  a.off_refn = t->off_refn;
+  a.off_dphi64 = t->off_dphi64;
+  a.mask = mask;
+  a.num_points = (int)t->q;
+  a.k = (int)t->k;
+  a.tile_shift = tile_shift(o->tile);
+  a.tab_global = t->staged ? 0 : 1;
+  cudaError_t e = tlg::launch_coop(t->dtype, t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
+  if (!*found) return TLG_ERR_UNSUPPORTED;
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  g_last_family = TLG_STRATEGY_COOPERATIVE;
   return ok();
 }
 
@@ -794,15 +843,21 @@ tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_out
     tlg_status st = eval_sumfact(t, b, o, mask, s, &found);
     if (found) return st;
   }
-  const bool loops_only = strategy == TLG_STRATEGY_LOOPS;
-  if (t->dtype == TLG_SPLIT32) return eval_split(t, b, o, mask, s, loops_only);
-  if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, s, loops_only);
-  return eval_typed<double>(t, b, o, mask, s, loops_only);
+  if (strategy == TLG_STRATEGY_COOPERATIVE || (strategy == TLG_STRATEGY_AUTO && coop_preferred(t))) {
+    bool found = false;
+    tlg_status st = eval_coop(t, b, o, mask, s, &found);
+    if (found) return st;
+  }
+  const bool loops_only = strategy == TLG_STRATEGY_LOOPS || strategy == TLG_STRATEGY_SHARED;
+  const bool global_tables = strategy == TLG_STRATEGY_LOOPS;
+  if (t->dtype == TLG_SPLIT32) return eval_split(t, b, o, mask, s, loops_only, global_tables);
+  if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, s, loops_only, global_tables);
+  return eval_typed<double>(t, b, o, mask, s, loops_only, global_tables);
 }
 
 tlg_status tlg_set_strategy(int strategy) {
-  if (strategy < -1 || strategy > TLG_STRATEGY_SUMFACT)
-    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_strategy: strategy must be -1 .. 3");
+  if (strategy < -1 || strategy > TLG_STRATEGY_COOPERATIVE)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_strategy: strategy must be -1 .. 5");
   g_strategy.store(strategy, std::memory_order_relaxed);
   return ok();
 }

@@ -85,6 +85,12 @@ cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t sme
 cudaError_t launch_sumfact(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
                            bool* found);
 
+struct CoopArgs;
+// Defined in coop.cu: the cooperative kernel (four lanes per cell) for precision 4, 8 or 12, cells of
+// 2 or 3 dimensions and at most 128 nodes; `found` is false otherwise.
+cudaError_t launch_coop(int precision, int td, int gd, int k, const CoopArgs& a, size_t smem, cudaStream_t s,
+                        bool* found);
+
 struct VjpArgs;
 // Defined in vjp_f64.cu / vjp_split.cu; `found` is false when no kernel exists for (d, k). `smem`
 // is the dynamic shared memory: the staged tables (rounded up to 16 bytes) and the staging slots.

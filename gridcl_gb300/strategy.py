@@ -1,8 +1,11 @@
-"""Evaluation strategies (tetraloma-geometry/src/strategy.rs:373-407): which kernel family
+"""Evaluation strategies (tetraloma-geometry/src/strategy.rs:23-34, 373-407): which kernel family
 evaluates a block. Precedence as in the reference: a scoped setting (:func:`with_strategy`),
-then the environment variable ``TLG_GEOM_STRATEGY``, then the built-in policy ("auto": paired or
-unrolled kernels where compiled, sum factorisation for quadrilaterals and hexahedra at
-tensor-product rules above those degrees, loops otherwise)."""
+then the environment variable ``TLG_GEOM_STRATEGY``, then the built-in policy ("auto": sum
+factorisation for quadrilaterals, hexahedra and prisms at tensor-product rules in f64 and above
+the degrees with paired kernels, else the paired or unrolled kernels where compiled, the
+cooperative kernel above 27 nodes per cell, loops otherwise). "loops" reads the tables from
+global memory, "shared" stages them in shared memory, "cooperative" splits each cell's node
+sums over four lanes."""
 
 from __future__ import annotations
 
@@ -10,7 +13,7 @@ import contextlib
 
 from ._lib import check, lib
 
-STRATEGIES = {"auto": 0, "direct": 1, "loops": 2, "sumfact": 3}
+STRATEGIES = {"auto": 0, "direct": 1, "loops": 2, "sumfact": 3, "shared": 4, "cooperative": 5}
 _NAMES = {v: k for k, v in STRATEGIES.items()}
 _stack: list = []
 
@@ -26,7 +29,8 @@ def get_strategy() -> str:
 
 
 def last_kernel_family() -> str | None:
-    """The kernel family of this thread's last evaluation launch ("direct", "loops", "sumfact")."""
+    """The kernel family of this thread's last evaluation launch ("direct", "loops", "sumfact",
+    "shared", "cooperative")."""
     return _NAMES.get(lib().tlg_last_kernel_family()) if lib().tlg_last_kernel_family() else None
 
 

@@ -287,23 +287,33 @@ uint32_t tlg_quantise(double x, double lo, double hi);
 
 /* Evaluation strategy (the reference's strategy::choose, tetraloma-geometry/src/strategy.rs:
  * 373-407, with its precedence: a scoped setting, then the environment, then the built-in
- * policy). AUTO picks per element: for quadrilaterals and hexahedra at tensor-product point sets,
- * sum factorisation in f64 and above the degrees with paired kernels (Q1-Q2) in f32 and split
- * precision; otherwise the paired / unrolled kernels where compiled, the loops kernels else. DIRECT, LOOPS and SUMFACT force a kernel family where it
- * applies (sum factorisation needs a quadrilateral or hexahedron at a tensor-product point set,
- * no facet normals, and tile 16 in split precision; elsewhere the AUTO choice runs). The environment variable TLG_GEOM_STRATEGY (auto, direct, loops, sumfact) is read once;
- * tlg_set_strategy overrides it for the process until called with -1. */
+ * policy; the five strategies of strategy.rs:23-34). AUTO picks per element: for quadrilaterals,
+ * hexahedra and prisms at tensor-product point sets, sum factorisation in f64 and above the
+ * degrees with paired kernels (Q1-Q2, P1-P2) in f32 and split precision; otherwise the paired /
+ * unrolled kernels where compiled, the cooperative kernel for cells of more than 27 nodes, the
+ * loops kernels else. The others force a kernel family where it applies, and otherwise the
+ * AUTO choice runs:
+ *  - DIRECT: the paired / unrolled kernels (compiled elements, tile 16 for f32 and split);
+ *  - LOOPS: K at run time, tables read from global memory;
+ *  - SUMFACT: a quadrilateral, hexahedron or prism at a tensor-product point set, no facet
+ *    normals, tile 16 in split precision;
+ *  - SHARED: the loops kernels with the tables staged in shared memory (where they fit);
+ *  - COOPERATIVE: four lanes per cell (cells of 2 or 3 dimensions, up to 128 nodes, 64 in f64).
+ * The environment variable TLG_GEOM_STRATEGY (auto, direct, loops, sumfact, shared,
+ * cooperative) is read once; tlg_set_strategy overrides it for the process until called with -1. */
 typedef enum tlg_strategy {
   TLG_STRATEGY_AUTO = 0,
   TLG_STRATEGY_DIRECT = 1,
   TLG_STRATEGY_LOOPS = 2,
-  TLG_STRATEGY_SUMFACT = 3
+  TLG_STRATEGY_SUMFACT = 3,
+  TLG_STRATEGY_SHARED = 4,
+  TLG_STRATEGY_COOPERATIVE = 5
 } tlg_strategy;
 tlg_status tlg_set_strategy(int strategy);
 /* The strategy in effect (TLG_STRATEGY_*). */
 int tlg_get_strategy(void);
-/* The kernel family that ran in this thread's last launching tlg_eval_block: DIRECT (paired or
- * unrolled), LOOPS or SUMFACT; 0 before any (the reference's record_strategies test hook,
+/* The kernel family that ran in this thread's last launching tlg_eval_block (or tlg_vjp_block):
+ * DIRECT (paired or unrolled), LOOPS, SUMFACT, SHARED or COOPERATIVE; 0 before any (the reference's record_strategies test hook,
  * tetraloma-geometry/src/testing.rs:34-43). */
 int tlg_last_kernel_family(void);
 

@@ -58,7 +58,7 @@ def factors_for(gd, td):
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32", "split"])
-@pytest.mark.parametrize("strategy", ["direct", "loops", "sumfact"])
+@pytest.mark.parametrize("strategy", ["direct", "loops", "sumfact", "shared", "cooperative"])
 @pytest.mark.parametrize("cell,n,degree,rdeg,gd", CASES)
 def test_strategies_match_the_oracle(cuda, cell, n, degree, rdeg, gd, strategy, precision):
     mesh = mesh_for(cell, n, degree, gd)
@@ -70,12 +70,12 @@ def test_strategies_match_the_oracle(cuda, cell, n, degree, rdeg, gd, strategy, 
     with tg.with_strategy(strategy):
         got = tg.geometric_factors_block(g, 0, ps, names, precision="split" if precision == "split" else "native")
         family = tg.last_kernel_family()
-    if strategy == "sumfact":
-        assert family == "sumfact"
-    elif strategy == "loops":
-        assert family == "loops"
-    else:
-        assert family in ("direct", "loops")
+    if strategy in ("sumfact", "loops", "cooperative"):
+        assert family == strategy
+    elif strategy == "shared":  # tables beyond the shared-memory budget stay in global memory
+        assert family in ("shared", "loops")
+    else:  # where no unrolled kernel applies, the loops kernel over staged tables runs
+        assert family in ("direct", "loops", "shared")
     absx = g.nodes.double().cpu().numpy() + np.array(g.origin[:gd])
     want = orc.eval_block(cell, degree, absx, mesh.blocks[0].cells, pts, factors=[KEYS[f] for f in names])
     base = orc.TOL_F64 if precision == "f64" else orc.TOL_F32
@@ -170,3 +170,118 @@ def test_prism_without_a_product_rule(cuda):
     with tg.with_strategy("sumfact"):
         tg.geometric_factors_block(g, 0, tg.PointSet("Prism", pts, np.ones(len(pts))), ("detj",))
         assert tg.last_kernel_family() != "sumfact"
+
+
+HIGH = [
+    # (cell, n, degree, rule degree, gdim): beyond the unrolled kernels
+    ("Tetrahedron", 2, 4, 5, 3),
+    ("Tetrahedron", 1, 5, 6, 3),
+    ("Triangle", 3, 6, 8, 2),
+    ("Triangle", 0, 5, 6, 3),
+    ("Quadrilateral", 2, 6, 8, 2),
+    ("Hexahedron", 2, 3, 5, 3),
+]
+
+
+def high_mesh(cell, n, degree, gd):
+    if cell == "Triangle" and gd == 3:
+        return meshes.perturbed_radius(meshes.sphere(1, degree), 0.02)
+    if cell in ("Triangle", "Quadrilateral"):
+        m = meshes.square_box(cell, n, degree)
+        m.nodes = meshes.jitter_interior(m.nodes, m.nodes, 0.02 / n, 2026)
+        return m
+    return meshes.curved_box(cell, n, degree, jitter=0.02)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32", "split"])
+@pytest.mark.parametrize("strategy", ["auto", "loops", "shared", "cooperative"])
+@pytest.mark.parametrize("cell,n,degree,rdeg,gd", HIGH)
+def test_high_degree_strategies(cuda, cell, n, degree, rdeg, gd, strategy, precision):
+    """Cells of 21 to 64 nodes under the loops, shared and cooperative kernels (and AUTO, which
+    picks the cooperative kernel above 27 nodes) against the oracle; a non-tensor rule (the
+    collapsed Gauss rule of a hexahedron, shuffled) keeps sum factorisation out."""
+    mesh = high_mesh(cell, n, degree, gd)
+    td = refcell_tdim(cell)
+    g = tg.Geometry.from_host(mesh, dtype=F32 if precision == "f32" else F64)
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    pts = pts[np.random.default_rng(1).permutation(len(pts))]
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    names = factors_for(gd, td)
+    with tg.with_strategy(strategy):
+        got = tg.geometric_factors_block(g, 0, ps, names, precision="split" if precision == "split" else "native")
+        family = tg.last_kernel_family()
+    k = mesh.blocks[0].cells.shape[1]
+    if strategy == "auto":
+        assert family in (("cooperative",) if k > 27 else ("loops", "shared"))
+    elif strategy == "shared":  # tables beyond the shared-memory budget stay in global memory
+        assert family in ("shared", "loops")
+    else:
+        assert family == strategy
+    absx = g.nodes.double().cpu().numpy() + np.array(g.origin[:gd])
+    want = orc.eval_block(cell, degree, absx, mesh.blocks[0].cells, pts, factors=[KEYS[f] for f in names])
+    base = orc.TOL_F64 if precision == "f64" else orc.TOL_F32
+    nodes = orc.node_ratio(cell, degree)
+    s_val = orc.tolerance_scale(cell, degree, "Equispaced", pts, "values") * nodes
+    s_der = orc.tolerance_scale(cell, degree, "Equispaced", pts) * nodes
+    if precision == "f32":
+        ratio = orc.origin_ratio(absx, np.array(g.origin[:gd]), want["j"])
+        s_val, s_der = s_val * ratio, s_der * ratio
+    cond = orc.condition_scale(want["j"], td, gd)
+    scale = {"points": s_val, "jacobian": s_der, "detj": s_der, "pinv": s_der * cond, "normals": s_der * cond}
+    for f in names:
+        err = orc.rel_err(got[f].to_host_cell_major(), want[KEYS[f]])
+        assert err < base * scale[f], (f, err, base * scale[f])
+
+
+def refcell_tdim(cell):
+    return tg.refcell.tdim(cell)
+
+
+@pytest.mark.parametrize("tile", [1, 2, 4, 8, 16])
+def test_cooperative_tiles_and_ranges(cuda, tile):
+    """The cooperative kernel at every output tile and on a cell range that starts mid-block
+    (ragged last warp run): the same values as the loops kernel."""
+    mesh = meshes.curved_box("Tetrahedron", 2, 4, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=F64)
+    pts, _ = tg.refcell.gauss_rule("Tetrahedron", 5)
+    ps = tg.PointSet("Tetrahedron", pts, np.ones(len(pts)))
+    names = ("points", "jacobian", "detj", "pinv")
+    with tg.with_strategy("cooperative"):
+        got = tg.geometric_factors_block(g, 0, ps, names, tile=tile, max_chunk_cells=37)
+        assert tg.last_kernel_family() == "cooperative"
+    with tg.with_strategy("loops"):
+        want = tg.geometric_factors_block(g, 0, ps, names, tile=tile, max_chunk_cells=37)
+    for f in names:
+        assert orc.rel_err(got[f].to_host_cell_major(), want[f].to_host_cell_major()) < 1e-14, f
+
+
+@pytest.mark.parametrize("dtype", [F64, F32])
+def test_cooperative_facet_normals(cuda, dtype):
+    mesh = meshes.curved_box("Tetrahedron", 2, 4, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=dtype)
+    ps = tg.facet_point_set("Tetrahedron", 4)
+    with tg.with_strategy("cooperative"):
+        got = tg.facet_normals_block(g, 0, ps).to_host_cell_major()
+        assert tg.last_kernel_family() == "cooperative"
+    with tg.with_strategy("loops"):
+        want = tg.facet_normals_block(g, 0, ps).to_host_cell_major()
+    assert orc.rel_err(got, want) < (1e-13 if dtype == F64 else 1e-5)
+
+
+def test_cooperative_split_recomputes(cuda):
+    """Split precision under the cooperative kernel counts the FP64 recomputes of points above the
+    condition limit as the loops kernel does (up to points whose estimate rounds across the limit
+    in the two summation orders)."""
+    mesh = meshes.curved_box("Tetrahedron", 2, 4, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=F64)
+    pts, _ = tg.refcell.gauss_rule("Tetrahedron", 5)
+    ps = tg.PointSet("Tetrahedron", pts, np.ones(len(pts)))
+    counts = {}
+    for strat in ("cooperative", "loops"):
+        rec = torch.zeros(1, dtype=torch.int64, device="cuda")
+        with tg.with_strategy(strat):
+            tg.geometric_factors_block(g, 0, ps, ("detj", "pinv"), precision="split", cond_limit=1.5,
+                                       recomputed=rec)
+        counts[strat] = int(rec.item())
+    assert counts["loops"] > 0
+    assert abs(counts["cooperative"] - counts["loops"]) <= max(2, counts["loops"] // 100)
