@@ -66,6 +66,7 @@ def parse():
     p.add_argument("--adjoint-n", type=int, default=128, help="Q2 hexahedra per direction (adjoint)")
     p.add_argument("--fd-nodes", type=int, default=1000, help="nodes of the adjoint's central-difference check")
     p.add_argument("--hex-n", type=int, default=64, help="hexahedra per direction (hex_strategies)")
+    p.add_argument("--ho-n", type=int, default=16, help="subcells per direction (high_order)")
     return p.parse_args()
 
 
@@ -766,7 +767,7 @@ def run_extra(args):
           "ordering": extra_ordering, "p1_box": extra_p1_box,
           "hex_strategies": lambda: extra_hex_strategies(args.hex_n),
           "prism_strategies": lambda: extra_hex_strategies(args.hex_n, "Prism"),
-          "high_order": extra_high_order}[args.workload]
+          "high_order": lambda: extra_high_order(args.ho_n)}[args.workload]
     print(json.dumps(fn()), flush=True)
 
 

@@ -355,7 +355,12 @@ tlg_status eval_coop(const tlg_tables* t, const tlg_block* b, const tlg_outputs*
   for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
   a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 256.0f;
   a.last_node = (uint32_t)(b->num_nodes - 1);
-  a.tab_bytes = t->bytes;
+  // Only phi, dphi and the reference normals are staged (the FP64 recompute's table stays in
+  // global memory), and only up to a third of the shared memory, so that three CTAs fit an SM.
+  const size_t es = t->dtype == TLG_F64 ? 8 : 4;
+  const size_t prefix = (t->off_refn + (size_t)t->q * t->td * es + 15) / 16 * 16;
+  const bool stage = prefix <= (size_t)75 * 1024;
+  a.tab_bytes = stage ? (uint32_t)prefix : 0;
   a.off_dphi = t->off_dphi;
   a.off_refn = t->off_refn;
   a.off_dphi64 = t->off_dphi64;
@@ -363,8 +368,8 @@ tlg_status eval_coop(const tlg_tables* t, const tlg_block* b, const tlg_outputs*
   a.num_points = (int)t->q;
   a.k = (int)t->k;
   a.tile_shift = tile_shift(o->tile);
-  a.tab_global = t->staged ? 0 : 1;
-  cudaError_t e = tlg::launch_coop(t->dtype, t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
+  a.tab_global = stage ? 0 : 1;
+  cudaError_t e = tlg::launch_coop(t->dtype, t->td, t->gd, (int)t->k, a, stage ? prefix : 0, stream, found);
   if (!*found) return TLG_ERR_UNSUPPORTED;
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
   g_last_family = TLG_STRATEGY_COOPERATIVE;

@@ -9,8 +9,8 @@
 // group (two butterfly steps, lanes 2 apart then 1 apart) leaves lane p with the complete sums of
 // point p of the group, (s0 + s2) + (s1 + s3) over the lanes' partials, and lane p runs that
 // point's epilogue (det J, K, normals, facet normals, the stores; in split precision the condition
-// estimate and the FP64 recompute). The tables are read from shared memory where they fit, else
-// from global memory.
+// estimate and the FP64 recompute). phi, dphi and the reference normals are read from shared
+// memory where they take at most a third of it, else from global memory (L1-cached).
 //
 // Compared with the loops kernel (one cell per thread, each node's coordinates gathered again at
 // every point) the coordinates are gathered once, and a lane keeps K / 4 of them instead of K.
@@ -28,7 +28,8 @@ struct CoopArgs {
   const uint32_t* dofmap;
   const uint32_t* flags;
   const unsigned char* tab;  // phi [Q][K] at 0, dphi [Q][K][TD] at off_dphi, refn [Q][TD] at off_refn
-                             // (the arithmetic's type); split: the f64 dphi [Q][K][TD] at off_dphi64
+                             // (the arithmetic's type; the first tab_bytes staged unless tab_global);
+                             // split: the f64 dphi [Q][K][TD] at off_dphi64, read from global memory
   void* out[6];              // points, jacobian, detj, pinv, normals, facet normals
   int* err;
   unsigned long long* recomputed;
@@ -178,7 +179,7 @@ __global__ void __launch_bounds__(kEvalThreads) coop_kernel(const __grid_constan
         if (!(kap <= a.cond_limit) && (mask & (kOutJacobian | kOutDetJ | kOutPinv))) {
           float jr[LJ], kr[LJ], dr;
           recompute_f64_rt<TD, GD>(static_cast<const double*>(a.nodes), row, K, a.last_node,
-                                   reinterpret_cast<const double*>(tabs + a.off_dphi64) + (int64_t)q * K * TD,
+                                   reinterpret_cast<const double*>(a.tab + a.off_dphi64) + (int64_t)q * K * TD,
                                    jr, &dr, kr, 1);
 #pragma unroll
           for (int i = 0; i < LJ; ++i) {
