@@ -31,7 +31,8 @@ from .geometry import (
     pull_back_block,
     vjp_block,
 )
-from .strategy import get_strategy, last_kernel_family, set_strategy, with_strategy
+from .strategy import (get_strategy, last_kernel_family, last_launch_family, record_strategies, set_strategy,
+                       with_strategy)
 from . import meshes, refcell
 
 __all__ = [
@@ -39,5 +40,6 @@ __all__ = [
     "QuadRule", "detj_block", "facet_normals_block", "facet_point_set", "fd_check",
     "geometric_factors_block", "jacobians_block", "lib", "measure_block", "meshes", "normals_block",
     "node_incidence", "physical_points_block", "pseudo_inverse_block", "pull_back_block", "refcell", "vjp_block",
-    "get_strategy", "last_kernel_family", "set_strategy", "with_strategy",
+    "get_strategy", "last_kernel_family", "last_launch_family", "record_strategies", "set_strategy",
+    "with_strategy",
 ]

@@ -109,8 +109,12 @@ SIGNATURES = [
     ("tlg_measure_static_max_cells", _L, []),
     ("tlg_selftest_conversions", _I, [_P, _L, _P, _P]),
     ("tlg_set_strategy", _I, [_I]),
+    ("tlg_set_family_strategy", _I, [_I, _I]),
+    ("tlg_get_family_override", _I, [_I]),
+    ("tlg_get_family_strategy", _I, [_I, ctypes.POINTER(ctypes.c_int)]),
     ("tlg_get_strategy", _I, []),
     ("tlg_last_kernel_family", _I, []),
+    ("tlg_last_launch_family", _I, []),
     ("tlg_order_cells", _I, [_I, _I, _P, _L, _I, _P, _L, _I, _P]),
     ("tlg_number_nodes", _I, [_P, _L, _I, _L, _P, _P]),
     ("tlg_hilbert_key", ctypes.c_uint64, [_P, _I, _I]),

@@ -2,6 +2,7 @@
 // tables, and the launches of the evaluation and E-vector kernels.
 #include <algorithm>
 #include <atomic>
+#include <cctype>
 #include <cmath>
 #include <cstdlib>
 #include <cstdio>
@@ -124,29 +125,108 @@ void narrow_into(std::vector<unsigned char>& buf, size_t off, const double* src,
 
 // The paired-FP32 kernel: an f32 mesh (split = false) or split precision (split = true).
 // `found` is false when no paired kernel exists for the element (nothing launched).
-// Evaluation strategy: tlg_set_strategy's setting (-1: none), else TLG_GEOM_STRATEGY, else auto.
-std::atomic<int> g_strategy{-1};
-// The kernel family of the last launch of tlg_eval_block on this thread (TLG_STRATEGY_*, 0: none).
+// Strategies per kernel family (tetraloma-geometry/src/strategy.rs:311-407): this thread's
+// override (tlg_set_family_strategy, tlg_set_strategy), else TLG_GEOM_STRATEGY, else the policy
+// (TLG_STRATEGY_AUTO). -1: no override.
+constexpr int kFamilies = 6;
+thread_local int g_override[kFamilies] = {-1, -1, -1, -1, -1, -1};
+// The strategy that ran in this thread's last launch (TLG_STRATEGY_*, 0: none) and its family.
 thread_local int g_last_family = 0;
+thread_local int g_last_kind = -1;
 
-int env_strategy() {
-  static const int v = [] {
+const char* const kFamilyNames[kFamilies] = {"EVector", "Points", "Jacobian", "Normals", "FacetNormals", "PullBack"};
+
+// A strategy name of the environment variable: policy (or auto), direct, loops, sumfact, shared,
+// cooperative; -1 for anything else.
+int strategy_named(std::string n) {
+  while (!n.empty() && n.front() == ' ') n.erase(n.begin());
+  while (!n.empty() && n.back() == ' ') n.pop_back();
+  const char* names[] = {"policy", "direct", "loops", "sumfact", "shared", "cooperative"};
+  for (int i = 0; i < 6; ++i)
+    if (n == names[i]) return i;
+  if (n == "auto") return TLG_STRATEGY_AUTO;
+  return -1;
+}
+
+struct EnvStrategies {
+  int s[kFamilies] = {-1, -1, -1, -1, -1, -1};
+  std::string error;  // non-empty: the variable is invalid (every launch then fails)
+};
+
+// TLG_GEOM_STRATEGY, read once: one strategy name for every family, or a comma list of
+// <family>=<strategy> (families EVector, Points, Jacobian, Normals, FacetNormals, PullBack, in any
+// case), each family at most once (strategy.rs:311-337).
+const EnvStrategies& env_strategies() {
+  static const EnvStrategies v = [] {
+    EnvStrategies r;
     const char* e = std::getenv("TLG_GEOM_STRATEGY");
-    if (!e) return (int)TLG_STRATEGY_AUTO;
-    const std::string s(e);
-    if (s == "direct") return (int)TLG_STRATEGY_DIRECT;
-    if (s == "loops") return (int)TLG_STRATEGY_LOOPS;
-    if (s == "sumfact") return (int)TLG_STRATEGY_SUMFACT;
-    if (s == "shared") return (int)TLG_STRATEGY_SHARED;
-    if (s == "cooperative") return (int)TLG_STRATEGY_COOPERATIVE;
-    return (int)TLG_STRATEGY_AUTO;
+    if (!e || !*e) return r;
+    const std::string val(e);
+    const std::string invalid = "TLG_GEOM_STRATEGY=" + val +
+                                ": expected policy, direct, loops, sumfact, shared or cooperative, or a comma "
+                                "list of <family>=<strategy> with the families EVector, Points, Jacobian, "
+                                "Normals, FacetNormals and PullBack";
+    const int one = strategy_named(val);
+    if (one >= 0) {
+      for (int& x : r.s) x = one;
+      return r;
+    }
+    size_t pos = 0;
+    while (pos <= val.size()) {
+      size_t comma = val.find(',', pos);
+      if (comma == std::string::npos) comma = val.size();
+      const std::string item = val.substr(pos, comma - pos);
+      const size_t eq = item.find('=');
+      int fam = -1;
+      if (eq != std::string::npos) {
+        std::string f = item.substr(0, eq);
+        while (!f.empty() && f.front() == ' ') f.erase(f.begin());
+        while (!f.empty() && f.back() == ' ') f.pop_back();
+        for (int i = 0; i < kFamilies; ++i) {
+          const std::string n = kFamilyNames[i];
+          bool same = n.size() == f.size();
+          for (size_t c = 0; same && c < n.size(); ++c) same = std::tolower((unsigned char)n[c]) == std::tolower((unsigned char)f[c]);
+          if (same) fam = i;
+        }
+      }
+      const int st = eq == std::string::npos ? -1 : strategy_named(item.substr(eq + 1));
+      if (fam < 0 || st < 0) {
+        r.error = invalid;
+        return r;
+      }
+      if (r.s[fam] >= 0) {
+        r.error = invalid + ": " + kFamilyNames[fam] + " given twice";
+        return r;
+      }
+      r.s[fam] = st;
+      pos = comma + 1;
+    }
+    return r;
   }();
   return v;
 }
 
-int current_strategy() {
-  const int s = g_strategy.load(std::memory_order_relaxed);
-  return s >= 0 ? s : env_strategy();
+// The strategy wanted for a family (override, environment, policy); false with the error set when
+// the environment variable is invalid.
+bool wanted_strategy(int family, int* out) {
+  const EnvStrategies& env = env_strategies();
+  if (!env.error.empty()) {
+    fail(TLG_ERR_INVALID_ARGUMENT, env.error);
+    return false;
+  }
+  if (g_override[family] >= 0) *out = g_override[family];
+  else if (env.s[family] >= 0) *out = env.s[family];
+  else *out = TLG_STRATEGY_AUTO;
+  return true;
+}
+
+// The family whose strategy decides a fused launch: J, det J and K are the Jacobian family; else
+// normals, facet normals, points, in that order.
+int principal_family(uint32_t mask) {
+  if (mask & (tlg::kOutJacobian | tlg::kOutDetJ | tlg::kOutPinv)) return TLG_FAMILY_JACOBIAN;
+  if (mask & tlg::kOutNormals) return TLG_FAMILY_NORMALS;
+  if (mask & tlg::kOutFacetNormals) return TLG_FAMILY_FACET_NORMALS;
+  return TLG_FAMILY_POINTS;
 }
 
 // The policy of TLG_STRATEGY_AUTO for tables with sum-factorisation data, from GB300 timings of
@@ -266,12 +346,12 @@ void fill_pair_args(const tlg_tables* t, const tlg_block* b, const tlg_outputs* 
 }
 
 tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
-                      cudaStream_t stream, bool loops_only, bool global_tables) {
+                      cudaStream_t stream, bool allow_direct, bool global_tables) {
   if (o->tile != 16)
     return fail(TLG_ERR_UNSUPPORTED, "tlg_eval_block: split precision runs with tile 16, not " +
                                          std::to_string(o->tile));
   bool found = false;
-  tlg_status st = loops_only ? TLG_ERR_UNSUPPORTED : eval_pair(t, b, o, mask, true, stream, &found);
+  tlg_status st = allow_direct ? eval_pair(t, b, o, mask, true, stream, &found) : TLG_ERR_UNSUPPORTED;
   if (found) return st;
   // No paired kernel for this element, or tables beyond the shared-memory budget.
   tlg::PairArgs a;
@@ -286,7 +366,7 @@ tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs
 
 template <typename F>
 tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
-                      cudaStream_t stream, bool loops_only, bool global_tables) {
+                      cudaStream_t stream, bool allow_direct, bool global_tables) {
   tlg::EvalArgs<F> a;
   std::memset(&a, 0, sizeof(a));
   a.nodes = static_cast<const F*>(b->nodes);
@@ -312,12 +392,14 @@ tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs
   a.num_points = (int)t->q;
   a.tile_shift = shift;
   a.k_runtime = (int)t->k;
+  // The unrolled kernels read staged tables; the loops kernel reads them staged or from global
+  // memory.
   a.tab_global = t->staged && !global_tables ? 0 : 1;
-  a.loops_only = loops_only ? 1 : 0;
+  a.loops_only = allow_direct && t->staged ? 0 : 1;
   bool direct = false;
   cudaError_t e;
   if constexpr (sizeof(F) == 4) {
-    if (shift == 4 && !loops_only) {  // the GPU tile: the paired-FP32 kernel, when compiled
+    if (shift == 4 && allow_direct) {  // the GPU tile: the paired-FP32 kernel, when compiled
       tlg_status st = eval_pair(t, b, o, mask, false, stream, &direct);
       if (direct) return st;
     }
@@ -377,6 +459,20 @@ tlg_status eval_coop(const tlg_tables* t, const tlg_block* b, const tlg_outputs*
 }
 
 }  // namespace
+
+namespace tlg {
+
+bool check_strategy(int family) {
+  int s = 0;
+  return wanted_strategy(family, &s);
+}
+
+void record_launch(int family, int strategy) {
+  g_last_kind = family;
+  g_last_family = strategy;
+}
+
+}  // namespace tlg
 
 extern "C" {
 
@@ -842,34 +938,63 @@ tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_out
   if (b->num_nodes > (int64_t)UINT32_MAX + 1 || b->num_cells > (int64_t)UINT32_MAX)
     return fail(TLG_ERR_TOO_LARGE, "tlg_eval_block: node or cell count does not fit u32");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int strategy = current_strategy();
-  if (strategy == TLG_STRATEGY_SUMFACT || (strategy == TLG_STRATEGY_AUTO && sumfact_preferred(t))) {
+  const int family = principal_family(mask);
+  int strategy = TLG_STRATEGY_AUTO;
+  if (!wanted_strategy(family, &strategy)) return TLG_ERR_INVALID_ARGUMENT;
+  g_last_kind = family;
+  // A forced strategy that does not apply runs the loops kernel (strategy.rs:400-404); AUTO
+  // falls through to the unrolled kernels, then the loops kernel over staged tables.
+  const bool is_auto = strategy == TLG_STRATEGY_AUTO;
+  if (strategy == TLG_STRATEGY_SUMFACT || (is_auto && sumfact_preferred(t))) {
     bool found = false;
     tlg_status st = eval_sumfact(t, b, o, mask, s, &found);
     if (found) return st;
   }
-  if (strategy == TLG_STRATEGY_COOPERATIVE || (strategy == TLG_STRATEGY_AUTO && coop_preferred(t))) {
+  if (strategy == TLG_STRATEGY_COOPERATIVE || (is_auto && coop_preferred(t))) {
     bool found = false;
     tlg_status st = eval_coop(t, b, o, mask, s, &found);
     if (found) return st;
   }
-  const bool loops_only = strategy == TLG_STRATEGY_LOOPS || strategy == TLG_STRATEGY_SHARED;
-  const bool global_tables = strategy == TLG_STRATEGY_LOOPS;
-  if (t->dtype == TLG_SPLIT32) return eval_split(t, b, o, mask, s, loops_only, global_tables);
-  if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, s, loops_only, global_tables);
-  return eval_typed<double>(t, b, o, mask, s, loops_only, global_tables);
+  const bool allow_direct = is_auto || strategy == TLG_STRATEGY_DIRECT;
+  const bool global_tables = !(is_auto || strategy == TLG_STRATEGY_SHARED);
+  if (t->dtype == TLG_SPLIT32) return eval_split(t, b, o, mask, s, allow_direct, global_tables);
+  if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, s, allow_direct, global_tables);
+  return eval_typed<double>(t, b, o, mask, s, allow_direct, global_tables);
 }
 
 tlg_status tlg_set_strategy(int strategy) {
   if (strategy < -1 || strategy > TLG_STRATEGY_COOPERATIVE)
     return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_strategy: strategy must be -1 .. 5");
-  g_strategy.store(strategy, std::memory_order_relaxed);
+  for (int& x : g_override) x = strategy;
   return ok();
 }
 
-int tlg_get_strategy(void) { return current_strategy(); }
+tlg_status tlg_set_family_strategy(int family, int strategy) {
+  if (family < 0 || family >= kFamilies)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_family_strategy: family must be 0 .. 5");
+  if (strategy < -1 || strategy > TLG_STRATEGY_COOPERATIVE)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_family_strategy: strategy must be -1 .. 5");
+  g_override[family] = strategy;
+  return ok();
+}
+
+int tlg_get_family_override(int family) { return family >= 0 && family < kFamilies ? g_override[family] : -1; }
+
+tlg_status tlg_get_family_strategy(int family, int* strategy) {
+  if (family < 0 || family >= kFamilies || !strategy)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_get_family_strategy: family must be 0 .. 5");
+  if (!wanted_strategy(family, strategy)) return TLG_ERR_INVALID_ARGUMENT;
+  return ok();
+}
+
+int tlg_get_strategy(void) {
+  int s = TLG_STRATEGY_AUTO;
+  return wanted_strategy(TLG_FAMILY_JACOBIAN, &s) ? s : -1;
+}
 
 int tlg_last_kernel_family(void) { return g_last_family; }
+
+int tlg_last_launch_family(void) { return g_last_kind; }
 
 tlg_status tlg_evector(const tlg_block* b, int nodes_per_cell, int64_t first_cell, int64_t chunk_cells,
                        int64_t stride, void* out, void* stream) {
@@ -883,6 +1008,7 @@ tlg_status tlg_evector(const tlg_block* b, int nodes_per_cell, int64_t first_cel
   const int64_t padded = (chunk_cells + 15) / 16 * 16;  // VECTOR_PAD
   if (stride < padded) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_evector: stride below the padded chunk");
   if (chunk_cells == 0) return ok();
+  if (!tlg::check_strategy(TLG_FAMILY_EVECTOR)) return TLG_ERR_INVALID_ARGUMENT;
   if (!b->nodes || !b->dofmap) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_evector: NULL nodes or dofmap");
   if (b->num_nodes < 1) return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_evector: cells but no nodes");
   if (b->num_nodes > (int64_t)UINT32_MAX + 1)
@@ -902,6 +1028,7 @@ tlg_status tlg_evector(const tlg_block* b, int nodes_per_cell, int64_t first_cel
         b->num_cells - 1, last_node, nodes_per_cell, b->gdim, padded, stride);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "tlg_evector launch");
+  tlg::record_launch(TLG_FAMILY_EVECTOR, TLG_STRATEGY_LOOPS);
   return ok();
 }
 
@@ -1007,7 +1134,11 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
                                                   " bytes) exceed 227 KiB of shared memory");
   bool found = false;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int strategy = current_strategy();
+  // The adjoint follows the Jacobian family's strategy: sum factorisation where wanted (or AUTO)
+  // and it applies, else the node-row kernel.
+  int strategy = TLG_STRATEGY_AUTO;
+  if (!wanted_strategy(TLG_FAMILY_JACOBIAN, &strategy)) return TLG_ERR_INVALID_ARGUMENT;
+  g_last_kind = TLG_FAMILY_JACOBIAN;
   if (strategy == TLG_STRATEGY_SUMFACT || (strategy == TLG_STRATEGY_AUTO && vjp_sumfact_preferred(t))) {
     tlg_status st = vjp_sumfact(t, a, s, &found);
     if (found) return st;

@@ -9,8 +9,9 @@ namespace tlg {
 cudaError_t TLG_LAUNCH(int td, int gd, int k, const EvalArgs<TLG_F>& a, size_t smem,
                        cudaStream_t s, bool* direct) {
 #ifdef TLG_WITH_DIRECT
-  // Unrolled kernels are compiled for f64 and the GPU tile of 16 cells, tables staged.
-  *direct = a.tile_shift == 4 && !a.tab_global && !a.loops_only;
+  // Unrolled kernels are compiled for f64 and the GPU tile of 16 cells; they read staged tables
+  // (the host clears loops_only only when the tables are staged).
+  *direct = a.tile_shift == 4 && !a.loops_only;
 #define TLG_DIRECT(TD, GD, K) \
   if (*direct && td == TD && gd == GD && k == K) \
     return launch_persistent(eval_direct_kernel<TLG_F, TD, GD, K, 16>, a, a.padded, smem, s);

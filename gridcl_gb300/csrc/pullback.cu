@@ -516,6 +516,7 @@ tlg_status tlg_pull_back_block(const tlg_basis* basis, const tlg_block* b, const
   if (refinements > 0 && b->dtype != TLG_F64)
     return basis_fail(TLG_ERR_INVALID_ARGUMENT, "tlg_pull_back_block: mixed precision refines f64 meshes");
   if (num_cells == 0 || num_points == 0) return tlg::ok();
+  if (!tlg::check_strategy(TLG_FAMILY_PULL_BACK)) return TLG_ERR_INVALID_ARGUMENT;
   if (!x || !xi || !step || !b->nodes || !b->dofmap)
     return basis_fail(TLG_ERR_INVALID_ARGUMENT, "tlg_pull_back_block: NULL points, outputs, nodes or dofmap");
   if (b->num_nodes < 1) return basis_fail(TLG_ERR_LENGTH_MISMATCH, "tlg_pull_back_block: cells but no nodes");
@@ -587,5 +588,6 @@ tlg_status tlg_pull_back_block(const tlg_basis* basis, const tlg_block* b, const
 #undef TLG_PB
 #undef TLG_PBS
   if (e != cudaSuccess) return tlg::cuda_fail(e, "tlg_pull_back_block launch");
+  tlg::record_launch(TLG_FAMILY_PULL_BACK, TLG_STRATEGY_LOOPS);
   return tlg::ok();
 }

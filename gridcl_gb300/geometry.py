@@ -29,6 +29,7 @@ import numpy as np
 import torch
 
 from . import refcell
+from .strategy import _note_launch
 from ._lib import CELL_IDS, FAMILY_IDS, GridError, TlgBlock, TlgOutputs, check, lib
 
 VECTOR_PAD = 16  # tetraloma-device/src/buffer.rs:28
@@ -166,6 +167,7 @@ class Geometry:
             data = torch.empty((k, gd, stride), dtype=self.dtype, device=self.nodes.device)
             check(lib().tlg_evector(ctypes.byref(desc), k, first, cnt, stride, data.data_ptr(),
                                     current_stream_handle()))
+            _note_launch()
             chunks.append(EVectorChunk(first, cnt, data))
             first += cnt
         if max_chunk_cells is None:
@@ -362,6 +364,7 @@ def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points
         for f in names:
             setattr(o, f, fields[f].chunks[ci].data.data_ptr())
         check(lib().tlg_eval_block(tables.handle, ctypes.byref(desc), ctypes.byref(o), stream))
+        _note_launch()
     return fields
 
 
@@ -499,6 +502,7 @@ def pull_back_block(g: Geometry, b: int, x: QuadField, tolerance: float | None =
         check(lib().tlg_pull_back_block(h, ctypes.byref(desc), ch.data.data_ptr(), 0, ch.first_cell,
                                         ch.num_cells, 0, nq, tile, tol, max_iterations, nref,
                                         cxi.data.data_ptr(), cst.data.data_ptr(), stream))
+        _note_launch()
     return xi, step
 
 
@@ -580,6 +584,7 @@ def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: s
     stream = current_stream_handle()
     check(lib().tlg_vjp_block(tables.handle, ctypes.byref(desc), ctypes.byref(o), ctypes.byref(ct),
                               local.data_ptr(), local.shape[0], stream))
+    _note_launch()
     inc = node_incidence(g, b)
     grad = torch.empty((g.nodes.shape[0], gd), dtype=torch.float64, device=dev)
     check(lib().tlg_vjp_gather(inc.offsets.data_ptr(), inc.entries.data_ptr(), g.nodes.shape[0], gd,

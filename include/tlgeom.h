@@ -286,21 +286,37 @@ uint64_t tlg_hilbert_key(const uint32_t* x, int d, int bits);
 uint32_t tlg_quantise(double x, double lo, double hi);
 
 /* Evaluation strategy (the reference's strategy::choose, tetraloma-geometry/src/strategy.rs:
- * 373-407, with its precedence: a scoped setting, then the environment, then the built-in
- * policy; the five strategies of strategy.rs:23-34). AUTO picks per element: for quadrilaterals,
- * hexahedra and prisms at tensor-product point sets, sum factorisation in f64 and above the
- * degrees with paired kernels (Q1-Q2, P1-P2) in f32 and split precision; otherwise the paired /
- * unrolled kernels where compiled, the cooperative kernel for cells of more than 27 nodes, the
- * loops kernels else. The others force a kernel family where it applies, and otherwise the
- * AUTO choice runs:
+ * 311-407, with its precedence per kernel family: this thread's setting, then the environment,
+ * then the built-in policy; the five strategies of strategy.rs:23-34). AUTO picks per element:
+ * for quadrilaterals, hexahedra and prisms at tensor-product point sets, sum factorisation in f64
+ * and above the degrees with paired kernels (Q1-Q2, P1-P2) in f32 and split precision; otherwise
+ * the paired / unrolled kernels where compiled, the cooperative kernel for cells of more than 27
+ * nodes, the loops kernels else (tables staged where they fit: recorded as SHARED, else LOOPS).
+ * The others force a kernel family where it applies, and otherwise the
+ * loops kernel runs, as in the reference (recorded as LOOPS):
  *  - DIRECT: the paired / unrolled kernels (compiled elements, tile 16 for f32 and split);
  *  - LOOPS: K at run time, tables read from global memory;
  *  - SUMFACT: a quadrilateral, hexahedron or prism at a tensor-product point set, no facet
  *    normals, tile 16 in split precision;
  *  - SHARED: the loops kernels with the tables staged in shared memory (where they fit);
  *  - COOPERATIVE: four lanes per cell (cells of 2 or 3 dimensions, up to 128 nodes, 64 in f64).
- * The environment variable TLG_GEOM_STRATEGY (auto, direct, loops, sumfact, shared,
- * cooperative) is read once; tlg_set_strategy overrides it for the process until called with -1. */
+ * A fused launch follows the strategy of its principal family: Jacobian when J, det J or K is
+ * among its outputs, else Normals, FacetNormals, Points. The adjoint follows the Jacobian family
+ * (sum factorisation where it applies, else the node-row kernel); the E-vector and the pull-back
+ * have one kernel each (recorded as LOOPS: K and the degree at run time). The environment variable
+ * TLG_GEOM_STRATEGY is read once: one strategy name (policy or auto, direct, loops, sumfact,
+ * shared, cooperative) for every family, or a comma list <family>=<strategy> of the families
+ * EVector, Points, Jacobian, Normals, FacetNormals, PullBack (each at most once); an invalid value
+ * makes every launch fail with TLG_ERR_INVALID_ARGUMENT. tlg_set_strategy sets this thread's
+ * setting of every family, tlg_set_family_strategy of one (-1 clears it, 0 selects the policy). */
+typedef enum tlg_kernel_family {
+  TLG_FAMILY_EVECTOR = 0,
+  TLG_FAMILY_POINTS = 1,
+  TLG_FAMILY_JACOBIAN = 2,
+  TLG_FAMILY_NORMALS = 3,
+  TLG_FAMILY_FACET_NORMALS = 4,
+  TLG_FAMILY_PULL_BACK = 5
+} tlg_kernel_family;
 typedef enum tlg_strategy {
   TLG_STRATEGY_AUTO = 0,
   TLG_STRATEGY_DIRECT = 1,
@@ -310,12 +326,20 @@ typedef enum tlg_strategy {
   TLG_STRATEGY_COOPERATIVE = 5
 } tlg_strategy;
 tlg_status tlg_set_strategy(int strategy);
-/* The strategy in effect (TLG_STRATEGY_*). */
+tlg_status tlg_set_family_strategy(int family, int strategy);
+/* This thread's setting of a family (-1: none). */
+int tlg_get_family_override(int family);
+/* The strategy in effect for a family (setting, environment, policy). */
+tlg_status tlg_get_family_strategy(int family, int* strategy);
+/* The strategy in effect for the Jacobian family; -1 when the environment variable is invalid. */
 int tlg_get_strategy(void);
-/* The kernel family that ran in this thread's last launching tlg_eval_block (or tlg_vjp_block):
- * DIRECT (paired or unrolled), LOOPS, SUMFACT, SHARED or COOPERATIVE; 0 before any (the reference's record_strategies test hook,
- * tetraloma-geometry/src/testing.rs:34-43). */
+/* The strategy that ran in this thread's last launch (tlg_eval_block, tlg_vjp_block, tlg_evector,
+ * tlg_pull_back_block): DIRECT (paired or unrolled), LOOPS, SUMFACT, SHARED or COOPERATIVE; 0
+ * before any (the reference's record_strategies test hook, tetraloma-geometry/src/testing.rs:
+ * 34-43). */
 int tlg_last_kernel_family(void);
+/* The family (TLG_FAMILY_*) whose strategy decided that launch; -1 before any. */
+int tlg_last_launch_family(void);
 
 /* ---------------------------------------------------------------------------------------
  * Measure (tetraloma-geometry/src/measure.rs:15-185): per-cell sums of det J * w over the

@@ -285,3 +285,41 @@ def test_cooperative_split_recomputes(cuda):
         counts[strat] = int(rec.item())
     assert counts["loops"] > 0
     assert abs(counts["cooperative"] - counts["loops"]) <= max(2, counts["loops"] // 100)
+
+
+def test_per_family_settings_and_records(cuda):
+    """A fused launch follows its principal family; a forced strategy that does not apply runs
+    loops; record_strategies sees every launch with its family (testing.rs:11-43)."""
+    mesh = meshes.curved_box("Hexahedron", 2, 2, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=F64)
+    pts, _ = tg.refcell.gauss_rule("Hexahedron", 4)
+    ps = tg.PointSet("Hexahedron", pts, np.ones(len(pts)))
+    with tg.record_strategies() as rec:
+        with tg.with_strategy("loops", family="Points"), tg.with_strategy("sumfact", family="Jacobian"):
+            tg.geometric_factors_block(g, 0, ps, ("points",))
+            tg.geometric_factors_block(g, 0, ps, ("points", "detj"))
+        with tg.with_strategy("sumfact"):
+            tets = meshes.curved_box("Tetrahedron", 1, 2, jitter=0.0)
+            gt = tg.Geometry.from_host(tets, dtype=F64)
+            tp, _ = tg.refcell.gauss_rule("Tetrahedron", 2)
+            tg.geometric_factors_block(gt, 0, tg.PointSet("Tetrahedron", tp, np.ones(len(tp))), ("detj",))
+        with tg.with_strategy("direct", family="Normals"):
+            sph = tg.Geometry.from_host(meshes.sphere(1, 2), dtype=F64)
+            sp, _ = tg.refcell.gauss_rule("Triangle", 2)
+            tg.geometric_factors_block(sph, 0, tg.PointSet("Triangle", sp, np.ones(len(sp))), ("normals",))
+        g.evector(0, max_chunk_cells=None)
+    assert rec[:4] == [("Points", "loops"), ("Jacobian", "sumfact"), ("Jacobian", "loops"), ("Normals", "direct")]
+    assert rec[4][0] == "EVector"
+
+
+def test_forced_strategy_that_does_not_apply_runs_loops(cuda):
+    """Cooperative above 128 nodes and sum factorisation at a non-tensor rule fall back to loops
+    (strategy.rs:400-404)."""
+    mesh = meshes.curved_box("Tetrahedron", 1, 8, jitter=0.0)  # 165 nodes per cell
+    g = tg.Geometry.from_host(mesh, dtype=F32)
+    pts, _ = tg.refcell.gauss_rule("Tetrahedron", 4)
+    ps = tg.PointSet("Tetrahedron", pts, np.ones(len(pts)))
+    for strat in ("cooperative", "sumfact", "direct"):
+        with tg.with_strategy(strat):
+            tg.geometric_factors_block(g, 0, ps, ("detj",))
+            assert tg.last_kernel_family() == "loops", strat
