@@ -43,7 +43,7 @@ struct tlg_tables {
   unsigned char* dev = nullptr;  // phi [Q][K] | dphi [Q][K][TD] | refn [Q][TD] | error word
   uint32_t bytes = 0;            // table bytes (multiple of 16), error word excluded
   bool staged = true;            // the tables fit the kernels' shared-memory budget
-  uint32_t off_dphi = 0, off_refn = 0, off_phi2 = 0, off_dphi2 = 0, off_dphi64 = 0;
+  uint32_t off_dphi = 0, off_refn = 0, off_rows2 = 0, off_dphi64 = 0;
   // The adjoint's table after the error word (codimension 0, f64 or split tables; 0 bytes when
   // absent or too large to stage): per node of each point (f64) or point pair (split) the 32
   // bytes phi, dphi_0 .. dphi_{TD-1}, zero padding, as f64 values or f32 pairs.
@@ -336,8 +336,7 @@ void fill_pair_args(const tlg_tables* t, const tlg_block* b, const tlg_outputs* 
   a.last_node = (uint32_t)(b->num_nodes - 1);
   a.tab_bytes = t->bytes;
   a.off_refn = t->off_refn;
-  a.off_phi2 = t->off_phi2;
-  a.off_dphi2 = t->off_dphi2;
+  a.off_rows2 = t->off_rows2;
   a.off_dphi64 = t->off_dphi64;
   a.off_dphi = t->off_dphi;
   a.k_runtime = (int)t->k;
@@ -751,14 +750,15 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
     t->off_dphi = align16(n_phi * es);
     t->off_refn = align16(t->off_dphi + n_dphi * es);
     size_t total = align16(t->off_refn + std::max<size_t>(n_refn, 1) * es);
-    // Point pairs for the paired-FP32 kernels: phi2 [QP][K][2], dphi2 [QP][K][TD][2], f32; an odd
-    // last point is paired with itself.
+    // Point pairs for the paired-FP32 kernels: rows2 [QP][K][RW] f32, per node of a point pair
+    // phi, dphi_0 .. dphi_{TD-1} as (point 2p, point 2p + 1) pairs, zero padded to RW = 8 (TD > 1)
+    // or 4 (TD = 1) floats, so that a node's row is one or two 16-byte shared loads; an odd last
+    // point is paired with itself.
     const int64_t qp = (npoints + 1) / 2;
+    const int rw = td == 1 ? 4 : 8;
     if (dtype != TLG_F64) {
-      t->off_phi2 = (uint32_t)total;
-      total = align16(total + std::max<size_t>((size_t)qp * k * 2, 1) * 4);
-      t->off_dphi2 = (uint32_t)total;
-      total = align16(total + std::max<size_t>((size_t)qp * k * td * 2, 1) * 4);
+      t->off_rows2 = (uint32_t)total;
+      total = align16(total + std::max<size_t>((size_t)qp * k * rw, 1) * 4);
     }
     if (dtype == TLG_SPLIT32) {  // the f64 derivative table of the FP64 recompute follows
       t->off_dphi64 = (uint32_t)total;
@@ -822,18 +822,17 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
     if (ref_normals) std::memcpy(refn.data(), ref_normals, n_refn * sizeof(double));
     if (dtype == TLG_SPLIT32) narrow_into<double>(t->host, t->off_dphi64, dphi.data(), n_dphi);
     if (dtype != TLG_F64) {
-      std::vector<double> phi2((size_t)qp * k * 2), dphi2((size_t)qp * k * td * 2);
+      std::vector<double> rows2((size_t)qp * k * rw, 0.0);
       for (int64_t p = 0; p < qp; ++p)
         for (int h = 0; h < 2; ++h) {
           const int64_t q = std::min<int64_t>(2 * p + h, npoints - 1);
           for (int64_t i = 0; i < k; ++i) {
-            phi2[(p * k + i) * 2 + h] = phi[q * k + i];
-            for (int d = 0; d < td; ++d)
-              dphi2[((p * k + i) * td + d) * 2 + h] = dphi[(q * k + i) * td + d];
+            double* r = &rows2[(size_t)((p * k + i) * rw)];
+            r[h] = phi[q * k + i];
+            for (int d = 0; d < td; ++d) r[2 * (d + 1) + h] = dphi[(q * k + i) * td + d];
           }
         }
-      narrow_into<float>(t->host, t->off_phi2, phi2.data(), phi2.size());
-      narrow_into<float>(t->host, t->off_dphi2, dphi2.data(), dphi2.size());
+      narrow_into<float>(t->host, t->off_rows2, rows2.data(), rows2.size());
     }
     if (t->vjp_bytes > 0) {
       const int pn = dtype == TLG_SPLIT32 ? 2 : 1;  // points per table row

@@ -78,14 +78,14 @@ struct PairArgs {
   const void* nodes;
   const uint32_t* dofmap;
   const uint32_t* flags;
-  const unsigned char* tab;  // phi | dphi | refn | phi2 [QP][K][2] | dphi2 [QP][K][TD][2] | dphi64
+  const unsigned char* tab;  // phi | dphi | refn | rows2 [QP][K][RW] | dphi64
   float* out[6];
   int* err;
   unsigned long long* recomputed;  // may be null
   int64_t first_cell, padded, range_cells, out_first_cell, last_cell, last_flag;
   double origin[3];
   float cond_limit;
-  uint32_t last_node, tab_bytes, off_refn, off_phi2, off_dphi2, off_dphi64, mask;
+  uint32_t last_node, tab_bytes, off_refn, off_rows2, off_dphi64, mask;
   int num_points;
   uint32_t off_dphi;  // the f32 derivative table [Q][K][TD] (split loops kernel; phi [Q][K] at 0)
   int k_runtime;      // K (split loops kernel)
@@ -446,8 +446,9 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
   constexpr int LJ = TD * GD;
   using A = Ar<float2>;
   using M = Factors<float2, TD, GD>;
-  const float2* phi2 = reinterpret_cast<const float2*>(tabs + a.off_phi2);
-  const float2* dphi2 = reinterpret_cast<const float2*>(tabs + a.off_dphi2);
+  // Per node of a point pair: (phi, dphi_0) in one 16-byte row, (dphi_1, dphi_2) in the next.
+  constexpr int RW4 = TD == 1 ? 1 : 2;  // 16-byte rows per node
+  const float4* rows2 = reinterpret_cast<const float4*>(tabs + a.off_rows2);
   const float* refn = reinterpret_cast<const float*>(tabs + a.off_refn);
   const double* dphi64 = reinterpret_cast<const double*>(tabs + a.off_dphi64);
   const int nq = a.num_points;
@@ -514,17 +515,79 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
 
     for (int qp = 0; qp < nqp; ++qp) {
       const bool both = 2 * qp + 1 < nq;
-      if (mask & kOutPoints) {
-        float2 s[GD];
-        const float2* w = phi2 + qp * K;
+      const float4* rq = rows2 + (int64_t)qp * K * RW4;
+      // One pass over the nodes: X and J of the pair from each node's one or two 16-byte rows
+      // (X accumulated only when asked for; J only when anything beyond X is).
+      const bool want_x = (mask & kOutPoints) != 0;
+      float2 s[GD], j[LJ];
+      {
+        float2 w[4];
+        const float4 r0 = rq[K0 * RW4];
+        w[0] = make_float2(r0.x, r0.y);
+        w[1] = make_float2(r0.z, r0.w);
+        if constexpr (TD > 1) {
+          const float4 r1 = rq[K0 * RW4 + 1];
+          w[2] = make_float2(r1.x, r1.y);
+          w[3] = make_float2(r1.z, r1.w);
+        }
 #pragma unroll
-        for (int g = 0; g < GD; ++g) s[g] = A::mul(A::splat(x[K0][g]), w[K0]);
+        for (int g = 0; g < GD; ++g) s[g] = A::mul(A::splat(x[K0][g]), w[0]);
+#pragma unroll
+        for (int d = 0; d < TD; ++d)
+#pragma unroll
+          for (int g = 0; g < GD; ++g) j[d * GD + g] = A::mul(A::splat(x[K0][g]), w[1 + d]);
+      }
+      // Below 27 nodes X and J share one pass over the rows; at 27 the shared pass holds too many
+      // rows in flight (238 registers against 168 for two passes), so X and J take a pass each.
+      constexpr bool kOnePass = K < 27;
+      if (want_x && want_j && kOnePass) {
 #pragma unroll
         for (int k = K0 + 1; k < K; ++k) {
-          const float2 wk = w[k];
+          float2 w[4];
+          const float4 r0 = rq[k * RW4];
+          w[0] = make_float2(r0.x, r0.y);
+          w[1] = make_float2(r0.z, r0.w);
+          if constexpr (TD > 1) {
+            const float4 r1 = rq[k * RW4 + 1];
+            w[2] = make_float2(r1.x, r1.y);
+            w[3] = make_float2(r1.z, r1.w);
+          }
 #pragma unroll
-          for (int g = 0; g < GD; ++g) s[g] = A::fma(A::splat(x[k][g]), wk, s[g]);
+          for (int g = 0; g < GD; ++g) s[g] = A::fma(A::splat(x[k][g]), w[0], s[g]);
+#pragma unroll
+          for (int d = 0; d < TD; ++d)
+#pragma unroll
+            for (int g = 0; g < GD; ++g) j[d * GD + g] = A::fma(A::splat(x[k][g]), w[1 + d], j[d * GD + g]);
         }
+      } else {
+        if (want_x) {
+#pragma unroll
+          for (int k = K0 + 1; k < K; ++k) {
+            const float4 r0 = rq[k * RW4];
+            const float2 w0 = make_float2(r0.x, r0.y);
+#pragma unroll
+            for (int g = 0; g < GD; ++g) s[g] = A::fma(A::splat(x[k][g]), w0, s[g]);
+          }
+        }
+        if (want_j) {
+#pragma unroll
+          for (int k = K0 + 1; k < K; ++k) {
+            float2 w[4];
+            const float4 r0 = rq[k * RW4];
+            w[1] = make_float2(r0.z, r0.w);
+            if constexpr (TD > 1) {
+              const float4 r1 = rq[k * RW4 + 1];
+              w[2] = make_float2(r1.x, r1.y);
+              w[3] = make_float2(r1.z, r1.w);
+            }
+#pragma unroll
+            for (int d = 0; d < TD; ++d)
+#pragma unroll
+              for (int g = 0; g < GD; ++g) j[d * GD + g] = A::fma(A::splat(x[k][g]), w[1 + d], j[d * GD + g]);
+          }
+        }
+      }
+      if (want_x) {
 #pragma unroll
         for (int g = 0; g < GD; ++g) {
           if constexpr (SPLIT) s[g] = A::add(A::splat(xh[g]), A::add(A::splat(xl[g]), s[g]));
@@ -533,23 +596,6 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
         cx.put2(s, both);
       }
       if (!want_j) continue;
-      float2 j[LJ];
-      const float2* dq = dphi2 + qp * K * TD;
-#pragma unroll
-      for (int d = 0; d < TD; ++d) {
-        const float2 w0 = dq[K0 * TD + d];
-#pragma unroll
-        for (int g = 0; g < GD; ++g) j[d * GD + g] = A::mul(A::splat(x[K0][g]), w0);
-      }
-#pragma unroll
-      for (int k = K0 + 1; k < K; ++k) {
-#pragma unroll
-        for (int d = 0; d < TD; ++d) {
-          const float2 w = dq[k * TD + d];
-#pragma unroll
-          for (int g = 0; g < GD; ++g) j[d * GD + g] = A::fma(A::splat(x[k][g]), w, j[d * GD + g]);
-        }
-      }
       float2 kk[LJ];
       const bool want_k = (mask & (kOutPinv | kOutFacetNormals)) != 0 || SPLIT;
       if (want_k) M::pinv(j, kk);
