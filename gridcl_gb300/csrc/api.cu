@@ -52,12 +52,14 @@ struct tlg_tables {
   // the adjoint's: per direction d, B_d [m_d][N] = l_i(u_d[a]) and D_d [m_d][N] = l_i'(u_d[a]) in the
   // arithmetic's type, then perm [K] u32 (lexicographic node index -> Lagrange node); offsets
   // relative to the section.
-  // Prisms: psi, d_x psi, d_y psi [m_t][NT] of the triangle rule in B_0, D_0, D_1 (B_1 empty), the
-  // interval's l, l' [m_z][N] in B_2, D_2, perm [N * NT] (index c NT + t -> Lagrange node); point
-  // q = i sf_qs[0] + j sf_qs[1].
+  // The section holds the block headers (tlg::SfBlock each), the blocks' tables, the permutation
+  // and, for facet rules, the reference normals [Q][TD] in the arithmetic's type; offsets are
+  // relative to the section. Prisms: per block psi, d_x psi, d_y psi [m_t][NT] in B_0, D_0, D_1,
+  // the interval's l, l' [m_z][N] in B_2, D_2, perm [N * NT] (index c NT + t -> Lagrange node).
   bool sf_ok = false, sf_prism = false;
-  int sf_n = 0, sf_m[3] = {1, 1, 1}, sf_qs[2] = {0, 0};
-  uint32_t off_sf = 0, sf_bytes = 0, sf_offb[3] = {0, 0, 0}, sf_offd[3] = {0, 0, 0}, sf_offperm = 0;
+  int sf_n = 0, sf_nblocks = 0;
+  tlg::SfBlock sf_block0{};  // the first block (the adjoint's single-block rule)
+  uint32_t off_sf = 0, sf_bytes = 0, sf_offperm = 0, sf_offrefn = 0;
   int* err = nullptr;
   std::vector<unsigned char> host;  // host copy of the device bytes
 };
@@ -247,7 +249,7 @@ bool coop_preferred(const tlg_tables* t) { return t->k > 27; }
 tlg_status eval_sumfact(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
                         cudaStream_t stream, bool* found) {
   *found = false;
-  if (!t->sf_ok || (mask & tlg::kOutFacetNormals) || (t->dtype == TLG_SPLIT32 && o->tile != 16))
+  if (!t->sf_ok || (t->dtype == TLG_SPLIT32 && o->tile != 16))
     return TLG_ERR_UNSUPPORTED;
   tlg::SfArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -257,8 +259,8 @@ tlg_status eval_sumfact(const tlg_tables* t, const tlg_block* b, const tlg_outpu
   a.tab = t->dev + t->off_sf;
   a.tab_bytes = t->sf_bytes;
   a.dphi64 = t->dtype == TLG_SPLIT32 ? reinterpret_cast<const double*>(t->dev + t->off_dphi64) : nullptr;
-  void* outs[5] = {o->points, o->jacobian, o->detj, o->pinv, o->normals};
-  for (int i = 0; i < 5; ++i) a.out[i] = outs[i];
+  void* outs[6] = {o->points, o->jacobian, o->detj, o->pinv, o->normals, o->facet_normals};
+  for (int i = 0; i < 6; ++i) a.out[i] = outs[i];
   a.err = t->err;
   a.recomputed = o->recomputed;
   a.first_cell = o->first_cell;
@@ -272,15 +274,10 @@ tlg_status eval_sumfact(const tlg_tables* t, const tlg_block* b, const tlg_outpu
   for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
   a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 256.0f;
   a.last_node = (uint32_t)(b->num_nodes - 1);
-  for (int d = 0; d < 3; ++d) {
-    a.off_b[d] = t->sf_offb[d];
-    a.off_d[d] = t->sf_offd[d];
-    a.m[d] = t->sf_m[d];
-  }
+  a.nblocks = t->sf_nblocks;
   a.off_perm = t->sf_offperm;
+  a.off_refn = t->sf_offrefn;
   a.prism = t->sf_prism;
-  a.qs[0] = t->sf_qs[0];
-  a.qs[1] = t->sf_qs[1];
   a.mask = mask;
   a.num_points = (int)t->q;
   const size_t fbytes = t->dtype == TLG_F64 ? 8 : 4;
@@ -556,159 +553,285 @@ void lagrange_1d(const std::vector<double>& s, double x, double* val, double* de
   }
 }
 
-// The sum-factorisation tables of a quadrilateral or hexahedron at `points`, when the points are
-// a tensor product (direction 0 fastest, as the collapsed rules order them) and the Lagrange
-// nodes a tensor lattice: per direction the 1D rule u_d, B_d = l(u_d), D_d = l'(u_d), and the
-// lexicographic-to-Lagrange node permutation. Returns false when the structure is absent.
-bool tensor_tables(int cell, int degree, int family, const double* pts, int64_t nq, int* m,
-                   std::vector<double>* B, std::vector<double>* D, std::vector<uint32_t>& perm) {
-  const int td = tlg::tdim(cell);
-  const int n = degree + 1;
-  if (nq < 1) return false;
-  // Points per direction.
-  int64_t m0 = 1;
-  while (m0 < nq) {
-    bool same = true;
-    for (int d = 1; d < td; ++d) same = same && pts[m0 * td + d] == pts[d];
-    if (!same) break;
-    ++m0;
+// Sum factorisation over tensor blocks. A point set is cut, in order, into maximal blocks whose
+// points are a tensor product: on quadrilaterals and hexahedra up to one 1D point set per
+// direction (point q = o + a s_0 + b s_1 + c s_2, a direction of one point keeps its coordinate),
+// on prisms a set of (x, y) points times a set of z points. A Gauss rule is one block; a facet
+// rule one block per facet (or fewer, where facets line up). Per block the tables B_d = l(u_d),
+// D_d = l'(u_d) (prisms: the triangle's psi, d_x psi, d_y psi and the interval's l, l'), checked
+// against the element's full tabulation before use.
+struct SfBlockHost {
+  int64_t o = 0;
+  int m[3] = {1, 1, 1};
+  int64_t s[3] = {0, 0, 0};
+  std::vector<double> B[3], D[3];
+};
+
+// Point sets of more blocks than this, or of fewer than two points per block on average, are not
+// taken as tensor point sets.
+constexpr int kMaxSfBlocks = 16;
+
+// The largest tensor block of a quadrilateral or hexahedron point set starting at q0: directions
+// are added fastest first, each while the points repeat the block so far with one more coordinate
+// varying. Sets o, m, s and the 1D coordinates u; returns the block's point count.
+int64_t next_tensor_block(const double* pts, int64_t nq, int td, int64_t q0, SfBlockHost& b,
+                          std::vector<double>* u) {
+  auto P = [&](int64_t q, int d) { return pts[q * td + d]; };
+  b.o = q0;
+  for (int d = 0; d < 3; ++d) {
+    b.m[d] = 1;
+    b.s[d] = 0;
+    u[d].assign(1, d < td ? P(q0, d) : 0.0);
   }
-  int64_t m1 = nq / m0, m2 = 1;
-  if (td == 3) {
-    m1 = 1;
-    while (m1 * m0 < nq && pts[m1 * m0 * td + 2] == pts[2] && pts[m1 * m0 * td] == pts[0]) ++m1;
-    m2 = nq / (m0 * m1);
-  }
-  if (m0 * m1 * m2 != nq) return false;
-  m[0] = (int)m0;
-  m[1] = (int)m1;
-  m[2] = (int)m2;
-  std::vector<double> u[3];
-  for (int64_t a0 = 0; a0 < m0; ++a0) u[0].push_back(pts[a0 * td]);
-  for (int64_t a1 = 0; a1 < m1; ++a1) u[1].push_back(pts[a1 * m0 * td + 1]);
-  if (td == 3)
-    for (int64_t a2 = 0; a2 < m2; ++a2) u[2].push_back(pts[a2 * m0 * m1 * td + 2]);
-  for (int64_t q = 0; q < nq; ++q) {
-    const int64_t idx[3] = {q % m0, (q / m0) % m1, q / (m0 * m1)};
-    for (int d = 0; d < td; ++d)
-      if (pts[q * td + d] != u[d][idx[d]]) return false;
-  }
-  // 1D nodes and the node permutation.
-  std::vector<double> s1 = tlg::lagrange_points(tlg::kInterval, degree, family);
-  std::sort(s1.begin(), s1.end());
-  const std::vector<double> lp = tlg::lagrange_points(cell, degree, family);
-  const int64_t k = tlg::num_lagrange_nodes(cell, degree);
-  perm.assign((size_t)k, 0xFFFFFFFFu);
-  for (int64_t kk = 0; kk < k; ++kk) {
-    int64_t l = 0, scale = 1;
-    for (int d = 0; d < td; ++d) {
-      int found = -1;
-      for (int i = 0; i < n; ++i)
-        if (std::fabs(lp[kk * td + d] - s1[i]) < 1e-12) found = i;
-      if (found < 0) return false;
-      l += found * scale;
-      scale *= n;
+  bool used[3] = {false, false, false};
+  int64_t size = 1;
+  for (int level = 0; level < td; ++level) {
+    const int64_t q1 = q0 + size;
+    if (q1 >= nq) break;
+    int dir = -1, ndiff = 0;
+    for (int e = 0; e < td; ++e)
+      if (P(q1, e) != P(q0, e)) {
+        dir = e;
+        ++ndiff;
+      }
+    if (ndiff != 1 || used[dir]) break;
+    // Copies j = 1, 2, ... of the block so far, each with its own value of `dir`.
+    std::vector<double> vals(1, P(q0, dir));
+    int64_t m = 1;
+    while (q0 + (m + 1) * size <= nq) {
+      const int64_t base = q0 + m * size;
+      const double v = P(base, dir);
+      bool ok = std::find(vals.begin(), vals.end(), v) == vals.end();
+      for (int64_t r = 0; ok && r < size; ++r)
+        for (int e = 0; ok && e < td; ++e)
+          ok = e == dir ? P(base + r, e) == v : P(base + r, e) == P(q0 + r, e);
+      if (!ok) break;
+      vals.push_back(v);
+      ++m;
     }
-    if (perm[(size_t)l] != 0xFFFFFFFFu) return false;
-    perm[(size_t)l] = (uint32_t)kk;
+    if (m < 2) break;
+    used[dir] = true;
+    b.m[dir] = (int)m;
+    b.s[dir] = size;
+    u[dir] = vals;
+    size *= m;
   }
-  for (int d = 0; d < td; ++d) {
-    B[d].assign(u[d].size() * n, 0.0);
-    D[d].assign(u[d].size() * n, 0.0);
-    for (size_t a = 0; a < u[d].size(); ++a) lagrange_1d(s1, u[d][a], &B[d][a * n], &D[d][a * n]);
-  }
-  return true;
+  return size;
 }
 
-// The prism tables when the points are a triangle rule times points in z (either index order)
-// and the prism basis is the product of the triangle's and the interval's: the product of the
-// factor tables equals the full tabulation `tab` ([deriv][q][k]) to 1e-10 at every point and node.
-bool prism_tables(int degree, int family, const double* pts, int64_t nq, const std::vector<double>& tab, int* m,
-                  int* qs, std::vector<double>* B, std::vector<double>* D, std::vector<uint32_t>& perm) {
-  const int n = degree + 1, nt = n * (n + 1) / 2;
-  const int64_t k = (int64_t)nt * n;
-  if (nq < 1 || tlg::num_lagrange_nodes(tlg::kPrism, degree) != k) return false;
-  int64_t mt = 0, mz = 0, st = 0, sz = 0, run = 1;
-  while (run < nq && pts[run * 3 + 2] == pts[2]) ++run;
-  if (run > 1 || nq == 1) {  // z slowest: q = i + mt j
-    mt = run;
-    mz = nq / mt;
-    st = 1;
-    sz = mt;
-  } else {  // z fastest: q = j + mz i
-    run = 1;
-    while (run < nq && pts[run * 3] == pts[0] && pts[run * 3 + 1] == pts[1]) ++run;
-    mz = run;
-    mt = nq / mz;
-    sz = 1;
-    st = mz;
+// The largest prism block starting at q0: (x, y) points times z points, z the slowest or the
+// fastest index (the larger block of the two).
+int64_t next_prism_block(const double* pts, int64_t nq, int64_t q0, SfBlockHost& b, std::vector<double>& tri,
+                         std::vector<double>& zs) {
+  auto X = [&](int64_t q) { return pts[q * 3]; };
+  auto Y = [&](int64_t q) { return pts[q * 3 + 1]; };
+  auto Z = [&](int64_t q) { return pts[q * 3 + 2]; };
+  // z slowest: groups of mt points with one z each, repeating the (x, y) of the first group.
+  int64_t mt = 1;
+  while (q0 + mt < nq && Z(q0 + mt) == Z(q0)) ++mt;
+  int64_t mz = 1;
+  std::vector<double> zsl(1, Z(q0));
+  while (q0 + (mz + 1) * mt <= nq) {
+    const int64_t base = q0 + mz * mt;
+    const double z = Z(base);
+    bool ok = std::find(zsl.begin(), zsl.end(), z) == zsl.end();
+    for (int64_t i = 0; ok && i < mt; ++i)
+      ok = Z(base + i) == z && X(base + i) == X(q0 + i) && Y(base + i) == Y(q0 + i);
+    if (!ok) break;
+    zsl.push_back(z);
+    ++mz;
   }
-  if (mt * mz != nq) return false;
-  std::vector<double> tri((size_t)mt * 2), zs((size_t)mz);
-  for (int64_t i = 0; i < mt; ++i)
-    for (int d = 0; d < 2; ++d) tri[(size_t)(i * 2 + d)] = pts[i * st * 3 + d];
-  for (int64_t j = 0; j < mz; ++j) zs[(size_t)j] = pts[j * sz * 3 + 2];
-  for (int64_t i = 0; i < mt; ++i)
-    for (int64_t j = 0; j < mz; ++j) {
-      const double* x = pts + (i * st + j * sz) * 3;
-      if (x[0] != tri[(size_t)(i * 2)] || x[1] != tri[(size_t)(i * 2 + 1)] || x[2] != zs[(size_t)j]) return false;
+  // z fastest: groups of mz2 points with one (x, y) each, repeating the z of the first group.
+  int64_t mz2 = 1;
+  while (q0 + mz2 < nq && X(q0 + mz2) == X(q0) && Y(q0 + mz2) == Y(q0)) ++mz2;
+  int64_t mt2 = 1;
+  while (q0 + (mt2 + 1) * mz2 <= nq) {
+    const int64_t base = q0 + mt2 * mz2;
+    bool ok = true;
+    for (int64_t j = 0; ok && j < mz2; ++j)
+      ok = X(base + j) == X(base) && Y(base + j) == Y(base) && Z(base + j) == Z(q0 + j);
+    for (int64_t i = 0; ok && i < mt2; ++i)  // a new (x, y)
+      ok = !(X(q0 + i * mz2) == X(base) && Y(q0 + i * mz2) == Y(base));
+    if (!ok) break;
+    ++mt2;
+  }
+  b.o = q0;
+  b.m[1] = 1;
+  b.s[1] = 0;
+  if (mt * mz >= mt2 * mz2) {
+    b.m[0] = (int)mt;
+    b.m[2] = (int)mz;
+    b.s[0] = 1;
+    b.s[2] = mt;
+    tri.resize((size_t)mt * 2);
+    for (int64_t i = 0; i < mt; ++i) {
+      tri[(size_t)(2 * i)] = X(q0 + i);
+      tri[(size_t)(2 * i + 1)] = Y(q0 + i);
     }
-  std::vector<double> tt, lt, s1, lp;
+    zs = zsl;
+    return mt * mz;
+  }
+  b.m[0] = (int)mt2;
+  b.m[2] = (int)mz2;
+  b.s[0] = mz2;
+  b.s[2] = 1;
+  tri.resize((size_t)mt2 * 2);
+  for (int64_t i = 0; i < mt2; ++i) {
+    tri[(size_t)(2 * i)] = X(q0 + i * mz2);
+    tri[(size_t)(2 * i + 1)] = Y(q0 + i * mz2);
+  }
+  zs.resize((size_t)mz2);
+  for (int64_t j = 0; j < mz2; ++j) zs[(size_t)j] = Z(q0 + j);
+  return mt2 * mz2;
+}
+
+// The node permutation of a quadrilateral or hexahedron (lexicographic index over the sorted 1D
+// nodes -> Lagrange node) or of a prism (index c NT + t over the interval's sorted nodes and the
+// triangle's nodes -> Lagrange node); false when the nodes are not such a lattice.
+bool sf_permutation(int cell, int degree, int family, std::vector<double>& s1, std::vector<double>& lt,
+                    std::vector<uint32_t>& perm) {
+  const int td = tlg::tdim(cell);
+  const int n = degree + 1;
+  std::vector<double> lp;
   try {
-    tt = tlg::tabulate(tlg::kTriangle, degree, family, tri.data(), (long)mt, 1);
-    lt = tlg::lagrange_points(tlg::kTriangle, degree, family);
     s1 = tlg::lagrange_points(tlg::kInterval, degree, family);
-    lp = tlg::lagrange_points(tlg::kPrism, degree, family);
+    lp = tlg::lagrange_points(cell, degree, family);
+    if (cell == tlg::kPrism) lt = tlg::lagrange_points(tlg::kTriangle, degree, family);
   } catch (const std::exception&) {
     return false;
   }
   std::sort(s1.begin(), s1.end());
-  if ((int64_t)lt.size() != (int64_t)nt * 2 || (int)s1.size() != n || (int64_t)lp.size() != k * 3) return false;
+  if ((int)s1.size() != n) return false;
+  const int64_t k = tlg::num_lagrange_nodes(cell, degree);
+  if ((int64_t)lp.size() != k * td) return false;
   perm.assign((size_t)k, 0xFFFFFFFFu);
+  auto find1 = [&](double v) {
+    int found = -1;
+    for (int i = 0; i < n; ++i)
+      if (std::fabs(v - s1[i]) < 1e-12) found = i;
+    return found;
+  };
   for (int64_t kk = 0; kk < k; ++kk) {
-    int ft = -1, fc = -1;
-    for (int t = 0; t < nt; ++t)
-      if (std::fabs(lp[kk * 3] - lt[t * 2]) < 1e-12 && std::fabs(lp[kk * 3 + 1] - lt[t * 2 + 1]) < 1e-12) ft = t;
-    for (int c = 0; c < n; ++c)
-      if (std::fabs(lp[kk * 3 + 2] - s1[c]) < 1e-12) fc = c;
-    if (ft < 0 || fc < 0 || perm[(size_t)(fc * nt + ft)] != 0xFFFFFFFFu) return false;
-    perm[(size_t)(fc * nt + ft)] = (uint32_t)kk;
+    int64_t l = 0;
+    if (cell == tlg::kPrism) {
+      const int nt = n * (n + 1) / 2;
+      if ((int)lt.size() != nt * 2 || k != (int64_t)nt * n) return false;
+      int ft = -1;
+      for (int t = 0; t < nt; ++t)
+        if (std::fabs(lp[kk * 3] - lt[t * 2]) < 1e-12 && std::fabs(lp[kk * 3 + 1] - lt[t * 2 + 1]) < 1e-12) ft = t;
+      const int fc = find1(lp[kk * 3 + 2]);
+      if (ft < 0 || fc < 0) return false;
+      l = (int64_t)fc * nt + ft;
+    } else {
+      int64_t scale = 1;
+      for (int d = 0; d < td; ++d) {
+        const int f = find1(lp[kk * td + d]);
+        if (f < 0) return false;
+        l += f * scale;
+        scale *= n;
+      }
+    }
+    if (perm[(size_t)l] != 0xFFFFFFFFu) return false;
+    perm[(size_t)l] = (uint32_t)kk;
   }
-  B[0].assign((size_t)(mt * nt), 0.0);
-  D[0].assign((size_t)(mt * nt), 0.0);
-  B[1].clear();
-  D[1].assign((size_t)(mt * nt), 0.0);
-  for (int64_t i = 0; i < mt; ++i)
-    for (int t = 0; t < nt; ++t) {
-      B[0][(size_t)(i * nt + t)] = tt[(size_t)(i * nt + t)];
-      D[0][(size_t)(i * nt + t)] = tt[(size_t)((mt + i) * nt + t)];
-      D[1][(size_t)(i * nt + t)] = tt[(size_t)((2 * mt + i) * nt + t)];
-    }
-  B[2].assign((size_t)(mz * n), 0.0);
-  D[2].assign((size_t)(mz * n), 0.0);
-  for (int64_t j = 0; j < mz; ++j) lagrange_1d(s1, zs[(size_t)j], &B[2][(size_t)(j * n)], &D[2][(size_t)(j * n)]);
-  // The product identity against the prism's own tabulation.
-  for (int64_t i = 0; i < mt; ++i)
-    for (int64_t j = 0; j < mz; ++j) {
-      const int64_t q = i * st + j * sz;
-      for (int c = 0; c < n; ++c)
-        for (int t = 0; t < nt; ++t) {
-          const int64_t kk = perm[(size_t)(c * nt + t)];
-          const double l = B[2][(size_t)(j * n + c)], ld = D[2][(size_t)(j * n + c)];
-          const double want[4] = {B[0][(size_t)(i * nt + t)] * l, D[0][(size_t)(i * nt + t)] * l,
-                                  D[1][(size_t)(i * nt + t)] * l, B[0][(size_t)(i * nt + t)] * ld};
-          for (int r = 0; r < 4; ++r) {
-            const double got = tab[(size_t)((r * nq + q) * k + kk)];
-            if (!(std::fabs(got - want[r]) <= 1e-10 * std::max(1.0, std::fabs(got)))) return false;
-          }
-        }
-    }
-  m[0] = (int)mt;
-  m[1] = 1;
-  m[2] = (int)mz;
-  qs[0] = (int)st;
-  qs[1] = (int)sz;
   return true;
+}
+
+// The tensor blocks of `points` for a quadrilateral, hexahedron or prism, with their tables and
+// the permutation; false when the point set is not a tensor point set or a table product misses
+// the full tabulation `tab` ([deriv][q][k]) by more than 1e-10.
+bool sf_blocks(int cell, int degree, int family, const double* pts, int64_t nq, const std::vector<double>& tab,
+               std::vector<SfBlockHost>& blocks, std::vector<uint32_t>& perm) {
+  const int td = tlg::tdim(cell);
+  const int n = degree + 1;
+  const int64_t k = tlg::num_lagrange_nodes(cell, degree);
+  std::vector<double> s1, lt;
+  if (nq < 1 || !sf_permutation(cell, degree, family, s1, lt, perm)) return false;
+  blocks.clear();
+  for (int64_t q0 = 0; q0 < nq;) {
+    if ((int)blocks.size() >= kMaxSfBlocks) return false;
+    SfBlockHost b;
+    int64_t size = 0;
+    if (cell == tlg::kPrism) {
+      std::vector<double> tri, zs;
+      size = next_prism_block(pts, nq, q0, b, tri, zs);
+      const int nt = n * (n + 1) / 2;
+      std::vector<double> tt;
+      try {
+        tt = tlg::tabulate(tlg::kTriangle, degree, family, tri.data(), (long)b.m[0], 1);
+      } catch (const std::exception&) {
+        return false;
+      }
+      const int mt = b.m[0];
+      b.B[0].assign((size_t)mt * nt, 0.0);
+      b.D[0].assign((size_t)mt * nt, 0.0);
+      b.D[1].assign((size_t)mt * nt, 0.0);
+      for (int i = 0; i < mt; ++i)
+        for (int t = 0; t < nt; ++t) {
+          b.B[0][(size_t)(i * nt + t)] = tt[(size_t)(i * nt + t)];
+          b.D[0][(size_t)(i * nt + t)] = tt[(size_t)((mt + i) * nt + t)];
+          b.D[1][(size_t)(i * nt + t)] = tt[(size_t)((2 * mt + i) * nt + t)];
+        }
+      b.B[2].assign((size_t)b.m[2] * n, 0.0);
+      b.D[2].assign((size_t)b.m[2] * n, 0.0);
+      for (int j = 0; j < b.m[2]; ++j)
+        lagrange_1d(s1, zs[(size_t)j], &b.B[2][(size_t)(j * n)], &b.D[2][(size_t)(j * n)]);
+      // Identity: psi_t(i) l_c(z_j) and its derivatives against the prism's tabulation.
+      for (int i = 0; i < mt; ++i)
+        for (int j = 0; j < b.m[2]; ++j) {
+          const int64_t q = b.o + i * b.s[0] + j * b.s[2];
+          for (int c = 0; c < n; ++c)
+            for (int t = 0; t < nt; ++t) {
+              const int64_t kk = perm[(size_t)(c * nt + t)];
+              const double l = b.B[2][(size_t)(j * n + c)], ld = b.D[2][(size_t)(j * n + c)];
+              const double want[4] = {b.B[0][(size_t)(i * nt + t)] * l, b.D[0][(size_t)(i * nt + t)] * l,
+                                      b.D[1][(size_t)(i * nt + t)] * l, b.B[0][(size_t)(i * nt + t)] * ld};
+              for (int r = 0; r < 4; ++r) {
+                const double got = tab[(size_t)((r * nq + q) * k + kk)];
+                if (!(std::fabs(got - want[r]) <= 1e-10 * std::max(1.0, std::fabs(got)))) return false;
+              }
+            }
+        }
+    } else {
+      std::vector<double> u[3];
+      size = next_tensor_block(pts, nq, td, q0, b, u);
+      for (int d = 0; d < td; ++d) {
+        b.B[d].assign((size_t)b.m[d] * n, 0.0);
+        b.D[d].assign((size_t)b.m[d] * n, 0.0);
+        for (int a = 0; a < b.m[d]; ++a)
+          lagrange_1d(s1, u[d][(size_t)a], &b.B[d][(size_t)(a * n)], &b.D[d][(size_t)(a * n)]);
+      }
+      // Identity: prod_d l_{i_d}(u_d) and its derivatives against the tabulation.
+      const int m2 = td == 3 ? b.m[2] : 1;
+      for (int c2 = 0; c2 < m2; ++c2)
+        for (int b1 = 0; b1 < b.m[1]; ++b1)
+          for (int a0 = 0; a0 < b.m[0]; ++a0) {
+            const int64_t q = b.o + a0 * b.s[0] + b1 * b.s[1] + c2 * b.s[2];
+            const int pt[3] = {a0, b1, c2};
+            for (int64_t l = 0; l < k; ++l) {
+              int64_t rest = l;
+              int idx[3] = {0, 0, 0};
+              for (int d = 0; d < td; ++d) {
+                idx[d] = (int)(rest % n);
+                rest /= n;
+              }
+              const int64_t kk = perm[(size_t)l];
+              for (int r = 0; r <= td; ++r) {
+                double want = 1.0;
+                for (int d = 0; d < td; ++d) {
+                  const std::vector<double>& T = (r == d + 1) ? b.D[d] : b.B[d];
+                  want *= T[(size_t)(pt[d] * n + idx[d])];
+                }
+                const double got = tab[(size_t)((r * nq + q) * k + kk)];
+                if (!(std::fabs(got - want) <= 1e-10 * std::max(1.0, std::fabs(got)))) return false;
+              }
+            }
+          }
+    }
+    blocks.push_back(std::move(b));
+    q0 += size;
+  }
+  return nq >= 2 * (int64_t)blocks.size();
 }
 
 }  // namespace
@@ -778,39 +901,59 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       const size_t vb = (size_t)(dtype == TLG_SPLIT32 ? qp : npoints) * k * 32;
       if (vb > 0 && vb <= (size_t)160 * 1024) t->vjp_bytes = (uint32_t)vb;
     }
-    std::vector<double> sf_b[3], sf_d[3];
+    std::vector<SfBlockHost> sf;
     std::vector<uint32_t> sf_perm;
-    if ((cell == tlg::kQuadrilateral || cell == tlg::kHexahedron) && degree + 1 <= 6)
-      t->sf_ok = tensor_tables(cell, degree, family, points, npoints, t->sf_m, sf_b, sf_d, sf_perm);
-    if (cell == tlg::kPrism && degree <= 3 && gdim == 3) {
-      t->sf_ok = prism_tables(degree, family, points, npoints, tab, t->sf_m, t->sf_qs, sf_b, sf_d, sf_perm);
-      t->sf_prism = t->sf_ok;
+    if (((cell == tlg::kQuadrilateral || cell == tlg::kHexahedron) && degree + 1 <= 6) ||
+        (cell == tlg::kPrism && degree <= 3 && gdim == 3)) {
+      t->sf_ok = sf_blocks(cell, degree, family, points, npoints, tab, sf, sf_perm);
+      t->sf_prism = t->sf_ok && cell == tlg::kPrism;
     }
     t->off_sf = (uint32_t)align16(t->off_vjp + t->vjp_bytes);
+    std::vector<tlg::SfBlock> heads;
     if (t->sf_ok) {
       t->sf_n = degree + 1;
-      size_t off = 0;
-      for (int d = 0; d < td; ++d) {
-        t->sf_offb[d] = (uint32_t)off;
-        off = align16(off + sf_b[d].size() * es);
-        t->sf_offd[d] = (uint32_t)off;
-        off = align16(off + sf_d[d].size() * es);
+      t->sf_nblocks = (int)sf.size();
+      size_t off = align16(sf.size() * sizeof(tlg::SfBlock));
+      heads.resize(sf.size());
+      for (size_t bi = 0; bi < sf.size(); ++bi) {
+        tlg::SfBlock& h = heads[bi];
+        std::memset(&h, 0, sizeof(h));
+        h.o = (int)sf[bi].o;
+        for (int d = 0; d < 3; ++d) {
+          h.m[d] = sf[bi].m[d];
+          h.s[d] = (int)sf[bi].s[d];
+          h.off_b[d] = (uint32_t)off;
+          off = align16(off + sf[bi].B[d].size() * es);
+          h.off_d[d] = (uint32_t)off;
+          off = align16(off + sf[bi].D[d].size() * es);
+        }
       }
+      t->sf_block0 = heads[0];
       t->sf_offperm = (uint32_t)off;
-      t->sf_bytes = (uint32_t)align16(off + sf_perm.size() * 4);
+      off = align16(off + sf_perm.size() * 4);
+      t->sf_offrefn = (uint32_t)off;
+      if (ref_normals) off = align16(off + (size_t)npoints * td * es);
+      t->sf_bytes = (uint32_t)off;
     }
     t->host.assign(t->off_sf + t->sf_bytes, 0);
     if (t->sf_ok) {
-      for (int d = 0; d < td; ++d) {
-        if (dtype == TLG_F64) {
-          narrow_into<double>(t->host, t->off_sf + t->sf_offb[d], sf_b[d].data(), sf_b[d].size());
-          narrow_into<double>(t->host, t->off_sf + t->sf_offd[d], sf_d[d].data(), sf_d[d].size());
-        } else {
-          narrow_into<float>(t->host, t->off_sf + t->sf_offb[d], sf_b[d].data(), sf_b[d].size());
-          narrow_into<float>(t->host, t->off_sf + t->sf_offd[d], sf_d[d].data(), sf_d[d].size());
+      std::memcpy(t->host.data() + t->off_sf, heads.data(), heads.size() * sizeof(tlg::SfBlock));
+      for (size_t bi = 0; bi < sf.size(); ++bi)
+        for (int d = 0; d < 3; ++d) {
+          const size_t ob = t->off_sf + heads[bi].off_b[d], od = t->off_sf + heads[bi].off_d[d];
+          if (dtype == TLG_F64) {
+            narrow_into<double>(t->host, ob, sf[bi].B[d].data(), sf[bi].B[d].size());
+            narrow_into<double>(t->host, od, sf[bi].D[d].data(), sf[bi].D[d].size());
+          } else {
+            narrow_into<float>(t->host, ob, sf[bi].B[d].data(), sf[bi].B[d].size());
+            narrow_into<float>(t->host, od, sf[bi].D[d].data(), sf[bi].D[d].size());
+          }
         }
-      }
       std::memcpy(t->host.data() + t->off_sf + t->sf_offperm, sf_perm.data(), sf_perm.size() * 4);
+      if (ref_normals) {
+        if (dtype == TLG_F64) narrow_into<double>(t->host, t->off_sf + t->sf_offrefn, ref_normals, (size_t)npoints * td);
+        else narrow_into<float>(t->host, t->off_sf + t->sf_offrefn, ref_normals, (size_t)npoints * td);
+      }
     }
     // Reorder [deriv][q][k] into phi [q][k] and dphi [q][k][d].
     std::vector<double> phi(n_phi), dphi(n_dphi), refn(n_refn, 0.0);
@@ -1036,7 +1179,11 @@ namespace {
 // Hexahedra with a tensor-product rule and 2 or 3 nodes per direction have the sum-factorised
 // adjoint.
 bool vjp_sumfact_preferred(const tlg_tables* t) {
-  return t->sf_ok && t->cell == tlg::kHexahedron && (t->sf_n == 2 || t->sf_n == 3);
+  // One block in rule order (direction 0 fastest): the kernel loads the next point's cotangents
+  // ahead and walks the points in that order.
+  const tlg::SfBlock& h = t->sf_block0;
+  return t->sf_ok && t->cell == tlg::kHexahedron && (t->sf_n == 2 || t->sf_n == 3) && t->sf_nblocks == 1 &&
+         h.o == 0 && h.s[0] == 1 && h.s[1] == h.m[0] && h.s[2] == h.m[0] * h.m[1];
 }
 
 // The sum-factorised adjoint from the arguments of the node-row kernel; `found` is false when
@@ -1067,9 +1214,9 @@ tlg_status vjp_sumfact(const tlg_tables* t, const tlg::VjpArgs& v, cudaStream_t 
   a.last_node = v.last_node;
   a.tab_bytes = t->sf_bytes;
   for (int d = 0; d < 3; ++d) {
-    a.off_b[d] = t->sf_offb[d];
-    a.off_d[d] = t->sf_offd[d];
-    a.m[d] = t->sf_m[d];
+    a.off_b[d] = t->sf_block0.off_b[d];
+    a.off_d[d] = t->sf_block0.off_d[d];
+    a.m[d] = t->sf_block0.m[d];
   }
   a.off_perm = t->sf_offperm;
   a.num_points = v.num_points;

@@ -84,6 +84,9 @@ cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t sme
 // N nodes per direction; `found` is false when none is compiled for (td, gd, n).
 cudaError_t launch_sumfact(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
                            bool* found);
+// Defined in sumfact_fn.cu: the same with facet normals among the outputs (codimension 0).
+cudaError_t launch_sumfact_fn(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
+                              bool* found);
 
 struct CoopArgs;
 // Defined in coop.cu: the cooperative kernel (four lanes per cell) for precision 4, 8 or 12, cells of

@@ -7,40 +7,6 @@
 
 namespace tlg {
 
-namespace {
-
-template <typename F, bool SPLIT>
-cudaError_t launch_sf(int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s, bool* found) {
-  *found = true;
-  if (a.prism) {
-    if (n == 2) return launch_persistent(sumfact_prism_kernel<F, SPLIT, 2>, a, a.padded, smem, s);
-    if (n == 3) return launch_persistent(sumfact_prism_kernel<F, SPLIT, 3>, a, a.padded, smem, s);
-    if (n == 4) return launch_persistent(sumfact_prism_kernel<F, SPLIT, 4>, a, a.padded, smem, s);
-    *found = false;
-    return cudaSuccess;
-  }
-#define TLG_SF(TD, GD, NN) \
-  if (td == TD && gd == GD && n == NN) \
-    return launch_persistent(sumfact_kernel<F, SPLIT, TD, GD, NN>, a, a.padded, smem, s);
-  TLG_SF(3, 3, 2)
-  TLG_SF(3, 3, 3)
-  TLG_SF(3, 3, 4)
-  TLG_SF(2, 2, 2)
-  TLG_SF(2, 2, 3)
-  TLG_SF(2, 2, 4)
-  TLG_SF(2, 2, 5)
-  TLG_SF(2, 2, 6)
-  TLG_SF(2, 3, 2)
-  TLG_SF(2, 3, 3)
-  TLG_SF(2, 3, 4)
-  TLG_SF(2, 3, 5)
-  TLG_SF(2, 3, 6)
-#undef TLG_SF
-  *found = false;
-  return cudaSuccess;
-}
-
-}  // namespace
 
 cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t smem, int threads, cudaStream_t s,
                                bool* found) {
@@ -74,10 +40,11 @@ cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t sme
 
 cudaError_t launch_sumfact(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
                            bool* found) {
+  if (a.mask & kOutFacetNormals) return launch_sumfact_fn(precision, td, gd, n, a, smem, s, found);
   switch (precision) {
-    case 4: return launch_sf<float, false>(td, gd, n, a, smem, s, found);
-    case 8: return launch_sf<double, false>(td, gd, n, a, smem, s, found);
-    default: return launch_sf<float, true>(td, gd, n, a, smem, s, found);
+    case 4: return launch_sf<float, false, false>(td, gd, n, a, smem, s, found);
+    case 8: return launch_sf<double, false, false>(td, gd, n, a, smem, s, found);
+    default: return launch_sf<float, true, false>(td, gd, n, a, smem, s, found);
   }
 }
 

@@ -24,24 +24,36 @@
 #include <type_traits>
 
 #include "eval.cuh"
+#include "eval_launch.cuh"
 
 namespace tlg {
+
+// One tensor block of a point set: point q = o + a s[0] + b s[1] + c s[2] for a < m[0], b < m[1],
+// c < m[2]; per direction d the tables B_d [m_d][N] at off_b[d] and D_d at off_d[d] (bytes from the
+// section's start). Prisms: direction 0 the (x, y) points with psi at off_b[0], d_x psi at
+// off_d[0], d_y psi at off_d[1]; direction 2 the z points.
+struct SfBlock {
+  int o, m[3], s[3];
+  uint32_t off_b[3], off_d[3];
+  int pad[3];
+};
+static_assert(sizeof(SfBlock) == 64, "block headers are 64 bytes");
 
 struct SfArgs {
   const void* nodes;
   const uint32_t* dofmap;
   const uint32_t* flags;
-  const unsigned char* tab;  // staged: B_d [m_d][N], D_d [m_d][N] per direction, perm [K] u32
+  const unsigned char* tab;  // staged: nblocks SfBlock headers, the blocks' tables, perm [K] u32,
+                             // reference normals [Q][TD] (facet rules) at off_refn
   const double* dphi64;      // split: the f64 derivative table [Q][K][TD] (global) of the recompute
-  void* out[6];              // points, jacobian, detj, pinv, normals (facet normals: no tensor rule)
+  void* out[6];              // points, jacobian, detj, pinv, normals, facet normals
   int* err;
   unsigned long long* recomputed;
   int64_t first_cell, padded, range_cells, out_first_cell, last_cell, last_flag;
   double origin[3];
   float cond_limit;
-  uint32_t last_node, tab_bytes, off_b[3], off_d[3], off_perm, mask;
-  int m[3];  // points per direction (prisms: triangle points, 1, z points)
-  int qs[2];  // prisms: the point index strides of the triangle point and of the z point
+  uint32_t last_node, tab_bytes, off_perm, off_refn, mask;
+  int nblocks;
   int prism;  // the table is a prism's
   int num_points;
   int tile_shift;  // log2 of the output tile
@@ -50,10 +62,12 @@ struct SfArgs {
 // Shared memory of the coordinate slots: K * GD values of F per thread.
 inline size_t sumfact_slot_bytes(int k, int gd, size_t f_bytes) { return (size_t)k * gd * kEvalThreads * f_bytes; }
 
-// One point's outputs from X (relative, before the origin) and J.
-template <typename F, bool SPLIT, int TD, int GD>
+// One point's outputs from X (relative, before the origin) and J. FN: the facet normals are among
+// them (a separate instantiation: their epilogue costs up to 60 registers).
+template <typename F, bool SPLIT, int TD, int GD, bool FN>
 __device__ __forceinline__ void sf_point(const SfArgs& a, int q, int64_t tile_idx, int lane, F* x, F* j, F sign,
-                                         const F* xh, const F* xl, const uint32_t* row, int K, int64_t c) {
+                                         const F* xh, const F* xl, const uint32_t* row, int K, int64_t c,
+                                         const F* refn) {
   constexpr int LJ = TD * GD;
   using A = Ar<F>;
   using M = Factors<F, TD, GD>;
@@ -66,7 +80,7 @@ __device__ __forceinline__ void sf_point(const SfArgs& a, int q, int64_t tile_id
   }
   if ((mask & ~kOutPoints) == 0) return;
   F kk[LJ];
-  if ((mask & kOutPinv) || SPLIT) M::pinv(j, kk);
+  if ((mask & kOutPinv) || SPLIT || FN) M::pinv(j, kk);
   F dj = (mask & kOutDetJ) || SPLIT ? M::detj(j) : F(0);
   if constexpr (SPLIT) {
     const F kap = M::condition(j, kk);
@@ -86,6 +100,13 @@ __device__ __forceinline__ void sf_point(const SfArgs& a, int q, int64_t tile_id
   if (mask & kOutJacobian) store_point(static_cast<F*>(a.out[1]), tile_idx, q, nq, LJ, lane, a.tile_shift, j, LJ);
   if (mask & kOutDetJ) store_point(static_cast<F*>(a.out[2]), tile_idx, q, nq, 1, lane, a.tile_shift, &dj, 1);
   if (mask & kOutPinv) store_point(static_cast<F*>(a.out[3]), tile_idx, q, nq, LJ, lane, a.tile_shift, kk, LJ);
+  if constexpr (FN && TD == GD) {
+    if (mask & kOutFacetNormals) {
+      F n[GD];
+      M::facet_normal(kk, refn + q * TD, n);
+      store_point(static_cast<F*>(a.out[5]), tile_idx, q, nq, GD, lane, a.tile_shift, n, GD);
+    }
+  }
   if constexpr (TD + 1 == GD) {
     if (mask & kOutNormals) {
       F n[GD];
@@ -96,7 +117,7 @@ __device__ __forceinline__ void sf_point(const SfArgs& a, int q, int64_t tile_id
 }
 
 // F: arithmetic and output type; SPLIT: f64 nodes shifted by node 0 and rounded to F = float.
-template <typename F, bool SPLIT, int TD, int GD, int N>
+template <typename F, bool SPLIT, int TD, int GD, int N, bool FN>
 __global__ void __launch_bounds__(kEvalThreads) sumfact_kernel(const __grid_constant__ SfArgs a) {
   using NT = typename std::conditional<SPLIT, double, F>::type;  // node type
   using A = Ar<F>;
@@ -108,14 +129,9 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_kernel(const __grid_cons
   stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
   F* xs = reinterpret_cast<F*>(smem + (a.tab_bytes + 15) / 16 * 16) + threadIdx.x;
   const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
-  const F* B0 = reinterpret_cast<const F*>(smem + a.off_b[0]);
-  const F* D0 = reinterpret_cast<const F*>(smem + a.off_d[0]);
-  const F* B1 = reinterpret_cast<const F*>(smem + a.off_b[1]);
-  const F* D1 = reinterpret_cast<const F*>(smem + a.off_d[1]);
-  const F* B2 = reinterpret_cast<const F*>(smem + a.off_b[2]);
-  const F* D2 = reinterpret_cast<const F*>(smem + a.off_d[2]);
+  const SfBlock* blocks = reinterpret_cast<const SfBlock*>(smem);
+  const F* refn = reinterpret_cast<const F*>(smem + a.off_refn);
   const NT* nodes = static_cast<const NT*>(a.nodes);
-  const int m0 = a.m[0], m1 = a.m[1], m2 = TD == 3 ? a.m[2] : 1;
   const uint32_t mask = a.mask;
 
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
@@ -163,108 +179,120 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_kernel(const __grid_cons
     const int64_t tile_idx = o >> a.tile_shift;
     const int lane = (int)(o & ((1 << a.tile_shift) - 1));
 
-    if constexpr (TD == 3) {
-      for (int c2 = 0; c2 < m2; ++c2) {
-        F U[GD][N][N], V[GD][N][N];
-#pragma unroll
-        for (int g = 0; g < GD; ++g)
-#pragma unroll
-          for (int jj = 0; jj < N; ++jj)
-#pragma unroll
-            for (int i = 0; i < N; ++i) U[g][jj][i] = V[g][jj][i] = F(0);
-#pragma unroll
-        for (int k = 0; k < N; ++k) {
-          const F bk = B2[c2 * N + k], dk = D2[c2 * N + k];
-#pragma unroll
-          for (int jj = 0; jj < N; ++jj)
-#pragma unroll
-            for (int i = 0; i < N; ++i)
-#pragma unroll
-              for (int g = 0; g < GD; ++g) {
-                const F xv = xs[((i + N * (jj + N * k)) * GD + g) * T];
-                U[g][jj][i] = A::fma(xv, bk, U[g][jj][i]);
-                V[g][jj][i] = A::fma(xv, dk, V[g][jj][i]);
-              }
-        }
-        for (int b1 = 0; b1 < m1; ++b1) {
-          F UU[GD][N], UD[GD][N], VU[GD][N];
+    for (int bk = 0; bk < a.nblocks; ++bk) {
+      const SfBlock& h = blocks[bk];
+      const F* B0 = reinterpret_cast<const F*>(smem + h.off_b[0]);
+      const F* D0 = reinterpret_cast<const F*>(smem + h.off_d[0]);
+      const F* B1 = reinterpret_cast<const F*>(smem + h.off_b[1]);
+      const F* D1 = reinterpret_cast<const F*>(smem + h.off_d[1]);
+      const F* B2 = reinterpret_cast<const F*>(smem + h.off_b[2]);
+      const F* D2 = reinterpret_cast<const F*>(smem + h.off_d[2]);
+      const int m0 = h.m[0], m1 = h.m[1], m2 = TD == 3 ? h.m[2] : 1;
+      const int s0 = h.s[0], s1 = h.s[1], s2 = h.s[2], qo = h.o;
+      if constexpr (TD == 3) {
+        for (int c2 = 0; c2 < m2; ++c2) {
+          F U[GD][N][N], V[GD][N][N];
 #pragma unroll
           for (int g = 0; g < GD; ++g)
 #pragma unroll
-            for (int i = 0; i < N; ++i) UU[g][i] = UD[g][i] = VU[g][i] = F(0);
+            for (int jj = 0; jj < N; ++jj)
+#pragma unroll
+              for (int i = 0; i < N; ++i) U[g][jj][i] = V[g][jj][i] = F(0);
+#pragma unroll
+          for (int k = 0; k < N; ++k) {
+            const F bk = B2[c2 * N + k], dk = D2[c2 * N + k];
+#pragma unroll
+            for (int jj = 0; jj < N; ++jj)
+#pragma unroll
+              for (int i = 0; i < N; ++i)
+#pragma unroll
+                for (int g = 0; g < GD; ++g) {
+                  const F xv = xs[((i + N * (jj + N * k)) * GD + g) * T];
+                  U[g][jj][i] = A::fma(xv, bk, U[g][jj][i]);
+                  V[g][jj][i] = A::fma(xv, dk, V[g][jj][i]);
+                }
+          }
+          for (int b1 = 0; b1 < m1; ++b1) {
+            F UU[GD][N], UD[GD][N], VU[GD][N];
+#pragma unroll
+            for (int g = 0; g < GD; ++g)
+#pragma unroll
+              for (int i = 0; i < N; ++i) UU[g][i] = UD[g][i] = VU[g][i] = F(0);
+#pragma unroll
+            for (int jj = 0; jj < N; ++jj) {
+              const F bj = B1[b1 * N + jj], dj = D1[b1 * N + jj];
+#pragma unroll
+              for (int g = 0; g < GD; ++g)
+#pragma unroll
+                for (int i = 0; i < N; ++i) {
+                  UU[g][i] = A::fma(U[g][jj][i], bj, UU[g][i]);
+                  UD[g][i] = A::fma(U[g][jj][i], dj, UD[g][i]);
+                  VU[g][i] = A::fma(V[g][jj][i], bj, VU[g][i]);
+                }
+            }
+            for (int a0 = 0; a0 < m0; ++a0) {
+              F x[GD], j[LJ];
+#pragma unroll
+              for (int g = 0; g < GD; ++g) {
+                F s = F(0), j0 = F(0), j1 = F(0), j2 = F(0);
+#pragma unroll
+                for (int i = 0; i < N; ++i) {
+                  const F bi = B0[a0 * N + i], di = D0[a0 * N + i];
+                  s = A::fma(UU[g][i], bi, s);
+                  j0 = A::fma(UU[g][i], di, j0);
+                  j1 = A::fma(UD[g][i], bi, j1);
+                  j2 = A::fma(VU[g][i], bi, j2);
+                }
+                x[g] = s;
+                j[0 * GD + g] = j0;
+                j[1 * GD + g] = j1;
+                j[2 * GD + g] = j2;
+              }
+              sf_point<F, SPLIT, TD, GD, FN>(a, qo + a0 * s0 + b1 * s1 + c2 * s2, tile_idx, lane, x, j, sign, xh, xl, row, K,
+                                         c, refn);
+            }
+          }
+        }
+      } else {
+        for (int b1 = 0; b1 < m1; ++b1) {
+          F U[GD][N], V[GD][N];
+#pragma unroll
+          for (int g = 0; g < GD; ++g)
+#pragma unroll
+            for (int i = 0; i < N; ++i) U[g][i] = V[g][i] = F(0);
 #pragma unroll
           for (int jj = 0; jj < N; ++jj) {
             const F bj = B1[b1 * N + jj], dj = D1[b1 * N + jj];
 #pragma unroll
-            for (int g = 0; g < GD; ++g)
+            for (int i = 0; i < N; ++i)
 #pragma unroll
-              for (int i = 0; i < N; ++i) {
-                UU[g][i] = A::fma(U[g][jj][i], bj, UU[g][i]);
-                UD[g][i] = A::fma(U[g][jj][i], dj, UD[g][i]);
-                VU[g][i] = A::fma(V[g][jj][i], bj, VU[g][i]);
+              for (int g = 0; g < GD; ++g) {
+                const F xv = xs[((i + N * jj) * GD + g) * T];
+                U[g][i] = A::fma(xv, bj, U[g][i]);
+                V[g][i] = A::fma(xv, dj, V[g][i]);
               }
           }
           for (int a0 = 0; a0 < m0; ++a0) {
             F x[GD], j[LJ];
 #pragma unroll
             for (int g = 0; g < GD; ++g) {
-              F s = F(0), j0 = F(0), j1 = F(0), j2 = F(0);
+              F s = F(0), j0 = F(0), j1 = F(0);
 #pragma unroll
               for (int i = 0; i < N; ++i) {
                 const F bi = B0[a0 * N + i], di = D0[a0 * N + i];
-                s = A::fma(UU[g][i], bi, s);
-                j0 = A::fma(UU[g][i], di, j0);
-                j1 = A::fma(UD[g][i], bi, j1);
-                j2 = A::fma(VU[g][i], bi, j2);
+                s = A::fma(U[g][i], bi, s);
+                j0 = A::fma(U[g][i], di, j0);
+                j1 = A::fma(V[g][i], bi, j1);
               }
               x[g] = s;
               j[0 * GD + g] = j0;
               j[1 * GD + g] = j1;
-              j[2 * GD + g] = j2;
             }
-            sf_point<F, SPLIT, TD, GD>(a, a0 + m0 * (b1 + m1 * c2), tile_idx, lane, x, j, sign, xh, xl, row, K, c);
+            sf_point<F, SPLIT, TD, GD, FN>(a, qo + a0 * s0 + b1 * s1, tile_idx, lane, x, j, sign, xh, xl, row, K, c, refn);
           }
         }
       }
-    } else {
-      for (int b1 = 0; b1 < m1; ++b1) {
-        F U[GD][N], V[GD][N];
-#pragma unroll
-        for (int g = 0; g < GD; ++g)
-#pragma unroll
-          for (int i = 0; i < N; ++i) U[g][i] = V[g][i] = F(0);
-#pragma unroll
-        for (int jj = 0; jj < N; ++jj) {
-          const F bj = B1[b1 * N + jj], dj = D1[b1 * N + jj];
-#pragma unroll
-          for (int i = 0; i < N; ++i)
-#pragma unroll
-            for (int g = 0; g < GD; ++g) {
-              const F xv = xs[((i + N * jj) * GD + g) * T];
-              U[g][i] = A::fma(xv, bj, U[g][i]);
-              V[g][i] = A::fma(xv, dj, V[g][i]);
-            }
-        }
-        for (int a0 = 0; a0 < m0; ++a0) {
-          F x[GD], j[LJ];
-#pragma unroll
-          for (int g = 0; g < GD; ++g) {
-            F s = F(0), j0 = F(0), j1 = F(0);
-#pragma unroll
-            for (int i = 0; i < N; ++i) {
-              const F bi = B0[a0 * N + i], di = D0[a0 * N + i];
-              s = A::fma(U[g][i], bi, s);
-              j0 = A::fma(U[g][i], di, j0);
-              j1 = A::fma(V[g][i], bi, j1);
-            }
-            x[g] = s;
-            j[0 * GD + g] = j0;
-            j[1 * GD + g] = j1;
-          }
-          sf_point<F, SPLIT, TD, GD>(a, a0 + m0 * b1, tile_idx, lane, x, j, sign, xh, xl, row, K, c);
-        }
-      }
-    }
+    }  // blocks
   }
 }
 
@@ -276,10 +304,11 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_kernel(const __grid_cons
 // then per z point j with the interval basis:
 //   X_g = sum_c BV_g[c] l_c(z_j), J(g, 0) = sum_c BX_g[c] l_c(z_j), J(g, 1) = sum_c BY_g[c] l_c(z_j),
 //   J(g, 2) = sum_c BV_g[c] l_c'(z_j):
-// 3 NT N per triangle point and 4 N per point and coordinate instead of 4 NT N per point. Table:
-// psi [m_t][NT] at off_b[0], d_x psi at off_d[0], d_y psi at off_d[1], l [m_z][N] at off_b[2], l' at
-// off_d[2]; perm maps the index c NT + t to the Lagrange node; point q = i qs[0] + j qs[1].
-template <typename F, bool SPLIT, int N>
+// 3 NT N per triangle point and 4 N per point and coordinate instead of 4 NT N per point. Per
+// block: psi [m_t][NT] at off_b[0], d_x psi at off_d[0], d_y psi at off_d[1], l [m_z][N] at
+// off_b[2], l' at off_d[2]; perm maps the index c NT + t to the Lagrange node; point
+// q = o + i s[0] + j s[2].
+template <typename F, bool SPLIT, int N, bool FN>
 __global__ void __launch_bounds__(kEvalThreads) sumfact_prism_kernel(const __grid_constant__ SfArgs a) {
   using NT_ = typename std::conditional<SPLIT, double, F>::type;  // node type
   using A = Ar<F>;
@@ -290,13 +319,9 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_prism_kernel(const __gri
   stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
   F* xs = reinterpret_cast<F*>(smem + (a.tab_bytes + 15) / 16 * 16) + threadIdx.x;
   const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
-  const F* PV = reinterpret_cast<const F*>(smem + a.off_b[0]);
-  const F* PX = reinterpret_cast<const F*>(smem + a.off_d[0]);
-  const F* PY = reinterpret_cast<const F*>(smem + a.off_d[1]);
-  const F* LV = reinterpret_cast<const F*>(smem + a.off_b[2]);
-  const F* LD = reinterpret_cast<const F*>(smem + a.off_d[2]);
+  const SfBlock* blocks = reinterpret_cast<const SfBlock*>(smem);
+  const F* refn = reinterpret_cast<const F*>(smem + a.off_refn);
   const NT_* nodes = static_cast<const NT_*>(a.nodes);
-  const int mt = a.m[0], mz = a.m[2], st = a.qs[0], sz = a.qs[1];
 
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < a.padded;
        c += (int64_t)gridDim.x * blockDim.x) {
@@ -337,48 +362,93 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_prism_kernel(const __gri
     const int64_t tile_idx = o >> a.tile_shift;
     const int lane = (int)(o & ((1 << a.tile_shift) - 1));
 
-    for (int i = 0; i < mt; ++i) {
-      F bv[GD][N], bx[GD][N], by[GD][N];
+    for (int bk = 0; bk < a.nblocks; ++bk) {
+      const SfBlock& h = blocks[bk];
+      const F* PV = reinterpret_cast<const F*>(smem + h.off_b[0]);
+      const F* PX = reinterpret_cast<const F*>(smem + h.off_d[0]);
+      const F* PY = reinterpret_cast<const F*>(smem + h.off_d[1]);
+      const F* LV = reinterpret_cast<const F*>(smem + h.off_b[2]);
+      const F* LD = reinterpret_cast<const F*>(smem + h.off_d[2]);
+      const int mt = h.m[0], mz = h.m[2], st = h.s[0], sz = h.s[2], qo = h.o;
+      for (int i = 0; i < mt; ++i) {
+        F bv[GD][N], bx[GD][N], by[GD][N];
 #pragma unroll
-      for (int g = 0; g < GD; ++g)
+        for (int g = 0; g < GD; ++g)
 #pragma unroll
-        for (int cc = 0; cc < N; ++cc) bv[g][cc] = bx[g][cc] = by[g][cc] = F(0);
-      // (f64 P3: a rolled loop, the unrolled one spills.)
+          for (int cc = 0; cc < N; ++cc) bv[g][cc] = bx[g][cc] = by[g][cc] = F(0);
+        // (f64 P3: a rolled loop, the unrolled one spills.)
 #pragma unroll(sizeof(F) == 8 && N >= 4 ? 1 : NT)
-      for (int t = 0; t < NT; ++t) {
-        const F w = PV[i * NT + t], wx = PX[i * NT + t], wy = PY[i * NT + t];
+        for (int t = 0; t < NT; ++t) {
+          const F w = PV[i * NT + t], wx = PX[i * NT + t], wy = PY[i * NT + t];
 #pragma unroll
-        for (int cc = 0; cc < N; ++cc)
+          for (int cc = 0; cc < N; ++cc)
+#pragma unroll
+            for (int g = 0; g < GD; ++g) {
+              const F xv = xs[((cc * NT + t) * GD + g) * T];
+              bv[g][cc] = A::fma(xv, w, bv[g][cc]);
+              bx[g][cc] = A::fma(xv, wx, bx[g][cc]);
+              by[g][cc] = A::fma(xv, wy, by[g][cc]);
+            }
+        }
+        for (int jz = 0; jz < mz; ++jz) {
+          F x[GD], j[LJ];
 #pragma unroll
           for (int g = 0; g < GD; ++g) {
-            const F xv = xs[((cc * NT + t) * GD + g) * T];
-            bv[g][cc] = A::fma(xv, w, bv[g][cc]);
-            bx[g][cc] = A::fma(xv, wx, bx[g][cc]);
-            by[g][cc] = A::fma(xv, wy, by[g][cc]);
-          }
-      }
-      for (int jz = 0; jz < mz; ++jz) {
-        F x[GD], j[LJ];
+            F s0 = F(0), j0 = F(0), j1 = F(0), j2 = F(0);
 #pragma unroll
-        for (int g = 0; g < GD; ++g) {
-          F s0 = F(0), j0 = F(0), j1 = F(0), j2 = F(0);
-#pragma unroll
-          for (int cc = 0; cc < N; ++cc) {
-            const F l = LV[jz * N + cc], ld = LD[jz * N + cc];
-            s0 = A::fma(bv[g][cc], l, s0);
-            j0 = A::fma(bx[g][cc], l, j0);
-            j1 = A::fma(by[g][cc], l, j1);
-            j2 = A::fma(bv[g][cc], ld, j2);
+            for (int cc = 0; cc < N; ++cc) {
+              const F l = LV[jz * N + cc], ld = LD[jz * N + cc];
+              s0 = A::fma(bv[g][cc], l, s0);
+              j0 = A::fma(bx[g][cc], l, j0);
+              j1 = A::fma(by[g][cc], l, j1);
+              j2 = A::fma(bv[g][cc], ld, j2);
+            }
+            x[g] = s0;
+            j[0 * GD + g] = j0;
+            j[1 * GD + g] = j1;
+            j[2 * GD + g] = j2;
           }
-          x[g] = s0;
-          j[0 * GD + g] = j0;
-          j[1 * GD + g] = j1;
-          j[2 * GD + g] = j2;
+          sf_point<F, SPLIT, TD, GD, FN>(a, qo + i * st + jz * sz, tile_idx, lane, x, j, F(1), xh, xl, row, K, c, refn);
         }
-        sf_point<F, SPLIT, TD, GD>(a, i * st + jz * sz, tile_idx, lane, x, j, F(1), xh, xl, row, K, c);
       }
-    }
+    }  // blocks
   }
+}
+
+
+// Dispatch of the forward sum-factorised kernels (instantiated in sumfact.cu without, and in
+// sumfact_fn.cu with, facet normals).
+template <typename F, bool SPLIT, bool FN>
+cudaError_t launch_sf(int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s, bool* found) {
+  *found = true;
+  if (a.prism) {
+    if (n == 2) return launch_persistent(sumfact_prism_kernel<F, SPLIT, 2, FN>, a, a.padded, smem, s);
+    if (n == 3) return launch_persistent(sumfact_prism_kernel<F, SPLIT, 3, FN>, a, a.padded, smem, s);
+    if (n == 4) return launch_persistent(sumfact_prism_kernel<F, SPLIT, 4, FN>, a, a.padded, smem, s);
+    *found = false;
+    return cudaSuccess;
+  }
+#define TLG_SF(TD, GD, NN) \
+  if (td == TD && gd == GD && n == NN) \
+    return launch_persistent(sumfact_kernel<F, SPLIT, TD, GD, NN, FN>, a, a.padded, smem, s);
+  TLG_SF(3, 3, 2)
+  TLG_SF(3, 3, 3)
+  TLG_SF(3, 3, 4)
+  TLG_SF(2, 2, 2)
+  TLG_SF(2, 2, 3)
+  TLG_SF(2, 2, 4)
+  TLG_SF(2, 2, 5)
+  TLG_SF(2, 2, 6)
+  if constexpr (!FN) {  // facet normals need codimension 0
+    TLG_SF(2, 3, 2)
+    TLG_SF(2, 3, 3)
+    TLG_SF(2, 3, 4)
+    TLG_SF(2, 3, 5)
+    TLG_SF(2, 3, 6)
+  }
+#undef TLG_SF
+  *found = false;
+  return cudaSuccess;
 }
 
 }  // namespace tlg

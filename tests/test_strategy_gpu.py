@@ -161,12 +161,11 @@ def test_prism_rules_in_both_orders(cuda, order, precision):
 
 
 def test_prism_without_a_product_rule(cuda):
-    """Points that are not a triangle rule times z points run another family under sumfact."""
+    """Points that are not unions of (x, y) sets times z sets run loops under sumfact."""
     mesh = meshes.curved_box("Prism", 2, 2, jitter=0.02)
     g = tg.Geometry.from_host(mesh, dtype=F64)
-    pts, _ = tg.refcell.gauss_rule("Prism", 4)
-    pts = pts.copy()
-    pts[0, 2] += 1e-3
+    rng = np.random.default_rng(12)
+    pts = rng.uniform(0.05, 0.45, size=(20, 3))
     with tg.with_strategy("sumfact"):
         tg.geometric_factors_block(g, 0, tg.PointSet("Prism", pts, np.ones(len(pts))), ("detj",))
         assert tg.last_kernel_family() != "sumfact"
@@ -323,3 +322,52 @@ def test_forced_strategy_that_does_not_apply_runs_loops(cuda):
         with tg.with_strategy(strat):
             tg.geometric_factors_block(g, 0, ps, ("detj",))
             assert tg.last_kernel_family() == "loops", strat
+
+
+@pytest.mark.parametrize("precision", ["f64", "split"])
+@pytest.mark.parametrize("cell,n,degree,fdeg", [("Quadrilateral", 3, 2, 4), ("Quadrilateral", 2, 3, 6),
+                                                ("Hexahedron", 2, 1, 2), ("Hexahedron", 2, 2, 4),
+                                                ("Hexahedron", 2, 3, 6), ("Prism", 2, 1, 2), ("Prism", 2, 2, 4),
+                                                ("Prism", 2, 3, 6)])
+def test_sumfact_on_facet_rules(cuda, cell, n, degree, fdeg, precision):
+    """Facet rules are unions of tensor blocks (one per facet): det J, K and the facet normals run
+    sum-factorised and agree with the loops kernel (the reference's
+    forced_sumfact_runs_for_derived_factors_and_facet_rules, tests/strategy.rs:363-438)."""
+    mesh = mesh_for(cell, n, degree, 2 if cell == "Quadrilateral" else 3)
+    g = tg.Geometry.from_host(mesh, dtype=F64)
+    ps = tg.facet_point_set(cell, fdeg)
+    names = ("detj", "pinv", "facet_normals")
+    prec = "split" if precision == "split" else "native"
+    with tg.with_strategy("sumfact"):
+        got = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+        assert tg.last_kernel_family() == "sumfact"
+    with tg.with_strategy("loops"):
+        want = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+        assert tg.last_kernel_family() == "loops"
+    tol = 1e-13 if precision == "f64" else 2e-5
+    for f in names:
+        assert orc.rel_err(got[f].to_host_cell_major(), want[f].to_host_cell_major()) < tol, f
+    absx = g.nodes.double().cpu().numpy() + np.array(g.origin[:g.gdim])
+    ref = orc.eval_block(cell, degree, absx, mesh.blocks[0].cells, ps.points, factors=("detj",))
+    assert orc.rel_err(got["detj"].to_host_cell_major(), ref["detj"]) < (1e-12 if precision == "f64" else 1e-5)
+
+
+@pytest.mark.parametrize("cell,degree,rdeg,dtype,prec", [
+    ("Hexahedron", 2, 4, F64, "native"), ("Hexahedron", 3, 6, F64, "split"), ("Tetrahedron", 4, 5, F64, "split"),
+    ("Tetrahedron", 2, 4, F32, "native"), ("Prism", 3, 6, F32, "native"), ("Triangle", 6, 8, F64, "native")])
+def test_policy_matches_its_forced_choice_bitwise(cuda, cell, degree, rdeg, dtype, prec):
+    """Under the policy the values are those of forcing the strategy it chose, bit for bit
+    (tests/strategy.rs:138-182)."""
+    mesh = high_mesh(cell, 2, degree, 2 if cell == "Triangle" else 3)
+    g = tg.Geometry.from_host(mesh, dtype=dtype)
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    names = ("points", "jacobian", "detj", "pinv")
+    with tg.record_strategies() as rec:
+        auto = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+    chosen = rec[-1][1]
+    with tg.with_strategy(chosen):
+        forced = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+        assert tg.last_kernel_family() == chosen
+    for f in names:
+        assert torch.equal(auto[f].chunks[0].data, forced[f].chunks[0].data), (f, chosen)
