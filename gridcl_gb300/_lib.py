@@ -71,7 +71,8 @@ class TlgOutputs(ctypes.Structure):
 
 
 class TlgCotangents(ctypes.Structure):
-    _fields_ = [("points", ctypes.c_void_p), ("detj", ctypes.c_void_p), ("pinv", ctypes.c_void_p)]
+    _fields_ = [("points", ctypes.c_void_p), ("detj", ctypes.c_void_p), ("pinv", ctypes.c_void_p),
+                ("normals", ctypes.c_void_p)]
 
 
 # (name, restype, argtypes) of every entry point declared in include/tlgeom.h.

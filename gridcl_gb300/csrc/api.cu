@@ -1227,6 +1227,60 @@ tlg_status vjp_sumfact(const tlg_tables* t, const tlg::VjpArgs& v, cudaStream_t 
   return ok();
 }
 
+// The adjoint below codimension 0 (vjp_surface.cu) from the node-row kernel's arguments: phi and
+// dphi staged when they and the thread slots (2 K GD values per thread) fit, else read from global
+// memory; 32 to 128 threads per CTA.
+tlg_status vjp_surface(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, const tlg_cotangents* ct,
+                       const tlg::VjpArgs& v, cudaStream_t s) {
+  const bool split = t->dtype == TLG_SPLIT32;
+  const size_t fbytes = split ? 4 : 8;
+  const size_t per_thread = 2 * (size_t)t->k * t->gd * fbytes;
+  const size_t budget = (size_t)227 * 1024;
+  const size_t prefix = (size_t)t->off_refn;  // phi and dphi
+  bool global = !(prefix + 32 * per_thread <= budget);
+  const size_t avail = budget - (global ? 0 : prefix);
+  int threads = (int)std::min<size_t>(128, avail / per_thread / 32 * 32);
+  if (threads < 32) return fail(TLG_ERR_ALLOCATION_TOO_LARGE, "tlg_vjp_block: too many nodes per cell");
+  tlg::VjpSurfArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = v.nodes;
+  a.dofmap = v.dofmap;
+  a.flags = b->flags;
+  a.tab = t->dev;
+  a.ct[0] = ct->points;
+  a.ct[1] = ct->detj;
+  a.ct[2] = ct->pinv;
+  a.ct[3] = ct->normals;
+  a.out[0] = o->points;
+  a.out[1] = o->jacobian;
+  a.out[2] = o->detj;
+  a.out[3] = o->pinv;
+  a.out[4] = o->normals;
+  a.local = v.local;
+  a.err = v.err;
+  a.first_cell = v.first_cell;
+  a.padded = v.padded;
+  a.out_first_cell = v.out_first_cell;
+  a.last_cell = v.last_cell;
+  a.range_end = v.range_end;
+  const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
+  a.last_flag = nflags - 1;
+  for (int g = 0; g < 3; ++g) a.origin[g] = v.origin[g];
+  a.last_node = v.last_node;
+  a.tab_bytes = global ? 0 : (uint32_t)prefix;
+  a.off_dphi = t->off_dphi;
+  a.k = (int)t->k;
+  a.num_points = v.num_points;
+  a.tab_global = global ? 1 : 0;
+  const size_t smem = (global ? 0 : (prefix + 15) / 16 * 16) + (size_t)threads * per_thread;
+  bool found = false;
+  cudaError_t e = tlg::launch_vjp_surface(split, t->td, t->gd, a, smem, threads, s, &found);
+  if (!found) return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: no adjoint kernel for this element");
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_block launch");
+  g_last_family = TLG_STRATEGY_LOOPS;
+  return ok();
+}
+
 }  // namespace
 
 tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o,
@@ -1235,11 +1289,11 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
   if (t->dtype != TLG_F64 && t->dtype != TLG_SPLIT32)
     return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: the adjoint runs with f64 or split-precision tables");
   if (b->dtype != TLG_F64) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: the adjoint reads f64 meshes");
-  if (t->td != t->gd || b->gdim != t->gd)
-    return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: the adjoint needs a block of codimension 0");
+  if (b->gdim != t->gd) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: block and tables differ in gdim");
   if (o->tile != 16) return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: the adjoint runs with tile 16");
-  if (o->normals || o->facet_normals)
-    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: no normals in the fused forward");
+  if (o->facet_normals) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: no facet normals in the fused forward");
+  if ((o->normals || ct->normals) && t->td + 1 != t->gd)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: normals exist for TD + 1 = GD only");
   if (o->first_cell < 0 || o->num_cells < 0 || o->first_cell + o->num_cells > b->num_cells ||
       o->out_first_cell < 0 || o->out_first_cell % 16 != 0)
     return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: bad cell range");
@@ -1272,6 +1326,12 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
   const bool split = t->dtype == TLG_SPLIT32;
   a.num_points = (int)t->q;
   if (t->q == 0) return ok();
+  // The adjoint follows the Jacobian family's strategy: sum factorisation where wanted (or AUTO)
+  // and it applies, else the node-row kernel (the kernel below codimension 0 has K at run time).
+  int strategy = TLG_STRATEGY_AUTO;
+  if (!wanted_strategy(TLG_FAMILY_JACOBIAN, &strategy)) return TLG_ERR_INVALID_ARGUMENT;
+  g_last_kind = TLG_FAMILY_JACOBIAN;
+  if (t->td < t->gd) return vjp_surface(t, b, o, ct, a, static_cast<cudaStream_t>(stream));
   if (t->vjp_bytes == 0)
     return fail(TLG_ERR_ALLOCATION_TOO_LARGE, "tlg_vjp_block: the adjoint's table exceeds 160 KiB of shared memory");
   const size_t smem = (t->vjp_bytes + 15) / 16 * 16 + tlg::vjp_stage_bytes(split, t->td, (int)t->k);
@@ -1280,11 +1340,6 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
                                                   " bytes) exceed 227 KiB of shared memory");
   bool found = false;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // The adjoint follows the Jacobian family's strategy: sum factorisation where wanted (or AUTO)
-  // and it applies, else the node-row kernel.
-  int strategy = TLG_STRATEGY_AUTO;
-  if (!wanted_strategy(TLG_FAMILY_JACOBIAN, &strategy)) return TLG_ERR_INVALID_ARGUMENT;
-  g_last_kind = TLG_FAMILY_JACOBIAN;
   if (strategy == TLG_STRATEGY_SUMFACT || (strategy == TLG_STRATEGY_AUTO && vjp_sumfact_preferred(t))) {
     tlg_status st = vjp_sumfact(t, a, s, &found);
     if (found) return st;

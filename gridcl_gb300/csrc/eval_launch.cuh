@@ -95,6 +95,10 @@ cudaError_t launch_coop(int precision, int td, int gd, int k, const CoopArgs& a,
                         bool* found);
 
 struct VjpArgs;
+struct VjpSurfArgs;
+// Defined in vjp_surface.cu: the adjoint below codimension 0 (TD < GD), `threads` per CTA.
+cudaError_t launch_vjp_surface(bool split, int td, int gd, const VjpSurfArgs& a, size_t smem, int threads,
+                               cudaStream_t s, bool* found);
 // Defined in vjp_f64.cu / vjp_split.cu; `found` is false when no kernel exists for (d, k). `smem`
 // is the dynamic shared memory: the staged tables (rounded up to 16 bytes) and the staging slots.
 cudaError_t launch_vjp_f64(int d, int k, const VjpArgs& a, size_t smem, cudaStream_t s, bool* found);

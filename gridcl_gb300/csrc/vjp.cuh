@@ -36,6 +36,22 @@
 
 namespace tlg {
 
+// Arguments of the adjoint below codimension 0 (vjp_surface.cu).
+struct VjpSurfArgs {
+  const void* nodes;
+  const uint32_t* dofmap;
+  const uint32_t* flags;
+  const unsigned char* tab;  // phi [Q][K] at 0, dphi [Q][K][TD] at off_dphi (staged unless tab_global)
+  const void* ct[4];         // cotangents: points, detj (area element), pinv, normals, or null
+  void* out[5];              // fused forward: points, jacobian, detj, pinv, normals, or null
+  void* local;               // contributions [cell][K][R]
+  int* err;
+  int64_t first_cell, padded, out_first_cell, last_cell, range_end, last_flag;
+  double origin[3];
+  uint32_t last_node, tab_bytes, off_dphi;
+  int k, num_points, tab_global;
+};
+
 struct VjpArgs {
   const void* nodes;
   const uint32_t* dofmap;

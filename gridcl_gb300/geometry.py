@@ -538,16 +538,15 @@ def node_incidence(g: Geometry, b: int) -> NodeIncidence:
 def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: str = "native",
               forward=(), out: dict | None = None, local: torch.Tensor | None = None):
     """Cotangents of the node coordinates (``[node][GD]`` f64) for the cotangent fields
-    ``{"points", "detj", "pinv"}`` (QuadFields of tile 16, f64, or f32 with
-    ``precision="split"``; missing entries are zero) of block b, codimension 0. J, det J and K
-    are recomputed. The factors named in `forward` are evaluated in the same pass (fused
-    forward + adjoint) and returned: ``(grad, fields)``."""
+    ``{"points", "detj", "pinv", "normals"}`` (QuadFields of tile 16, f64, or f32 with
+    ``precision="split"``; missing entries are zero; "detj" is the area element and "normals"
+    the unit normals of curves and surfaces, TD + 1 = GD) of block b. J, det J and K are
+    recomputed. The factors named in `forward` are evaluated in the same pass (fused forward +
+    adjoint) and returned: ``(grad, fields)``."""
     from ._lib import TlgCotangents
 
     blk = g.blocks[b]
     td, gd = blk.element.tdim, g.gdim
-    if td != gd:
-        raise GridError(4, "the adjoint needs a block of codimension 0")
     if g.dtype != torch.float64:
         raise GridError(1, "the adjoint reads f64 meshes")
     if precision == "split":
@@ -559,7 +558,7 @@ def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: s
     else:
         raise GridError(1, f"unknown precision {precision!r}")
     for name in forward:
-        if name not in ("points", "jacobian", "detj", "pinv"):
+        if name not in ("points", "jacobian", "detj", "pinv", "normals") or (name == "normals" and td + 1 != gd):
             raise GridError(1, f"no fused forward factor {name}")
     k = blk.element.nodes_per_cell
     nq = len(pts)
@@ -570,7 +569,7 @@ def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: s
     if local is None:
         local = torch.empty((max(blk.num_cells, 1), k, 4 if gd == 3 else gd), dtype=fdt, device=dev)
     ct = TlgCotangents()
-    for name in ("points", "detj", "pinv"):
+    for name in ("points", "detj", "pinv", "normals"):
         f = cotangents.get(name)
         if f is not None:
             if f.tile != GPU_QUAD_TILE or len(f.chunks) != 1 or f.chunks[0].data.dtype != fdt:
@@ -646,12 +645,13 @@ class Batch:
 
 def fd_check(g: Geometry, b: int, pts: PointSet, cotangents: dict, grad: np.ndarray, sample,
              h: float = 1e-6) -> dict:
-    """Central differences of L = sum over cells and points of (xbar . x + dbar det J + Kbar : K)
-    against the node cotangents `grad` ([node][GD]) at the node indices `sample`, with the f64
-    forward kernels. Each (node, coordinate, sign) perturbs a private copy of the cells around the
-    node only (the other cells do not change L), and all copies are evaluated in one launch.
-    `cotangents` holds cell-major host arrays ("points" [c][q][GD], "detj" [c][q], "pinv"
-    [c][q][TD GD]), missing ones zero. Returns the largest |fd - grad| / max(1, |grad|)."""
+    """Central differences of L = sum over cells and points of (xbar . x + dbar det J + Kbar : K
+    + nbar . n) against the node cotangents `grad` ([node][GD]) at the node indices `sample`, with
+    the f64 forward kernels. Each (node, coordinate, sign) perturbs a private copy of the cells
+    around the node only (the other cells do not change L), and all copies are evaluated in one
+    launch. `cotangents` holds cell-major host arrays ("points" [c][q][GD], "detj" [c][q], "pinv"
+    [c][q][TD GD], "normals" [c][q][GD]), missing ones zero. Returns the largest
+    |fd - grad| / max(1, |grad|)."""
     blk = g.blocks[b]
     k = blk.element.nodes_per_cell
     gd = g.gdim
@@ -682,9 +682,12 @@ def fd_check(g: Geometry, b: int, pts: PointSet, cotangents: dict, grad: np.ndar
                 nodes[(start + j) * k + kk, c] += s * h
         start += cells.size
     sub_dofmap = np.arange(all_cells.size * k, dtype=np.uint32).reshape(-1, k)
-    sub = Geometry([GeometryBlock(blk.element, torch.from_numpy(sub_dofmap.view(np.int32)).to(g.nodes.device))],
+    sub_flags = None if blk.flags is None or blk.flags.numel() == 0 else \
+        blk.flags[torch.from_numpy(np.minimum(all_cells, blk.flags.numel() - 1).astype(np.int64)).to(blk.flags.device)]
+    sub = Geometry([GeometryBlock(blk.element, torch.from_numpy(sub_dofmap.view(np.int32)).to(g.nodes.device),
+                                  sub_flags)],
                    torch.from_numpy(nodes).to(g.nodes.device), g.origin)
-    names = [f for f in ("points", "detj", "pinv") if cotangents.get(f) is not None]
+    names = [f for f in ("points", "detj", "pinv", "normals") if cotangents.get(f) is not None]
     fields = geometric_factors_block(sub, 0, pts, names)
     per_cell = np.zeros(all_cells.size)
     for f in names:

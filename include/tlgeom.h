@@ -213,14 +213,18 @@ tlg_status tlg_csr_build(const uint32_t* dofmap, int64_t num_cells, int nodes_pe
 
 /* Cotangent fields (QuadField chunks of the evaluated range, tile 16); NULL means zero. */
 typedef struct tlg_cotangents {
-  const void* points; /* dL/dx, GD components */
-  const void* detj;   /* dL/d(det J) */
-  const void* pinv;   /* dL/dK, TD * GD components, K(t, g) at g * TD + t */
+  const void* points;  /* dL/dx, GD components */
+  const void* detj;    /* dL/d(det J), or dL/da of the area element below codimension 0 */
+  const void* pinv;    /* dL/dK, TD * GD components, K(t, g) at g * TD + t */
+  const void* normals; /* dL/dn, GD components (TD + 1 = GD only) */
 } tlg_cotangents;
 
-/* Per-cell contributions to the node cotangents of a codimension-0 block range (TD = GD),
- * J, det J and K recomputed: local[(cell * K + k) * R + g] = sum_q phi_k(q) xbar(q, g)
- * + sum_d Jbar(q)(g, d) dphi_k(q)[d], Jbar = dbar det J K^T - K^T Kbar K^T, for the cells of the
+/* Per-cell contributions to the node cotangents of a block range, J, det J and K recomputed:
+ * local[(cell * K + k) * R + g] = sum_q phi_k(q) xbar(q, g) + sum_d Jbar(q)(g, d) dphi_k(q)[d],
+ * Jbar = dbar det J K^T - K^T Kbar K^T in codimension 0; below it (curves, surfaces: TD < GD)
+ * Jbar = dbar a K^T - K^T Kbar K^T + P Kbar^T G^-1 + the normal term (a the area element,
+ * G = J^T J, P = I - J K, normals n = s v / |v| with v = J0 x J1 or (J0_y, -J0_x), s from bit 0 of
+ * the block's flags; the forward fields may include normals), for the cells of the
  * range (cell = block cell index; rows of R = 4 values for GD = 3, the fourth zero, else R = GD;
  * local holds local_cells >= block->num_cells cells, 16-byte aligned). With
  * TLG_F64 tables everything is f64; with TLG_SPLIT32 tables the mesh is f64, the arithmetic FP32

@@ -294,6 +294,136 @@ int orc_vjp(int d, int k, int nq, int64_t ncells, const double* nodes, int64_t n
   return ORC_OK;
 }
 
+/*
+ * Adjoint of a block of any codimension, restated in f64: the node cotangents of
+ * L = sum_c sum_q [xbar . x + dbar a + Kbar : K + nbar . n] with a = det J (codimension 0) or the
+ * area element sqrt(det(J^T J)), K the (pseudo-)inverse and n the unit normal of codimension-1
+ * blocks (sign flipped where bit 0 of the cell's flag is set; flags may be NULL). Codimension 0
+ * without normals is orc_vjp. For td < gd, with G = J^T J and P = I - J K:
+ *   dL/dJ = dbar a K^T - K^T Kbar K^T + P Kbar^T G^-1 + (normal term),
+ * the normal term from n = s v / |v|, v = J0 x J1 (gd 3) or (J0_y, -J0_x) (gd 2): with
+ * w = s (nbar - (nbar . v^) v^) / |v|, dL/dJ0 += J1 x w, dL/dJ1 += w x J0 (gd 3), or
+ * dL/dJ0 += (-w_y, w_x) (gd 2). nbar [cell][q][gd] may be NULL.
+ */
+int orc_vjp2(int td, int gd, int k, int nq, int64_t ncells, const double* nodes, int64_t nnodes,
+             const uint32_t* dofmap, const double* tab, const uint32_t* flags, int64_t nflags,
+             const double* xbar, const double* dbar, const double* kbar, const double* nbar, double* grad) {
+  if (td < 1 || gd < td || gd > 3 || k < 1 || k > ORC_MAX_K || nq < 0 || ncells < 0 || nnodes < 1) return ORC_BAD_ARGS;
+  if (nbar && td + 1 != gd) return ORC_BAD_ARGS;
+  if (td == gd) return orc_vjp(td, k, nq, ncells, nodes, nnodes, dofmap, tab, xbar, dbar, kbar, grad);
+  for (int64_t i = 0; i < nnodes * gd; ++i) grad[i] = 0.0;
+  double xc[ORC_MAX_K * 3], gl[ORC_MAX_K * 3];
+  for (int64_t c = 0; c < ncells; ++c) {
+    uint32_t idx[ORC_MAX_K];
+    for (int i = 0; i < k; ++i) {
+      uint32_t n = dofmap[c * k + i];
+      if ((int64_t)n >= nnodes) n = (uint32_t)(nnodes - 1);
+      idx[i] = n;
+      for (int g = 0; g < gd; ++g) xc[i * gd + g] = nodes[(int64_t)n * gd + g];
+    }
+    const double sgn = (flags && c < nflags && (flags[c] & 1u)) ? -1.0 : 1.0;
+    for (int i = 0; i < k * gd; ++i) gl[i] = 0.0;
+    for (int q = 0; q < nq; ++q) {
+      const int64_t cq = c * nq + q;
+      double j[6], kk[6], gm[4], gi[4];
+      for (int dd = 0; dd < td; ++dd)
+        for (int g = 0; g < gd; ++g) {
+          double s = 0.0;
+          for (int i = 0; i < k; ++i) s += xc[i * gd + g] * tab[((int64_t)(1 + dd) * nq + q) * k + i];
+          j[dd * gd + g] = s;
+        }
+#define J_(g, dd) j[(dd) * gd + (g)]
+#define K_(t, g) kk[(g) * td + (t)]
+      for (int a = 0; a < td; ++a)
+        for (int b = 0; b < td; ++b) {
+          double s = 0.0;
+          for (int g = 0; g < gd; ++g) s += J_(g, a) * J_(g, b);
+          gm[a * td + b] = s;
+        }
+      if (td == 1) {
+        gi[0] = 1.0 / gm[0];
+      } else {
+        const double det = gm[0] * gm[3] - gm[1] * gm[2];
+        gi[0] = gm[3] / det;
+        gi[1] = -gm[1] / det;
+        gi[2] = -gm[2] / det;
+        gi[3] = gm[0] / det;
+      }
+      for (int t = 0; t < td; ++t)
+        for (int g = 0; g < gd; ++g) {
+          double s = 0.0;
+          for (int u = 0; u < td; ++u) s += gi[t * td + u] * J_(g, u);
+          K_(t, g) = s;
+        }
+      const double area = detj_of(j, td, gd);
+      double jb[6] = {0, 0, 0, 0, 0, 0};
+#define JB(g, dd) jb[(dd) * gd + (g)]
+      if (dbar)
+        for (int g = 0; g < gd; ++g)
+          for (int dd = 0; dd < td; ++dd) JB(g, dd) += dbar[cq] * area * K_(dd, g);
+      if (kbar) {
+        const double* kb = kbar + cq * td * gd;  /* Kbar(t, g) at g * td + t */
+        double pm[9];
+        for (int g = 0; g < gd; ++g)
+          for (int h = 0; h < gd; ++h) {
+            double s = g == h ? 1.0 : 0.0;
+            for (int t = 0; t < td; ++t) s -= J_(g, t) * K_(t, h);
+            pm[g * gd + h] = s;
+          }
+        for (int g = 0; g < gd; ++g)
+          for (int dd = 0; dd < td; ++dd) {
+            double v = 0.0;
+            for (int t = 0; t < td; ++t)
+              for (int h = 0; h < gd; ++h) v -= K_(t, g) * kb[h * td + t] * K_(dd, h);
+            for (int h = 0; h < gd; ++h)
+              for (int t = 0; t < td; ++t) v += pm[g * gd + h] * kb[h * td + t] * gi[t * td + dd];
+            JB(g, dd) += v;
+          }
+      }
+      if (nbar) {
+        double v[3], w[3], len = 0.0, dot = 0.0;
+        if (gd == 2) {
+          v[0] = J_(1, 0);
+          v[1] = -J_(0, 0);
+        } else {
+          v[0] = J_(1, 0) * J_(2, 1) - J_(2, 0) * J_(1, 1);
+          v[1] = J_(2, 0) * J_(0, 1) - J_(0, 0) * J_(2, 1);
+          v[2] = J_(0, 0) * J_(1, 1) - J_(1, 0) * J_(0, 1);
+        }
+        for (int g = 0; g < gd; ++g) len += v[g] * v[g];
+        len = sqrt(len);
+        const double* nb = nbar + cq * gd;
+        for (int g = 0; g < gd; ++g) dot += nb[g] * v[g] / len;
+        for (int g = 0; g < gd; ++g) w[g] = sgn * (nb[g] - dot * v[g] / len) / len;
+        if (gd == 2) {
+          JB(0, 0) += -w[1];
+          JB(1, 0) += w[0];
+        } else {
+          /* J1 x w into column 0, w x J0 into column 1 */
+          JB(0, 0) += J_(1, 1) * w[2] - J_(2, 1) * w[1];
+          JB(1, 0) += J_(2, 1) * w[0] - J_(0, 1) * w[2];
+          JB(2, 0) += J_(0, 1) * w[1] - J_(1, 1) * w[0];
+          JB(0, 1) += w[1] * J_(2, 0) - w[2] * J_(1, 0);
+          JB(1, 1) += w[2] * J_(0, 0) - w[0] * J_(2, 0);
+          JB(2, 1) += w[0] * J_(1, 0) - w[1] * J_(0, 0);
+        }
+      }
+      for (int i = 0; i < k; ++i)
+        for (int g = 0; g < gd; ++g) {
+          double v = xbar ? tab[(int64_t)q * k + i] * xbar[cq * gd + g] : 0.0;
+          for (int dd = 0; dd < td; ++dd) v += JB(g, dd) * tab[((int64_t)(1 + dd) * nq + q) * k + i];
+          gl[i * gd + g] += v;
+        }
+#undef JB
+#undef K_
+#undef J_
+    }
+    for (int i = 0; i < k; ++i)
+      for (int g = 0; g < gd; ++g) grad[(int64_t)idx[i] * gd + g] += gl[i * gd + g];
+  }
+  return ORC_OK;
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

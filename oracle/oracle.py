@@ -61,6 +61,9 @@ def load():
         lib.orc_vjp.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64, p,
                                 ctypes.c_int64, p, p, p, p, p, p]
         lib.orc_vjp.restype = ctypes.c_int
+        lib.orc_vjp2.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int64, p,
+                                 ctypes.c_int64, p, p, p, ctypes.c_int64, p, p, p, p, p]
+        lib.orc_vjp2.restype = ctypes.c_int
         _lib = lib
     return _lib
 
@@ -112,9 +115,11 @@ def eval_block(cell: str, degree: int, nodes_abs: np.ndarray, dofmap: np.ndarray
 
 
 def vjp(cell: str, degree: int, nodes_abs: np.ndarray, dofmap: np.ndarray, points: np.ndarray,
-        xbar=None, dbar=None, kbar=None, family: str = "Equispaced", tab=None) -> np.ndarray:
-    """Node cotangents ``[node][gdim]`` (f64) of sum(xbar . x + dbar det J + kbar : K) over a
-    codimension-0 block; cotangents cell-major ``[cell][q][...]`` or None."""
+        xbar=None, dbar=None, kbar=None, family: str = "Equispaced", tab=None, nbar=None,
+        flags=None) -> np.ndarray:
+    """Node cotangents ``[node][gdim]`` (f64) of sum(xbar . x + dbar det J + kbar : K + nbar . n)
+    over a block (det J the area element and n the unit normal, sign flipped by bit 0 of `flags`,
+    below codimension 0); cotangents cell-major ``[cell][q][...]`` or None."""
     td = refcell.tdim(cell)
     nodes_abs = np.ascontiguousarray(nodes_abs, dtype=np.float64)
     dofmap = np.ascontiguousarray(dofmap, dtype=np.uint32)
@@ -124,12 +129,15 @@ def vjp(cell: str, degree: int, nodes_abs: np.ndarray, dofmap: np.ndarray, point
         tab = refcell.tabulate(cell, degree, points, 1, family)
     tab = np.ascontiguousarray(tab, dtype=np.float64)
     conv = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float64)
-    xbar, dbar, kbar = conv(xbar), conv(dbar), conv(kbar)
+    xbar, dbar, kbar, nbar = conv(xbar), conv(dbar), conv(kbar), conv(nbar)
+    fl = None if flags is None else np.ascontiguousarray(flags, dtype=np.uint32)
     grad = np.zeros_like(nodes_abs)
-    rc = load().orc_vjp(td, k, points.shape[0], ncells, _ptr(nodes_abs), nodes_abs.shape[0],
-                        _ptr(dofmap), _ptr(tab), _ptr(xbar), _ptr(dbar), _ptr(kbar), _ptr(grad))
+    gd = nodes_abs.shape[1]
+    rc = load().orc_vjp2(td, gd, k, points.shape[0], ncells, _ptr(nodes_abs), nodes_abs.shape[0],
+                         _ptr(dofmap), _ptr(tab), _ptr(fl), 0 if fl is None else fl.shape[0], _ptr(xbar),
+                         _ptr(dbar), _ptr(kbar), _ptr(nbar), _ptr(grad))
     if rc != 0:
-        raise ValueError(f"orc_vjp rejected its arguments ({rc})")
+        raise ValueError(f"orc_vjp2 rejected its arguments ({rc})")
     return grad
 
 

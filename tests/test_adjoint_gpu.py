@@ -257,3 +257,119 @@ def test_adjoint_auto_policy(cuda, cell, degree, rdeg, family):
     with tg.with_strategy("auto"):
         tg.vjp_block(g, 0, ps, ct, precision="split")
         assert tg.last_kernel_family() == family
+
+
+def curve(n, degree, gd):
+    """n curved intervals of degree `degree` on a closed curve in the plane (gd 2) or on a helix
+    turn (gd 3, open)."""
+    nodes, cells = [], []
+    per = degree
+    total = n * per + (1 if gd == 3 else 0)
+    for c in range(n):
+        last = (c + 1) * per if gd == 3 else ((c + 1) * per) % (n * per)
+        cells.append([c * per, last] + [c * per + i for i in range(1, degree)])
+    for i in range(total):
+        t = 2 * np.pi * i / (n * per)
+        r = 1 + 0.05 * np.sin(3 * t)
+        nodes.append([r * np.cos(t), r * np.sin(t)] + ([0.3 * t] if gd == 3 else []))
+    return meshes.HostMesh(gd, np.array(nodes), [meshes.HostBlock("Interval", degree, np.array(cells, dtype=np.uint32))])
+
+
+def surface_case(kind):
+    if kind == "sphere":
+        return meshes.perturbed_radius(meshes.sphere(1, 2), 0.05), "Triangle", 2, 4
+    if kind == "sphere3":
+        return meshes.perturbed_radius(meshes.sphere(1, 3), 0.05), "Triangle", 3, 5
+    if kind == "quads":
+        m = meshes.square_box("Quadrilateral", 3, 2)
+        x = meshes.jitter_interior(m.nodes, m.nodes, 0.02 / 3, 2026)
+        z = 0.1 * np.sin(2 * np.pi * x[:, 0]) * np.sin(2 * np.pi * x[:, 1])
+        return meshes.HostMesh(3, np.column_stack([x, z]), m.blocks), "Quadrilateral", 2, 4
+    if kind == "circle":
+        return curve(9, 3, 2), "Interval", 3, 5
+    return curve(8, 2, 3), "Interval", 2, 4
+
+
+@pytest.mark.parametrize("kind", ["sphere", "sphere3", "quads", "circle", "helix"])
+def test_surface_adjoint_matches_the_oracle(cuda, kind):
+    """Below codimension 0: cotangents on x, the area element, the pseudo-inverse and (TD + 1 = GD)
+    the unit normals, with seeded flipped cells, against the oracle's adjoint (itself checked
+    against central differences); f64 within 1e-11, split precision (f32 cotangents) within 2e-5."""
+    mesh, cell, degree, rdeg = surface_case(kind)
+    ncells = mesh.blocks[0].num_cells
+    flags = np.random.default_rng(3).integers(0, 2, ncells).astype(np.uint32)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64, flags=[flags])
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    td, gd = tg.refcell.tdim(cell), g.gdim
+    rng = np.random.default_rng(17)
+    ct, host = cotangent_fields(rng, ncells, len(pts), torch.float64, gd)
+    if td + 1 == gd:
+        f = tg.QuadField.uninit(ncells, len(pts), gd, 16, torch.float64)
+        f.chunks[0].data.copy_(torch.from_numpy(rng.standard_normal(f.chunks[0].data.numel())))
+        ct["normals"] = f
+        host["normals"] = f.to_host_cell_major()
+    pinv_len = td * gd
+    if ct["pinv"].length != pinv_len:  # cotangent_fields makes gd * gd components
+        f = tg.QuadField.uninit(ncells, len(pts), pinv_len, 16, torch.float64)
+        f.chunks[0].data.copy_(torch.from_numpy(rng.standard_normal(f.chunks[0].data.numel())))
+        ct["pinv"] = f
+        host["pinv"] = f.to_host_cell_major()
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[:gd])
+    want = orc.vjp(cell, degree, absx, mesh.blocks[0].cells, pts, host["points"], host["detj"][..., 0],
+                   host["pinv"], nbar=host.get("normals"), flags=flags)
+    got, _ = tg.vjp_block(g, 0, ps, ct)
+    assert orc.rel_err(got.cpu().numpy(), want) < 1e-11
+    ct32 = {k: tg.QuadField([tg.geometry.QuadChunk(0, ncells, v.chunks[0].data.float())], ncells, len(pts),
+                            v.length, 16) for k, v in ct.items()}
+    host32 = {k: v.to_host_cell_major().astype(np.float64) for k, v in ct32.items()}
+    want32 = orc.vjp(cell, degree, absx, mesh.blocks[0].cells, pts, host32["points"], host32["detj"][..., 0],
+                     host32["pinv"], nbar=host32.get("normals"), flags=flags)
+    got32, _ = tg.vjp_block(g, 0, ps, ct32, precision="split")
+    assert orc.rel_err(got32.cpu().numpy(), want32) < 2e-5
+
+
+@pytest.mark.parametrize("precision", ["native", "split"])
+def test_surface_fused_forward(cuda, precision):
+    """The surface adjoint's fused forward (x, J, area element, K, normals) equals the forward
+    kernels' to rounding."""
+    mesh, cell, degree, rdeg = surface_case("sphere")
+    flags = np.random.default_rng(3).integers(0, 2, mesh.blocks[0].num_cells).astype(np.uint32)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64, flags=[flags])
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    dt = torch.float64 if precision == "native" else torch.float32
+    ct, _ = cotangent_fields(np.random.default_rng(3), mesh.blocks[0].num_cells, len(pts), dt, 3)
+    del ct["pinv"]
+    names = ("points", "jacobian", "detj", "pinv", "normals")
+    _, fused = tg.vjp_block(g, 0, ps, ct, precision=precision, forward=names)
+    plain = tg.geometric_factors_block(g, 0, ps, names, precision=precision)
+    tol = 1e-13 if precision == "native" else 2e-6
+    for k in names:
+        assert orc.rel_err(fused[k].to_host_cell_major(), plain[k].to_host_cell_major()) < tol, k
+
+
+def test_surface_adjoint_fd_check(cuda):
+    mesh, cell, degree, rdeg = surface_case("sphere")
+    flags = np.random.default_rng(5).integers(0, 2, mesh.blocks[0].num_cells).astype(np.uint32)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64, flags=[flags])
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    rng = np.random.default_rng(8)
+    nc, nq = mesh.blocks[0].num_cells, len(pts)
+    host = {"detj": rng.standard_normal((nc, nq)), "normals": rng.standard_normal((nc, nq, 3)),
+            "pinv": rng.standard_normal((nc, nq, 6))}
+    ct = {}
+    for name, v in host.items():
+        ln = 1 if name == "detj" else v.shape[-1]
+        f = tg.QuadField.uninit(nc, nq, ln, 16, torch.float64)
+        vals = v.reshape(nc, nq, ln)
+        pad = np.zeros((-(-nc // 16) * 16, nq, ln))
+        pad[:nc] = vals
+        pad[nc:] = vals[-1]
+        f.chunks[0].data.copy_(torch.from_numpy(pad.reshape(-1, 16, nq, ln).transpose(0, 2, 3, 1).ravel()))
+        ct[name] = f
+    grad, _ = tg.vjp_block(g, 0, ps, ct)
+    sample = np.random.default_rng(9).choice(mesh.num_nodes, 12, replace=False)
+    res = tg.fd_check(g, 0, ps, host, grad.cpu().numpy(), sample)
+    assert res["max_rel_err"] < 1e-6, res

@@ -198,3 +198,53 @@ def test_oracle_pull_back_centres_and_outside_points():
     far = centres + np.array([0.0, 2.0])  # two cell widths away
     xi, step = orc.pull_back("Quadrilateral", 1, m.nodes, cells, far, tolerance=1e-5)
     assert np.all(xi <= float(np.float32(1.1))) and np.all(step > 1e-5)
+
+
+def _circle(n, degree, radius=1.0):
+    """n curved intervals of degree `degree` on a circle (nodes of each interval equispaced in
+    angle, interior nodes first after the two vertices, as the interval's Lagrange order)."""
+    from gridcl_gb300 import meshes
+    nodes, cells = [], []
+    per = degree  # nodes per interval beyond its first vertex
+    for c in range(n):
+        cells.append([c * per, ((c + 1) * per) % (n * per)] + [c * per + i for i in range(1, degree)])
+    for i in range(n * per):
+        t = 2 * np.pi * i / (n * per)
+        r = radius * (1 + 0.05 * np.sin(3 * t))
+        nodes.append([r * np.cos(t), r * np.sin(t)])
+    return meshes.HostMesh(2, np.array(nodes), [meshes.HostBlock("Interval", degree, np.array(cells, dtype=np.uint32))])
+
+
+@pytest.mark.parametrize("kind", ["sphere", "circle"])
+def test_surface_adjoint_against_central_differences(kind):
+    """The oracle's adjoint below codimension 0 (area element, pseudo-inverse, unit normals with
+    flipped cells) against central differences (step 1e-6) of the oracle's own forward pass."""
+    from gridcl_gb300 import meshes
+    if kind == "sphere":
+        mesh = meshes.perturbed_radius(meshes.sphere(1, 2), 0.05)
+        cell, degree, pts = "Triangle", 2, rc.gauss_rule("Triangle", 4)[0]
+    else:
+        mesh = _circle(7, 3)
+        cell, degree, pts = "Interval", 3, rc.gauss_rule("Interval", 5)[0]
+    cells = mesh.blocks[0].cells
+    x = np.asarray(mesh.nodes, dtype=np.float64)
+    nc, nq, gd, td = cells.shape[0], len(pts), x.shape[1], rc.tdim(cell)
+    rng = np.random.default_rng(21)
+    xb, db = rng.standard_normal((nc, nq, gd)), rng.standard_normal((nc, nq))
+    kb, nb = rng.standard_normal((nc, nq, td * gd)), rng.standard_normal((nc, nq, gd))
+    flags = rng.integers(0, 2, nc).astype(np.uint32)
+    grad = orc.vjp(cell, degree, x, cells, pts, xb, db, kb, nbar=nb, flags=flags)
+
+    def functional(y):
+        f = orc.eval_block(cell, degree, y, cells, pts, factors=("x", "detj", "k", "normals"), flags=flags)
+        return (np.sum(f["x"] * xb) + np.sum(f["detj"][..., 0] * db) + np.sum(f["k"] * kb)
+                + np.sum(f["normals"] * nb))
+
+    h = 1e-6
+    for n in rng.choice(x.shape[0], 6, replace=False):
+        for g in range(gd):
+            xp, xm = x.copy(), x.copy()
+            xp[n, g] += h
+            xm[n, g] -= h
+            fd = (functional(xp) - functional(xm)) / (2 * h)
+            assert abs(fd - grad[n, g]) <= 1e-6 * max(1.0, abs(grad[n, g])), (n, g, fd, grad[n, g])
