@@ -311,6 +311,77 @@ def extra_hybrid():
     return res
 
 
+def extra_hybrid_adjoint():
+    """The benchmark spec's batched fused forward + adjoint on the hybrid mesh (2,000,000 Q2 hex, 27
+    points; 300,000 P2 prisms, 21; 50,000 P3 tets, 24): seeded standard-normal cotangents on det J
+    and K; one graph launch of the split-precision fused forward (x/J/detJ/K) + adjoint + node
+    sums against the plain per-block FP64 forward followed by the per-block FP64 adjoint."""
+    import torch
+
+    import gridcl_gb300 as tg
+    from gridcl_gb300 import meshes, refcell
+
+    mesh = meshes.hybrid_box(2_000_000, 300_000, 50_000)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    rule = tg.QuadRule([tg.PointSet("Hexahedron", *refcell.gauss_rule("Hexahedron", 4)),
+                        tg.PointSet("Prism", *refcell.collapsed_rule("Prism", (3, 1, 7))),
+                        tg.PointSet("Tetrahedron", *refcell.collapsed_rule("Tetrahedron", (4, 3, 2)))])
+    factors = ("points", "jacobian", "detj", "pinv")
+    gen = torch.Generator(device="cuda").manual_seed(2026)
+    ct64, ct32 = [], []
+    qpts = 0
+    for blk in g.blocks:
+        nq = len(rule.get(blk.element.cell))
+        qpts += blk.num_cells * nq
+        c = {}
+        for name, length in (("detj", 1), ("pinv", 9)):
+            f = tg.QuadField.uninit(blk.num_cells, nq, length, 16, torch.float64)
+            f.chunks[0].data.normal_(generator=gen)
+            c[name] = f
+        ct64.append(c)
+        ct32.append({k: tg.QuadField([tg.geometry.QuadChunk(0, blk.num_cells, v.chunks[0].data.float())],
+                                     blk.num_cells, nq, v.length, 16) for k, v in c.items()})
+    for b in range(len(g.blocks)):
+        tg.node_incidence(g, b)
+    fwd64 = [tg.geometric_factors_block(g, b, rule.get(blk.element.cell), factors) for b, blk in enumerate(g.blocks)]
+    locals64 = [torch.empty((blk.num_cells, blk.element.nodes_per_cell, 4), dtype=torch.float64, device="cuda")
+                for blk in g.blocks]
+    grad64 = torch.zeros((g.nodes.shape[0], 3), dtype=torch.float64, device="cuda")
+
+    def plain():
+        grad64.zero_()
+        for b, blk in enumerate(g.blocks):
+            ps = rule.get(blk.element.cell)
+            tg.geometric_factors_block(g, b, ps, factors, out=fwd64[b])
+            gb, _ = tg.vjp_block(g, b, ps, ct64[b], local=locals64[b])
+            grad64.add_(gb)
+
+    plain()
+    plain_ms = event_ms(plain, reps=2, warm=1)
+    want = grad64.clone()
+    batch = tg.AdjointBatch(g, rule, ct32, precision="split", forward=factors)
+    batch.launch()
+    fused_ms = event_ms(batch.launch)
+    gerr = float((batch.grad - want).abs().max() / want.abs().max())
+    ferr = {b: rel_err_fields(batch.fields[b], fwd64[b]) for b in range(len(g.blocks))}
+    alg = 0
+    for blk in g.blocks:
+        nq = len(rule.get(blk.element.cell))
+        cells, k = blk.num_cells, blk.element.nodes_per_cell
+        alg += cells * nq * (10 + 22) * 4 + cells * k * 4 + 2 * cells * k * 16 + cells * k * 4
+    nn = g.nodes.shape[0]
+    alg += nn * 3 * 8 + nn * 3 * 8 * (1 + 2) + len(g.blocks) * nn * 4  # nodes, grad zero + add, offsets
+    return {"workload": "hybrid 2,000,000 Q2 hex + 300,000 P2 prisms + 50,000 P3 tets: forward x/J/detJ/K + "
+                        "adjoint from detJ and K cotangents + node sums",
+            "qpoints": int(qpts),
+            "plain_fp64_per_block_fwd_then_vjp": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3)},
+            "batched_fused_split_graph": {"ms": fused_ms, "value": qpts / (fused_ms * 1e-3),
+                                          "speedup_vs_plain_fp64": plain_ms / fused_ms,
+                                          "algorithmic_bytes": int(alg),
+                                          "hbm_gbs": alg / (fused_ms * 1e-3) / 1e9,
+                                          "grad_rel_err_vs_fp64": gerr, "forward_rel_err_vs_fp64": ferr}}
+
+
 def extra_sphere():
     """Surface TD=2, GD=3: 4,194,304 degree-4 triangles of the refined icosahedron (first cells of
     9 refinements), radius x (1 + 0.02 U), 28-point rule; x, J, area element, normals, K; split
@@ -754,7 +825,7 @@ def run_ours(args):
 
 
 EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "pull_back", "ordering", "p1_box",
-          "hex_strategies", "prism_strategies", "high_order")
+          "hex_strategies", "prism_strategies", "high_order", "hybrid_forward_adjoint")
 
 
 def run_extra(args):
@@ -767,7 +838,8 @@ def run_extra(args):
           "ordering": extra_ordering, "p1_box": extra_p1_box,
           "hex_strategies": lambda: extra_hex_strategies(args.hex_n),
           "prism_strategies": lambda: extra_hex_strategies(args.hex_n, "Prism"),
-          "high_order": lambda: extra_high_order(args.ho_n)}[args.workload]
+          "high_order": lambda: extra_high_order(args.ho_n),
+          "hybrid_forward_adjoint": extra_hybrid_adjoint}[args.workload]
     print(json.dumps(fn()), flush=True)
 
 

@@ -10,6 +10,7 @@ tetraloma-geometry's API.
 
 from ._lib import GridError, lib
 from .geometry import (
+    AdjointBatch,
     Batch,
     CoordinateElement,
     Geometry,
@@ -36,7 +37,7 @@ from .strategy import (get_strategy, last_kernel_family, last_launch_family, rec
 from . import meshes, refcell
 
 __all__ = [
-    "Batch", "CoordinateElement", "Geometry", "GeometryBlock", "GridError", "PointSet", "QuadField",
+    "AdjointBatch", "Batch", "CoordinateElement", "Geometry", "GeometryBlock", "GridError", "PointSet", "QuadField",
     "QuadRule", "detj_block", "facet_normals_block", "facet_point_set", "fd_check",
     "geometric_factors_block", "jacobians_block", "lib", "measure_block", "meshes", "normals_block",
     "node_incidence", "physical_points_block", "pseudo_inverse_block", "pull_back_block", "refcell", "vjp_block",

@@ -1363,6 +1363,144 @@ tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int6
   return ok();
 }
 
+tlg_status tlg_vjp_gather_add(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int gdim,
+                              const void* local, int local_dtype, double* grad, void* stream) {
+  if (!offsets || !grad || num_nodes < 0 || gdim < 1 || gdim > 3 || (local_dtype != 4 && local_dtype != 8))
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_gather_add: bad arguments");
+  if (num_nodes == 0) return ok();
+  cudaError_t e = tlg::launch_vjp_gather(offsets, entries, num_nodes, gdim, local, local_dtype, grad,
+                                         static_cast<cudaStream_t>(stream), true);
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_gather_add launch");
+  return ok();
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Adjoint batches: the per-cell contributions of every block on parallel branches of one CUDA
+// graph, then the node sums block by block onto one gradient.
+
+struct tlg_vjp_batch {
+  std::vector<const tlg_tables*> tables;
+  std::vector<tlg_block> blocks;
+  std::vector<tlg_outputs> outputs;
+  std::vector<tlg_cotangents> cotangents;
+  std::vector<void*> locals;
+  std::vector<int64_t> local_cells;
+  std::vector<const uint32_t*> offsets, entries;
+  int64_t num_nodes = 0;
+  int gdim = 0;
+  double* grad = nullptr;
+  cudaStream_t capture = nullptr;
+  std::vector<cudaStream_t> streams;
+  std::vector<cudaEvent_t> events;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" {
+
+tlg_status tlg_vjp_batch_create(const tlg_tables* const* tables, const tlg_block* blocks, const tlg_outputs* outputs,
+                                const tlg_cotangents* cotangents, void* const* locals, const int64_t* local_cells,
+                                const uint32_t* const* offsets, const uint32_t* const* entries, int64_t num_nodes,
+                                int gdim, double* grad, int num_blocks, tlg_vjp_batch** out) {
+  if (!out || num_blocks < 0 || !grad || gdim < 1 || gdim > 3 || num_nodes < 0 ||
+      (num_blocks > 0 && (!tables || !blocks || !outputs || !cotangents || !locals || !local_cells || !offsets ||
+                          !entries)))
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_batch_create: NULL or bad argument");
+  *out = nullptr;
+  auto b = new tlg_vjp_batch();
+  for (int i = 0; i < num_blocks; ++i) {
+    if (!tables[i] || !offsets[i] || tables[i]->gd != gdim) {
+      delete b;
+      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_batch_create: NULL tables or CSR, or another gdim");
+    }
+    b->tables.push_back(tables[i]);
+    b->blocks.push_back(blocks[i]);
+    b->outputs.push_back(outputs[i]);
+    b->cotangents.push_back(cotangents[i]);
+    b->locals.push_back(locals[i]);
+    b->local_cells.push_back(local_cells[i]);
+    b->offsets.push_back(offsets[i]);
+    b->entries.push_back(entries[i]);
+  }
+  b->num_nodes = num_nodes;
+  b->gdim = gdim;
+  b->grad = grad;
+  cudaError_t e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
+  for (int i = 0; i < num_blocks && e == cudaSuccess; ++i) {
+    cudaStream_t st;
+    e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking);
+    if (e == cudaSuccess) b->streams.push_back(st);
+  }
+  for (int i = 0; i < num_blocks + 1 && e == cudaSuccess; ++i) {
+    cudaEvent_t ev;
+    e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) b->events.push_back(ev);
+  }
+  if (e != cudaSuccess) {
+    tlg_vjp_batch_destroy(b);
+    return cuda_fail(e, "tlg_vjp_batch_create");
+  }
+  *out = b;
+  return ok();
+}
+
+tlg_status tlg_vjp_batch_destroy(tlg_vjp_batch* b) {
+  if (!b) return ok();
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (auto st : b->streams) cudaStreamDestroy(st);
+  for (auto ev : b->events) cudaEventDestroy(ev);
+  if (b->capture) cudaStreamDestroy(b->capture);
+  delete b;
+  return ok();
+}
+
+tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* b, void* stream) {
+  if (!b) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_batch_launch: NULL batch");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!b->exec) {
+    // Capture: the gradient zeroed, the blocks' contributions on parallel branches, then the node
+    // sums in block order (each adds its block's sums onto the gradient: deterministic).
+    cudaError_t e = cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_batch_launch: begin capture");
+    tlg_status st = TLG_OK;
+    const size_t nb = b->tables.size();
+    e = cudaMemsetAsync(b->grad, 0, (size_t)b->num_nodes * b->gdim * sizeof(double), b->capture);
+    if (e == cudaSuccess) e = cudaEventRecord(b->events[nb], b->capture);
+    for (size_t i = 0; i < nb && e == cudaSuccess && st == TLG_OK; ++i) {
+      e = cudaStreamWaitEvent(b->streams[i], b->events[nb], 0);
+      if (e != cudaSuccess) break;
+      st = tlg_vjp_block(b->tables[i], &b->blocks[i], &b->outputs[i], &b->cotangents[i], b->locals[i],
+                         b->local_cells[i], b->streams[i]);
+      if (st == TLG_OK) e = cudaEventRecord(b->events[i], b->streams[i]);
+      if (e == cudaSuccess && st == TLG_OK) e = cudaStreamWaitEvent(b->capture, b->events[i], 0);
+    }
+    for (size_t i = 0; i < nb && e == cudaSuccess && st == TLG_OK; ++i) {
+      const int ldt = b->tables[i]->dtype == TLG_SPLIT32 ? 4 : 8;
+      st = tlg_vjp_gather_add(b->offsets[i], b->entries[i], b->num_nodes, b->gdim, b->locals[i], ldt, b->grad,
+                              b->capture);
+    }
+    cudaGraph_t graph = nullptr;
+    const std::string msg = tlg_last_error();
+    cudaError_t ee = cudaStreamEndCapture(b->capture, &graph);
+    if (st != TLG_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return fail(st, msg);
+    }
+    if (e == cudaSuccess) e = ee;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_batch_launch: capture");
+  }
+  cudaError_t e = cudaGraphLaunch(b->exec, s);
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_batch_launch");
+  return ok();
+}
+
+}  // extern "C"
+
+extern "C" {
+
 // ---------------------------------------------------------------------------------------
 // Batches: every block of a hybrid mesh in one CUDA graph launch, launch shapes autotuned.
 

@@ -104,6 +104,6 @@ cudaError_t launch_vjp_surface(bool split, int td, int gd, const VjpSurfArgs& a,
 cudaError_t launch_vjp_f64(int d, int k, const VjpArgs& a, size_t smem, cudaStream_t s, bool* found);
 cudaError_t launch_vjp_split(int d, int k, const VjpArgs& a, size_t smem, cudaStream_t s, bool* found);
 cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int d,
-                              const void* local, int local_dtype, double* grad, cudaStream_t s);
+                              const void* local, int local_dtype, double* grad, cudaStream_t s, bool add = false);
 
 }  // namespace tlg

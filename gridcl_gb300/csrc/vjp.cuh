@@ -426,7 +426,8 @@ constexpr int kGatherChunk = 1024;
 
 template <typename L, int D>
 __global__ void __launch_bounds__(kGatherNodes) vjp_gather_kernel(const uint32_t* offsets, const uint32_t* entries,
-                                                                  int64_t num_nodes, const L* local, double* grad) {
+                                                                  int64_t num_nodes, const L* local, double* grad,
+                                                                  int add) {
   constexpr int R = vjp_row(D);
   using Row = VjpRow<L, R>;
   __shared__ typename Row::T rows[kGatherChunk];
@@ -460,9 +461,10 @@ __global__ void __launch_bounds__(kGatherNodes) vjp_gather_kernel(const uint32_t
         for (int g = 0; g < D; ++g) acc[g].add(Row::get(rows[i - c], g));
       __syncthreads();
     }
-    if (n < num_nodes)
+    // add: the block's sums go onto grad (one f64 addition each), nodes without entries untouched.
+    if (n < num_nodes && (!add || e > b))
 #pragma unroll
-      for (int g = 0; g < D; ++g) grad[n * D + g] = acc[g].value();
+      for (int g = 0; g < D; ++g) grad[n * D + g] = add ? __dadd_rn(grad[n * D + g], acc[g].value()) : acc[g].value();
   }
 }
 

@@ -6,13 +6,13 @@
 namespace tlg {
 
 cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int d,
-                              const void* local, int local_dtype, double* grad, cudaStream_t s) {
+                              const void* local, int local_dtype, double* grad, cudaStream_t s, bool add) {
   int64_t blocks = (num_nodes + kGatherNodes - 1) / kGatherNodes;
   if (blocks < 1) blocks = 1;
   if (blocks > 152 * 64) blocks = 152 * 64;
 #define TLG_GATHER(L, DD) \
   vjp_gather_kernel<L, DD><<<(unsigned)blocks, kGatherNodes, 0, s>>>(offsets, entries, num_nodes, \
-                                                            static_cast<const L*>(local), grad)
+                                                            static_cast<const L*>(local), grad, add ? 1 : 0)
   if (local_dtype == 4) {
     if (d == 1) TLG_GATHER(float, 1);
     else if (d == 2) TLG_GATHER(float, 2);

@@ -643,6 +643,76 @@ class Batch:
             pass
 
 
+class AdjointBatch:
+    """The fused forward + adjoint of every block of `g` in one CUDA graph launch
+    (``tlg_vjp_batch_*``): the point set of each block from `rule`, the cotangent fields of block b
+    in ``cotangents[b]`` (as for :func:`vjp_block`), the forward fields `forward` written in the
+    same pass (``self.fields[b]``), the node cotangents of the whole mesh in ``self.grad``
+    (``[node][GD]`` f64, summed block by block). ``launch()`` runs the graph."""
+
+    def __init__(self, g: Geometry, rule: "QuadRule", cotangents: list, precision: str = "split", forward=()):
+        from ._lib import TlgCotangents
+
+        if g.dtype != torch.float64:
+            raise GridError(1, "the adjoint reads f64 meshes")
+        n = len(g.blocks)
+        fdt = torch.float32 if precision == "split" else torch.float64
+        code = SPLIT32 if precision == "split" else g.dtype
+        dev = g.nodes.device
+        self.g, self.fields, self.locals, self._keep = g, [], [], []
+        descs = (TlgBlock * max(n, 1))()
+        outs = (TlgOutputs * max(n, 1))()
+        cts = (TlgCotangents * max(n, 1))()
+        handles = (ctypes.c_void_p * max(n, 1))()
+        locals_ = (ctypes.c_void_p * max(n, 1))()
+        lcells = (ctypes.c_int64 * max(n, 1))()
+        offs = (ctypes.c_void_p * max(n, 1))()
+        ents = (ctypes.c_void_p * max(n, 1))()
+        gd = g.gdim
+        for b, blk in enumerate(g.blocks):
+            pts = rule.get(blk.element.cell)
+            td, k = blk.element.tdim, blk.element.nodes_per_cell
+            t = pts.tables(blk.element, gd, code)
+            f = {name: QuadField.uninit(blk.num_cells, len(pts), FACTOR_LEN[name](td, gd), GPU_QUAD_TILE, fdt, dev)
+                 for name in forward}
+            self.fields.append(f)
+            loc = torch.empty((max(blk.num_cells, 1), k, 4 if gd == 3 else gd), dtype=fdt, device=dev)
+            self.locals.append(loc)
+            inc = node_incidence(g, b)
+            self._keep += [t, inc]
+            descs[b] = g.block_desc(b)
+            o = outs[b]
+            o.first_cell, o.num_cells, o.out_first_cell, o.tile = 0, blk.num_cells, 0, GPU_QUAD_TILE
+            for name, fld in f.items():
+                setattr(o, name, fld.chunks[0].data.data_ptr())
+            for name in ("points", "detj", "pinv", "normals"):
+                fld = cotangents[b].get(name)
+                if fld is not None:
+                    if fld.tile != GPU_QUAD_TILE or len(fld.chunks) != 1 or fld.chunks[0].data.dtype != fdt:
+                        raise GridError(1, f"cotangent {name}: one chunk of tile 16 and dtype {fdt} expected")
+                    setattr(cts[b], name, fld.chunks[0].data.data_ptr())
+            handles[b] = t.handle
+            locals_[b] = loc.data_ptr()
+            lcells[b] = loc.shape[0]
+            offs[b] = inc.offsets.data_ptr()
+            ents[b] = inc.entries.data_ptr()
+        self.grad = torch.empty((g.nodes.shape[0], gd), dtype=torch.float64, device=dev)
+        self._ctypes = (descs, outs, cts, handles, locals_, lcells, offs, ents, cotangents)
+        h = ctypes.c_void_p()
+        check(lib().tlg_vjp_batch_create(handles, descs, outs, cts, locals_, lcells, offs, ents, g.nodes.shape[0],
+                                         gd, self.grad.data_ptr(), n, ctypes.byref(h)))
+        self.handle = h
+
+    def launch(self) -> None:
+        check(lib().tlg_vjp_batch_launch(self.handle, current_stream_handle()))
+
+    def __del__(self):
+        try:
+            lib().tlg_vjp_batch_destroy(self.handle)
+        except Exception:
+            pass
+
+
 def fd_check(g: Geometry, b: int, pts: PointSet, cotangents: dict, grad: np.ndarray, sample,
              h: float = 1e-6) -> dict:
     """Central differences of L = sum over cells and points of (xbar . x + dbar det J + Kbar : K

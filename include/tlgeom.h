@@ -242,6 +242,26 @@ tlg_status tlg_vjp_block(const tlg_tables* tables, const tlg_block* block, const
  * rounded once to f64. Deterministic. */
 tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes,
                           int gdim, const void* local, int local_dtype, double* grad, void* stream);
+/* The same sums added onto grad (one f64 addition per node and component), nodes without entries
+ * untouched: node cotangents of several blocks, block by block. */
+tlg_status tlg_vjp_gather_add(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes,
+                              int gdim, const void* local, int local_dtype, double* grad, void* stream);
+
+/* Adjoint batches (the hybrid mesh's fused forward + adjoint in one CUDA graph launch): per block
+ * its tables, block, outputs (forward fields or none), cotangents, contribution rows (local,
+ * local_cells as in tlg_vjp_block) and node CSR (tlg_csr_build of its dofmap over num_nodes
+ * nodes); grad [num_nodes][gdim] f64. The graph zeroes grad, runs every block's tlg_vjp_block on
+ * its own branch, then tlg_vjp_gather_add block by block. Captured on the first launch; the
+ * pointers are used as given at every launch. */
+typedef struct tlg_vjp_batch tlg_vjp_batch;
+tlg_status tlg_vjp_batch_create(const tlg_tables* const* tables, const tlg_block* blocks,
+                                const tlg_outputs* outputs, const tlg_cotangents* cotangents,
+                                void* const* locals, const int64_t* local_cells,
+                                const uint32_t* const* offsets, const uint32_t* const* entries,
+                                int64_t num_nodes, int gdim, double* grad, int num_blocks,
+                                tlg_vjp_batch** out);
+tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* batch, void* stream);
+tlg_status tlg_vjp_batch_destroy(tlg_vjp_batch* batch);
 
 /* ---------------------------------------------------------------------------------------
  * Pull-back (tetraloma-geometry/src/pull_back.rs:94-330, 566): the reference point xi of each

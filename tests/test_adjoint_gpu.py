@@ -373,3 +373,32 @@ def test_surface_adjoint_fd_check(cuda):
     sample = np.random.default_rng(9).choice(mesh.num_nodes, 12, replace=False)
     res = tg.fd_check(g, 0, ps, host, grad.cpu().numpy(), sample)
     assert res["max_rel_err"] < 1e-6, res
+
+
+@pytest.mark.parametrize("precision", ["native", "split"])
+def test_adjoint_batch_equals_the_blocks(cuda, precision):
+    """The hybrid mesh's fused forward + adjoint in one graph launch: the node cotangents are the
+    per-block adjoints' summed in block order, bit for bit, and the forward fields those of the
+    per-block fused passes."""
+    mesh = meshes.hybrid_box(300, 120, 60)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    rule = tg.QuadRule([tg.PointSet("Hexahedron", *tg.refcell.gauss_rule("Hexahedron", 4)),
+                        tg.PointSet("Prism", *tg.refcell.collapsed_rule("Prism", (3, 1, 7))),
+                        tg.PointSet("Tetrahedron", *tg.refcell.collapsed_rule("Tetrahedron", (4, 3, 2)))])
+    dt = torch.float64 if precision == "native" else torch.float32
+    rng = np.random.default_rng(31)
+    cts = []
+    for blk in g.blocks:
+        ct, _ = cotangent_fields(rng, blk.num_cells, len(rule.get(blk.element.cell)), dt)
+        cts.append(ct)
+    names = ("points", "jacobian", "detj", "pinv")
+    batch = tg.AdjointBatch(g, rule, cts, precision=precision, forward=names)
+    batch.launch()
+    batch.launch()  # a second launch replays the graph
+    want = torch.zeros_like(batch.grad)
+    for b, blk in enumerate(g.blocks):
+        grad, fields = tg.vjp_block(g, b, rule.get(blk.element.cell), cts[b], precision=precision, forward=names)
+        want += grad
+        for k in names:
+            assert torch.equal(fields[k].chunks[0].data, batch.fields[b][k].chunks[0].data), (b, k)
+    assert torch.equal(batch.grad, want)
