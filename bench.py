@@ -60,7 +60,8 @@ def parse():
     p.add_argument("--n", type=int, default=64, help="subcells per direction")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
-                   help="skip the other workloads (hybrid batch, sphere surface, Q2 adjoint, pull-back, P1 box)")
+                   help="skip the other workloads (hybrid batch, hybrid forward + adjoint, sphere surface, "
+                        "Q2 adjoint, pull-back, ordering, P1 box)")
     p.add_argument("--workload", choices=["main", *EXTRAS], default="main",
                    help="run one of the other workloads alone and print its JSON object")
     p.add_argument("--adjoint-n", type=int, default=128, help="Q2 hexahedra per direction (adjoint)")
@@ -805,7 +806,8 @@ def run_ours(args):
             line["recomputed_points"] = recomputed
         if not args.no_extras and world == 1:
             workloads = {}
-            for name, fn in (("hybrid_batched", extra_hybrid), ("sphere_surface", extra_sphere),
+            for name, fn in (("hybrid_batched", extra_hybrid), ("hybrid_forward_adjoint", extra_hybrid_adjoint),
+                             ("sphere_surface", extra_sphere),
                              ("q2_forward_adjoint", lambda: extra_adjoint(args.adjoint_n, args.fd_nodes)),
                              ("pull_back", extra_pull_back), ("ordering", extra_ordering),
                              ("p1_box", extra_p1_box)):
