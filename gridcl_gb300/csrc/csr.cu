@@ -13,7 +13,8 @@
 //  3. tile_scatter: each CTA walks its tile in rounds of 256 entries in entry order; in a round,
 //     a thread's rank among equal digits comes from its warp (__match_any_sync) and the earlier
 //     warps' counts, so entries of one digit keep their order.
-// Then csr_offsets marks where each node's run starts in the sorted keys.
+// Then csr_offsets (and csr_fill_gaps, for long runs of nodes without entries) mark where each
+// node's run starts in the sorted keys.
 #include <algorithm>
 #include <cstdint>
 #include <string>
@@ -182,14 +183,32 @@ __global__ void init_entries(const uint32_t* dofmap, int64_t n, uint32_t last_no
   }
 }
 
-// offsets[m] = first position of a key >= m, for m = 0..num_nodes.
+// offsets[m] = first position of a key >= m, for m = 0..num_nodes. Position i (0 <= i <= n)
+// starts the nodes keys[i - 1] + 1 .. keys[i] (from 0 at i = 0; up to num_nodes at i = n). Runs of
+// at most kShortRun nodes are written by the position's thread; longer ones (the nodes before a
+// block's first key or after its last, in a mesh of several blocks) are left to csr_fill_gaps.
+constexpr int64_t kShortRun = 256;
+
 __global__ void csr_offsets(const uint32_t* keys, int64_t n, int64_t num_nodes, uint32_t* offsets) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x) {
     const int64_t lo = i == 0 ? -1 : (int64_t)keys[i - 1];
-    const int64_t hi = i == n ? num_nodes - 1 : (int64_t)keys[i] - 0;
-    // nodes lo + 1 .. hi start at position i (and, at i == n, nodes after the last key too)
-    const int64_t last = i == n ? num_nodes : hi;
+    const int64_t last = i == n ? num_nodes : (int64_t)keys[i];
+    if (last - lo > kShortRun) continue;
     for (int64_t m = lo + 1; m <= last; ++m) offsets[m] = (uint32_t)i;
+  }
+}
+
+// The nodes left unset (0xFFFFFFFF) by csr_offsets: a binary search over the sorted keys.
+__global__ void csr_fill_gaps(const uint32_t* keys, int64_t n, int64_t num_nodes, uint32_t* offsets) {
+  for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m <= num_nodes; m += (int64_t)gridDim.x * blockDim.x) {
+    if (offsets[m] != 0xFFFFFFFFu) continue;
+    int64_t lo = 0, hi = n;  // first position with keys[pos] >= m
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) / 2;
+      if ((int64_t)keys[mid] < m) lo = mid + 1;
+      else hi = mid;
+    }
+    offsets[m] = (uint32_t)lo;
   }
 }
 
@@ -291,8 +310,11 @@ tlg_status tlg_csr_build(const uint32_t* dofmap, int64_t num_cells, int nodes_pe
     cudaError_t e = cudaMemcpyAsync(entries, w.vals_a, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) return tlg::cuda_fail(e, "tlg_csr_build copy");
   }
+  cudaError_t e = cudaMemsetAsync(offsets, 0xFF, (size_t)(num_nodes + 1) * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return tlg::cuda_fail(e, "tlg_csr_build offsets");
   tlg::csr_offsets<<<tlg::grid_of(n + 1, 256), 256, 0, s>>>(w.keys_a, n, num_nodes, offsets);
-  cudaError_t e = cudaGetLastError();
+  tlg::csr_fill_gaps<<<tlg::grid_of(num_nodes + 1, 256), 256, 0, s>>>(w.keys_a, n, num_nodes, offsets);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return tlg::cuda_fail(e, "tlg_csr_build");
   return tlg::ok();
 }

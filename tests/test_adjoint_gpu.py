@@ -402,3 +402,18 @@ def test_adjoint_batch_equals_the_blocks(cuda, precision):
         for k in names:
             assert torch.equal(fields[k].chunks[0].data, batch.fields[b][k].chunks[0].data), (b, k)
     assert torch.equal(batch.grad, want)
+
+
+def test_csr_with_long_runs_of_unused_nodes(cuda):
+    """Offsets across long runs of nodes without entries (a block's nodes in the middle of a large
+    node array, as in a mesh of several blocks) against the host's stable sort."""
+    rng = np.random.default_rng(6)
+    nodes = rng.random((20_000, 3))
+    cells = rng.integers(7_000, 7_300, size=(500, 4)).astype(np.uint32)
+    cells[::97, 0] = 19_999
+    mesh = meshes.HostMesh(3, nodes, [meshes.HostBlock("Tetrahedron", 1, cells)])
+    g = tg.Geometry.from_host(mesh)
+    inc = tg.node_incidence(g, 0)
+    offsets, entries = stable_csr(cells, 20_000)
+    assert np.array_equal(inc.offsets.cpu().numpy().view(np.uint32), offsets)
+    assert np.array_equal(inc.entries.cpu().numpy().view(np.uint32)[: entries.size], entries)
