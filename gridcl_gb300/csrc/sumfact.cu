@@ -13,7 +13,7 @@ cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t sme
   *found = true;
 #define TLG_VSF(F, SPLIT, NN) \
   if (n == NN) { \
-    auto kern = vjp_sumfact_kernel<F, SPLIT, NN>; \
+    auto kern = a.m[0] == NN ? vjp_sumfact_kernel<F, SPLIT, NN, NN> : vjp_sumfact_kernel<F, SPLIT, NN, 0>; \
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
     if (e != cudaSuccess) return e; \
     int per_sm = 0, sms = 1, dev = 0; \

@@ -495,7 +495,9 @@ inline size_t vjp_sumfact_extra_bytes(int n, int threads, size_t f_bytes) {
          f_bytes * ((size_t)threads * (k * 3 + 2 * 3 * (size_t)n * n) + (size_t)(threads + 1) * k * 3);
 }
 
-template <typename F, bool SPLIT, int N>
+// M0 > 0: the rule has M0 points in direction 0 (the point loop of a row unrolled, so that the
+// rows' points overlap); 0: at run time.
+template <typename F, bool SPLIT, int N, int M0>
 __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_constant__ VjpSfArgs a) {
   using NT = typename std::conditional<SPLIT, double, F>::type;
   using A = Ar<F>;
@@ -630,7 +632,8 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
               VU[g][i] = A::fma(V[g][jj][i], bj, VU[g][i]);
             }
         }
-        for (int a0 = 0; a0 < m0; ++a0) {
+        #pragma unroll
+        for (int a0 = 0; a0 < (M0 > 0 ? M0 : m0); ++a0) {
           const int q = a0 + m0 * (b1 + m1 * c2);
           F nxt[D + 1 + LJ];
           load_ct(min(q + 1, nq - 1), nxt);
