@@ -1,7 +1,8 @@
-// The C ABI of include/tlgeom.h: argument checks with the reference's error kinds, device
-// tables, and the launches of the evaluation and E-vector kernels.
+// The C ABI of include/tlgeom.h: argument checks with the reference's error kinds, the device
+// tables (tabulations, point pairs, the adjoint's node rows, sum-factorisation blocks), the
+// strategy settings and policy, and the launches of the evaluation, E-vector and adjoint kernels,
+// singly and as CUDA-graph batches.
 #include <algorithm>
-#include <atomic>
 #include <cctype>
 #include <cmath>
 #include <cstdlib>
