@@ -592,8 +592,8 @@ def extra_hex_strategies(n: int = 64, cell: str = "Hexahedron"):
 
 def extra_high_order(n: int = 16):
     """Curved tetrahedra P4-P6 (6 n^3 cells, 35 / 56 / 84 nodes) at the collapsed Gauss rules of
-    degree 2p, x/J/detJ/K, under the loops (global tables), shared (staged tables) and
-    cooperative kernels and AUTO, in split precision, f64 and f32: ms per launch and the family.
+    degree 2p, x/J/detJ/K, under the loops (global tables), shared (staged tables), cooperative
+    and tensor-core kernels and AUTO, in split precision, f64 and f32: ms per launch and the family.
     Run with --workload high_order (not part of the default run)."""
     import torch
 
@@ -610,7 +610,7 @@ def extra_high_order(n: int = 16):
         for prec, dt in (("split", torch.float64), ("native", torch.float64), ("native", torch.float32)):
             g = tg.Geometry.from_host(mesh, dtype=dt)
             row = {"qpoints": int(qpts)}
-            for strat in ("loops", "shared", "cooperative", "auto"):
+            for strat in ("loops", "shared", "cooperative", "tensor", "auto"):
                 with tg.with_strategy(strat):
                     f = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
                     fam = tg.last_kernel_family()

@@ -22,6 +22,7 @@
 #include "refcell.h"
 #include "status.h"
 #include "coop.cuh"
+#include "tc.cuh"
 #include "sumfact.cuh"
 #include "vjp.cuh"
 
@@ -61,6 +62,11 @@ struct tlg_tables {
   int sf_n = 0, sf_nblocks = 0;
   tlg::SfBlock sf_block0{};  // the first block (the adjoint's single-block rule)
   uint32_t off_sf = 0, sf_bytes = 0, sf_offperm = 0, sf_offrefn = 0;
+  // Tensor-core section (f32 and split tables, TD >= 2), after the sum-factorisation section, read
+  // from global memory: the basis in mma fragment order, [col tile][k-step][lane] x 4 f32
+  // (b0 head, b1 head, b0 tail, b1 tail) of B[k][4 q + r] (r = 0 phi, 1 + d dphi_d).
+  uint64_t off_tc = 0;
+  int tc_ksteps = 0, tc_col_tiles = 0;
   int* err = nullptr;
   std::vector<unsigned char> host;  // host copy of the device bytes
 };
@@ -144,8 +150,8 @@ const char* const kFamilyNames[kFamilies] = {"EVector", "Points", "Jacobian", "N
 int strategy_named(std::string n) {
   while (!n.empty() && n.front() == ' ') n.erase(n.begin());
   while (!n.empty() && n.back() == ' ') n.pop_back();
-  const char* names[] = {"policy", "direct", "loops", "sumfact", "shared", "cooperative"};
-  for (int i = 0; i < 6; ++i)
+  const char* names[] = {"policy", "direct", "loops", "sumfact", "shared", "cooperative", "tensor"};
+  for (int i = 0; i < 7; ++i)
     if (n == names[i]) return i;
   if (n == "auto") return TLG_STRATEGY_AUTO;
   return -1;
@@ -166,7 +172,7 @@ const EnvStrategies& env_strategies() {
     if (!e || !*e) return r;
     const std::string val(e);
     const std::string invalid = "TLG_GEOM_STRATEGY=" + val +
-                                ": expected policy, direct, loops, sumfact, shared or cooperative, or a comma "
+                                ": expected policy, direct, loops, sumfact, shared, cooperative or tensor, or a comma "
                                 "list of <family>=<strategy> with the families EVector, Points, Jacobian, "
                                 "Normals, FacetNormals and PullBack";
     const int one = strategy_named(val);
@@ -244,6 +250,11 @@ bool sumfact_preferred(const tlg_tables* t) { return t->sf_ok && (t->dtype == TL
 // The policy of TLG_STRATEGY_AUTO beyond the compiled unrolled kernels (more than 27 nodes per
 // cell): the cooperative kernel instead of the loops kernel.
 bool coop_preferred(const tlg_tables* t) { return t->k > 27; }
+
+// The tensor-core kernel is not in the policy: on GB300 it measured level with the cooperative
+// kernel at P4/P5 tetrahedra and slower at P6 (f32 1.42 ms cooperative, 2.03 ms tensor), with up
+// to 5x the cooperative kernel's error (3xTF32 rounds the tails at 2^-22).
+bool tc_preferred(const tlg_tables*) { return false; }
 
 // The sum-factorised kernel; `found` is false when it does not apply (no tensor structure, facet
 // normals, split precision at a tile other than 16, or no instantiation): nothing is launched.
@@ -406,6 +417,49 @@ tlg_status eval_typed(const tlg_tables* t, const tlg_block* b, const tlg_outputs
   }
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
   g_last_family = direct ? TLG_STRATEGY_DIRECT : a.tab_global ? TLG_STRATEGY_LOOPS : TLG_STRATEGY_SHARED;
+  return ok();
+}
+
+// The tensor-core kernel (f32 and split tables, TD >= 2, tile 16); `found` is false where it does
+// not apply (nothing launched).
+tlg_status eval_tc(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                   cudaStream_t stream, bool* found) {
+  *found = false;
+  if (t->tc_ksteps == 0 || o->tile != 16 || (t->dtype != TLG_F32 && t->dtype != TLG_SPLIT32))
+    return TLG_ERR_UNSUPPORTED;
+  const size_t smem = tlg::tc_smem_bytes(t->tc_ksteps, t->gd);
+  if (smem > (size_t)227 * 1024) return TLG_ERR_UNSUPPORTED;
+  const bool split = t->dtype == TLG_SPLIT32;
+  tlg::TcArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = b->nodes;
+  a.dofmap = b->dofmap;
+  a.flags = b->flags;
+  a.bfrag = reinterpret_cast<const float4*>(t->dev + t->off_tc);
+  a.refn = reinterpret_cast<const float*>(t->dev + t->off_refn);
+  a.dphi64 = split ? reinterpret_cast<const double*>(t->dev + t->off_dphi64) : nullptr;
+  void* outs[6] = {o->points, o->jacobian, o->detj, o->pinv, o->normals, o->facet_normals};
+  for (int i = 0; i < 6; ++i) a.out[i] = outs[i];
+  a.recomputed = split ? o->recomputed : nullptr;
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + 15) / 16 * 16;
+  a.range_cells = o->num_cells;
+  a.out_first_cell = o->out_first_cell;
+  a.last_cell = b->num_cells - 1;
+  const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
+  a.last_flag = nflags - 1;
+  for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
+  a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 256.0f;
+  a.last_node = (uint32_t)(b->num_nodes - 1);
+  a.mask = mask;
+  a.k = (int)t->k;
+  a.ksteps = t->tc_ksteps;
+  a.num_points = (int)t->q;
+  a.col_tiles = t->tc_col_tiles;
+  cudaError_t e = tlg::launch_tc(split, t->td, t->gd, a, smem, stream, found);
+  if (!*found) return TLG_ERR_UNSUPPORTED;
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  g_last_family = TLG_STRATEGY_TENSOR;
   return ok();
 }
 
@@ -936,7 +990,15 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       if (ref_normals) off = align16(off + (size_t)npoints * td * es);
       t->sf_bytes = (uint32_t)off;
     }
-    t->host.assign(t->off_sf + t->sf_bytes, 0);
+    // The tensor-core section.
+    size_t host_bytes = (size_t)t->off_sf + t->sf_bytes;
+    if (dtype != TLG_F64 && td >= 2 && k > 10 && npoints > 0) {
+      t->tc_ksteps = (int)((k + 7) / 8);
+      t->tc_col_tiles = (int)((npoints + 1) / 2);
+      t->off_tc = align16(host_bytes);
+      host_bytes = t->off_tc + (size_t)t->tc_col_tiles * t->tc_ksteps * 32 * 16;
+    }
+    t->host.assign(host_bytes, 0);
     if (t->sf_ok) {
       std::memcpy(t->host.data() + t->off_sf, heads.data(), heads.size() * sizeof(tlg::SfBlock));
       for (size_t bi = 0; bi < sf.size(); ++bi)
@@ -977,6 +1039,36 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
           }
         }
       narrow_into<float>(t->host, t->off_rows2, rows2.data(), rows2.size());
+      if (t->tc_ksteps > 0) {
+        // B[k][4 q + r] narrowed to f32, split into TF32 head (round to nearest, ties away) and
+        // tail; lane = 4 grp + tig holds B[8 ks + tig][8 j + grp] and B[8 ks + tig + 4][8 j + grp].
+        auto bval = [&](int64_t kk, int64_t col) -> float {
+          const int64_t q = col / 4, r = col % 4;
+          if (kk >= k || q >= npoints || r > td) return 0.0f;
+          return (float)(r == 0 ? phi[q * k + kk] : dphi[(q * k + kk) * td + (r - 1)]);
+        };
+        auto head = [](float x) {
+          uint32_t u;
+          std::memcpy(&u, &x, 4);
+          if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x1000u) & 0xFFFFE000u;
+          float h;
+          std::memcpy(&h, &u, 4);
+          return h;
+        };
+        float* dst = reinterpret_cast<float*>(t->host.data() + t->off_tc);
+        for (int j = 0; j < t->tc_col_tiles; ++j)
+          for (int ks = 0; ks < t->tc_ksteps; ++ks)
+            for (int lane = 0; lane < 32; ++lane) {
+              const int grp = lane >> 2, tig = lane & 3;
+              const float v0 = bval(8 * ks + tig, 8 * j + grp), v1 = bval(8 * ks + tig + 4, 8 * j + grp);
+              const float h0 = head(v0), h1 = head(v1);
+              float* e = dst + (((size_t)j * t->tc_ksteps + ks) * 32 + lane) * 4;
+              e[0] = h0;
+              e[1] = h1;
+              e[2] = head(v0 - h0);
+              e[3] = head(v1 - h1);
+            }
+      }
     }
     if (t->vjp_bytes > 0) {
       const int pn = dtype == TLG_SPLIT32 ? 2 : 1;  // points per table row
@@ -1093,6 +1185,11 @@ tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_out
     tlg_status st = eval_sumfact(t, b, o, mask, s, &found);
     if (found) return st;
   }
+  if (strategy == TLG_STRATEGY_TENSOR || (is_auto && tc_preferred(t))) {
+    bool found = false;
+    tlg_status st = eval_tc(t, b, o, mask, s, &found);
+    if (found) return st;
+  }
   if (strategy == TLG_STRATEGY_COOPERATIVE || (is_auto && coop_preferred(t))) {
     bool found = false;
     tlg_status st = eval_coop(t, b, o, mask, s, &found);
@@ -1106,8 +1203,8 @@ tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_out
 }
 
 tlg_status tlg_set_strategy(int strategy) {
-  if (strategy < -1 || strategy > TLG_STRATEGY_COOPERATIVE)
-    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_strategy: strategy must be -1 .. 5");
+  if (strategy < -1 || strategy > TLG_STRATEGY_TENSOR)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_strategy: strategy must be -1 .. 6");
   for (int& x : g_override) x = strategy;
   return ok();
 }
@@ -1115,8 +1212,8 @@ tlg_status tlg_set_strategy(int strategy) {
 tlg_status tlg_set_family_strategy(int family, int strategy) {
   if (family < 0 || family >= kFamilies)
     return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_family_strategy: family must be 0 .. 5");
-  if (strategy < -1 || strategy > TLG_STRATEGY_COOPERATIVE)
-    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_family_strategy: strategy must be -1 .. 5");
+  if (strategy < -1 || strategy > TLG_STRATEGY_TENSOR)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_set_family_strategy: strategy must be -1 .. 6");
   g_override[family] = strategy;
   return ok();
 }

@@ -88,6 +88,10 @@ cudaError_t launch_sumfact(int precision, int td, int gd, int n, const SfArgs& a
 cudaError_t launch_sumfact_fn(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
                               bool* found);
 
+struct TcArgs;
+// Defined in tc.cu: the tensor-core kernel (split: f64 mesh, else f32 mesh), TD >= 2, tile 16.
+cudaError_t launch_tc(bool split, int td, int gd, const TcArgs& a, size_t smem, cudaStream_t s, bool* found);
+
 struct CoopArgs;
 // Defined in coop.cu: the cooperative kernel (four lanes per cell) for precision 4, 8 or 12, cells of
 // 2 or 3 dimensions and at most 128 nodes; `found` is false otherwise.

@@ -6,10 +6,12 @@ this thread's scoped setting (:func:`with_strategy`), then the environment varia
 built-in policy ("policy"/"auto": sum factorisation for quadrilaterals, hexahedra and prisms at
 tensor-product rules in f64 and above the degrees with paired kernels, else the paired or
 unrolled kernels where compiled, the cooperative kernel above 27 nodes per cell, loops
-otherwise). "loops" reads the tables from global memory, "shared" stages them in shared memory,
-"cooperative" splits each cell's node sums over four lanes. A forced strategy that does not
-apply runs "loops", as in the reference. A fused launch follows its principal family: Jacobian
-when J, det J or K is among its outputs, else Normals, FacetNormals, Points."""
+otherwise). "loops" reads the tables from global
+memory, "shared" stages them in shared memory, "cooperative" splits each cell's node sums over
+four lanes, "tensor" (an extension of the reference's five) runs the node-by-basis contraction on
+the tensor cores (3xTF32). A forced strategy that does not apply runs "loops", as in the
+reference. A fused launch follows its principal family: Jacobian when J, det J or K is among its
+outputs, else Normals, FacetNormals, Points."""
 
 from __future__ import annotations
 
@@ -19,7 +21,7 @@ import threading
 
 from ._lib import GridError, check, lib
 
-STRATEGIES = {"auto": 0, "direct": 1, "loops": 2, "sumfact": 3, "shared": 4, "cooperative": 5}
+STRATEGIES = {"auto": 0, "direct": 1, "loops": 2, "sumfact": 3, "shared": 4, "cooperative": 5, "tensor": 6}
 _ALIASES = {"policy": 0}
 FAMILIES = {"EVector": 0, "Points": 1, "Jacobian": 2, "Normals": 3, "FacetNormals": 4, "PullBack": 5}
 _NAMES = {v: k for k, v in STRATEGIES.items()}
@@ -61,7 +63,7 @@ def get_strategy(family: str = "Jacobian") -> str:
 
 def last_kernel_family() -> str | None:
     """The strategy that ran in this thread's last launch ("direct", "loops", "sumfact",
-    "shared", "cooperative")."""
+    "shared", "cooperative", "tensor")."""
     return _NAMES.get(lib().tlg_last_kernel_family()) if lib().tlg_last_kernel_family() else None
 
 

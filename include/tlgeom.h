@@ -323,13 +323,16 @@ uint32_t tlg_quantise(double x, double lo, double hi);
  *  - SUMFACT: a quadrilateral, hexahedron or prism at a tensor-product point set, no facet
  *    normals, tile 16 in split precision;
  *  - SHARED: the loops kernels with the tables staged in shared memory (where they fit);
- *  - COOPERATIVE: four lanes per cell (cells of 2 or 3 dimensions, up to 128 nodes, 64 in f64).
+ *  - COOPERATIVE: four lanes per cell (cells of 2 or 3 dimensions, up to 128 nodes, 64 in f64);
+ *  - TENSOR (an extension; the reference has none): the node-by-basis contraction on the tensor
+ *    cores (mma.sync TF32 in three products, FP32-level error), f32 and split tables, TD >= 2,
+ *    tile 16, more than 10 nodes (not in the AUTO policy: no faster than COOPERATIVE here).
  * A fused launch follows the strategy of its principal family: Jacobian when J, det J or K is
  * among its outputs, else Normals, FacetNormals, Points. The adjoint follows the Jacobian family
  * (sum factorisation where it applies, else the node-row kernel); the E-vector and the pull-back
  * have one kernel each (recorded as LOOPS: K and the degree at run time). The environment variable
  * TLG_GEOM_STRATEGY is read once: one strategy name (policy or auto, direct, loops, sumfact,
- * shared, cooperative) for every family, or a comma list <family>=<strategy> of the families
+ * shared, cooperative, tensor) for every family, or a comma list <family>=<strategy> of the families
  * EVector, Points, Jacobian, Normals, FacetNormals, PullBack (each at most once); an invalid value
  * makes every launch fail with TLG_ERR_INVALID_ARGUMENT. tlg_set_strategy sets this thread's
  * setting of every family, tlg_set_family_strategy of one (-1 clears it, 0 selects the policy). */
@@ -347,7 +350,8 @@ typedef enum tlg_strategy {
   TLG_STRATEGY_LOOPS = 2,
   TLG_STRATEGY_SUMFACT = 3,
   TLG_STRATEGY_SHARED = 4,
-  TLG_STRATEGY_COOPERATIVE = 5
+  TLG_STRATEGY_COOPERATIVE = 5,
+  TLG_STRATEGY_TENSOR = 6
 } tlg_strategy;
 tlg_status tlg_set_strategy(int strategy);
 tlg_status tlg_set_family_strategy(int family, int strategy);

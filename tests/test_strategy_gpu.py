@@ -58,7 +58,7 @@ def factors_for(gd, td):
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32", "split"])
-@pytest.mark.parametrize("strategy", ["direct", "loops", "sumfact", "shared", "cooperative"])
+@pytest.mark.parametrize("strategy", ["direct", "loops", "sumfact", "shared", "cooperative", "tensor"])
 @pytest.mark.parametrize("cell,n,degree,rdeg,gd", CASES)
 def test_strategies_match_the_oracle(cuda, cell, n, degree, rdeg, gd, strategy, precision):
     mesh = mesh_for(cell, n, degree, gd)
@@ -70,7 +70,10 @@ def test_strategies_match_the_oracle(cuda, cell, n, degree, rdeg, gd, strategy, 
     with tg.with_strategy(strategy):
         got = tg.geometric_factors_block(g, 0, ps, names, precision="split" if precision == "split" else "native")
         family = tg.last_kernel_family()
-    if strategy in ("sumfact", "loops", "cooperative"):
+    k = mesh.blocks[0].cells.shape[1]
+    if strategy == "tensor":  # f32 and split tables of more than 10 nodes; loops elsewhere
+        assert family == ("tensor" if precision != "f64" and k > 10 else "loops")
+    elif strategy in ("sumfact", "loops", "cooperative"):
         assert family == strategy
     elif strategy == "shared":  # tables beyond the shared-memory budget stay in global memory
         assert family in ("shared", "loops")
@@ -193,7 +196,7 @@ def high_mesh(cell, n, degree, gd):
 
 
 @pytest.mark.parametrize("precision", ["f64", "f32", "split"])
-@pytest.mark.parametrize("strategy", ["auto", "loops", "shared", "cooperative"])
+@pytest.mark.parametrize("strategy", ["auto", "loops", "shared", "cooperative", "tensor"])
 @pytest.mark.parametrize("cell,n,degree,rdeg,gd", HIGH)
 def test_high_degree_strategies(cuda, cell, n, degree, rdeg, gd, strategy, precision):
     """Cells of 21 to 64 nodes under the loops, shared and cooperative kernels (and AUTO, which
@@ -211,9 +214,14 @@ def test_high_degree_strategies(cuda, cell, n, degree, rdeg, gd, strategy, preci
         family = tg.last_kernel_family()
     k = mesh.blocks[0].cells.shape[1]
     if strategy == "auto":
-        assert family in (("cooperative",) if k > 27 else ("loops", "shared"))
+        if k > 27:
+            assert family == "cooperative"
+        else:
+            assert family in ("loops", "shared")
     elif strategy == "shared":  # tables beyond the shared-memory budget stay in global memory
         assert family in ("shared", "loops")
+    elif strategy == "tensor":
+        assert family == ("loops" if precision == "f64" else "tensor")
     else:
         assert family == strategy
     absx = g.nodes.double().cpu().numpy() + np.array(g.origin[:gd])
@@ -371,3 +379,58 @@ def test_policy_matches_its_forced_choice_bitwise(cuda, cell, degree, rdeg, dtyp
         assert tg.last_kernel_family() == chosen
     for f in names:
         assert torch.equal(auto[f].chunks[0].data, forced[f].chunks[0].data), (f, chosen)
+
+
+@pytest.mark.parametrize("precision", ["f32", "split"])
+@pytest.mark.parametrize("cell,degree,rdeg,gd", [("Tetrahedron", 5, 6, 3), ("Tetrahedron", 3, 4, 3),
+                                                 ("Triangle", 6, 8, 2), ("Triangle", 5, 6, 3),
+                                                 ("Quadrilateral", 4, 5, 2)])
+def test_tensor_kernel_against_the_oracle(cuda, cell, degree, rdeg, gd, precision):
+    """The 3xTF32 tensor-core contraction on coordinates relative to each cell's first node against
+    the oracle within the f32 tolerance (surfaces with flipped normals, an odd point count, a cell
+    count that is not a multiple of 16): the mma fragment layout is the one the kernel assumes (a
+    wrong one would not agree), and it stays within 4x of the FP32 cooperative kernel's error."""
+    mesh = high_mesh(cell, 2, degree, gd)
+    if cell == "Tetrahedron":
+        mesh = mesh.first_cells(37)
+    flags = np.random.default_rng(4).integers(0, 2, mesh.blocks[0].num_cells).astype(np.uint32)
+    g = tg.Geometry.from_host(mesh, dtype=F32 if precision == "f32" else F64, flags=[flags])
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    pts = pts[:-1]  # an odd number of points
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    td = tg.refcell.tdim(cell)
+    names = factors_for(gd, td)
+    prec = "split" if precision == "split" else "native"
+    with tg.with_strategy("tensor"):
+        got = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+        assert tg.last_kernel_family() == "tensor"
+    with tg.with_strategy("cooperative"):
+        coop = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+    absx = g.nodes.double().cpu().numpy() + np.array(g.origin[:gd])
+    keys = [KEYS[f] for f in names]
+    want = orc.eval_block(cell, degree, absx, mesh.blocks[0].cells, pts, factors=keys, flags=flags)
+    nodes = orc.node_ratio(cell, degree)
+    s_val = orc.tolerance_scale(cell, degree, "Equispaced", pts, "values") * nodes
+    s_der = orc.tolerance_scale(cell, degree, "Equispaced", pts) * nodes
+    if precision == "f32":
+        ratio = orc.origin_ratio(absx, np.array(g.origin[:gd]), want["j"])
+        s_val, s_der = s_val * ratio, s_der * ratio
+    cond = orc.condition_scale(want["j"], td, gd)
+    scale = {"points": s_val, "jacobian": s_der, "detj": s_der, "pinv": s_der * cond, "normals": s_der * cond}
+    for f in names:
+        err = orc.rel_err(got[f].to_host_cell_major(), want[KEYS[f]])
+        assert err < orc.TOL_F32 * scale[f], (f, err)
+        base = orc.rel_err(coop[f].to_host_cell_major(), want[KEYS[f]])
+        assert err < 8 * base + 1e-6, (f, err, base)  # 3xTF32 against FP32 arithmetic
+
+
+def test_tensor_facet_normals(cuda):
+    mesh = meshes.curved_box("Tetrahedron", 2, 4, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=F32)
+    ps = tg.facet_point_set("Tetrahedron", 4)
+    with tg.with_strategy("tensor"):
+        got = tg.facet_normals_block(g, 0, ps).to_host_cell_major()
+        assert tg.last_kernel_family() == "tensor"
+    with tg.with_strategy("loops"):
+        want = tg.facet_normals_block(g, 0, ps).to_host_cell_major()
+    assert orc.rel_err(got, want) < 2e-5
