@@ -221,6 +221,24 @@ def gpu_hold(ms: float = 1.0):
     torch.cuda._sleep(int(ms * 2.0e6))
 
 
+def max_over_ranks(x: float, device: str = "cuda") -> float:
+    """The largest value of `x` over the ranks of the process group (`x` itself without one): the
+    slowest rank's time, which the whole-job rate divides by."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: int, world: int, ms: float) -> float:
+    """Units per second of the whole job: every rank processes `units_per_rank` (replicas, weak
+    scaling) in at most `ms` milliseconds."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def time_steps(step, steps, flush, stream):
     """CUDA-event time of each step (L2 flushed before each, outside the events); mean ms."""
     import torch
@@ -691,10 +709,7 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
     sampler.mark(t_wall0, t_wall1)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = max_over_ranks(ms)
 
     # The plain FP64 GPU path on the same mesh: its rate, and the split path's error against it.
     plain = None
@@ -759,10 +774,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
     vol = float(results[e2e_steps - 1])
-    t = torch.tensor([e2e_ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms)
     sampler.stop()
 
     if rank == 0:
@@ -778,7 +790,7 @@ def run_ours(args):
         achieved = alg / (ms * 1e-3) / 1e9
         dtype = {"split": "f32", "f64": "f64", "f32": "f32"}[args.mode]
         line = {
-            "metric": METRIC, "value": world * qpts / (ms_max * 1e-3), "unit": "qpoints/s",
+            "metric": METRIC, "value": whole_job_rate(qpts, world, ms_max), "unit": "qpoints/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic (seeded sin-mapped, jittered P2 tetrahedral box)",
@@ -794,7 +806,7 @@ def run_ours(args):
                                      if args.mode in NCU_TRAFFIC_64 else None),
                          "algorithmic_bytes_per_launch": alg,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in peaks else "fallback 6800"},
-            "e2e": {"value": world * qpts / (e2e_ms * 1e-3), "unit": "qpoints/s",
+            "e2e": {"value": whole_job_rate(qpts, world, e2e_ms), "unit": "qpoints/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": out_es, "ms_per_step": e2e_ms,
                     "measure": vol, "steps": e2e_steps,
                     "pipeline": "host copies of step i+1 overlap the evaluation of step i"},
