@@ -1430,21 +1430,19 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
   if (!wanted_strategy(TLG_FAMILY_JACOBIAN, &strategy)) return TLG_ERR_INVALID_ARGUMENT;
   g_last_kind = TLG_FAMILY_JACOBIAN;
   if (t->td < t->gd) return vjp_surface(t, b, o, ct, a, static_cast<cudaStream_t>(stream));
-  if (t->vjp_bytes == 0)
-    return fail(TLG_ERR_ALLOCATION_TOO_LARGE, "tlg_vjp_block: the adjoint's table exceeds 160 KiB of shared memory");
   const size_t smem = (t->vjp_bytes + 15) / 16 * 16 + tlg::vjp_stage_bytes(split, t->td, (int)t->k);
-  if (smem > (size_t)227 * 1024)
-    return fail(TLG_ERR_ALLOCATION_TOO_LARGE, "tlg_vjp_block: tables and staging (" + std::to_string(smem) +
-                                                  " bytes) exceed 227 KiB of shared memory");
   bool found = false;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (strategy == TLG_STRATEGY_SUMFACT || (strategy == TLG_STRATEGY_AUTO && vjp_sumfact_preferred(t))) {
     tlg_status st = vjp_sumfact(t, a, s, &found);
     if (found) return st;
   }
-  cudaError_t e = split ? tlg::launch_vjp_split(t->td, (int)t->k, a, smem, s, &found)
-                        : tlg::launch_vjp_f64(t->td, (int)t->k, a, smem, s, &found);
-  if (!found) return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: no adjoint kernel for this element");
+  cudaError_t e = cudaSuccess;
+  if (t->vjp_bytes > 0 && smem <= (size_t)227 * 1024)
+    e = split ? tlg::launch_vjp_split(t->td, (int)t->k, a, smem, s, &found)
+              : tlg::launch_vjp_f64(t->td, (int)t->k, a, smem, s, &found);
+  // No node-row kernel for the element (or its table does not fit): K at run time.
+  if (!found) return vjp_surface(t, b, o, ct, a, s);
   if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_block launch");
   g_last_family = TLG_STRATEGY_DIRECT;
   return ok();

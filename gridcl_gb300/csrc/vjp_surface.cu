@@ -1,4 +1,7 @@
-// The adjoint below codimension 0: curves in 2D or 3D and surfaces in 3D (TD < GD), with
+// The adjoint with K at run time: below codimension 0 (curves in 2D or 3D and surfaces in 3D,
+// TD < GD), and in codimension 0 for the elements without a node-row kernel (P4+ tetrahedra, Q3+
+// hexahedra at other than tensor rules, ...), where P = 0 and the area element is det J. Below
+// codimension 0, with
 // cotangents on x, the area element a = sqrt(det(J^T J)), the pseudo-inverse K = G^-1 J^T
 // (G = J^T J) and, for TD + 1 = GD, the unit normal n = s v / |v| (v = J0 x J1 in 3D,
 // (J0_y, -J0_x) in 2D; s = -1 where bit 0 of the cell's flag is set). Per point
@@ -137,7 +140,25 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_surface_kernel(const __grid_
       for (int g = 0; g < GD; ++g)
 #pragma unroll
         for (int d = 0; d < TD; ++d) jb[d * GD + g] = db * area * kk[g * TD + d];
-      if (ctk) {
+      if (ctk && TD == GD) {  // codimension 0: P = 0, Jbar -= K^T Kbar K^T
+        F kb[LJ];
+#pragma unroll
+        for (int i = 0; i < LJ; ++i) kb[i] = ctk[TLG_AT(q, LJ, i)];
+#pragma unroll
+        for (int g = 0; g < GD; ++g)
+#pragma unroll
+          for (int d = 0; d < TD; ++d) {
+            F v = F(0);
+#pragma unroll
+            for (int t = 0; t < TD; ++t) {
+              F kt = F(0);
+#pragma unroll
+              for (int h = 0; h < GD; ++h) kt = A::fma(kb[h * TD + t], kk[h * TD + d], kt);
+              v = A::fma(-kk[g * TD + t], kt, v);
+            }
+            jb[d * GD + g] += v;
+          }
+      } else if (ctk) {
         F kb[LJ], gi[TD * TD], pm[GD * GD];
 #pragma unroll
         for (int i = 0; i < LJ; ++i) kb[i] = ctk[TLG_AT(q, LJ, i)];
@@ -265,10 +286,16 @@ cudaError_t launch_vjp_surface(bool split, int td, int gd, const VjpSurfArgs& a,
     TLG_VS(float, true, 1, 2)
     TLG_VS(float, true, 1, 3)
     TLG_VS(float, true, 2, 3)
+    TLG_VS(float, true, 1, 1)
+    TLG_VS(float, true, 2, 2)
+    TLG_VS(float, true, 3, 3)
   } else {
     TLG_VS(double, false, 1, 2)
     TLG_VS(double, false, 1, 3)
     TLG_VS(double, false, 2, 3)
+    TLG_VS(double, false, 1, 1)
+    TLG_VS(double, false, 2, 2)
+    TLG_VS(double, false, 3, 3)
   }
 #undef TLG_VS
   *found = false;

@@ -417,3 +417,31 @@ def test_csr_with_long_runs_of_unused_nodes(cuda):
     offsets, entries = stable_csr(cells, 20_000)
     assert np.array_equal(inc.offsets.cpu().numpy().view(np.uint32), offsets)
     assert np.array_equal(inc.entries.cpu().numpy().view(np.uint32)[: entries.size], entries)
+
+
+@pytest.mark.parametrize("precision", ["native", "split"])
+@pytest.mark.parametrize("cell,n,degree,rdeg", [("Tetrahedron", 2, 4, 5), ("Hexahedron", 2, 3, 5),
+                                                ("Triangle", 3, 5, 6), ("Quadrilateral", 2, 4, 5)])
+def test_runtime_k_adjoint_for_elements_without_node_row_kernels(cuda, cell, n, degree, rdeg, precision):
+    """Codimension-0 elements without a compiled node-row kernel (P4 tetrahedra, Q3 hexahedra at a
+    shuffled rule, P5 triangles, Q4 quadrilaterals) run the adjoint with K at run time, against the
+    oracle."""
+    mesh = jittered_box(cell, n, degree)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    pts = pts[np.random.default_rng(2).permutation(len(pts))]
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    ncells = mesh.blocks[0].num_cells
+    dt = torch.float64 if precision == "native" else torch.float32
+    ct, host = cotangent_fields(np.random.default_rng(23), ncells, len(pts), dt, g.gdim)
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[: g.gdim])
+    want = orc.vjp(cell, degree, absx, mesh.blocks[0].cells, pts, host["points"], host["detj"][..., 0],
+                   host["pinv"])
+    names = ("points", "detj", "pinv")
+    got, fused = tg.vjp_block(g, 0, ps, ct, precision=precision, forward=names)
+    assert tg.last_kernel_family() == "loops"
+    assert orc.rel_err(got.cpu().numpy(), want) < (1e-11 if precision == "native" else 5e-5)
+    plain = tg.geometric_factors_block(g, 0, ps, names, precision=precision)
+    for k in names:  # the forward kernels sum in another order (cooperative or paired kernels)
+        assert orc.rel_err(fused[k].to_host_cell_major(), plain[k].to_host_cell_major()) < (
+            1e-13 if precision == "native" else 1e-5), k
