@@ -1,4 +1,4 @@
-"""Benchmark of the fused geometry evaluation on one GB300 (the driver's contract).
+"""Benchmark of the fused geometry evaluation on one GB300.
 
 Workload: curved P2 tetrahedra, 64^3 subcells x 6 = 1,572,864 cells (10 nodes each,
 2,146,689 nodes), node coordinates mapped by x' = x + 0.05 sin(2 pi y) sin(2 pi z) (cyclic)
@@ -331,7 +331,7 @@ def extra_hybrid():
 
 
 def extra_hybrid_adjoint():
-    """The benchmark spec's batched fused forward + adjoint on the hybrid mesh (2,000,000 Q2 hex, 27
+    """The batched fused forward + adjoint on the hybrid mesh (2,000,000 Q2 hex, 27
     points; 300,000 P2 prisms, 21; 50,000 P3 tets, 24): seeded standard-normal cotangents on det J
     and K; one graph launch of the split-precision fused forward (x/J/detJ/K) + adjoint + node
     sums against the plain per-block FP64 forward followed by the per-block FP64 adjoint."""

@@ -8,8 +8,7 @@
 //   dL/dJ = dbar a K^T - K^T Kbar K^T + P Kbar^T G^-1 + (normal term),  P = I - J K,
 // the normal term from w = s (nbar - (nbar . v^) v^) / |v|: dL/dJ0 += J1 x w, dL/dJ1 += w x J0
 // (3D) or dL/dJ0 += (-w_y, w_x) (2D); the contributions L(cell, k, g) = sum_q phi_k xbar_g +
-// sum_d dphi_k[d] dL/dJ(g, d) go to the rows the gather reads. This is the benchmark spec's adjoint
-// "on x, det J, J^-1 and normals" where normals exist.
+// sum_d dphi_k[d] dL/dJ(g, d) go to the rows the gather reads.
 //
 // One cell per thread; the cell's coordinates and its contributions sit in the thread's slots in
 // shared memory (K x GD each, interleaved over the threads), K at run time. f64 with TLG_F64
