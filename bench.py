@@ -741,7 +741,7 @@ def run_ours(args):
     host_nodes = g.nodes.cpu().pin_memory()
     host_dofmap = g.blocks[0].dofmap.cpu().pin_memory()
     h2d = host_nodes.numel() * host_nodes.element_size() + host_dofmap.numel() * 4
-    e2e_steps = max(6, min(args.steps, 20))
+    e2e_steps = max(6, min(args.steps, 60))
     geoms = [g, tg.Geometry.from_host(mesh, dtype=mesh_dtype)]
     copy_stream = torch.cuda.Stream()
     comp = torch.cuda.current_stream()
