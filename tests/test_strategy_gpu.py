@@ -434,3 +434,23 @@ def test_tensor_facet_normals(cuda):
     with tg.with_strategy("loops"):
         want = tg.facet_normals_block(g, 0, ps).to_host_cell_major()
     assert orc.rel_err(got, want) < 2e-5
+
+
+@pytest.mark.parametrize("strategy,cell,degree,rdeg,dtype,prec", [
+    ("sumfact", "Hexahedron", 2, 4, F64, "native"), ("sumfact", "Hexahedron", 2, 4, F64, "split"),
+    ("sumfact", "Prism", 2, 4, F32, "native"), ("tensor", "Tetrahedron", 4, 5, F32, "native"),
+    ("tensor", "Tetrahedron", 4, 5, F64, "split"), ("cooperative", "Tetrahedron", 4, 5, F64, "split")])
+def test_chunked_ranges_equal_one_launch(cuda, strategy, cell, degree, rdeg, dtype, prec):
+    """Chunks of 37 cells (ranges starting mid-tile, outputs at chunk offsets) give the values of
+    one launch over the block, bit for bit, for each kernel family."""
+    mesh = meshes.curved_box(cell, 3, degree, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=dtype)
+    pts, _ = tg.refcell.gauss_rule(cell, rdeg)
+    ps = tg.PointSet(cell, pts, np.ones(len(pts)))
+    names = ("points", "jacobian", "detj", "pinv")
+    with tg.with_strategy(strategy):
+        whole = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+        assert tg.last_kernel_family() == strategy
+        parts = tg.geometric_factors_block(g, 0, ps, names, precision=prec, max_chunk_cells=37)
+    for f in names:
+        assert np.array_equal(whole[f].to_host_cell_major(), parts[f].to_host_cell_major()), f
