@@ -441,8 +441,8 @@ def test_tensor_facet_normals(cuda):
     ("sumfact", "Prism", 2, 4, F32, "native"), ("tensor", "Tetrahedron", 4, 5, F32, "native"),
     ("tensor", "Tetrahedron", 4, 5, F64, "split"), ("cooperative", "Tetrahedron", 4, 5, F64, "split")])
 def test_chunked_ranges_equal_one_launch(cuda, strategy, cell, degree, rdeg, dtype, prec):
-    """Chunks of 37 cells (ranges starting mid-tile, outputs at chunk offsets) give the values of
-    one launch over the block, bit for bit, for each kernel family."""
+    """Chunks of at most 37 cells (32-cell ranges at block offsets, each chunk's own output) give
+    the values of one launch over the block, bit for bit, for each kernel family."""
     mesh = meshes.curved_box(cell, 3, degree, jitter=0.02)
     g = tg.Geometry.from_host(mesh, dtype=dtype)
     pts, _ = tg.refcell.gauss_rule(cell, rdeg)
