@@ -103,6 +103,8 @@ SIGNATURES = [
     ("tlg_vjp_block", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs),
                            ctypes.POINTER(TlgCotangents), _P, _L, _P]),
     ("tlg_vjp_gather", _I, [_P, _P, _L, _I, _P, _I, _P, _P]),
+    ("tlg_measure_workspace_bytes", _L, [_I, _L]),
+    ("tlg_measure", _I, [_P, _I, _L, _L, _I, _P, _P, _L, _P, _P]),
     ("tlg_vjp_gather_add", _I, [_P, _P, _L, _I, _P, _I, _P, _P]),
     ("tlg_vjp_batch_create", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs),
                                   ctypes.POINTER(TlgCotangents), _P, _P, _P, _P, _L, _I, _P, _I, _P]),

@@ -123,6 +123,9 @@ __global__ void __launch_bounds__(256) cell_block_sums_kernel(const F* detj, con
 
 namespace {
 
+tlg_status measure_into(const void* detj, int dtype, int64_t num_cells, int64_t num_points, int shift,
+                        const void* weights, void* scratch, void* result, cudaStream_t s);
+
 // Device address of g_measure_scratch for each device, found once per device (with that device
 // current) by the first call made on it.
 std::mutex g_scratch_mutex;
@@ -228,6 +231,44 @@ tlg_status tlg_measure_static(const void* detj, int dtype, int64_t num_cells, in
   void* scratch = nullptr;
   tlg_status st = static_scratch(&scratch);
   if (st != TLG_OK) return st;
+  return measure_into(detj, dtype, num_cells, num_points, shift, weights, scratch, result, s);
+}
+
+int64_t tlg_measure_workspace_bytes(int dtype, int64_t num_cells) {
+  if ((dtype != TLG_F32 && dtype != TLG_F64) || num_cells < 0) return -1;
+  const int64_t level1 = (num_cells + tlg::kSumBlock - 1) / tlg::kSumBlock;
+  return level1 > 1 ? (level1 + tlg::tree_elems(level1)) * dtype : 0;
+}
+
+tlg_status tlg_measure(const void* detj, int dtype, int64_t num_cells, int64_t num_points, int tile,
+                       const void* weights, void* workspace, int64_t workspace_bytes, void* result, void* stream) {
+  int shift = -1;
+  for (int s = 0; s <= 4; ++s)
+    if (tile == (1 << s)) shift = s;
+  if (shift < 0 || (dtype != TLG_F32 && dtype != TLG_F64) || num_cells < 0 || num_points < 0 ||
+      num_points > (1 << 30) || !result)
+    return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_measure: bad tile, dtype, sizes or result");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (num_cells == 0 || num_points == 0) {
+    cudaError_t e = cudaMemsetAsync(result, 0, dtype, s);
+    return e == cudaSuccess ? tlg::ok() : tlg::cuda_fail(e, "tlg_measure");
+  }
+  if (!detj || !weights) return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_measure: NULL input");
+  const int64_t need = tlg_measure_workspace_bytes(dtype, num_cells);
+  if (workspace_bytes < need || (need > 0 && !workspace))
+    return tlg::fail(TLG_ERR_LENGTH_MISMATCH, "tlg_measure: workspace of " + std::to_string(workspace_bytes) +
+                                                  " bytes, " + std::to_string(need) + " needed");
+  return measure_into(detj, dtype, num_cells, num_points, shift, weights, workspace, result, s);
+}
+
+}  // extern "C"
+
+namespace {
+
+// Level 1 (sums of 64 consecutive cell sums) straight from the det J field into `scratch` (or the
+// result when there is one value), then the tree.
+tlg_status measure_into(const void* detj, int dtype, int64_t num_cells, int64_t num_points, int shift,
+                        const void* weights, void* scratch, void* result, cudaStream_t s) {
   const int64_t level1 = (num_cells + tlg::kSumBlock - 1) / tlg::kSumBlock;
   const unsigned grid = tlg::grid_for(num_cells, 256);
   cudaError_t e = cudaSuccess;
@@ -246,10 +287,10 @@ tlg_status tlg_measure_static(const void* detj, int dtype, int64_t num_cells, in
     e = cudaGetLastError();
     if (e == cudaSuccess && level1 > 1) e = tlg::sum_tree<double>(l1, level1, l1 + level1, static_cast<double*>(result), s);
   }
-  return e == cudaSuccess ? tlg::ok() : tlg::cuda_fail(e, "tlg_measure_static launch");
+  return e == cudaSuccess ? tlg::ok() : tlg::cuda_fail(e, "measure launch");
 }
 
-}  // extern "C"
+}  // namespace
 
 // ----------------------------------------------------------------------------------------
 // Self-test of the integer conversions used by the split kernels.

@@ -425,9 +425,16 @@ def measure_block(g: Geometry, b: int, pts: PointSet, detj: QuadField | None = N
         detj = detj_block(g, b, pts)
     dt = detj.chunks[0].data.dtype
     es = _DTYPES[dt]
-    sums = torch.empty(blk.num_cells, dtype=dt, device=dev)
     w = pts.weights_device(dt, dev)
     stream = current_stream_handle()
+    if len(detj.chunks) == 1:  # one launch for the cell sums and the tree's first level
+        nbytes = int(lib().tlg_measure_workspace_bytes(es, blk.num_cells))
+        work = torch.empty(max(nbytes, es), dtype=torch.uint8, device=dev)  # stream-ordered reuse
+        result = torch.empty(1, dtype=dt, device=dev)
+        check(lib().tlg_measure(detj.chunks[0].data.data_ptr(), es, blk.num_cells, detj.num_points, detj.tile,
+                                w.data_ptr(), work.data_ptr(), nbytes, result.data_ptr(), stream))
+        return float(result.item()) if sync else result
+    sums = torch.empty(blk.num_cells, dtype=dt, device=dev)
     for ch in detj.chunks:
         check(lib().tlg_measure_cell_sums(ch.data.data_ptr(), es, ch.num_cells, detj.num_points,
                                           detj.tile, w.data_ptr(),

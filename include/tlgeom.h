@@ -407,6 +407,14 @@ tlg_status tlg_sum(const void* x, int dtype, int64_t n, void* workspace, int64_t
 tlg_status tlg_measure_static(const void* detj, int dtype, int64_t num_cells, int64_t num_points,
                               int tile, const void* weights, void* result, void* stream);
 int64_t tlg_measure_static_max_cells(void);
+/* The same measure with a workspace of the caller (no size limit, no shared scratch):
+ * tlg_measure_workspace_bytes(dtype, num_cells) bytes, 0 for up to 64 cells; -1 for bad
+ * arguments. Level 1 of the tree comes straight from the det J field (one launch fewer than
+ * tlg_measure_cell_sums + tlg_sum), with the same bits. */
+int64_t tlg_measure_workspace_bytes(int dtype, int64_t num_cells);
+tlg_status tlg_measure(const void* detj, int dtype, int64_t num_cells, int64_t num_points, int tile,
+                       const void* weights, void* workspace, int64_t workspace_bytes, void* result,
+                       void* stream);
 
 /* Self-test of the split kernels' integer f64 -> f32 rounding and f32 -> f64 widening against
  * the conversion instructions: mismatches[0] += the number of x[0..n) (device f64 values) whose

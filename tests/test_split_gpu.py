@@ -162,3 +162,38 @@ def test_measure_of_a_split_field(cuda):
     plain = tg.measure_block(g, 0, ps)  # the f64 path
     assert abs(blocking - plain) < 1e-6 * abs(plain)
     assert abs(plain - 1.0) < 1e-12  # the curved map keeps the unit cube's boundary
+
+
+@pytest.mark.parametrize("ncells", [1, 64, 65, 4097, 262145])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_fused_measure_equals_two_steps(cuda, ncells, dtype):
+    """tlg_measure (level 1 of the tree straight from det J, the caller's workspace) gives the bits
+    of tlg_measure_cell_sums followed by tlg_sum, and measure_block over one chunk equals it over
+    several chunks."""
+    from gridcl_gb300._lib import check, lib
+    from gridcl_gb300.geometry import current_stream_handle
+
+    rng = np.random.default_rng(ncells)
+    nq = 7
+    f = tg.QuadField.uninit(ncells, nq, 1, 16, dtype)
+    f.chunks[0].data.copy_(torch.from_numpy(rng.random(f.chunks[0].data.numel())))
+    w = torch.from_numpy(rng.random(nq)).to(dtype).cuda()
+    es = 8 if dtype == torch.float64 else 4
+    s = current_stream_handle()
+    nbytes = int(lib().tlg_measure_workspace_bytes(es, ncells))
+    work = torch.empty(max(nbytes, es), dtype=torch.uint8, device="cuda")
+    fused = torch.empty(1, dtype=dtype, device="cuda")
+    check(lib().tlg_measure(f.chunks[0].data.data_ptr(), es, ncells, nq, 16, w.data_ptr(), work.data_ptr(),
+                            nbytes, fused.data_ptr(), s))
+    sums = torch.empty(ncells, dtype=dtype, device="cuda")
+    check(lib().tlg_measure_cell_sums(f.chunks[0].data.data_ptr(), es, ncells, nq, 16, w.data_ptr(),
+                                      sums.data_ptr(), s))
+    tb = int(lib().tlg_sum_workspace_bytes(es, ncells))
+    tw = torch.empty(max(tb, es), dtype=torch.uint8, device="cuda")
+    two = torch.empty(1, dtype=dtype, device="cuda")
+    check(lib().tlg_sum(sums.data_ptr(), es, ncells, tw.data_ptr(), tb, two.data_ptr(), s))
+    assert torch.equal(fused, two)
+    if nbytes > 0:
+        with pytest.raises(tg.GridError):
+            check(lib().tlg_measure(f.chunks[0].data.data_ptr(), es, ncells, nq, 16, w.data_ptr(),
+                                    work.data_ptr(), nbytes - 1, fused.data_ptr(), s))
