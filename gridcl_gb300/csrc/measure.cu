@@ -16,6 +16,28 @@ namespace tlg {
 
 constexpr int kSumBlock = 64;  // measure.rs:44
 
+// det J * w summed over the points of one cell, in point order: d0*w0, then fma(d_q, w_q, acc).
+// The loads are issued eight at a time ahead of the fma chain, so that each thread keeps several
+// reads in flight; the order of the arithmetic does not depend on that.
+template <typename F>
+__device__ __forceinline__ F cell_sum(const F* __restrict__ detj, const F* __restrict__ weights,
+                                      int64_t base, int num_points, int tile_shift) {
+  constexpr int U = 8;
+  F acc = F(0);
+  for (int q0 = 0; q0 < num_points; q0 += U) {
+    F v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+      v[u] = q0 + u < num_points ? __ldg(detj + base + ((int64_t)(q0 + u) << tile_shift)) : F(0);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int q = q0 + u;
+      if (q < num_points) acc = q == 0 ? v[u] * __ldg(weights) : fma(v[u], __ldg(weights + q), acc);
+    }
+  }
+  return acc;
+}
+
 template <typename F>
 __global__ void __launch_bounds__(256) cell_sums_kernel(const F* detj, const F* weights, F* out,
                                                         int64_t num_cells, int num_points,
@@ -24,21 +46,42 @@ __global__ void __launch_bounds__(256) cell_sums_kernel(const F* detj, const F* 
   for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < num_cells;
        c += (int64_t)gridDim.x * blockDim.x) {
     const int64_t base = (((c >> tile_shift) * num_points) << tile_shift) + (c & mask);
-    F acc = detj[base] * weights[0];
-    for (int q = 1; q < num_points; ++q) acc = fma(detj[base + ((int64_t)q << tile_shift)], weights[q], acc);
-    out[c] = acc;
+    out[c] = cell_sum(detj, weights, base, num_points, tile_shift);
   }
 }
 
+// Left fold ((v0 + v1) + v2) + ... of the `count` <= 64 values a warp holds two per lane (lane l:
+// v[l] in lo, v[32 + l] in hi); every lane gets the result. The shuffles do not depend on the
+// running sum, so they issue ahead of the chain of adds.
+template <typename F>
+__device__ __forceinline__ F warp_fold(F lo, F hi, int count) {
+  F acc = __shfl_sync(0xffffffffu, lo, 0);
+#pragma unroll
+  for (int j = 1; j < 32; ++j) {
+    const F v = __shfl_sync(0xffffffffu, lo, j);
+    if (j < count) acc += v;
+  }
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const F v = __shfl_sync(0xffffffffu, hi, j);
+    if (32 + j < count) acc += v;
+  }
+  return acc;
+}
+
+// One level of the tree: out[i] = x[64 i] + ... + x[64 i + 63] (fewer at the end), summed in that
+// order. One warp per output: two coalesced loads, then the fold.
 template <typename F>
 __global__ void __launch_bounds__(256) block_sum_kernel(const F* x, F* out, int64_t len, int64_t num_out) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < num_out;
-       i += (int64_t)gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < num_out; i += warps) {
     const int64_t start = i * kSumBlock;
-    const int64_t end = start + kSumBlock < len ? start + kSumBlock : len;
-    F acc = x[start];
-    for (int64_t j = start + 1; j < end; ++j) acc += x[j];
-    out[i] = acc;
+    const int count = (int)(len - start < kSumBlock ? len - start : kSumBlock);
+    const F lo = lane < count ? x[start + lane] : F(0);
+    const F hi = 32 + lane < count ? x[start + 32 + lane] : F(0);
+    const F acc = warp_fold(lo, hi, count);
+    if (lane == 0) out[i] = acc;
   }
 }
 
@@ -68,7 +111,7 @@ cudaError_t sum_tree(const F* x, int64_t n, F* work, F* result, cudaStream_t s) 
   while (n > 1) {
     const int64_t m = (n + kSumBlock - 1) / kSumBlock;
     F* dst = m == 1 ? result : next;
-    block_sum_kernel<F><<<grid_for(m, 256), 256, 0, s>>>(cur, dst, n, m);
+    block_sum_kernel<F><<<grid_for(m * 32, 256), 256, 0, s>>>(cur, dst, n, m);
     cur = dst;
     next = dst + m;
     n = m;
@@ -87,35 +130,46 @@ constexpr int64_t kStaticMaxCells = int64_t(1) << 24;  // 16,777,216 cells
 constexpr int64_t kStaticScratchElems = 266368;
 static __device__ __align__(256) double g_measure_scratch[kStaticScratchElems];  // 2,130,944 bytes
 
+// Level 1 straight from det J: one warp per 64 consecutive cells, lane l summing cells l and
+// 32 + l over the points (sixteen loads in flight), then the fold of the 64 cell sums.
 template <typename F>
 __global__ void __launch_bounds__(256) cell_block_sums_kernel(const F* detj, const F* weights, F* out,
                                                               int64_t num_cells, int num_points,
                                                               int tile_shift) {
-  __shared__ F sums[256];
+  const int lane = threadIdx.x & 31;
   const int64_t mask = (1 << tile_shift) - 1;
   const int64_t nblocks = (num_cells + kSumBlock - 1) / kSumBlock;
-  for (int64_t base_cell = (int64_t)blockIdx.x * 256; base_cell < num_cells;
-       base_cell += (int64_t)gridDim.x * 256) {
-    const int64_t c = base_cell + threadIdx.x;
-    if (c < num_cells) {
-      const int64_t base = (((c >> tile_shift) * num_points) << tile_shift) + (c & mask);
-      F acc = detj[base] * weights[0];
-      for (int q = 1; q < num_points; ++q) acc = fma(detj[base + ((int64_t)q << tile_shift)], weights[q], acc);
-      sums[threadIdx.x] = acc;
-    }
-    __syncthreads();
-    if (threadIdx.x < 256 / kSumBlock) {
-      const int64_t i = base_cell / kSumBlock + threadIdx.x;  // level-1 value index
-      const int64_t start = i * kSumBlock;
-      if (i < nblocks) {
-        const int64_t end = start + kSumBlock < num_cells ? start + kSumBlock : num_cells;
-        const int local = (int)(start - base_cell);
-        F acc = sums[local];
-        for (int64_t j = start + 1; j < end; ++j) acc += sums[local + (int)(j - start)];
-        out[i] = acc;
+  const int64_t warps = (int64_t)gridDim.x * (blockDim.x >> 5);
+  for (int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < nblocks; i += warps) {
+    const int64_t start = i * kSumBlock;
+    const int count = (int)(num_cells - start < kSumBlock ? num_cells - start : kSumBlock);
+    const int64_t c0 = start + lane, c1 = start + 32 + lane;
+    const bool v0 = lane < count, v1 = 32 + lane < count;
+    const int64_t b0 = (((c0 >> tile_shift) * num_points) << tile_shift) + (c0 & mask);
+    const int64_t b1 = (((c1 >> tile_shift) * num_points) << tile_shift) + (c1 & mask);
+    F a0 = F(0), a1 = F(0);
+    constexpr int U = 8;
+    for (int q0 = 0; q0 < num_points; q0 += U) {
+      F d0[U], d1[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int64_t off = (int64_t)(q0 + u) << tile_shift;
+        const bool in = q0 + u < num_points;
+        d0[u] = in && v0 ? __ldg(detj + b0 + off) : F(0);
+        d1[u] = in && v1 ? __ldg(detj + b1 + off) : F(0);
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int q = q0 + u;
+        if (q < num_points) {
+          const F w = __ldg(weights + q);
+          a0 = q == 0 ? d0[u] * w : fma(d0[u], w, a0);
+          a1 = q == 0 ? d1[u] * w : fma(d1[u], w, a1);
+        }
       }
     }
-    __syncthreads();
+    const F acc = warp_fold(a0, a1, count);
+    if (lane == 0) out[i] = acc;
   }
 }
 
@@ -270,7 +324,7 @@ namespace {
 tlg_status measure_into(const void* detj, int dtype, int64_t num_cells, int64_t num_points, int shift,
                         const void* weights, void* scratch, void* result, cudaStream_t s) {
   const int64_t level1 = (num_cells + tlg::kSumBlock - 1) / tlg::kSumBlock;
-  const unsigned grid = tlg::grid_for(num_cells, 256);
+  const unsigned grid = tlg::grid_for(level1 * 32, 256);
   cudaError_t e = cudaSuccess;
   if (dtype == TLG_F32) {
     float* l1 = level1 == 1 ? static_cast<float*>(result) : static_cast<float*>(scratch);
