@@ -735,9 +735,10 @@ def run_ours(args):
 
     # End to end through the public API, pipelined as a streaming user would run it: every step
     # copies its inputs (nodes and dofmap) from pinned host memory into one of two device input
-    # sets on a copy stream, evaluates them and takes the measure on the compute stream, and
-    # copies the measure back into pinned host memory; the copy of step i + 1 overlaps the
-    # evaluation of step i. The timed region ends when the last result has reached the host.
+    # sets on a copy stream, evaluates them on the compute stream (the evaluation also sums each
+    # cell's det J * w, its cell_measure) and sums those into the measure, and copies the measure
+    # back into pinned host memory; the copy of step i + 1 overlaps the evaluation of step i. The
+    # timed region ends when the last result has reached the host.
     host_nodes = g.nodes.cpu().pin_memory()
     host_dofmap = g.blocks[0].dofmap.cpu().pin_memory()
     h2d = host_nodes.numel() * host_nodes.element_size() + host_dofmap.numel() * 4
@@ -748,6 +749,7 @@ def run_ours(args):
     copied = [torch.cuda.Event() for _ in geoms]
     consumed = [torch.cuda.Event() for _ in geoms]
     results = torch.zeros(e2e_steps, dtype=out["detj"].chunks[0].data.dtype).pin_memory()
+    cell_meas = torch.empty(g.blocks[0].num_cells, dtype=results.dtype, device=g.nodes.device)
 
     def e2e_step(i):
         k = i % 2
@@ -758,8 +760,8 @@ def run_ours(args):
             gk.blocks[0].dofmap.copy_(host_dofmap, non_blocking=True)
             copied[k].record(copy_stream)
         comp.wait_event(copied[k])
-        f = tg.geometric_factors_block(gk, 0, ps, factors, out=out, precision=precision)
-        r = tg.measure_block(gk, 0, ps, detj=f["detj"], sync=False)
+        tg.geometric_factors_block(gk, 0, ps, factors, out=out, precision=precision, cell_measure=cell_meas)
+        r = tg.measure_block(gk, 0, ps, cell_sums=cell_meas, sync=False)
         consumed[k].record(comp)
         results[i % e2e_steps].copy_(r[0], non_blocking=True)
 

@@ -67,6 +67,8 @@ class TlgOutputs(ctypes.Structure):
         ("facet_normals", ctypes.c_void_p),
         ("cond_limit", ctypes.c_double),
         ("recomputed", ctypes.c_void_p),
+        ("weights", ctypes.c_void_p),
+        ("cell_measure", ctypes.c_void_p),
     ]
 
 

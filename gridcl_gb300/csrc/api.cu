@@ -141,6 +141,7 @@ constexpr int kFamilies = 6;
 thread_local int g_override[kFamilies] = {-1, -1, -1, -1, -1, -1};
 // The strategy that ran in this thread's last launch (TLG_STRATEGY_*, 0: none) and its family.
 thread_local int g_last_family = 0;
+thread_local bool g_measure_fused = false;  // the last eval launch summed cell_measure
 thread_local int g_last_kind = -1;
 
 const char* const kFamilyNames[kFamilies] = {"EVector", "Points", "Jacobian", "Normals", "FacetNormals", "PullBack"};
@@ -314,10 +315,16 @@ tlg_status eval_pair(const tlg_tables* t, const tlg_block* b, const tlg_outputs*
     *found = false;
     return TLG_ERR_UNSUPPORTED;
   }
+  if (o->cell_measure) {  // summed as the points are evaluated
+    a.mask |= tlg::kOutCellMeasure;
+    a.weights = static_cast<const float*>(o->weights);
+    a.cell_measure = static_cast<float*>(o->cell_measure);
+  }
   cudaError_t e = tlg::launch_eval_pair(split, t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
   if (!*found) return TLG_ERR_UNSUPPORTED;
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
   g_last_family = TLG_STRATEGY_DIRECT;
+  g_measure_fused = o->cell_measure != nullptr;
   return ok();
 }
 
@@ -1138,6 +1145,46 @@ tlg_status tlg_tables_device_status(const tlg_tables* t, void* stream) {
   return ok();
 }
 
+}  // extern "C"
+
+namespace {
+
+// The strategy's kernel for one range (the reference's dispatch, strategy.rs:311-407).
+tlg_status eval_dispatch(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                         cudaStream_t s) {
+  const int family = principal_family(mask);
+  int strategy = TLG_STRATEGY_AUTO;
+  if (!wanted_strategy(family, &strategy)) return TLG_ERR_INVALID_ARGUMENT;
+  g_last_kind = family;
+  // A forced strategy that does not apply runs the loops kernel (strategy.rs:400-404); AUTO
+  // falls through to the unrolled kernels, then the loops kernel over staged tables.
+  const bool is_auto = strategy == TLG_STRATEGY_AUTO;
+  if (strategy == TLG_STRATEGY_SUMFACT || (is_auto && sumfact_preferred(t))) {
+    bool found = false;
+    tlg_status st = eval_sumfact(t, b, o, mask, s, &found);
+    if (found) return st;
+  }
+  if (strategy == TLG_STRATEGY_TENSOR || (is_auto && tc_preferred(t))) {
+    bool found = false;
+    tlg_status st = eval_tc(t, b, o, mask, s, &found);
+    if (found) return st;
+  }
+  if (strategy == TLG_STRATEGY_COOPERATIVE || (is_auto && coop_preferred(t))) {
+    bool found = false;
+    tlg_status st = eval_coop(t, b, o, mask, s, &found);
+    if (found) return st;
+  }
+  const bool allow_direct = is_auto || strategy == TLG_STRATEGY_DIRECT;
+  const bool global_tables = !(is_auto || strategy == TLG_STRATEGY_SHARED);
+  if (t->dtype == TLG_SPLIT32) return eval_split(t, b, o, mask, s, allow_direct, global_tables);
+  if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, s, allow_direct, global_tables);
+  return eval_typed<double>(t, b, o, mask, s, allow_direct, global_tables);
+}
+
+}  // namespace
+
+extern "C" {
+
 tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o,
                           void* stream) {
   if (!t || !b || !o) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: NULL argument");
@@ -1166,6 +1213,8 @@ tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_out
   if (o->facet_normals && (t->td != t->gd || !t->has_refn))
     return fail(TLG_ERR_INVALID_ARGUMENT,
                 "tlg_eval_block: facet normals need codimension 0 and tables with reference normals");
+  if (o->cell_measure && (!o->detj || !o->weights))
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: cell_measure needs the det J output and weights");
   if (o->num_cells == 0 || t->q == 0 || mask == 0) return ok();  // layout.rs:509-511
   if (!b->nodes || !b->dofmap) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_eval_block: NULL nodes or dofmap");
   if (b->num_nodes < 1)  // Geometry::new rejects cells without nodes (geometry.rs:268-275)
@@ -1173,33 +1222,14 @@ tlg_status tlg_eval_block(const tlg_tables* t, const tlg_block* b, const tlg_out
   if (b->num_nodes > (int64_t)UINT32_MAX + 1 || b->num_cells > (int64_t)UINT32_MAX)
     return fail(TLG_ERR_TOO_LARGE, "tlg_eval_block: node or cell count does not fit u32");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const int family = principal_family(mask);
-  int strategy = TLG_STRATEGY_AUTO;
-  if (!wanted_strategy(family, &strategy)) return TLG_ERR_INVALID_ARGUMENT;
-  g_last_kind = family;
-  // A forced strategy that does not apply runs the loops kernel (strategy.rs:400-404); AUTO
-  // falls through to the unrolled kernels, then the loops kernel over staged tables.
-  const bool is_auto = strategy == TLG_STRATEGY_AUTO;
-  if (strategy == TLG_STRATEGY_SUMFACT || (is_auto && sumfact_preferred(t))) {
-    bool found = false;
-    tlg_status st = eval_sumfact(t, b, o, mask, s, &found);
-    if (found) return st;
-  }
-  if (strategy == TLG_STRATEGY_TENSOR || (is_auto && tc_preferred(t))) {
-    bool found = false;
-    tlg_status st = eval_tc(t, b, o, mask, s, &found);
-    if (found) return st;
-  }
-  if (strategy == TLG_STRATEGY_COOPERATIVE || (is_auto && coop_preferred(t))) {
-    bool found = false;
-    tlg_status st = eval_coop(t, b, o, mask, s, &found);
-    if (found) return st;
-  }
-  const bool allow_direct = is_auto || strategy == TLG_STRATEGY_DIRECT;
-  const bool global_tables = !(is_auto || strategy == TLG_STRATEGY_SHARED);
-  if (t->dtype == TLG_SPLIT32) return eval_split(t, b, o, mask, s, allow_direct, global_tables);
-  if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, s, allow_direct, global_tables);
-  return eval_typed<double>(t, b, o, mask, s, allow_direct, global_tables);
+  g_measure_fused = false;
+  tlg_status st = eval_dispatch(t, b, o, mask, s);
+  if (st != TLG_OK || !o->cell_measure || g_measure_fused) return st;
+  // The kernel that ran does not sum the measure: per-cell sums over the det J it wrote (the
+  // range starts at a tile boundary of the output, so its cells start a tile there).
+  const int es = t->dtype == TLG_F64 ? 8 : 4;
+  const unsigned char* detj = static_cast<const unsigned char*>(o->detj) + o->out_first_cell * t->q * es;
+  return tlg_measure_cell_sums(detj, es, o->num_cells, t->q, o->tile, o->weights, o->cell_measure, stream);
 }
 
 tlg_status tlg_set_strategy(int strategy) {
@@ -1390,6 +1420,8 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
   if (b->gdim != t->gd) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: block and tables differ in gdim");
   if (o->tile != 16) return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block: the adjoint runs with tile 16");
   if (o->facet_normals) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: no facet normals in the fused forward");
+  if (o->cell_measure)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: cell_measure is summed by tlg_eval_block only");
   if ((o->normals || ct->normals) && t->td + 1 != t->gd)
     return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block: normals exist for TD + 1 = GD only");
   if (o->first_cell < 0 || o->num_cells < 0 || o->first_cell + o->num_cells > b->num_cells ||

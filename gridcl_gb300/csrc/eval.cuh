@@ -45,6 +45,7 @@ enum : uint32_t {
   kOutPinv = 8u,
   kOutNormals = 16u,
   kOutFacetNormals = 32u,
+  kOutCellMeasure = 64u,  // the paired kernels: per-cell sums of det J * w (PairArgs::cell_measure)
 };
 
 template <typename F>
@@ -89,6 +90,8 @@ struct PairArgs {
   int num_points;
   uint32_t off_dphi;  // the f32 derivative table [Q][K][TD] (split loops kernel; phi [Q][K] at 0)
   int k_runtime;      // K (split loops kernel)
+  const float* weights;  // [Q], with kOutCellMeasure
+  float* cell_measure;   // [range_cells], with kOutCellMeasure
 };
 
 // ----------------------------------------------------------------------------------------
@@ -513,6 +516,7 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
     if (mask & kOutNormals) cn.init(a.out[4], tile_idx, nq, lane);
     if (mask & kOutFacetNormals) cf.init(a.out[5], tile_idx, nq, lane);
 
+    float meas = 0.0f;  // sum of det J * w over the points so far, in point order
     for (int qp = 0; qp < nqp; ++qp) {
       const bool both = 2 * qp + 1 < nq;
       const float4* rq = rows2 + (int64_t)qp * K * RW4;
@@ -603,8 +607,9 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
       float* pd = (mask & kOutDetJ) ? cd.p : nullptr;
       float* pk = (mask & kOutPinv) ? ck.p : nullptr;
       if (mask & kOutJacobian) cj.put2(j, both);
+      float2 dj = A::splat(0.0f);
       if (mask & kOutDetJ) {
-        const float2 dj = M::detj(j);
+        dj = M::detj(j);
         cd.put2(&dj, both);
       }
       if (mask & kOutPinv) ck.put2(kk, both);
@@ -625,10 +630,12 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
           cn.put2(n, both);
         }
       }
+      bool redone = false;
       if constexpr (SPLIT) {
         // Near-degenerate points (or non-finite estimates) again in FP64.
         const float2 kap = M::condition(j, kk);
         if ((pj || pd || pk) && (!(kap.x <= a.cond_limit) || (both && !(kap.y <= a.cond_limit)))) {
+          redone = true;
           const double* nodes = static_cast<const double*>(a.nodes);
           const uint32_t* row = a.dofmap + cell * K;
           for (int h = 0; h < (both ? 2 : 1); ++h) {
@@ -642,7 +649,17 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
           }
         }
       }
+      if (mask & kOutCellMeasure) {
+        if (redone) {  // the det J values as stored (this thread's own writes)
+          dj.x = pd[0];
+          if (both) dj.y = pd[TILE];
+        }
+        const int q0 = 2 * qp;
+        meas = q0 == 0 ? dj.x * __ldg(a.weights) : fmaf(dj.x, __ldg(a.weights + q0), meas);
+        if (both) meas = fmaf(dj.y, __ldg(a.weights + q0 + 1), meas);
+      }
     }
+    if ((mask & kOutCellMeasure) && c < a.range_cells) a.cell_measure[c] = meas;
   }
 }
 

@@ -323,9 +323,14 @@ SPLIT32 = 12  # ABI code of the split-precision tables
 def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points", "jacobian", "detj", "pinv"),
                             tile: int = GPU_QUAD_TILE, max_chunk_cells: int | None = None,
                             out: dict | None = None, precision: str = "native",
-                            cond_limit: float = 0.0, recomputed: torch.Tensor | None = None) -> dict:
+                            cond_limit: float = 0.0, recomputed: torch.Tensor | None = None,
+                            cell_measure: torch.Tensor | None = None) -> dict:
     """Every factor in `factors` of block b at the points of `pts`, in one fused launch per
     chunk; returns ``{factor: QuadField}``. `out` may pass preallocated fields.
+
+    `cell_measure` (a contiguous CUDA tensor of the fields' type, one value per cell; "detj" among
+    the factors) receives each cell's sum of det J * w over the points, the values
+    :func:`measure_block` sums; the paired kernels add them up as they evaluate.
 
     ``precision="native"`` computes in the mesh's scalar type. ``precision="split"`` (f64 meshes)
     computes in FP32 on cell-shifted coordinates and returns f32 fields; points whose condition
@@ -352,6 +357,14 @@ def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points
     desc = g.block_desc(b)
     stream = current_stream_handle()
     nchunks = len(next(iter(fields.values())).chunks) if fields else 0
+    wptr = None
+    if cell_measure is not None:
+        if "detj" not in names:
+            raise GridError(1, "cell_measure needs detj among the factors")
+        if (cell_measure.dtype != out_dtype or not cell_measure.is_cuda or not cell_measure.is_contiguous()
+                or cell_measure.numel() < blk.num_cells):
+            raise GridError(1, f"cell_measure must be a contiguous CUDA {out_dtype} tensor of {blk.num_cells} values")
+        wptr = pts.weights_device(out_dtype, cell_measure.device).data_ptr()
     for ci in range(nchunks):
         o = TlgOutputs()
         ch0 = fields[names[0]].chunks[ci]
@@ -363,6 +376,9 @@ def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points
         o.recomputed = recomputed.data_ptr() if recomputed is not None else None
         for f in names:
             setattr(o, f, fields[f].chunks[ci].data.data_ptr())
+        if cell_measure is not None:
+            o.weights = wptr
+            o.cell_measure = cell_measure.data_ptr() + ch0.first_cell * cell_measure.element_size()
         check(lib().tlg_eval_block(tables.handle, ctypes.byref(desc), ctypes.byref(o), stream))
         _note_launch()
     return fields
@@ -411,16 +427,26 @@ def facet_point_set(cell: str, degree: int) -> PointSet:
 
 
 def measure_block(g: Geometry, b: int, pts: PointSet, detj: QuadField | None = None,
-                  sync: bool = True):
+                  sync: bool = True, cell_sums: torch.Tensor | None = None):
     """The measure of block b: sum over cells and points of det J * w, per cell then by a tree of
     64-value sums, all on the device in the det J field's type, read back once
     (tetraloma-geometry/src/measure.rs:141-185). `detj` may pass an already computed det J field
     of the same point set (an f32 field of split precision sums in f32). With ``sync=False`` the
-    result stays on the device: a one-element tensor, ready when the current stream reaches it."""
+    result stays on the device: a one-element tensor, ready when the current stream reaches it.
+    `cell_sums` may pass the per-cell sums an evaluation wrote (its ``cell_measure``); only the
+    tree over them runs then."""
     blk = g.blocks[b]
     dev = g.nodes.device
     if blk.num_cells == 0 or len(pts) == 0:
         return 0.0 if sync else torch.zeros(1, dtype=g.dtype, device=dev)
+    if cell_sums is not None:
+        dt = cell_sums.dtype
+        nbytes = int(lib().tlg_sum_workspace_bytes(_DTYPES[dt], blk.num_cells))
+        work = torch.empty(max(nbytes, 8), dtype=torch.uint8, device=dev)
+        result = torch.empty(1, dtype=dt, device=dev)
+        check(lib().tlg_sum(cell_sums.data_ptr(), _DTYPES[dt], blk.num_cells, work.data_ptr(), nbytes,
+                            result.data_ptr(), current_stream_handle()))
+        return float(result.item()) if sync else result
     if detj is None:
         detj = detj_block(g, b, pts)
     dt = detj.chunks[0].data.dtype
@@ -601,11 +627,14 @@ def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: s
 class Batch:
     """Every block of `g` evaluated by one CUDA graph launch (``tlg_batch_*``): the point set of
     each block from `rule`, the same factors and precision for all; fields allocated once
-    (``self.fields[b]``). ``tune()`` picks the launch shapes; ``launch()`` runs the graph."""
+    (``self.fields[b]``). ``tune()`` picks the launch shapes; ``launch()`` runs the graph. With
+    ``cell_measure=True`` (det J among the factors) each launch also writes the per-cell sums of
+    det J * w to ``self.cell_measure[b]``; ``measure()`` sums them into the mesh's measure."""
 
     def __init__(self, g: Geometry, rule: "QuadRule", factors=("points", "jacobian", "detj", "pinv"),
-                 precision: str = "native"):
+                 precision: str = "native", cell_measure: bool = False):
         self.g, self.rule, self.precision = g, rule, precision
+        self.cell_measure = []
         n = len(g.blocks)
         out_dtype = torch.float32 if precision == "split" else g.dtype
         code = SPLIT32 if precision == "split" else g.dtype
@@ -627,6 +656,13 @@ class Batch:
             o.first_cell, o.num_cells, o.out_first_cell, o.tile = 0, blk.num_cells, 0, GPU_QUAD_TILE
             for name in names:
                 setattr(o, name, f[name].chunks[0].data.data_ptr() if f[name].chunks else None)
+            if cell_measure:
+                if "detj" not in names:
+                    raise GridError(1, "cell_measure needs detj among the factors")
+                cm = torch.zeros(max(blk.num_cells, 1), dtype=out_dtype, device=g.nodes.device)
+                self.cell_measure.append(cm)
+                o.weights = pts.weights_device(out_dtype, g.nodes.device).data_ptr()
+                o.cell_measure = cm.data_ptr()
             handles[b] = t.handle
         self._descs, self._outs, self._handles = descs, outs, handles
         h = ctypes.c_void_p()
@@ -642,6 +678,14 @@ class Batch:
 
     def launch(self) -> None:
         check(lib().tlg_batch_launch(self.handle, current_stream_handle()))
+
+    def measure(self) -> float:
+        """The mesh's measure from the last launch's per-cell sums: the tree of each block, summed
+        over the blocks in order in f64 on the host."""
+        if not self.cell_measure:
+            raise GridError(1, "the batch was created without cell_measure")
+        return sum(measure_block(self.g, b, self.rule.get(blk.element.cell), cell_sums=self.cell_measure[b])
+                   for b, blk in enumerate(self.g.blocks))
 
     def __del__(self):
         try:

@@ -151,6 +151,15 @@ typedef struct tlg_outputs {
    * selects 256. `recomputed` (device u64, may be NULL) is incremented once per such point. */
   double cond_limit;
   unsigned long long* recomputed;
+  /* The measure of each cell of the range, sum_q det J(c, q) w_q in F, into cell_measure[c]
+   * (c = 0 .. num_cells - 1, counted from first_cell), summed in point order (d_0 w_0, then one
+   * fma per point) over the det J values written to `detj`: the values tlg_measure_cell_sums
+   * gives on that field (measure.rs:15-41), so tlg_sum over them is the block's measure. Needs
+   * `detj` and `weights` (device [Q] of F); NULL: not computed. The paired kernels sum as they
+   * evaluate; the other kernels are followed by a launch that reads det J back. tlg_eval_block
+   * and batches only. */
+  const void* weights;
+  void* cell_measure;
 } tlg_outputs;
 
 /* Fused evaluation of every requested factor of one block range in one launch: the
