@@ -644,7 +644,7 @@ def extra_high_order(n: int = 16):
 
 
 def extra_p1_box():
-    """BASELINE's CPU-runtime case: 8^3 x 6 = 3,072 P1 tetrahedra, interior nodes jittered by
+    """The CPU-runtime workload: 8^3 x 6 = 3,072 P1 tetrahedra, interior nodes jittered by
     +-0.1 h, 14 points (collapsed 7 x 2 x 1), f64; GPU against the oracle on the host cores."""
     import torch
 
