@@ -1587,13 +1587,14 @@ tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* b, void* stream) {
   if (!b) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_batch_launch: NULL batch");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!b->exec) {
-    // Capture: the gradient zeroed, the blocks' contributions on parallel branches, then the node
-    // sums in block order (each adds its block's sums onto the gradient: deterministic).
+    // Capture: the blocks' contributions on parallel branches, then the node sums in block order:
+    // the first block's sums written over the whole gradient (zero at nodes it does not touch),
+    // each further block's added onto it (deterministic).
     cudaError_t e = cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_batch_launch: begin capture");
     tlg_status st = TLG_OK;
     const size_t nb = b->tables.size();
-    e = cudaMemsetAsync(b->grad, 0, (size_t)b->num_nodes * b->gdim * sizeof(double), b->capture);
+    if (nb == 0) e = cudaMemsetAsync(b->grad, 0, (size_t)b->num_nodes * b->gdim * sizeof(double), b->capture);
     if (e == cudaSuccess) e = cudaEventRecord(b->events[nb], b->capture);
     for (size_t i = 0; i < nb && e == cudaSuccess && st == TLG_OK; ++i) {
       e = cudaStreamWaitEvent(b->streams[i], b->events[nb], 0);
@@ -1605,8 +1606,8 @@ tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* b, void* stream) {
     }
     for (size_t i = 0; i < nb && e == cudaSuccess && st == TLG_OK; ++i) {
       const int ldt = b->tables[i]->dtype == TLG_SPLIT32 ? 4 : 8;
-      st = tlg_vjp_gather_add(b->offsets[i], b->entries[i], b->num_nodes, b->gdim, b->locals[i], ldt, b->grad,
-                              b->capture);
+      st = (i == 0 ? tlg_vjp_gather : tlg_vjp_gather_add)(b->offsets[i], b->entries[i], b->num_nodes, b->gdim,
+                                                          b->locals[i], ldt, b->grad, b->capture);
     }
     cudaGraph_t graph = nullptr;
     const std::string msg = tlg_last_error();

@@ -259,9 +259,10 @@ tlg_status tlg_vjp_gather_add(const uint32_t* offsets, const uint32_t* entries, 
 /* Adjoint batches (the hybrid mesh's fused forward + adjoint in one CUDA graph launch): per block
  * its tables, block, outputs (forward fields or none), cotangents, contribution rows (local,
  * local_cells as in tlg_vjp_block) and node CSR (tlg_csr_build of its dofmap over num_nodes
- * nodes); grad [num_nodes][gdim] f64. The graph zeroes grad, runs every block's tlg_vjp_block on
- * its own branch, then tlg_vjp_gather_add block by block. Captured on the first launch; the
- * pointers are used as given at every launch. */
+ * nodes); grad [num_nodes][gdim] f64. The graph runs every block's tlg_vjp_block on its own
+ * branch, then tlg_vjp_gather for the first block (every node written, zero where the block has no
+ * entries) and tlg_vjp_gather_add for the others, block by block (no blocks: grad zeroed).
+ * Captured on the first launch; the pointers are used as given at every launch. */
 typedef struct tlg_vjp_batch tlg_vjp_batch;
 tlg_status tlg_vjp_batch_create(const tlg_tables* const* tables, const tlg_block* blocks,
                                 const tlg_outputs* outputs, const tlg_cotangents* cotangents,
