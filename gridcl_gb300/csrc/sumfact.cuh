@@ -576,8 +576,9 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
     const int64_t tq = (o / TILE) * nq;
     const int l16 = (int)(o % TILE);
 #define TLG_AT(q, len, comp) (((tq + (q)) * (len) + (comp)) * TILE + l16)
-    // The cotangents of a point (xbar, dbar, Kbar; zero where absent), loaded one point ahead
-    // (points run in rule order) so that their latency overlaps the current point's work.
+    // The cotangents of a point (xbar, dbar, Kbar; zero where absent), loaded PF points ahead
+    // (points run in rule order) so that their latency overlaps the work of the points between:
+    // two in f32 (registers to spare under the two CTAs per SM the slots allow), one in f64.
     auto load_ct = [&](int q, F* v) {
 #pragma unroll
       for (int g = 0; g < D; ++g) v[g] = ctx ? __ldg(ctx + TLG_AT(q, D, g)) : F(0);
@@ -585,8 +586,10 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
 #pragma unroll
       for (int i = 0; i < LJ; ++i) v[D + 1 + i] = ctk ? __ldg(ctk + TLG_AT(q, LJ, i)) : F(0);
     };
-    F cur[D + 1 + LJ];
+    constexpr int PF = sizeof(F) == 4 ? 2 : 1;
+    F cur[D + 1 + LJ], nx1[D + 1 + LJ];
     load_ct(0, cur);
+    if constexpr (PF == 2) load_ct(min(1, nq - 1), nx1);
 
     for (int c2 = 0; c2 < m2; ++c2) {
       F U[D][N][N], V[D][N][N];
@@ -635,8 +638,8 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
         #pragma unroll
         for (int a0 = 0; a0 < (M0 > 0 ? M0 : m0); ++a0) {
           const int q = a0 + m0 * (b1 + m1 * c2);
-          F nxt[D + 1 + LJ];
-          load_ct(min(q + 1, nq - 1), nxt);
+          F nx2[D + 1 + LJ];
+          load_ct(min(q + PF, nq - 1), nx2);
           F x[D], j[LJ];
 #pragma unroll
           for (int g = 0; g < D; ++g) {
@@ -705,7 +708,14 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
             }
           }
 #pragma unroll
-          for (int i = 0; i < D + 1 + LJ; ++i) cur[i] = nxt[i];
+          for (int i = 0; i < D + 1 + LJ; ++i) {
+            if constexpr (PF == 2) {
+              cur[i] = nx1[i];
+              nx1[i] = nx2[i];
+            } else {
+              cur[i] = nx2[i];
+            }
+          }
         }
         // The row into the plane accumulators.
 #pragma unroll
