@@ -497,6 +497,10 @@ inline size_t vjp_sumfact_extra_bytes(int n, int threads, size_t f_bytes) {
 
 // M0 > 0: the rule has M0 points in direction 0 (the point loop of a row unrolled, so that the
 // rows' points overlap); 0: at run time.
+#ifndef TLG_VJP_PF
+#define TLG_VJP_PF 2
+#endif
+
 template <typename F, bool SPLIT, int N, int M0>
 __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_constant__ VjpSfArgs a) {
   using NT = typename std::conditional<SPLIT, double, F>::type;
@@ -586,10 +590,11 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
 #pragma unroll
       for (int i = 0; i < LJ; ++i) v[D + 1 + i] = ctk ? __ldg(ctk + TLG_AT(q, LJ, i)) : F(0);
     };
-    constexpr int PF = sizeof(F) == 4 ? 2 : 1;
-    F cur[D + 1 + LJ], nx1[D + 1 + LJ];
-    load_ct(0, cur);
-    if constexpr (PF == 2) load_ct(min(1, nq - 1), nx1);
+    constexpr int PF = sizeof(F) == 4 ? TLG_VJP_PF : 1;
+    F buf[PF][D + 1 + LJ];  // buf[p]: the cotangents of point q + p
+#pragma unroll
+    for (int p = 0; p < PF; ++p) load_ct(min(p, nq - 1), buf[p]);
+    const F* cur = buf[0];
 
     for (int c2 = 0; c2 < m2; ++c2) {
       F U[D][N][N], V[D][N][N];
@@ -638,8 +643,8 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
         #pragma unroll
         for (int a0 = 0; a0 < (M0 > 0 ? M0 : m0); ++a0) {
           const int q = a0 + m0 * (b1 + m1 * c2);
-          F nx2[D + 1 + LJ];
-          load_ct(min(q + PF, nq - 1), nx2);
+          F nxt[D + 1 + LJ];
+          load_ct(min(q + PF, nq - 1), nxt);
           F x[D], j[LJ];
 #pragma unroll
           for (int g = 0; g < D; ++g) {
@@ -709,12 +714,9 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
           }
 #pragma unroll
           for (int i = 0; i < D + 1 + LJ; ++i) {
-            if constexpr (PF == 2) {
-              cur[i] = nx1[i];
-              nx1[i] = nx2[i];
-            } else {
-              cur[i] = nx2[i];
-            }
+#pragma unroll
+            for (int p = 0; p + 1 < PF; ++p) buf[p][i] = buf[p + 1][i];
+            buf[PF - 1][i] = nxt[i];
           }
         }
         // The row into the plane accumulators.
