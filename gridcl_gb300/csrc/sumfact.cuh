@@ -757,13 +757,21 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
     const int64_t cell0 = a.first_cell + cw;
     const int64_t nreal = min((int64_t)32, a.range_end - cell0);
     if (nreal > 0) {
+      // One (cell, node) row of R = 4 values per lane and step: a 16-byte (f32) or two 16-byte
+      // (f64) stores, consecutive lanes consecutive rows.
       F* dst = static_cast<F*>(a.local) + cell0 * (K * R);
       const F* lw = Lw + (threadIdx.x & ~31);  // the warp's contribution slots
-      for (int e = lane; e < nreal * (K * R); e += 32) {
-        const int cl = e / (K * R);
-        const int rem = e - cl * (K * R);
-        const int kk = rem / R, g = rem - kk * R;
-        dst[e] = g < D ? lw[(invperm[kk] * D + g) * S + cl] : F(0);
+      for (int t = lane; t < nreal * K; t += 32) {
+        const int cl = t / K;
+        const int kk = t - cl * K;
+        const F* src = lw + (int)invperm[kk] * D * S + cl;
+        F* row4 = dst + (int64_t)t * R;
+        if constexpr (sizeof(F) == 4) {
+          *reinterpret_cast<float4*>(row4) = make_float4(src[0], src[S], src[2 * S], 0.0f);
+        } else {
+          reinterpret_cast<double2*>(row4)[0] = make_double2(src[0], src[S]);
+          reinterpret_cast<double2*>(row4)[1] = make_double2(src[2 * S], 0.0);
+        }
       }
     }
     __syncwarp();
