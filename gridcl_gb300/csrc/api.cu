@@ -320,7 +320,9 @@ tlg_status eval_pair(const tlg_tables* t, const tlg_block* b, const tlg_outputs*
     a.weights = static_cast<const float*>(o->weights);
     a.cell_measure = static_cast<float*>(o->cell_measure);
   }
-  cudaError_t e = tlg::launch_eval_pair(split, t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
+  cudaError_t e = o->cell_measure
+                      ? tlg::launch_eval_pair_meas(split, t->td, t->gd, (int)t->k, a, t->bytes, stream, found)
+                      : tlg::launch_eval_pair(split, t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
   if (!*found) return TLG_ERR_UNSUPPORTED;
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
   g_last_family = TLG_STRATEGY_DIRECT;
@@ -1718,6 +1720,23 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
+  // The median of five launches timed one by one (after `fn` has run once untimed): robust
+  // against a launch slowed by a clock or power transition, which an average of back-to-back
+  // launches is not.
+  auto median_ms = [&](auto fn, float* ms) -> tlg_status {
+    tlg_status st = fn();
+    float t[5] = {0, 0, 0, 0, 0};
+    for (int r = 0; r < 5 && st == TLG_OK; ++r) {
+      cudaEventRecord(t0, s);
+      st = fn();
+      cudaEventRecord(t1, s);
+      cudaEventSynchronize(t1);
+      cudaEventElapsedTime(&t[r], t0, t1);
+    }
+    std::sort(t, t + 5);
+    *ms = t[2];
+    return st;
+  };
   for (size_t i = 0; i < b->tables.size(); ++i) {
     const std::string key = tune_key(b->tables[i], &b->outputs[i], b->outputs[i].num_cells);
     int mult = -1;
@@ -1727,24 +1746,19 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
       if (it != g_tune_cache.end()) mult = it->second;
     }
     if (mult < 0) {
-      // Candidates: CTAs per SM of the persistent grid (0: the occupancy limit); 3 timed runs each.
+      // Candidates: CTAs per SM of the persistent grid (0: the occupancy limit).
       const int cands[] = {0, 1, 2, 3, 4, 6, 8};
       float best = 1e30f;
       mult = 0;
       for (int c : cands) {
         const int grid = c == 0 ? 0 : c * sms;
-        tlg_status st = eval_with_grid(b, i, s, grid);
+        float ms = 0.0f;
+        tlg_status st = median_ms([&] { return eval_with_grid(b, i, s, grid); }, &ms);
         if (st != TLG_OK) {
           cudaEventDestroy(t0);
           cudaEventDestroy(t1);
           return st;
         }
-        cudaEventRecord(t0, s);
-        for (int r = 0; r < 3; ++r) eval_with_grid(b, i, s, grid);
-        cudaEventRecord(t1, s);
-        cudaEventSynchronize(t1);
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, t0, t1);
         if (ms < best) {
           best = ms;
           mult = c;
@@ -1757,7 +1771,7 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
   }
   // Joint pass: the graph runs the blocks concurrently, so each block's best grid alone is only
   // the start. One round of coordinate descent over each block's candidates, timing the whole
-  // graph (one warm launch, then three), keeps a change only when the graph gets faster.
+  // graph (the median of five launches), keeps a change only when the graph gets faster.
   std::string batch_key;
   for (size_t i = 0; i < b->tables.size(); ++i)
     batch_key += tune_key(b->tables[i], &b->outputs[i], b->outputs[i].num_cells) + ";";
@@ -1773,14 +1787,7 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
   } else if (b->tables.size() > 1) {
     auto time_graph = [&](float* ms) -> tlg_status {
       destroy_graph(b);
-      tlg_status st = tlg_batch_launch(b, s);
-      if (st != TLG_OK) return st;
-      cudaEventRecord(t0, s);
-      for (int r = 0; r < 3 && st == TLG_OK; ++r) st = tlg_batch_launch(b, s);
-      cudaEventRecord(t1, s);
-      cudaEventSynchronize(t1);
-      cudaEventElapsedTime(ms, t0, t1);
-      return st;
+      return median_ms([&] { return tlg_batch_launch(b, s); }, ms);
     };
     // Parallel branches or a serial chain: the concurrent branches of persistent kernels share
     // the SMs in an order the hardware picks, which can cost more than running them in turn.

@@ -45,7 +45,7 @@ enum : uint32_t {
   kOutPinv = 8u,
   kOutNormals = 16u,
   kOutFacetNormals = 32u,
-  kOutCellMeasure = 64u,  // the paired kernels: per-cell sums of det J * w (PairArgs::cell_measure)
+  kOutCellMeasure = 64u,  // per-cell sums of det J * w (PairArgs::cell_measure; the MEAS kernels)
 };
 
 template <typename F>
@@ -442,7 +442,7 @@ __device__ __noinline__ void recompute_f64(const double* __restrict__ nodes, con
 // The paired f32 kernel (tile 16).
 
 // Cells c0, c0 + step, ... below c_end of one block range, tables at `tabs` (shared memory).
-template <bool SPLIT, int TD, int GD, int K>
+template <bool SPLIT, int TD, int GD, int K, bool MEAS = false>
 __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned char* tabs, int64_t c0,
                                            int64_t c_end, int64_t step) {
   constexpr int TILE = 16;
@@ -516,7 +516,7 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
     if (mask & kOutNormals) cn.init(a.out[4], tile_idx, nq, lane);
     if (mask & kOutFacetNormals) cf.init(a.out[5], tile_idx, nq, lane);
 
-    float meas = 0.0f;  // sum of det J * w over the points so far, in point order
+    float meas = 0.0f;  // MEAS: the sum of det J * w over the points so far, in point order
     for (int qp = 0; qp < nqp; ++qp) {
       const bool both = 2 * qp + 1 < nq;
       const float4* rq = rows2 + (int64_t)qp * K * RW4;
@@ -649,7 +649,7 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
           }
         }
       }
-      if (mask & kOutCellMeasure) {
+      if constexpr (MEAS) {
         if (redone) {  // the det J values as stored (this thread's own writes)
           dj.x = pd[0];
           if (both) dj.y = pd[TILE];
@@ -659,16 +659,18 @@ __device__ __forceinline__ void pair_cells(const PairArgs& a, const unsigned cha
         if (both) meas = fmaf(dj.y, __ldg(a.weights + q0 + 1), meas);
       }
     }
-    if ((mask & kOutCellMeasure) && c < a.range_cells) a.cell_measure[c] = meas;
+    if constexpr (MEAS) {
+      if (c < a.range_cells) a.cell_measure[c] = meas;
+    }
   }
 }
 
-template <bool SPLIT, int TD, int GD, int K>
+template <bool SPLIT, int TD, int GD, int K, bool MEAS = false>
 __global__ void __launch_bounds__(kEvalThreads) eval_pair_kernel(const __grid_constant__ PairArgs a) {
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
   stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
-  pair_cells<SPLIT, TD, GD, K>(a, smem, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, a.padded,
+  pair_cells<SPLIT, TD, GD, K, MEAS>(a, smem, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, a.padded,
                                (int64_t)gridDim.x * blockDim.x);
 }
 

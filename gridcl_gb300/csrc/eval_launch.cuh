@@ -70,6 +70,10 @@ cudaError_t launch_eval_f64(int td, int gd, int k, const EvalArgs<double>& a, si
 // precision (split = true), tile 16; `found` is false when none exists for (td, gd, k).
 cudaError_t launch_eval_pair(bool split, int td, int gd, int k, const PairArgs& a, size_t smem,
                              cudaStream_t s, bool* found);
+// Defined in eval_pair_meas.cu: the same kernels summing each cell's det J * w into
+// a.cell_measure (a.weights [Q]) as they evaluate.
+cudaError_t launch_eval_pair_meas(bool split, int td, int gd, int k, const PairArgs& a, size_t smem,
+                                  cudaStream_t s, bool* found);
 // Defined in eval_pair.cu: split precision with K at run time (tile 16), tables staged in
 // shared memory or (tab_global) read from global memory.
 cudaError_t launch_split_loops(int td, int gd, bool tab_global, const PairArgs& a, size_t smem, cudaStream_t s);
