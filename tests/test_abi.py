@@ -57,3 +57,34 @@ def test_refcell_entry_points_report_capacity():
     assert L.tlg_lagrange_points(4, 2, 0, out.ctypes.data_as(ctypes.c_void_p), 3) == 2
     assert L.tlg_num_lagrange_nodes(4, 2) == 10
     assert L.tlg_num_lagrange_nodes(99, 2) == -1
+
+
+def tree_elems(n: int) -> int:
+    total = 0
+    while n > 1:
+        n = (n + 63) // 64
+        total += n
+    return total
+
+
+def test_measure_workspace_sizes_and_checks_on_the_host():
+    """tlg_measure's workspace: the tree over ceil(n / 64) level-1 sums (none at one level-1 value);
+    too small a workspace and bad arguments are refused before any device work."""
+    L = lib()
+    for n in (0, 1, 64, 65, 4096, 4097, 1_572_864, 16_777_217):
+        l1 = (n + 63) // 64
+        want = (l1 + tree_elems(l1)) if l1 > 1 else 0
+        assert L.tlg_measure_workspace_bytes(4, n) == 4 * want, n
+        assert L.tlg_measure_workspace_bytes(8, n) == 8 * want, n
+    assert L.tlg_measure_workspace_bytes(2, 10) == -1
+    assert L.tlg_measure_workspace_bytes(4, -1) == -1
+    assert L.tlg_measure_workspace_bytes(4, 1_572_864) == 99_868
+    host = np.zeros(16)  # stands in for device pointers: nothing is dereferenced on these paths
+    p = host.ctypes.data_as(ctypes.c_void_p)
+    need = L.tlg_measure_workspace_bytes(4, 10_000)
+    assert L.tlg_measure(p, 4, 10_000, 24, 16, p, p, need - 1, p, None) == 2
+    assert b"needed" in L.tlg_last_error()
+    assert L.tlg_measure(p, 4, 10_000, 24, 32, p, p, need, p, None) == 1  # tile 32
+    assert L.tlg_measure(p, 3, 10_000, 24, 16, p, p, need, p, None) == 1  # dtype
+    assert L.tlg_measure(None, 4, 10_000, 24, 16, p, p, need, p, None) == 1
+    assert L.tlg_measure(p, 4, 10_000, 24, 16, p, p, need, None, None) == 1
