@@ -441,6 +441,9 @@ def measure_block(g: Geometry, b: int, pts: PointSet, detj: QuadField | None = N
         return 0.0 if sync else torch.zeros(1, dtype=g.dtype, device=dev)
     if cell_sums is not None:
         dt = cell_sums.dtype
+        if (dt not in _DTYPES or not cell_sums.is_cuda or not cell_sums.is_contiguous()
+                or cell_sums.numel() < blk.num_cells):
+            raise GridError(1, f"cell_sums must be a contiguous CUDA f32 or f64 tensor of {blk.num_cells} values")
         nbytes = int(lib().tlg_sum_workspace_bytes(_DTYPES[dt], blk.num_cells))
         work = torch.empty(max(nbytes, 8), dtype=torch.uint8, device=dev)
         result = torch.empty(1, dtype=dt, device=dev)

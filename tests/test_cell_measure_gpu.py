@@ -116,6 +116,10 @@ def test_cell_measure_needs_det_j_and_weights(cuda):
     with pytest.raises(tg.GridError):
         tg.geometric_factors_block(g, 0, ps, ("detj",), precision="split",
                                    cell_measure=torch.empty(nc, dtype=torch.float64, device="cuda"))
+    for bad in (torch.empty(nc - 1, dtype=torch.float32, device="cuda"), torch.empty(nc, dtype=torch.float32),
+                torch.empty(nc, dtype=torch.int32, device="cuda")):
+        with pytest.raises(tg.GridError):
+            tg.measure_block(g, 0, ps, cell_sums=bad)
     f = tg.geometric_factors_block(g, 0, ps, ("detj",), precision="split")
     tables = ps.tables(g.blocks[0].element, 3, tg.geometry.SPLIT32)
     o = tg._lib.TlgOutputs()
