@@ -1309,8 +1309,8 @@ namespace {
 // Hexahedra with a tensor-product rule and 2 or 3 nodes per direction have the sum-factorised
 // adjoint.
 bool vjp_sumfact_preferred(const tlg_tables* t) {
-  // One block in rule order (direction 0 fastest): the kernel loads the next point's cotangents
-  // ahead and walks the points in that order.
+  // One block in rule order (direction 0 fastest): the kernel walks the points in that order and
+  // loads the cotangents of the points ahead of the current one.
   const tlg::SfBlock& h = t->sf_block0;
   return t->sf_ok && t->cell == tlg::kHexahedron && (t->sf_n == 2 || t->sf_n == 3) && t->sf_nblocks == 1 &&
          h.o == 0 && h.s[0] == 1 && h.s[1] == h.m[0] && h.s[2] == h.m[0] * h.m[1];
