@@ -15,11 +15,9 @@
 // Nodes are then numbered in the order of the first cell that uses them (each cell's nodes in
 // Lagrange order), unused nodes last in their old order.
 #include <algorithm>
-#include <array>
 #include <cmath>
 #include <cstdint>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "../../include/tlgeom.h"
@@ -106,37 +104,65 @@ std::vector<int64_t> hilbert_order(int cell, const uint32_t* cells, int64_t n, i
   return order;
 }
 
-struct KeyHash {
-  size_t operator()(const std::array<int64_t, 4>& a) const {
-    uint64_t h = 1469598103934665603ull;
-    for (int64_t v : a) h = (h ^ (uint64_t)v) * 1099511628211ull;
-    return (size_t)h;
-  }
+// The facet graph in compressed rows of sorted, distinct neighbours: every (facet key, cell) pair
+// sorted by key, the cells of each run of equal keys joined pairwise. A facet key is its sorted
+// vertex numbers, 32 bits each, packed into two 64-bit words (absent vertices all ones).
+struct FacetGraph {
+  std::vector<int64_t> start, len, nbr;  // row c: nbr[start[c] .. start[c] + len[c])
 };
 
-std::vector<int64_t> rcm_order(int cell, const uint32_t* cells, int64_t n, int k) {
+FacetGraph facet_graph(int cell, const uint32_t* cells, int64_t n, int k) {
   const int td = tlg::tdim(cell);
   const auto& facets = tlg::sub_entities(cell, td - 1);
-  std::unordered_map<std::array<int64_t, 4>, std::vector<int64_t>, KeyHash> by_key;
-  by_key.reserve((size_t)n * facets.size());
+  struct Entry {
+    uint64_t hi, lo;
+    int64_t cell;
+    bool operator<(const Entry& o) const {
+      return hi != o.hi ? hi < o.hi : lo != o.lo ? lo < o.lo : cell < o.cell;
+    }
+  };
+  std::vector<Entry> entries;
+  entries.reserve((size_t)n * facets.size());
   for (int64_t c = 0; c < n; ++c)
     for (const auto& f : facets) {
-      std::array<int64_t, 4> key = {-1, -1, -1, -1};
-      for (size_t j = 0; j < f.size(); ++j) key[j] = cells[c * k + f[j]];
-      std::sort(key.begin(), key.begin() + f.size());
-      by_key[key].push_back(c);
+      uint32_t v[4] = {UINT32_MAX, UINT32_MAX, UINT32_MAX, UINT32_MAX};
+      for (size_t j = 0; j < f.size(); ++j) v[j] = cells[c * k + f[j]];
+      std::sort(v, v + f.size());
+      entries.push_back({(uint64_t)v[0] << 32 | v[1], (uint64_t)v[2] << 32 | v[3], c});
     }
-  std::vector<std::vector<int64_t>> adj((size_t)n);
-  for (auto& kv : by_key)
-    for (int64_t a : kv.second)
-      for (int64_t b : kv.second)
-        if (a != b) adj[(size_t)a].push_back(b);
-  for (auto& r : adj) {
-    std::sort(r.begin(), r.end());
-    r.erase(std::unique(r.begin(), r.end()), r.end());
+  std::sort(entries.begin(), entries.end());
+  // Runs of equal keys; two passes over them: count each cell's pairs, then write them.
+  std::vector<std::pair<size_t, size_t>> runs;
+  for (size_t i = 0; i < entries.size();) {
+    size_t j = i + 1;
+    while (j < entries.size() && entries[j].hi == entries[i].hi && entries[j].lo == entries[i].lo) ++j;
+    if (j - i > 1) runs.push_back({i, j});
+    i = j;
   }
+  FacetGraph g;
+  g.start.assign((size_t)n + 1, 0);
+  g.len.assign((size_t)n, 0);
+  for (const auto& r : runs)
+    for (size_t a = r.first; a < r.second; ++a) g.start[(size_t)entries[a].cell + 1] += (int64_t)(r.second - r.first - 1);
+  for (int64_t c = 0; c < n; ++c) g.start[(size_t)c + 1] += g.start[(size_t)c];
+  g.nbr.resize((size_t)g.start[(size_t)n]);
+  std::vector<int64_t> fill(g.start.begin(), g.start.end() - 1);
+  for (const auto& r : runs)
+    for (size_t a = r.first; a < r.second; ++a)
+      for (size_t b = r.first; b < r.second; ++b)
+        if (a != b) g.nbr[(size_t)fill[(size_t)entries[a].cell]++] = entries[b].cell;
+  for (int64_t c = 0; c < n; ++c) {
+    auto first = g.nbr.begin() + g.start[(size_t)c], last = g.nbr.begin() + g.start[(size_t)c + 1];
+    std::sort(first, last);
+    g.len[(size_t)c] = std::unique(first, last) - first;
+  }
+  return g;
+}
+
+std::vector<int64_t> rcm_order(int cell, const uint32_t* cells, int64_t n, int k) {
+  const FacetGraph adj = facet_graph(cell, cells, n, k);
   auto rank_less = [&](int64_t a, int64_t b) {
-    const size_t da = adj[(size_t)a].size(), db = adj[(size_t)b].size();
+    const int64_t da = adj.len[(size_t)a], db = adj.len[(size_t)b];
     return da != db ? da < db : a < b;
   };
   std::vector<int64_t> starts((size_t)n);
@@ -153,8 +179,8 @@ std::vector<int64_t> rcm_order(int cell, const uint32_t* cells, int64_t n, int k
     while (head < order.size()) {
       const int64_t a = order[head++];
       next.clear();
-      for (int64_t b : adj[(size_t)a])
-        if (!visited[(size_t)b]) next.push_back(b);
+      for (int64_t e = adj.start[(size_t)a]; e < adj.start[(size_t)a] + adj.len[(size_t)a]; ++e)
+        if (!visited[(size_t)adj.nbr[(size_t)e]]) next.push_back(adj.nbr[(size_t)e]);
       std::sort(next.begin(), next.end(), rank_less);
       for (int64_t b : next) {
         visited[(size_t)b] = 1;
