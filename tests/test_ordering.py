@@ -106,3 +106,50 @@ def test_rcm_components_and_reversal():
     assert orders[0].tolist() == [2, 1, 0]
     _, orders, _ = meshes.reorder(m, "input")
     assert orders[0].tolist() == [0, 1, 2]
+
+
+def rcm_restated(cell: str, cells: np.ndarray) -> list:
+    """Reverse Cuthill-McKee as order.rs states it, in plain Python: the facet graph from the
+    reference cell's facets (the golden tables), components started at the least (degree,
+    position) cell, neighbours queued by (degree, position), the whole order reversed."""
+    import json
+    import pathlib
+
+    tables = json.loads((pathlib.Path(__file__).parent / "golden" / "refcell_tables.json").read_text())
+    td = {"Triangle": 2, "Quadrilateral": 2, "Tetrahedron": 3, "Hexahedron": 3, "Prism": 3}[cell]
+    facets = tables[cell]["sub_entities"][td - 1]
+    owners = {}
+    for c, row in enumerate(cells):
+        for f in facets:
+            owners.setdefault(tuple(sorted(int(row[j]) for j in f)), []).append(c)
+    adj = [set() for _ in range(len(cells))]
+    for cs in owners.values():
+        for a in cs:
+            adj[a].update(b for b in cs if b != a)
+    rank = lambda c: (len(adj[c]), c)
+    seen, order = [False] * len(cells), []
+    for s in sorted(range(len(cells)), key=rank):
+        if seen[s]:
+            continue
+        seen[s] = True
+        head = len(order)
+        order.append(s)
+        while head < len(order):
+            a = order[head]
+            head += 1
+            nxt = sorted((b for b in adj[a] if not seen[b]), key=rank)
+            for b in nxt:
+                seen[b] = True
+            order.extend(nxt)
+    return order[::-1]
+
+
+@pytest.mark.parametrize("cell,dim,n,degree", [("Tetrahedron", 3, 4, 2), ("Hexahedron", 3, 4, 1), ("Prism", 3, 3, 2),
+                                                ("Triangle", 2, 7, 3), ("Quadrilateral", 2, 6, 2)])
+def test_rcm_matches_the_restatement(cell, dim, n, degree):
+    """The library's reverse Cuthill-McKee (a sorted facet-key graph) against the plain-Python
+    restatement on shuffled boxes, prisms' triangle and quadrilateral facets included."""
+    box = meshes.cube_box(cell, n, degree) if dim == 3 else meshes.square_box(cell, n, degree)
+    mix = meshes.shuffled(box, seed=11)
+    _, orders, _ = meshes.reorder(mix, "rcm")
+    assert orders[0].tolist() == rcm_restated(cell, mix.blocks[0].cells)
