@@ -24,6 +24,7 @@
 #include "coop.cuh"
 #include "tc.cuh"
 #include "sumfact.cuh"
+#include "eval_df.cuh"
 #include "vjp.cuh"
 
 struct tlg_batch {
@@ -40,12 +41,20 @@ struct tlg_batch {
 
 struct tlg_tables {
   int cell, degree, family, td, gd, dtype;
+  // Double-float tables (TLG_DF64): dtype is TLG_F64 (every f64 section, so that the f64 kernels
+  // run on them), plus the double-float sections below.
+  bool df = false;
   int64_t k, q;
   bool has_refn;
   unsigned char* dev = nullptr;  // phi [Q][K] | dphi [Q][K][TD] | refn [Q][TD] | error word
   uint32_t bytes = 0;            // table bytes (multiple of 16), error word excluded
   bool staged = true;            // the tables fit the kernels' shared-memory budget
   uint32_t off_dphi = 0, off_refn = 0, off_rows2 = 0, off_dphi64 = 0;
+  // Double-float rows of the paired f64 kernels, inside the staged prefix (0 bytes beyond 27
+  // nodes per cell): per point pair p and node k, 1 + TD float4 (phi, dphi_0 .. dphi_{TD-1}), each
+  // (head of point 2p, head of point 2p + 1, tail of 2p, tail of 2p + 1); an odd last point pairs
+  // with itself.
+  uint32_t off_dfrows = 0, dfrows_bytes = 0;
   // The adjoint's table after the error word (codimension 0, f64 or split tables; 0 bytes when
   // absent or too large to stage): per node of each point (f64) or point pair (split) the 32
   // bytes phi, dphi_0 .. dphi_{TD-1}, zero padding, as f64 values or f32 pairs.
@@ -62,6 +71,9 @@ struct tlg_tables {
   int sf_n = 0, sf_nblocks = 0;
   tlg::SfBlock sf_block0{};  // the first block (the adjoint's single-block rule)
   uint32_t off_sf = 0, sf_bytes = 0, sf_offperm = 0, sf_offrefn = 0;
+  // Double-float tables: a copy of the sum-factorisation section after it (same headers and
+  // offsets) whose B_d and D_d entries are (head, tail) f32 pairs.
+  uint32_t off_sfdf = 0;
   // Tensor-core section (f32 and split tables, TD >= 2), after the sum-factorisation section, read
   // from global memory: the basis in mma fragment order, [col tile][k-step][lane] x 4 f32
   // (b0 head, b1 head, b0 tail, b1 tail) of B[k][4 q + r] (r = 0 phi, 1 + d dphi_d).
@@ -130,6 +142,15 @@ template <typename F>
 void narrow_into(std::vector<unsigned char>& buf, size_t off, const double* src, size_t n) {
   F* dst = reinterpret_cast<F*>(buf.data() + off);
   for (size_t i = 0; i < n; ++i) dst[i] = (F)src[i];
+}
+
+// f64 values as double-floats: (nearest f32, f32 nearest to the remainder) pairs.
+void split_into(std::vector<unsigned char>& buf, size_t off, const double* src, size_t n) {
+  float* dst = reinterpret_cast<float*>(buf.data() + off);
+  for (size_t i = 0; i < n; ++i) {
+    dst[2 * i] = (float)src[i];
+    dst[2 * i + 1] = (float)(src[i] - (double)(float)src[i]);
+  }
 }
 
 // The paired-FP32 kernel: an f32 mesh (split = false) or split precision (split = true).
@@ -246,7 +267,10 @@ int principal_family(uint32_t mask) {
 // Q3 - / 11.5 / 0.62; f32 Q2 1.15 / 17.6 / 1.39, Q3 - / 16.7 / 0.55. So: sum factorisation
 // always in f64, and in f32 and split precision above the degrees with paired kernels
 // (quadrilaterals and hexahedra Q1-Q2).
-bool sumfact_preferred(const tlg_tables* t) { return t->sf_ok && (t->dtype == TLG_F64 || t->sf_n >= 4); }
+bool sumfact_preferred(const tlg_tables* t) {
+  if (t->df) return false;  // (until the double-float sum factorisation exists)
+  return t->sf_ok && (t->dtype == TLG_F64 || t->sf_n >= 4);
+}
 
 // The policy of TLG_STRATEGY_AUTO beyond the compiled unrolled kernels (more than 27 nodes per
 // cell): the cooperative kernel instead of the loops kernel.
@@ -378,6 +402,41 @@ tlg_status eval_split(const tlg_tables* t, const tlg_block* b, const tlg_outputs
   cudaError_t e = tlg::launch_split_loops(t->td, t->gd, global, a, t->bytes, stream);
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
   g_last_family = global ? TLG_STRATEGY_LOOPS : TLG_STRATEGY_SHARED;
+  return ok();
+}
+
+// The double-float kernel (TLG_DF64 tables, tile 16); `found` is false where none is compiled or
+// the tables lack its rows (nothing launched).
+tlg_status eval_df(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                   cudaStream_t stream, bool* found) {
+  *found = false;
+  if (!t->df || t->dfrows_bytes == 0 || o->tile != 16 || !t->staged) return TLG_ERR_UNSUPPORTED;
+  tlg::DfArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = static_cast<const double*>(b->nodes);
+  a.dofmap = b->dofmap;
+  a.flags = b->flags;
+  a.tab = t->dev;
+  void* outs[6] = {o->points, o->jacobian, o->detj, o->pinv, o->normals, o->facet_normals};
+  for (int i = 0; i < 6; ++i) a.out[i] = static_cast<double*>(outs[i]);
+  a.err = t->err;
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + 15) / 16 * 16;
+  a.out_first_cell = o->out_first_cell;
+  a.last_cell = b->num_cells - 1;
+  const int64_t nflags = b->flags ? std::min<int64_t>(b->num_cells, b->num_flags) : 0;
+  a.last_flag = nflags - 1;
+  for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
+  a.last_node = (uint32_t)(b->num_nodes - 1);
+  a.tab_bytes = t->bytes;
+  a.off_rows = t->off_dfrows;
+  a.off_refn = t->off_refn;
+  a.mask = mask;
+  a.num_points = (int)t->q;
+  cudaError_t e = tlg::launch_eval_df(t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
+  if (!*found) return TLG_ERR_UNSUPPORTED;
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  g_last_family = TLG_STRATEGY_DIRECT;
   return ok();
 }
 
@@ -914,8 +973,10 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
     if (gdim < td || gdim > 3)
       return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: gdim " + std::to_string(gdim) +
                                                 " with tdim " + std::to_string(td));
-    if (dtype != TLG_F32 && dtype != TLG_F64 && dtype != TLG_SPLIT32)
-      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: dtype must be 4, 8 or 12");
+    if (dtype != TLG_F32 && dtype != TLG_F64 && dtype != TLG_SPLIT32 && dtype != TLG_DF64)
+      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: dtype must be 4, 8, 12 or 16");
+    const bool df = dtype == TLG_DF64;
+    if (df) dtype = TLG_F64;  // every f64 section, then the double-float ones
     if (degree < 1) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: degree must be >= 1");
     if (npoints < 0 || (npoints > 0 && !points))
       return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: bad points");
@@ -929,6 +990,7 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
     t->td = td;
     t->gd = gdim;
     t->dtype = dtype;
+    t->df = df;
     t->k = k;
     t->q = npoints;
     t->has_refn = ref_normals != nullptr;
@@ -950,6 +1012,11 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
     if (dtype == TLG_SPLIT32) {  // the f64 derivative table of the FP64 recompute follows
       t->off_dphi64 = (uint32_t)total;
       total = align16(total + std::max<size_t>(n_dphi, 1) * 8);
+    }
+    if (df && k <= 27 && npoints > 0) {  // the double-float rows of the paired f64 kernels
+      t->off_dfrows = (uint32_t)total;
+      t->dfrows_bytes = (uint32_t)((size_t)qp * k * (1 + td) * 16);
+      total = align16(total + t->dfrows_bytes);
     }
     // Tables beyond the shared-memory budget stay in global memory: the loops kernels read them
     // there (L1/L2-cached) instead of staging them.
@@ -998,9 +1065,10 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       t->sf_offrefn = (uint32_t)off;
       if (ref_normals) off = align16(off + (size_t)npoints * td * es);
       t->sf_bytes = (uint32_t)off;
+      if (df) t->off_sfdf = (uint32_t)align16((size_t)t->off_sf + t->sf_bytes);
     }
     // The tensor-core section.
-    size_t host_bytes = (size_t)t->off_sf + t->sf_bytes;
+    size_t host_bytes = t->off_sfdf ? (size_t)t->off_sfdf + t->sf_bytes : (size_t)t->off_sf + t->sf_bytes;
     if (dtype != TLG_F64 && td >= 2 && k > 10 && npoints > 0) {
       t->tc_ksteps = (int)((k + 7) / 8);
       t->tc_col_tiles = (int)((npoints + 1) / 2);
@@ -1026,6 +1094,14 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
         if (dtype == TLG_F64) narrow_into<double>(t->host, t->off_sf + t->sf_offrefn, ref_normals, (size_t)npoints * td);
         else narrow_into<float>(t->host, t->off_sf + t->sf_offrefn, ref_normals, (size_t)npoints * td);
       }
+      if (t->off_sfdf) {  // the same section with the tables as (head, tail) pairs
+        std::memcpy(t->host.data() + t->off_sfdf, t->host.data() + t->off_sf, t->sf_bytes);
+        for (size_t bi = 0; bi < sf.size(); ++bi)
+          for (int d = 0; d < 3; ++d) {
+            split_into(t->host, t->off_sfdf + heads[bi].off_b[d], sf[bi].B[d].data(), sf[bi].B[d].size());
+            split_into(t->host, t->off_sfdf + heads[bi].off_d[d], sf[bi].D[d].data(), sf[bi].D[d].size());
+          }
+      }
     }
     // Reorder [deriv][q][k] into phi [q][k] and dphi [q][k][d].
     std::vector<double> phi(n_phi), dphi(n_dphi), refn(n_refn, 0.0);
@@ -1036,6 +1112,19 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       }
     if (ref_normals) std::memcpy(refn.data(), ref_normals, n_refn * sizeof(double));
     if (dtype == TLG_SPLIT32) narrow_into<double>(t->host, t->off_dphi64, dphi.data(), n_dphi);
+    if (t->dfrows_bytes > 0) {
+      float* dst = reinterpret_cast<float*>(t->host.data() + t->off_dfrows);
+      for (int64_t p = 0; p < qp; ++p)
+        for (int64_t i = 0; i < k; ++i)
+          for (int r = 0; r <= td; ++r)
+            for (int h = 0; h < 2; ++h) {
+              const int64_t q = std::min<int64_t>(2 * p + h, npoints - 1);
+              const double v = r == 0 ? phi[q * k + i] : dphi[(q * k + i) * td + (r - 1)];
+              float* e = dst + ((p * k + i) * (1 + td) + r) * 4;
+              e[h] = (float)v;
+              e[2 + h] = (float)(v - (double)(float)v);
+            }
+    }
     if (dtype != TLG_F64) {
       std::vector<double> rows2((size_t)qp * k * rw, 0.0);
       for (int64_t p = 0; p < qp; ++p)
@@ -1178,6 +1267,11 @@ tlg_status eval_dispatch(const tlg_tables* t, const tlg_block* b, const tlg_outp
   }
   const bool allow_direct = is_auto || strategy == TLG_STRATEGY_DIRECT;
   const bool global_tables = !(is_auto || strategy == TLG_STRATEGY_SHARED);
+  if (t->df && allow_direct) {
+    bool found = false;
+    tlg_status st = eval_df(t, b, o, mask, s, &found);
+    if (found) return st;
+  }
   if (t->dtype == TLG_SPLIT32) return eval_split(t, b, o, mask, s, allow_direct, global_tables);
   if (t->dtype == TLG_F32) return eval_typed<float>(t, b, o, mask, s, allow_direct, global_tables);
   return eval_typed<double>(t, b, o, mask, s, allow_direct, global_tables);

@@ -78,6 +78,11 @@ cudaError_t launch_eval_pair_meas(bool split, int td, int gd, int k, const PairA
 // shared memory or (tab_global) read from global memory.
 cudaError_t launch_split_loops(int td, int gd, bool tab_global, const PairArgs& a, size_t smem, cudaStream_t s);
 
+struct DfArgs;
+// Defined in eval_df.cu: the double-float kernel (f64 mesh and fields) for (td, gd, k), tile 16;
+// `found` is false when none is compiled.
+cudaError_t launch_eval_df(int td, int gd, int k, const DfArgs& a, size_t smem, cudaStream_t s, bool* found);
+
 struct SfArgs;
 struct VjpSfArgs;
 // Defined in sumfact.cu: the sum-factorised adjoint of hexahedra (split: f32 arithmetic, else f64),

@@ -318,6 +318,7 @@ def _factor_names(g: Geometry, b: int, factors) -> list:
 
 
 SPLIT32 = 12  # ABI code of the split-precision tables
+DF64 = 16  # ABI code of the double-float tables (f64 fields computed on the FP32 pipe)
 
 
 def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points", "jacobian", "detj", "pinv"),
@@ -335,7 +336,10 @@ def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points
     ``precision="native"`` computes in the mesh's scalar type. ``precision="split"`` (f64 meshes)
     computes in FP32 on cell-shifted coordinates and returns f32 fields; points whose condition
     estimate exceeds `cond_limit` (0: 256) get det J and K from FP64, and `recomputed` (an int64
-    CUDA tensor of one element) counts them."""
+    CUDA tensor of one element) counts them. ``precision="df64"`` (f64 meshes) returns f64 fields
+    computed in double-float arithmetic on the FP32 pipe (pairs of f32, about 48 significant bits)
+    where the library has a double-float kernel for the element, and by the f64 kernels
+    elsewhere."""
     blk = g.blocks[b]
     names = _factor_names(g, b, factors)
     td, gd = blk.element.tdim, g.gdim
@@ -345,6 +349,11 @@ def geometric_factors_block(g: Geometry, b: int, pts: PointSet, factors=("points
             raise GridError(1, "split precision evaluates f64 meshes")
         tables = pts.tables(blk.element, gd, SPLIT32)
         out_dtype = torch.float32
+    elif precision == "df64":
+        if g.dtype != torch.float64:
+            raise GridError(1, "double-float precision evaluates f64 meshes")
+        tables = pts.tables(blk.element, gd, DF64)
+        out_dtype = torch.float64
     elif precision == "native":
         tables = pts.tables(blk.element, gd, g.dtype)
         out_dtype = g.dtype
@@ -639,8 +648,12 @@ class Batch:
         self.g, self.rule, self.precision = g, rule, precision
         self.cell_measure = []
         n = len(g.blocks)
+        if precision not in ("native", "split", "df64"):
+            raise GridError(1, f"unknown precision {precision!r}")
+        if precision != "native" and g.dtype != torch.float64:
+            raise GridError(1, f"{precision} precision evaluates f64 meshes")
         out_dtype = torch.float32 if precision == "split" else g.dtype
-        code = SPLIT32 if precision == "split" else g.dtype
+        code = {"split": SPLIT32, "df64": DF64}.get(precision, g.dtype)
         self.fields, self._tables = [], []
         descs = (TlgBlock * max(n, 1))()
         outs = (TlgOutputs * max(n, 1))()

@@ -51,8 +51,12 @@ typedef enum tlg_status {
 
 /* Scalar type of nodes and outputs: the byte size of F. TLG_SPLIT32 (tables only) selects the
  * split-precision evaluation: an f64 mesh, FP32 arithmetic on cell-shifted coordinates, f32
- * outputs, FP64 recompute of det J and K at points flagged by a condition estimate. */
-typedef enum tlg_dtype { TLG_F32 = 4, TLG_F64 = 8, TLG_SPLIT32 = 12 } tlg_dtype;
+ * outputs, FP64 recompute of det J and K at points flagged by a condition estimate. TLG_DF64
+ * (tables only) selects the double-float evaluation: an f64 mesh and f64 outputs, computed on the
+ * FP32 pipe in pairs of f32 (about 48 significant bits; errors of a few 1e-14 relative to the
+ * fields' largest values) where a double-float kernel exists for the element, by the f64 kernels
+ * elsewhere; its tables serve the f64 kernels too. */
+typedef enum tlg_dtype { TLG_F32 = 4, TLG_F64 = 8, TLG_SPLIT32 = 12, TLG_DF64 = 16 } tlg_dtype;
 
 /* tetraloma_dims::CellType (tetraloma-dims/src/dim.rs). */
 typedef enum tlg_cell {
