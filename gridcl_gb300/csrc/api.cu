@@ -433,7 +433,9 @@ tlg_status eval_df(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o
   a.off_refn = t->off_refn;
   a.mask = mask;
   a.num_points = (int)t->q;
-  cudaError_t e = tlg::launch_eval_df(t->td, t->gd, (int)t->k, a, t->bytes, stream, found);
+  const size_t smem = (size_t)(t->bytes + 15) / 16 * 16 + tlg::df_slot_bytes((int)t->k, t->gd);
+  if (smem > (size_t)227 * 1024) return TLG_ERR_UNSUPPORTED;
+  cudaError_t e = tlg::launch_eval_df(t->td, t->gd, (int)t->k, a, smem, stream, found);
   if (!*found) return TLG_ERR_UNSUPPORTED;
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
   g_last_family = TLG_STRATEGY_DIRECT;

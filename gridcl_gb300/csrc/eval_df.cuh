@@ -51,11 +51,17 @@ struct DfCursor {
   }
 };
 
+// Shared memory past the staged tables: per thread the double-float coordinates y_k (k >= 1) as
+// (head, tail) f32 pairs, [k - 1][g] with stride kEvalThreads (the lanes of a warp read
+// consecutive 8-byte slots).
+inline size_t df_slot_bytes(int k, int gd) { return (size_t)(k - 1) * gd * kEvalThreads * 8; }
+
 template <int TD, int GD, int K>
 __global__ void __launch_bounds__(kEvalThreads) eval_df_kernel(const __grid_constant__ DfArgs a) {
   constexpr int TILE = 16;
   constexpr int LJ = TD * GD;
   constexpr int RW = 1 + TD;  // float4 rows per node of a point pair
+  constexpr int T = kEvalThreads;
   using V = float2;
   using D = DF<V>;
   using B = Ar<V>;
@@ -66,6 +72,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_df_kernel(const __grid_cons
   stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
   const float4* rows = reinterpret_cast<const float4*>(smem + a.off_rows);
   const double* refn = reinterpret_cast<const double*>(smem + a.off_refn);
+  float2* ys = reinterpret_cast<float2*>(smem + (a.tab_bytes + 15) / 16 * 16) + threadIdx.x;
   const int nq = a.num_points;
   const int nqp = (nq + 1) / 2;
   const uint32_t mask = a.mask;
@@ -81,12 +88,16 @@ __global__ void __launch_bounds__(kEvalThreads) eval_df_kernel(const __grid_cons
     const uint32_t n0 = min(idx[0], a.last_node);
 #pragma unroll
     for (int g = 0; g < GD; ++g) x0[g] = __ldg(a.nodes + (int64_t)n0 * GD + g);
-    float yh[K][GD], yl[K][GD];  // k >= 1
+    // y_k = x_k - x_0 (k >= 1) into this thread's slots; the k = 0 term of every sum vanishes.
 #pragma unroll
     for (int k = 1; k < K; ++k) {
       const uint32_t n = min(idx[k], a.last_node);
 #pragma unroll
-      for (int g = 0; g < GD; ++g) df_split(__dsub_rn(__ldg(a.nodes + (int64_t)n * GD + g), x0[g]), yh[k][g], yl[k][g]);
+      for (int g = 0; g < GD; ++g) {
+        float h, l;
+        df_split(__dsub_rn(__ldg(a.nodes + (int64_t)n * GD + g), x0[g]), h, l);
+        ys[((k - 1) * GD + g) * T] = make_float2(h, l);
+      }
     }
     float oh[GD], ol[GD];  // x_0 + origin
 #pragma unroll
@@ -112,17 +123,35 @@ __global__ void __launch_bounds__(kEvalThreads) eval_df_kernel(const __grid_cons
     for (int qp = 0; qp < nqp; ++qp) {
       const bool both = 2 * qp + 1 < nq;
       const float4* rq = rows + (int64_t)qp * K * RW;
-      if (want_x) {
-        DfAcc<V> ax[GD];
+      // X - x_0 - origin and J of the pair, one node per iteration (a rolled loop: the unrolled
+      // one outgrows the instruction cache).
+      DfAcc<V> ax[GD], aj[LJ];
 #pragma unroll
-        for (int g = 0; g < GD; ++g) ax[g].zero();
+      for (int g = 0; g < GD; ++g) ax[g].zero();
 #pragma unroll
-        for (int k = 1; k < K; ++k) {
+      for (int i = 0; i < LJ; ++i) aj[i].zero();
+#pragma unroll 1
+      for (int k = 1; k < K; ++k) {
+        float2 y[GD];
+#pragma unroll
+        for (int g = 0; g < GD; ++g) y[g] = ys[((k - 1) * GD + g) * T];
+        if (want_x) {
           const float4 r = rq[k * RW];
 #pragma unroll
           for (int g = 0; g < GD; ++g)
-            ax[g].add(B::splat(yh[k][g]), B::splat(yl[k][g]), make_float2(r.x, r.y), make_float2(r.z, r.w));
+            ax[g].add(B::splat(y[g].x), B::splat(y[g].y), make_float2(r.x, r.y), make_float2(r.z, r.w));
         }
+        if (want_j) {
+#pragma unroll
+          for (int d = 0; d < TD; ++d) {
+            const float4 r = rq[k * RW + 1 + d];
+            const V th = make_float2(r.x, r.y), tl = make_float2(r.z, r.w);
+#pragma unroll
+            for (int g = 0; g < GD; ++g) aj[d * GD + g].add(B::splat(y[g].x), B::splat(y[g].y), th, tl);
+          }
+        }
+      }
+      if (want_x) {
         D xs[GD];
 #pragma unroll
         for (int g = 0; g < GD; ++g) xs[g] = A::add(A::make(B::splat(oh[g]), B::splat(ol[g])), ax[g].value());
@@ -130,23 +159,8 @@ __global__ void __launch_bounds__(kEvalThreads) eval_df_kernel(const __grid_cons
       }
       if (!want_j) continue;
       D j[LJ];
-      {
-        DfAcc<V> aj[LJ];
 #pragma unroll
-        for (int i = 0; i < LJ; ++i) aj[i].zero();
-#pragma unroll
-        for (int k = 1; k < K; ++k) {
-#pragma unroll
-          for (int d = 0; d < TD; ++d) {
-            const float4 r = rq[k * RW + 1 + d];
-            const V th = make_float2(r.x, r.y), tl = make_float2(r.z, r.w);
-#pragma unroll
-            for (int g = 0; g < GD; ++g) aj[d * GD + g].add(B::splat(yh[k][g]), B::splat(yl[k][g]), th, tl);
-          }
-        }
-#pragma unroll
-        for (int i = 0; i < LJ; ++i) j[i] = aj[i].value();
-      }
+      for (int i = 0; i < LJ; ++i) j[i] = aj[i].value();
       if (mask & kOutJacobian) cj.put2(j, both);
       if (mask & kOutDetJ) {
         const D dj = M::detj(j);
