@@ -25,6 +25,7 @@
 #include "tc.cuh"
 #include "sumfact.cuh"
 #include "eval_df.cuh"
+#include "sumfact_df.cuh"
 #include "vjp.cuh"
 
 struct tlg_batch {
@@ -71,9 +72,12 @@ struct tlg_tables {
   int sf_n = 0, sf_nblocks = 0;
   tlg::SfBlock sf_block0{};  // the first block (the adjoint's single-block rule)
   uint32_t off_sf = 0, sf_bytes = 0, sf_offperm = 0, sf_offrefn = 0;
-  // Double-float tables: a copy of the sum-factorisation section after it (same headers and
-  // offsets) whose B_d and D_d entries are (head, tail) f32 pairs.
-  uint32_t off_sfdf = 0;
+  // Double-float tables: the sum-factorisation section again after it, with headers of its own:
+  // B_d and D_d as (head, tail) f32 pairs [m_d][cols], except the direction whose points the
+  // kernels take two at a time (direction 0; the z points of prisms), stored per point pair as
+  // float4 (head of a, head of a + 1, tail of a, tail of a + 1) [ceil(m_d / 2)][cols], a + 1 clamped
+  // to the last point; then perm and the f64 reference normals.
+  uint32_t off_sfdf = 0, sfdf_bytes = 0, sfdf_offperm = 0, sfdf_offrefn = 0;
   // Tensor-core section (f32 and split tables, TD >= 2), after the sum-factorisation section, read
   // from global memory: the basis in mma fragment order, [col tile][k-step][lane] x 4 f32
   // (b0 head, b1 head, b0 tail, b1 tail) of B[k][4 q + r] (r = 0 phi, 1 + d dphi_d).
@@ -267,10 +271,7 @@ int principal_family(uint32_t mask) {
 // Q3 - / 11.5 / 0.62; f32 Q2 1.15 / 17.6 / 1.39, Q3 - / 16.7 / 0.55. So: sum factorisation
 // always in f64, and in f32 and split precision above the degrees with paired kernels
 // (quadrilaterals and hexahedra Q1-Q2).
-bool sumfact_preferred(const tlg_tables* t) {
-  if (t->df) return false;  // (until the double-float sum factorisation exists)
-  return t->sf_ok && (t->dtype == TLG_F64 || t->sf_n >= 4);
-}
+bool sumfact_preferred(const tlg_tables* t) { return t->sf_ok && (t->dtype == TLG_F64 || t->sf_n >= 4); }
 
 // The policy of TLG_STRATEGY_AUTO beyond the compiled unrolled kernels (more than 27 nodes per
 // cell): the cooperative kernel instead of the loops kernel.
@@ -286,7 +287,7 @@ bool tc_preferred(const tlg_tables*) { return false; }
 tlg_status eval_sumfact(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
                         cudaStream_t stream, bool* found) {
   *found = false;
-  if (!t->sf_ok || (t->dtype == TLG_SPLIT32 && o->tile != 16))
+  if (!t->sf_ok || ((t->dtype == TLG_SPLIT32 || t->df) && o->tile != 16))
     return TLG_ERR_UNSUPPORTED;
   tlg::SfArgs a;
   std::memset(&a, 0, sizeof(a));
@@ -318,9 +319,22 @@ tlg_status eval_sumfact(const tlg_tables* t, const tlg_block* b, const tlg_outpu
   a.mask = mask;
   a.num_points = (int)t->q;
   const size_t fbytes = t->dtype == TLG_F64 ? 8 : 4;
-  const size_t smem = (t->sf_bytes + 15) / 16 * 16 + tlg::sumfact_slot_bytes((int)t->k, t->gd, fbytes);
+  if (t->df) {  // the double-float section
+    a.tab = t->dev + t->off_sfdf;
+    a.tab_bytes = t->sfdf_bytes;
+    a.off_perm = t->sfdf_offperm;
+    a.off_refn = t->sfdf_offrefn;
+  }
+  // Double-float hexahedra without facet normals: three lanes per cell.
+  const bool three = t->df && t->cell == tlg::kHexahedron && !(mask & tlg::kOutFacetNormals);
+  const size_t slots = three    ? tlg::sumfact_df3_slot_bytes((int)t->k)
+                       : t->df ? tlg::sumfact_df_slot_bytes((int)t->k, t->gd)
+                               : tlg::sumfact_slot_bytes((int)t->k, t->gd, fbytes);
+  const size_t smem = (a.tab_bytes + 15) / 16 * 16 + slots;
   if (smem > (size_t)227 * 1024) return TLG_ERR_UNSUPPORTED;
-  cudaError_t e = tlg::launch_sumfact(t->dtype, t->td, t->gd, t->sf_n, a, smem, stream, found);
+  cudaError_t e = three   ? tlg::launch_sumfact_df3(t->sf_n, a, smem, stream, found)
+                  : t->df ? tlg::launch_sumfact_df(t->td, t->gd, t->sf_n, a, smem, stream, found)
+                          : tlg::launch_sumfact(t->dtype, t->td, t->gd, t->sf_n, a, smem, stream, found);
   if (!*found) return TLG_ERR_UNSUPPORTED;
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
   g_last_family = TLG_STRATEGY_SUMFACT;
@@ -1042,7 +1056,7 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       t->sf_prism = t->sf_ok && cell == tlg::kPrism;
     }
     t->off_sf = (uint32_t)align16(t->off_vjp + t->vjp_bytes);
-    std::vector<tlg::SfBlock> heads;
+    std::vector<tlg::SfBlock> heads, dfheads;
     if (t->sf_ok) {
       t->sf_n = degree + 1;
       t->sf_nblocks = (int)sf.size();
@@ -1067,10 +1081,32 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       t->sf_offrefn = (uint32_t)off;
       if (ref_normals) off = align16(off + (size_t)npoints * td * es);
       t->sf_bytes = (uint32_t)off;
-      if (df) t->off_sfdf = (uint32_t)align16((size_t)t->off_sf + t->sf_bytes);
+      if (df) {
+        dfheads = heads;
+        size_t doff = align16(sf.size() * sizeof(tlg::SfBlock));
+        const int pd = t->sf_prism ? 2 : 0;
+        for (size_t bi = 0; bi < sf.size(); ++bi)
+          for (int d = 0; d < 3; ++d) {
+            const int m = sf[bi].m[d];
+            auto bytes = [&](const std::vector<double>& v) {
+              const size_t cols = m > 0 ? v.size() / m : 0;
+              return d == pd ? (size_t)((m + 1) / 2) * cols * 16 : v.size() * 8;
+            };
+            dfheads[bi].off_b[d] = (uint32_t)doff;
+            doff = align16(doff + bytes(sf[bi].B[d]));
+            dfheads[bi].off_d[d] = (uint32_t)doff;
+            doff = align16(doff + bytes(sf[bi].D[d]));
+          }
+        t->sfdf_offperm = (uint32_t)doff;
+        doff = align16(doff + sf_perm.size() * 4);
+        t->sfdf_offrefn = (uint32_t)doff;
+        if (ref_normals) doff = align16(doff + (size_t)npoints * td * 8);
+        t->sfdf_bytes = (uint32_t)doff;
+        t->off_sfdf = (uint32_t)align16((size_t)t->off_sf + t->sf_bytes);
+      }
     }
     // The tensor-core section.
-    size_t host_bytes = t->off_sfdf ? (size_t)t->off_sfdf + t->sf_bytes : (size_t)t->off_sf + t->sf_bytes;
+    size_t host_bytes = t->off_sfdf ? (size_t)t->off_sfdf + t->sfdf_bytes : (size_t)t->off_sf + t->sf_bytes;
     if (dtype != TLG_F64 && td >= 2 && k > 10 && npoints > 0) {
       t->tc_ksteps = (int)((k + 7) / 8);
       t->tc_col_tiles = (int)((npoints + 1) / 2);
@@ -1096,13 +1132,34 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
         if (dtype == TLG_F64) narrow_into<double>(t->host, t->off_sf + t->sf_offrefn, ref_normals, (size_t)npoints * td);
         else narrow_into<float>(t->host, t->off_sf + t->sf_offrefn, ref_normals, (size_t)npoints * td);
       }
-      if (t->off_sfdf) {  // the same section with the tables as (head, tail) pairs
-        std::memcpy(t->host.data() + t->off_sfdf, t->host.data() + t->off_sf, t->sf_bytes);
+      if (t->off_sfdf) {  // the double-float section
+        unsigned char* base = t->host.data() + t->off_sfdf;
+        std::memcpy(base, dfheads.data(), dfheads.size() * sizeof(tlg::SfBlock));
+        const int pd = t->sf_prism ? 2 : 0;
         for (size_t bi = 0; bi < sf.size(); ++bi)
           for (int d = 0; d < 3; ++d) {
-            split_into(t->host, t->off_sfdf + heads[bi].off_b[d], sf[bi].B[d].data(), sf[bi].B[d].size());
-            split_into(t->host, t->off_sfdf + heads[bi].off_d[d], sf[bi].D[d].data(), sf[bi].D[d].size());
+            const int m = sf[bi].m[d];
+            auto write = [&](uint32_t off, const std::vector<double>& v) {
+              if (d != pd) {
+                split_into(t->host, t->off_sfdf + off, v.data(), v.size());
+                return;
+              }
+              const int cols = m > 0 ? (int)(v.size() / m) : 0;
+              float* dst = reinterpret_cast<float*>(base + off);
+              for (int pp = 0; pp < (m + 1) / 2; ++pp)
+                for (int c = 0; c < cols; ++c)
+                  for (int hh = 0; hh < 2; ++hh) {
+                    const double x = v[(size_t)std::min(2 * pp + hh, m - 1) * cols + c];
+                    float* e = dst + ((size_t)pp * cols + c) * 4;
+                    e[hh] = (float)x;
+                    e[2 + hh] = (float)(x - (double)(float)x);
+                  }
+            };
+            write(dfheads[bi].off_b[d], sf[bi].B[d]);
+            write(dfheads[bi].off_d[d], sf[bi].D[d]);
           }
+        std::memcpy(base + t->sfdf_offperm, sf_perm.data(), sf_perm.size() * 4);
+        if (ref_normals) narrow_into<double>(t->host, t->off_sfdf + t->sfdf_offrefn, ref_normals, (size_t)npoints * td);
       }
     }
     // Reorder [deriv][q][k] into phi [q][k] and dphi [q][k][d].

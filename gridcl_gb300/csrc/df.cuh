@@ -22,8 +22,7 @@
 // f64 <-> double-float conversions: df_split rounds an f64 to its nearest f32 (integer
 // operations) and the remainder with one FP64 subtraction; df_to_f64 assembles the f64 bit
 // pattern of h + l with integer operations and one FFMA (the f64 value of h, plus l in units of
-// 64 ulp of that f64: about 47 significant bits), taking the FP64 instructions only for h
-// outside [2^-81, 2^128) (zero, tiny, infinite, NaN).
+// 64 ulp of that f64: about 47 significant bits). Both are branch-free.
 #pragma once
 
 #include <cstdint>
@@ -147,57 +146,65 @@ struct DfAcc {
   __device__ __forceinline__ DF<V> value() const { return Ar<DF<V>>::fast_two_sum(s, c); }
 };
 
-static __device__ __noinline__ float d2f_slow(double x) { return __double2float_rn(x); }
-static __device__ __noinline__ double f2d_slow(float f) { return (double)f; }
-
-// d2f_rn and f2d_exact (convert.cuh) with their instruction paths (zero, subnormal, infinite, NaN
-// operands) out of line.
-__device__ __forceinline__ float d2f_rn_br(double x) {
+// f64 -> f32 rounded to nearest even and f32 -> f64, in integer operations without branches (a
+// branch per conversion costs more than the conversion): as convert.cuh's d2f_rn / f2d_exact for
+// normal values, with magnitudes below the f32 normal range flushed to a signed zero (below
+// 1.2e-38: far below any geometric value these kernels produce), overflow to infinity and NaN to
+// NaN.
+__device__ __forceinline__ float d2f_nb(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned e = (unsigned)(b >> 52) & 0x7FFu;
-  if (__builtin_expect(e - 897u >= 254u, 0)) return d2f_slow(x);
+  const unsigned sign = (unsigned)(b >> 63) << 31;
   const unsigned long long m = b & 0xFFFFFFFFFFFFFull;
-  unsigned r = ((unsigned)(b >> 63) << 31) | ((e - 896u) << 23) | (unsigned)(m >> 29);
+  unsigned r = sign | ((e - 896u) << 23) | (unsigned)(m >> 29);
   const unsigned rest = (unsigned)(m & 0x1FFFFFFFull);
   r += (unsigned)(rest > 0x10000000u) | ((unsigned)(rest == 0x10000000u) & r & 1u);
+  // Below 2^-126: zero; from 2^128 on: infinity, NaN stays NaN.
+  const unsigned special = e == 0x7FFu && m != 0 ? 0x7FC00000u : 0x7F800000u;
+  r = e < 897u ? sign : (e > 1150u ? sign | special : r);
   return __uint_as_float(r);
 }
 
-__device__ __forceinline__ double f2d_exact_br(float f) {
+__device__ __forceinline__ double f2d_nb(float f) {
   const uint32_t b = __float_as_uint(f);
   const uint32_t e = (b >> 23) & 0xFFu;
-  if (__builtin_expect(e - 1u >= 254u, 0)) return (b << 1) == 0u ? __longlong_as_double((long long)((uint64_t)(b >> 31) << 63)) : f2d_slow(f);
-  return __longlong_as_double(
-      (long long)(((uint64_t)(b >> 31) << 63) | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7FFFFFu) << 29)));
+  const uint32_t sign = b & 0x80000000u;
+  uint32_t hi = sign | (((b & 0x7FFFFFFFu) >> 3) + (e == 0xFFu ? (1792u << 20) : (896u << 20)));
+  uint32_t lo = b << 29;
+  hi = e == 0u ? sign : hi;  // zero (and f32 subnormals) to a signed zero
+  lo = e == 0u ? 0u : lo;
+  return __hiloint2double((int)hi, (int)lo);
 }
 
 // An f64 as the nearest f32 and the f32 nearest to the remainder (about 48 bits).
 __device__ __forceinline__ void df_split(double v, float& h, float& l) {
-  h = d2f_rn_br(v);
-  l = d2f_rn_br(__dsub_rn(v, f2d_exact_br(h)));
+  h = d2f_nb(v);
+  l = d2f_nb(__dsub_rn(v, f2d_nb(h)));
 }
 
-// The FP64 instructions' h + l, out of line: a branch the compiler cannot turn into predicated
-// FP64 instructions issued at every output.
-static __device__ __noinline__ double df_to_f64_slow(float h, float l) { return __dadd_rn((double)h, (double)l); }
-
-// h + l as an f64 (h, l normalised: |l| <= ulp(h) / 2).
+// h + l as an f64 (h, l normalised: |l| <= ulp(h) / 2), in integer operations and one FFMA,
+// without branches. For |h| in [2^-81, 2^128): the f64 of h plus l in units of 64 ulp of that
+// f64 (about 47 significant bits). Below 2^-81 l is dropped (the f64 of h, relative error 2^-24 of
+// a value under 4e-25), f32 subnormals and zero give a signed zero, infinity and NaN stay so.
 __device__ __forceinline__ double df_to_f64(float h, float l) {
   const uint32_t hb = __float_as_uint(h);
   const uint32_t eh = (hb >> 23) & 0xFFu;
-  if (__builtin_expect(eh - 46u > 208u, 0)) return df_to_f64_slow(h, l);
+  const bool scaled = eh - 46u <= 208u;
   // n = l / (64 ulp64(h)), rounded to nearest: |l| <= ulp32(h) / 2 = 2^28 ulp64(h), so |n| <= 2^22
-  // and 1.5 * 2^23 + n is exact in [2^23, 2^24], its low mantissa bits n.
-  const float scale = __uint_as_float((300u - eh) << 23);  // 2^(173 - eh)
-  const float t = __fmaf_rn(l, scale, 12582912.0f);
-  int n = (int)(__float_as_uint(t) - 0x4B400000u);
-  const int sgn = (int)hb >> 31;  // 0 or -1: a negative h adds -n to the magnitude
-  n = (n ^ sgn) - sgn;
+  // and 1.5 * 2^23 + n is exact in [2^23, 2^24], its low mantissa bits n. The scale carries h's
+  // sign, so that n is the change of h's magnitude.
+  const float scale = __uint_as_float(((300u << 23) - (hb & 0x7F800000u)) | (hb & 0x80000000u));
+  const float t = __fmaf_rn(l, scaled ? scale : 0.0f, 12582912.0f);
+  const int n = (int)(__float_as_uint(t) - 0x4B400000u);
   // A power of two h whose magnitude l lowers lands in the binade below, whose ulp is half: the
   // same change of value is twice as many units of the mantissa field there.
   const int shift = 6 + (int)(((hb << 9) == 0u) & (n < 0));
-  const uint32_t hi_word = (hb & 0x80000000u) | (((hb & 0x7FFFFFFFu) >> 3) + (896u << 20));
-  const uint64_t bits = (((uint64_t)hi_word << 32) | (uint64_t)(hb << 29)) + (uint64_t)((int64_t)n << shift);
+  const uint32_t sign = hb & 0x80000000u;
+  uint32_t hi = sign | (((hb & 0x7FFFFFFFu) >> 3) + (eh == 0xFFu ? (1792u << 20) : (896u << 20)));
+  uint32_t lo = hb << 29;
+  hi = eh == 0u ? sign : hi;
+  lo = eh == 0u ? 0u : lo;
+  const uint64_t bits = (((uint64_t)hi << 32) | lo) + (uint64_t)((int64_t)n << shift);
   return __longlong_as_double((long long)bits);
 }
 

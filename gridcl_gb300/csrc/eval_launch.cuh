@@ -93,6 +93,11 @@ cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t sme
 // N nodes per direction; `found` is false when none is compiled for (td, gd, n).
 cudaError_t launch_sumfact(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
                            bool* found);
+// Defined in sumfact_df.cu: the double-float sum-factorised kernels (f64 mesh and fields, tile 16;
+// a.tab the tables' double-float section), and those of hexahedra with three lanes per cell (no
+// facet normals; smem: the section and sumfact_df3_slot_bytes).
+cudaError_t launch_sumfact_df(int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s, bool* found);
+cudaError_t launch_sumfact_df3(int n, const SfArgs& a, size_t smem, cudaStream_t s, bool* found);
 // Defined in sumfact_fn.cu: the same with facet normals among the outputs (codimension 0).
 cudaError_t launch_sumfact_fn(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
                               bool* found);
