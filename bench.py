@@ -8,13 +8,18 @@ det J and K = J^-1 at every point (22 values). One step = one evaluation of the 
 device; `e2e` adds, every step, the host-to-device copy of the node and dofmap arrays from
 pinned host memory, the evaluation, the measure (sum of det J * w) and its read back.
 
-Modes (`--mode`): `split` (default): the f64 mesh evaluated in FP32 on cell-shifted
-coordinates into f32 fields, FP64 recompute at near-degenerate points; its error against the
-plain FP64 GPU path is measured per output in the same run and reported with it, together with
-that path's own rate. `f64`: the plain per-block FP64 path. `f32`: an f32 mesh in FP32.
+Modes (`--mode`): `df64` (default): the f64 mesh evaluated into f64 fields in double-float
+arithmetic on the FP32 pipe (f64-accurate: errors against the oracle of a few 1e-13, printed as
+`error_vs_oracle` over a seeded sample of 65,536 cells). `split`: FP32 arithmetic on cell-shifted
+coordinates into f32 fields (errors of about 1e-6), FP64 recompute at near-degenerate points.
+`f64`: the plain per-block FP64 path. `f32`: an f32 mesh in FP32. The run also times the other
+precisions of an f64 mesh on the same mesh (`plain_fp64_gpu`, `df64_gpu`, `split_gpu`, each with
+its errors against the oracle); `vs_baseline` is the line's speed-up over the plain FP64 GPU path
+of the same run, the metric's baseline.
 
 `--impl reference` times the CPU restatement of the reference's f64 evaluation (the oracle,
-C + OpenMP) on the host cores over the same workload.
+C + OpenMP) on the host cores over the same workload, with the mesh and rule built from the
+oracle's reference cells (this arm loads none of the library).
 
 Runs under torchrun for N > 1: every rank evaluates its own copy of the workload (replicas,
 weak scaling; the path has no exchange), rank 0 reports the whole-job rate over the slowest
@@ -56,7 +61,7 @@ def parse():
     p.add_argument("--steps", type=int, default=40)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--mode", choices=["split", "f64", "f32"], default="split")
+    p.add_argument("--mode", choices=["df64", "split", "f64", "f32"], default="df64")
     p.add_argument("--n", type=int, default=64, help="subcells per direction")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
@@ -71,16 +76,59 @@ def parse():
     return p.parse_args()
 
 
-def build_mesh(n: int):
+def build_mesh(n: int, lagrange_points=None):
     from gridcl_gb300 import meshes
 
-    return meshes.curved_box("Tetrahedron", n, 2, jitter=0.02, seed=2026)
+    return meshes.curved_box("Tetrahedron", n, 2, jitter=0.02, seed=2026, lagrange_points=lagrange_points)
 
 
 def rule():
     from gridcl_gb300 import refcell
 
     return refcell.collapsed_rule("Tetrahedron", RULE_COUNTS)
+
+
+SAMPLE_CELLS = 65536  # cells of the seeded sample compared with the oracle at full size
+
+
+def sample_cells(num_cells: int, count: int = SAMPLE_CELLS, seed: int = 2026) -> np.ndarray:
+    """A seeded sample of distinct cell indices (all cells when there are fewer), ascending."""
+    if num_cells <= count:
+        return np.arange(num_cells)
+    return np.sort(np.random.default_rng(seed).choice(num_cells, count, replace=False))
+
+
+def field_at(field, cells: np.ndarray) -> np.ndarray:
+    """Values of a one-chunk QuadField at the given cells, ``[cell][point][component]`` on the host
+    (gathered on the device from the tiled layout, field.rs:121-162)."""
+    import torch
+
+    t, q, length = field.tile, field.num_points, field.length
+    data = field.chunks[0].data
+    c = torch.from_numpy(np.asarray(cells, dtype=np.int64)).to(data.device)
+    qq = torch.arange(q, device=data.device)
+    kk = torch.arange(length, device=data.device)
+    idx = (((c // t)[:, None, None] * q + qq[None, :, None]) * length + kk[None, None, :]) * t + (c % t)[:, None, None]
+    return data[idx].double().cpu().numpy()
+
+
+def oracle_sample(mesh, geom, cell: str, degree: int, pts, cells: np.ndarray, block: int = 0,
+                  factors=("x", "j", "detj", "k")):
+    """The oracle's factors at the given cells (the stored node coordinates plus origin)."""
+    from oracle import oracle as orc
+
+    absx = geom.nodes.double().cpu().numpy() + np.array(geom.origin[: geom.gdim])
+    return orc.eval_block(cell, degree, absx, mesh.blocks[block].cells[cells], pts, factors=factors)
+
+
+def errors_vs_oracle(fields: dict, want: dict, cells: np.ndarray) -> dict:
+    """max |got - oracle| / max |oracle| per output over the sampled cells."""
+    names = {"points": "x", "jacobian": "j", "detj": "detj", "pinv": "k", "normals": "normals"}
+    out = {}
+    for f, fld in fields.items():
+        w = want[names[f]].reshape(len(cells), fld.num_points, -1)
+        out[f] = float(np.abs(field_at(fld, cells) - w).max() / np.abs(w).max())
+    return out
 
 
 def algorithmic_bytes(cells: int, k: int, nodes: int, gd: int, qpts: int, es: int, nout: int) -> int:
@@ -178,13 +226,17 @@ def cpu_baseline(mesh, pts, target_s: float = 10.0):
 
 
 def run_reference(args):
+    """The oracle (C + OpenMP restatement of the reference's f64 evaluation) over the workload on
+    the host cores. The mesh and the rule come from the oracle's own reference cells, so that this
+    arm loads none of the library."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    mesh = build_mesh(args.n)
-    pts, _ = rule()
     from oracle import oracle as orc
     from oracle import refcell as orc_refcell
+
+    mesh = build_mesh(args.n, lagrange_points=orc_refcell.lagrange_points)
+    pts, _ = orc_refcell.collapsed_rule("Tetrahedron", RULE_COUNTS)
 
     orc.build()
     cells = mesh.blocks[0].cells
@@ -288,7 +340,8 @@ def rel_err_fields(a: dict, b: dict) -> dict:
 def extra_hybrid():
     """Hybrid mesh, one graph launch: 2,000,000 Q2 hexahedra (27-point Gauss), 300,000 P2 prisms
     (21 points), 50,000 P3 tetrahedra (24 points); plain per-block FP64 launches against the
-    batched FP64 and split-precision graphs."""
+    batched FP64, double-float (f64-accurate) and split-precision graphs, each with its errors
+    against the oracle on 16,384 seeded cells per block."""
     import torch
 
     import gridcl_gb300 as tg
@@ -313,28 +366,36 @@ def extra_hybrid():
     res = {"workload": "hybrid: 2,000,000 Q2 hex (27 pts) + 300,000 P2 prisms (21) + 50,000 P3 tets (24), "
                        "sin-mapped + jittered, fused x/J/detJ/K", "qpoints": int(qpts),
            "plain_fp64_per_block": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3)}}
-    for precision in ("native", "split"):
+    samples = [sample_cells(b.num_cells, 16384, seed=7 + i) for i, b in enumerate(g.blocks)]
+    want = [oracle_sample(mesh, g, blk.element.cell, blk.element.degree, rule.get(blk.element.cell).points, samples[b],
+                          block=b) for b, blk in enumerate(g.blocks)]
+    res["plain_fp64_per_block"]["error_vs_oracle"] = {
+        b: errors_vs_oracle(plain_out[b], want[b], samples[b]) for b in range(len(g.blocks))}
+    for precision in ("native", "df64", "split"):
         batch = tg.Batch(g, rule, factors=factors, precision=precision)
         grids = batch.tune()
-        ms = event_ms(batch.launch)
-        key = "batched_fp64_graph" if precision == "native" else "batched_split_graph"
+        ms = event_ms(batch.launch, reps=10)
+        key = {"native": "batched_fp64_graph", "df64": "batched_df64_graph", "split": "batched_split_graph"}[precision]
         res[key] = {"ms": ms, "value": qpts / (ms * 1e-3), "tuned_grids": grids,
-                    "speedup_vs_plain_fp64": plain_ms / ms}
-        if precision == "split":
-            res[key]["rel_err_vs_fp64"] = {
-                b: rel_err_fields(batch.fields[b], plain_out[b]) for b in range(len(g.blocks))}
-            out_bytes = qpts * 22 * 4
-            in_bytes = sum(b.num_cells * b.element.nodes_per_cell * 4 for b in g.blocks) + g.nodes.numel() * 8
-            res[key]["hbm_gbs"] = (out_bytes + in_bytes) / (ms * 1e-3) / 1e9
+                    "speedup_vs_plain_fp64": plain_ms / ms,
+                    "error_vs_oracle": {b: errors_vs_oracle(batch.fields[b], want[b], samples[b])
+                                        for b in range(len(g.blocks))}}
+        es = 4 if precision == "split" else 8
+        out_bytes = qpts * 22 * es
+        in_bytes = sum(b.num_cells * b.element.nodes_per_cell * 4 for b in g.blocks) + g.nodes.numel() * 8
+        res[key]["hbm_gbs"] = (out_bytes + in_bytes) / (ms * 1e-3) / 1e9
         del batch
+    res["error_sample"] = "16,384 seeded cells per block against the oracle (f64)"
     return res
 
 
 def extra_hybrid_adjoint():
-    """The batched fused forward + adjoint on the hybrid mesh (2,000,000 Q2 hex, 27
-    points; 300,000 P2 prisms, 21; 50,000 P3 tets, 24): seeded standard-normal cotangents on det J
-    and K; one graph launch of the split-precision fused forward (x/J/detJ/K) + adjoint + node
-    sums against the plain per-block FP64 forward followed by the per-block FP64 adjoint."""
+    """The batched forward + adjoint on the hybrid mesh (2,000,000 Q2 hex, 27 points; 300,000 P2
+    prisms, 21; 50,000 P3 tets, 24): seeded standard-normal cotangents on det J and K; one graph
+    launch of (a) the double-float forward (f64-accurate x/J/detJ/K) and the split-precision
+    adjoint + node sums, (b) the split-precision fused forward + adjoint + node sums, against the
+    plain per-block FP64 forward followed by the per-block FP64 adjoint. Bandwidth figures count
+    compulsory traffic only (cotangents, fields, dofmaps, nodes, node cotangents)."""
     import torch
 
     import gridcl_gb300 as tg
@@ -378,33 +439,46 @@ def extra_hybrid_adjoint():
     plain()
     plain_ms = event_ms(plain, reps=2, warm=1)
     want = grad64.clone()
-    batch = tg.AdjointBatch(g, rule, ct32, precision="split", forward=factors)
-    batch.launch()
-    fused_ms = event_ms(batch.launch)
-    gerr = float((batch.grad - want).abs().max() / want.abs().max())
-    ferr = {b: rel_err_fields(batch.fields[b], fwd64[b]) for b in range(len(g.blocks))}
-    alg = 0
-    for blk in g.blocks:
-        nq = len(rule.get(blk.element.cell))
-        cells, k = blk.num_cells, blk.element.nodes_per_cell
-        alg += cells * nq * (10 + 22) * 4 + cells * k * 4 + 2 * cells * k * 16 + cells * k * 4
+    samples = [sample_cells(b.num_cells, 16384, seed=7 + i) for i, b in enumerate(g.blocks)]
+    orc_fwd = [oracle_sample(mesh, g, blk.element.cell, blk.element.degree, rule.get(blk.element.cell).points,
+                             samples[b], block=b) for b, blk in enumerate(g.blocks)]
     nn = g.nodes.shape[0]
-    alg += nn * 3 * 8 + nn * 3 * 8 * (1 + 2) + len(g.blocks) * nn * 4  # nodes, grad zero + add, offsets
-    return {"workload": "hybrid 2,000,000 Q2 hex + 300,000 P2 prisms + 50,000 P3 tets: forward x/J/detJ/K + "
-                        "adjoint from detJ and K cotangents + node sums",
-            "qpoints": int(qpts),
-            "plain_fp64_per_block_fwd_then_vjp": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3)},
-            "batched_fused_split_graph": {"ms": fused_ms, "value": qpts / (fused_ms * 1e-3),
-                                          "speedup_vs_plain_fp64": plain_ms / fused_ms,
-                                          "algorithmic_bytes": int(alg),
-                                          "hbm_gbs": alg / (fused_ms * 1e-3) / 1e9,
-                                          "grad_rel_err_vs_fp64": gerr, "forward_rel_err_vs_fp64": ferr}}
+
+    def compulsory(es_fields: int) -> int:
+        """Compulsory traffic of the step: f32 cotangents (det J, K) in, the forward fields out,
+        the dofmaps and the nodes in, the node cotangents out."""
+        total = nn * 3 * 8 * 2
+        for blk in g.blocks:
+            nq_b = len(rule.get(blk.element.cell))
+            total += blk.num_cells * nq_b * (10 * 4 + 22 * es_fields) + blk.num_cells * blk.element.nodes_per_cell * 4
+        return total
+
+    res = {"workload": "hybrid 2,000,000 Q2 hex + 300,000 P2 prisms + 50,000 P3 tets: forward x/J/detJ/K + "
+                       "adjoint from detJ and K cotangents + node sums",
+           "qpoints": int(qpts),
+           "plain_fp64_per_block_fwd_then_vjp": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3)},
+           "error_sample": "forward fields on 16,384 seeded cells per block against the oracle (f64); node "
+                           "cotangents against the plain FP64 path's"}
+    for precision, key, es in (("df64", "batched_df64_forward_split_adjoint_graph", 8),
+                               ("split", "batched_fused_split_graph", 4)):
+        batch = tg.AdjointBatch(g, rule, ct32, precision=precision, forward=factors)
+        batch.launch()
+        ms = event_ms(batch.launch, reps=10)
+        alg = compulsory(es)
+        res[key] = {"ms": ms, "value": qpts / (ms * 1e-3), "speedup_vs_plain_fp64": plain_ms / ms,
+                    "compulsory_bytes": int(alg), "hbm_gbs": alg / (ms * 1e-3) / 1e9,
+                    "grad_rel_err_vs_fp64": float((batch.grad - want).abs().max() / want.abs().max()),
+                    "forward_error_vs_oracle": {b: errors_vs_oracle(batch.fields[b], orc_fwd[b], samples[b])
+                                                for b in range(len(g.blocks))}}
+        del batch
+        torch.cuda.empty_cache()
+    return res
 
 
 def extra_sphere():
     """Surface TD=2, GD=3: 4,194,304 degree-4 triangles of the refined icosahedron (first cells of
-    9 refinements), radius x (1 + 0.02 U), 28-point rule; x, J, area element, normals, K; split
-    precision against FP64."""
+    9 refinements), radius x (1 + 0.02 U), 28-point rule; x, J, area element, normals, K; FP64,
+    double-float and split precision, each against the oracle on 65,536 seeded cells."""
     import torch
 
     import gridcl_gb300 as tg
@@ -421,14 +495,22 @@ def extra_sphere():
     recomputed = int(count.item())
     ms64 = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, factors, out=f64), reps=3)
     ms32 = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, factors, out=split, precision="split"))
-    out_bytes = qpts * 19 * 4
+    dfl = tg.geometric_factors_block(g, 0, ps, factors, precision="df64")
+    msdf = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, factors, out=dfl, precision="df64"))
+    sample = sample_cells(mesh.blocks[0].num_cells)
+    want = oracle_sample(mesh, g, "Triangle", 4, ps.points, sample, factors=("x", "j", "detj", "k", "normals"))
     in_bytes = mesh.blocks[0].cells.size * 4 + g.nodes.numel() * 8
     return {"workload": "sphere P4 triangles 4,194,304 cells, 28 pts, x/J/area/normals/K", "qpoints": int(qpts),
-            "fp64": {"ms": ms64, "value": qpts / (ms64 * 1e-3)},
+            "error_sample": f"{len(sample)} seeded cells against the oracle (f64)",
+            "fp64": {"ms": ms64, "value": qpts / (ms64 * 1e-3), "error_vs_oracle": errors_vs_oracle(f64, want, sample)},
+            "df64": {"ms": msdf, "value": qpts / (msdf * 1e-3), "speedup_vs_fp64": ms64 / msdf,
+                     "hbm_gbs": (qpts * 19 * 8 + in_bytes) / (msdf * 1e-3) / 1e9,
+                     "error_vs_oracle": errors_vs_oracle(dfl, want, sample)},
             "split": {"ms": ms32, "value": qpts / (ms32 * 1e-3), "speedup_vs_fp64": ms64 / ms32,
-                      "hbm_gbs": (out_bytes + in_bytes) / (ms32 * 1e-3) / 1e9,
+                      "hbm_gbs": (qpts * 19 * 4 + in_bytes) / (ms32 * 1e-3) / 1e9,
                       "fp64_recomputed_points": recomputed,
-                      "rel_err_vs_fp64": rel_err_fields(split, f64)}}
+                      "rel_err_vs_fp64": rel_err_fields(split, f64),
+                      "error_vs_oracle": errors_vs_oracle(split, want, sample)}}
 
 
 def extra_adjoint(n: int = 128, fd_nodes: int = 1000):
@@ -491,18 +573,34 @@ def extra_adjoint(n: int = 128, fd_nodes: int = 1000):
         fd = tg.fd_check(g, 0, ps, {"detj": host["detj"][..., 0], "pinv": host["pinv"]},
                          grad64.cpu().numpy(), sample)
     gerr = float((grad32 - grad64).abs().max() / grad64.abs().max())
-    # Compulsory traffic of the fused step: cotangents in, forward fields out, nodes and dofmap
-    # in, contributions out and back in through the CSR, node cotangents out.
-    alg = (qpts * 10 * 4 + qpts * 22 * 4 + ncells * 27 * 4 + g.nodes.numel() * 8
-           + 2 * ncells * 27 * 3 * 4 + g.nodes.numel() * 8 + (ncells * 27 + g.nodes.shape[0]) * 4)
+    # The double-float forward (f64-accurate fields) with the split-precision adjoint, one graph.
+    dfb = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct32], precision="df64", forward=factors)
+    dfb.launch()
+    df_ms = event_ms(dfb.launch)
+    sample = sample_cells(ncells)
+    want = oracle_sample(mesh, g, "Hexahedron", 2, ps.points, sample)
+
+    # Compulsory traffic: f32 cotangents in, the forward fields out, nodes and dofmap in, node
+    # cotangents out.
+    def compulsory(es_fields):
+        return qpts * 10 * 4 + qpts * 22 * es_fields + ncells * 27 * 4 + g.nodes.numel() * 8 * 2
+
     return {"workload": f"Q2 hex {n}^3, 27 pts, forward (x/J/detJ/K) + adjoint from detJ and K cotangents",
             "qpoints": int(qpts),
-            "plain_fp64_fwd_then_vjp": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3)},
+            "error_sample": f"forward fields on {len(sample)} seeded cells against the oracle (f64)",
+            "plain_fp64_fwd_then_vjp": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3),
+                                        "forward_error_vs_oracle": errors_vs_oracle(fwd64, want, sample)},
             "fused_split_fwd_vjp": {"ms": fused_ms, "value": qpts / (fused_ms * 1e-3),
                                     "speedup_vs_plain_fp64": plain_ms / fused_ms,
-                                    "hbm_gbs": alg / (fused_ms * 1e-3) / 1e9,
+                                    "hbm_gbs": compulsory(4) / (fused_ms * 1e-3) / 1e9,
                                     "grad_rel_err_vs_fp64": gerr,
-                                    "forward_rel_err_vs_fp64": rel_err_fields(fused, fwd64)},
+                                    "forward_rel_err_vs_fp64": rel_err_fields(fused, fwd64),
+                                    "forward_error_vs_oracle": errors_vs_oracle(fused, want, sample)},
+            "df64_fwd_split_vjp_graph": {"ms": df_ms, "value": qpts / (df_ms * 1e-3),
+                                         "speedup_vs_plain_fp64": plain_ms / df_ms,
+                                         "hbm_gbs": compulsory(8) / (df_ms * 1e-3) / 1e9,
+                                         "grad_rel_err_vs_fp64": float((dfb.grad - grad64).abs().max() / grad64.abs().max()),
+                                         "forward_error_vs_oracle": errors_vs_oracle(dfb.fields[0], want, sample)},
             "families": families,
             "fd_check_fp64": fd}
 
@@ -645,7 +743,8 @@ def extra_high_order(n: int = 16):
 
 def extra_p1_box():
     """The CPU-runtime workload: 8^3 x 6 = 3,072 P1 tetrahedra, interior nodes jittered by
-    +-0.1 h, 14 points (collapsed 7 x 2 x 1), f64; GPU against the oracle on the host cores."""
+    +-0.1 h, 14 points (collapsed 7 x 2 x 1); the FP64 and double-float GPU paths, every value held
+    against the oracle."""
     import torch
 
     import gridcl_gb300 as tg
@@ -655,12 +754,26 @@ def extra_p1_box():
     g = tg.Geometry.from_host(mesh, dtype=torch.float64)
     pts, w = refcell.collapsed_rule("Tetrahedron", (7, 2, 1))
     ps = tg.PointSet("Tetrahedron", pts, w)
-    out = tg.geometric_factors_block(g, 0, ps)
-    ms = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, out=out), reps=20)
     qpts = mesh.blocks[0].num_cells * len(ps)
+    every = np.arange(mesh.blocks[0].num_cells)
+    want = oracle_sample(mesh, g, "Tetrahedron", 1, pts, every)
     res = {"workload": "P1 tets 8^3x6, 14 pts, f64", "qpoints": int(qpts),
-           "gpu_fp64": {"ms": ms, "value": qpts / (ms * 1e-3)}}
+           "error_sample": "every cell and point against the oracle (f64)"}
+    for label, prec in (("gpu_fp64", "native"), ("gpu_df64", "df64")):
+        out = tg.geometric_factors_block(g, 0, ps, precision=prec)
+        ms = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, out=out, precision=prec), reps=20)
+        res[label] = {"ms": ms, "value": qpts / (ms * 1e-3), "error_vs_oracle": errors_vs_oracle(out, want, every)}
     return res
+
+
+def _roofline(alg: int, ms: float, peaks: dict, traffic):
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    achieved = alg / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "algorithmic_bytes_per_launch": int(alg),
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy), of measured" if "hbm_gbs" in peaks
+            else "fallback 6800 GB/s"}
+
 
 def run_ours(args):
     import torch
@@ -675,8 +788,8 @@ def run_ours(args):
     if world > 1:
         dist.init_process_group("nccl")
     mesh_dtype = torch.float32 if args.mode == "f32" else torch.float64
-    precision = "split" if args.mode == "split" else "native"
-    out_es = 8 if args.mode == "f64" else 4
+    precision = {"df64": "df64", "split": "split", "f64": "native", "f32": "native"}[args.mode]
+    out_es = 4 if args.mode in ("split", "f32") else 8
 
     mesh = build_mesh(args.n)
     pts, w = rule()
@@ -710,35 +823,46 @@ def run_ours(args):
         dist.barrier()
     sampler.mark(t_wall0, t_wall1)
     ms_max = max_over_ranks(ms)
+    family = tg.last_kernel_family()
 
-    # The plain FP64 GPU path on the same mesh: its rate, and the split path's error against it.
-    plain = None
-    if args.mode == "split":
-        ref = tg.geometric_factors_block(g, 0, ps, factors)
+    # The errors against the oracle on a seeded sample of 65,536 cells (the oracle's f64 evaluation
+    # of the stored coordinates, as the reference computes it).
+    sample = sample_cells(cells)
+    want = oracle_sample(mesh, g, "Tetrahedron", 2, pts, sample) if mesh_dtype == torch.float64 else None
+    main_err = errors_vs_oracle(out, want, sample) if want is not None else None
 
-        def plain_step():
-            tg.geometric_factors_block(g, 0, ps, factors, out=ref)
+    # The plain FP64 GPU path on the same mesh (the metric's baseline), and the other precisions.
+    others = {}
+    if mesh_dtype == torch.float64:
+        for label, prec in (("plain_fp64_gpu", "native"), ("df64_gpu", "df64"), ("split_gpu", "split")):
+            if prec == precision:
+                continue
+            f = tg.geometric_factors_block(g, 0, ps, factors, precision=prec)
 
-        plain_step()
-        torch.cuda.synchronize()
-        plain_ms = time_steps(plain_step, max(3, min(args.steps, 5)), flush, stream)
-        errs = {}
-        for f in factors:
-            a = out[f].chunks[0].data.double()
-            b = ref[f].chunks[0].data
-            errs[f] = float((a - b).abs().max() / b.abs().max())
-        plain = {"ms_per_step": plain_ms, "value": world * qpts / (plain_ms * 1e-3),
-                 "rel_err_vs_fp64": errs,
-                 "speedup": plain_ms / ms}
-        del ref
+            def other_step(f=f, prec=prec):
+                tg.geometric_factors_block(g, 0, ps, factors, out=f, precision=prec)
+
+            other_step()
+            torch.cuda.synchronize()
+            oms = time_steps(other_step, max(3, min(args.steps, 5)), flush, stream)
+            others[label] = {"ms_per_step": oms, "value": world * qpts / (oms * 1e-3), "family": tg.last_kernel_family(),
+                             "error_vs_oracle": errors_vs_oracle(f, want, sample)}
+            if prec == "split":
+                es_o = 4
+                alg_o = cells * k * 4 + g.nodes.shape[0] * 3 * 8 + qpts * 22 * es_o
+                others[label]["roofline"] = {"achieved": alg_o / (oms * 1e-3) / 1e9, "algorithmic_bytes_per_launch": alg_o}
+            del f
+        torch.cuda.empty_cache()
+    plain_ms = ms if precision == "native" and mesh_dtype == torch.float64 else others.get("plain_fp64_gpu", {}).get("ms_per_step")
     recomputed = int(count.item())
 
     # End to end through the public API, pipelined as a streaming user would run it: every step
     # copies its inputs (nodes and dofmap) from pinned host memory into one of two device input
-    # sets on a copy stream, evaluates them on the compute stream (the evaluation also sums each
-    # cell's det J * w, its cell_measure) and sums those into the measure, and copies the measure
-    # back into pinned host memory; the copy of step i + 1 overlaps the evaluation of step i. The
-    # timed region ends when the last result has reached the host.
+    # sets on a copy stream, evaluates them on the compute stream, takes the measure (the cell sums
+    # of det J * w, then their tree) and copies it back into pinned host memory; the copy of step
+    # i + 1 overlaps the evaluation of step i. The timed region ends when the last result has
+    # reached the host. The fields stay on the device (the reference's QuadField is
+    # device-resident; no field is read back).
     host_nodes = g.nodes.cpu().pin_memory()
     host_dofmap = g.blocks[0].dofmap.cpu().pin_memory()
     h2d = host_nodes.numel() * host_nodes.element_size() + host_dofmap.numel() * 4
@@ -752,17 +876,17 @@ def run_ours(args):
     cell_meas = torch.empty(g.blocks[0].num_cells, dtype=results.dtype, device=g.nodes.device)
 
     def e2e_step(i):
-        k = i % 2
-        gk = geoms[k]
+        kk = i % 2
+        gk = geoms[kk]
         with torch.cuda.stream(copy_stream):
-            copy_stream.wait_event(consumed[k])  # the evaluation two steps back has read set k
+            copy_stream.wait_event(consumed[kk])  # the evaluation two steps back has read set kk
             gk.nodes.copy_(host_nodes, non_blocking=True)
             gk.blocks[0].dofmap.copy_(host_dofmap, non_blocking=True)
-            copied[k].record(copy_stream)
-        comp.wait_event(copied[k])
+            copied[kk].record(copy_stream)
+        comp.wait_event(copied[kk])
         tg.geometric_factors_block(gk, 0, ps, factors, out=out, precision=precision, cell_measure=cell_meas)
         r = tg.measure_block(gk, 0, ps, cell_sums=cell_meas, sync=False)
-        consumed[k].record(comp)
+        consumed[kk].record(comp)
         results[i % e2e_steps].copy_(r[0], non_blocking=True)
 
     for i in range(4):
@@ -788,35 +912,35 @@ def run_ours(args):
             peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
         except (OSError, ValueError):
             pass
-        peak = float(peaks.get("hbm_gbs", 6800.0))
-        achieved = alg / (ms * 1e-3) / 1e9
-        dtype = {"split": "f32", "f64": "f64", "f32": "f32"}[args.mode]
+        dtype = {"df64": "f64", "split": "f32", "f64": "f64", "f32": "f32"}[args.mode]
+        traffic = NCU_TRAFFIC_64[args.mode] * qpts / QPOINTS_64 if args.mode in NCU_TRAFFIC_64 else None
         line = {
             "metric": METRIC, "value": whole_job_rate(qpts, world, ms_max), "unit": "qpoints/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": (plain_ms / ms_max) if plain_ms else None,
+            "vs_baseline_source": "the plain per-block FP64 GPU path on the same mesh, measured in this run "
+                                  "(the metric's baseline; no published number exists for this config)",
+            "dtype": dtype,
             "data": "synthetic (seeded sin-mapped, jittered P2 tetrahedral box)",
-            "config": {"workload": WORKLOAD, "mode": args.mode, "mesh_dtype": str(mesh_dtype),
-                       "cells": int(cells), "nodes_per_cell": int(k),
+            "config": {"workload": WORKLOAD, "mode": args.mode, "precision": precision, "mesh_dtype": str(mesh_dtype),
+                       "kernel_family": family, "cells": int(cells), "nodes_per_cell": int(k),
                        "nodes": int(g.nodes.shape[0]), "points": int(nq), "qpoints": int(qpts),
                        "outputs_per_qpoint": nout, "output_bytes": out_es, "tile": 16,
                        "l2": "256 MiB flush between steps (outside the timed events); outputs exceed L2",
                        "parallelism": f"replicas x{world}"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak,
-                         "traffic": (NCU_TRAFFIC_64[args.mode] * qpts / QPOINTS_64
-                                     if args.mode in NCU_TRAFFIC_64 else None),
-                         "algorithmic_bytes_per_launch": alg,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in peaks else "fallback 6800"},
+            "error_vs_oracle": main_err,
+            "error_sample": f"{len(sample)} seeded cells x {nq} points against the oracle (f64)",
+            "roofline": _roofline(alg, ms, peaks, traffic),
             "e2e": {"value": whole_job_rate(qpts, world, e2e_ms), "unit": "qpoints/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": out_es, "ms_per_step": e2e_ms,
                     "measure": vol, "steps": e2e_steps,
-                    "pipeline": "host copies of step i+1 overlap the evaluation of step i"},
+                    "pipeline": "host copies of step i+1 overlap the evaluation of step i; fields stay on the device"},
             "gpu_launches": args.steps,
             "clocks": sampler.summary(),
         }
-        if plain is not None:
-            line["plain_fp64_gpu"] = plain
+        line.update(others)
+        if args.mode == "split":
             line["recomputed_points"] = recomputed
         if not args.no_extras and world == 1:
             workloads = {}

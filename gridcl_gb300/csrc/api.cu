@@ -1671,6 +1671,8 @@ struct tlg_vjp_batch {
   std::vector<void*> locals;
   std::vector<int64_t> local_cells;
   std::vector<const uint32_t*> offsets, entries;
+  // Tables of a separate forward evaluation per block (tlg_vjp_batch_set_forward), or empty.
+  std::vector<const tlg_tables*> forward;
   int64_t num_nodes = 0;
   int gdim = 0;
   double* grad = nullptr;
@@ -1738,6 +1740,22 @@ tlg_status tlg_vjp_batch_destroy(tlg_vjp_batch* b) {
   return ok();
 }
 
+tlg_status tlg_vjp_batch_set_forward(tlg_vjp_batch* b, const tlg_tables* const* forward) {
+  if (!b) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_batch_set_forward: NULL batch");
+  std::vector<const tlg_tables*> f;
+  if (forward) {
+    for (size_t i = 0; i < b->tables.size(); ++i) {
+      if (!forward[i] || forward[i]->gd != b->gdim)
+        return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_batch_set_forward: NULL tables or another gdim");
+      f.push_back(forward[i]);
+    }
+  }
+  b->forward = f;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  return ok();
+}
+
 tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* b, void* stream) {
   if (!b) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_batch_launch: NULL batch");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1754,8 +1772,19 @@ tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* b, void* stream) {
     for (size_t i = 0; i < nb && e == cudaSuccess && st == TLG_OK; ++i) {
       e = cudaStreamWaitEvent(b->streams[i], b->events[nb], 0);
       if (e != cudaSuccess) break;
-      st = tlg_vjp_block(b->tables[i], &b->blocks[i], &b->outputs[i], &b->cotangents[i], b->locals[i],
-                         b->local_cells[i], b->streams[i]);
+      if (!b->forward.empty()) {
+        // The forward fields from their own tables, then the adjoint alone on the same branch.
+        st = tlg_eval_block(b->forward[i], &b->blocks[i], &b->outputs[i], b->streams[i]);
+        tlg_outputs adj = b->outputs[i];
+        adj.points = adj.jacobian = adj.detj = adj.pinv = adj.normals = adj.facet_normals = nullptr;
+        adj.cell_measure = nullptr;
+        if (st == TLG_OK)
+          st = tlg_vjp_block(b->tables[i], &b->blocks[i], &adj, &b->cotangents[i], b->locals[i], b->local_cells[i],
+                             b->streams[i]);
+      } else {
+        st = tlg_vjp_block(b->tables[i], &b->blocks[i], &b->outputs[i], &b->cotangents[i], b->locals[i],
+                           b->local_cells[i], b->streams[i]);
+      }
       if (st == TLG_OK) e = cudaEventRecord(b->events[i], b->streams[i]);
       if (e == cudaSuccess && st == TLG_OK) e = cudaStreamWaitEvent(b->capture, b->events[i], 0);
     }

@@ -715,16 +715,23 @@ class AdjointBatch:
     (``tlg_vjp_batch_*``): the point set of each block from `rule`, the cotangent fields of block b
     in ``cotangents[b]`` (as for :func:`vjp_block`), the forward fields `forward` written in the
     same pass (``self.fields[b]``), the node cotangents of the whole mesh in ``self.grad``
-    (``[node][GD]`` f64, summed block by block). ``launch()`` runs the graph."""
+    (``[node][GD]`` f64, summed block by block). ``launch()`` runs the graph.
+
+    ``precision="df64"``: the forward fields are f64 and come from the double-float kernels
+    (f64-accurate), each block's adjoint is the split-precision one (f32 cotangents, FP32
+    contributions summed per node in f64), both on the block's branch of the graph."""
 
     def __init__(self, g: Geometry, rule: "QuadRule", cotangents: list, precision: str = "split", forward=()):
         from ._lib import TlgCotangents
 
         if g.dtype != torch.float64:
             raise GridError(1, "the adjoint reads f64 meshes")
+        if precision not in ("native", "split", "df64"):
+            raise GridError(1, f"unknown precision {precision!r}")
         n = len(g.blocks)
-        fdt = torch.float32 if precision == "split" else torch.float64
-        code = SPLIT32 if precision == "split" else g.dtype
+        fdt = torch.float64 if precision == "native" else torch.float32  # cotangents, contributions
+        out_dt = torch.float32 if precision == "split" else torch.float64  # forward fields
+        code = g.dtype if precision == "native" else SPLIT32
         dev = g.nodes.device
         self.g, self.fields, self.locals, self._keep = g, [], [], []
         descs = (TlgBlock * max(n, 1))()
@@ -740,7 +747,9 @@ class AdjointBatch:
             pts = rule.get(blk.element.cell)
             td, k = blk.element.tdim, blk.element.nodes_per_cell
             t = pts.tables(blk.element, gd, code)
-            f = {name: QuadField.uninit(blk.num_cells, len(pts), FACTOR_LEN[name](td, gd), GPU_QUAD_TILE, fdt, dev)
+            if precision == "df64":
+                self._keep.append(pts.tables(blk.element, gd, DF64))
+            f = {name: QuadField.uninit(blk.num_cells, len(pts), FACTOR_LEN[name](td, gd), GPU_QUAD_TILE, out_dt, dev)
                  for name in forward}
             self.fields.append(f)
             loc = torch.empty((max(blk.num_cells, 1), k, 4 if gd == 3 else gd), dtype=fdt, device=dev)
@@ -769,6 +778,12 @@ class AdjointBatch:
         check(lib().tlg_vjp_batch_create(handles, descs, outs, cts, locals_, lcells, offs, ents, g.nodes.shape[0],
                                          gd, self.grad.data_ptr(), n, ctypes.byref(h)))
         self.handle = h
+        if precision == "df64":
+            fwd = (ctypes.c_void_p * max(n, 1))()
+            for b, blk in enumerate(g.blocks):
+                fwd[b] = rule.get(blk.element.cell).tables(blk.element, gd, DF64).handle
+            self._fwd = fwd
+            check(lib().tlg_vjp_batch_set_forward(h, fwd))
 
     def launch(self) -> None:
         check(lib().tlg_vjp_batch_launch(self.handle, current_stream_handle()))

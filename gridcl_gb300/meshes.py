@@ -95,10 +95,11 @@ def _axis_vertices(cell: str):
             "Tetrahedron": [1, 2, 3], "Prism": [1, 2, 3], "Hexahedron": [1, 2, 4]}[cell]
 
 
-def _assemble(cell: str, p: int, verts: np.ndarray, gdim: int, resolution: int):
+def _assemble(cell: str, p: int, verts: np.ndarray, gdim: int, resolution: int, lagrange_points=None):
     """Lagrange-node lattice keys of cells given by vertex keys `verts` [ncells][nv][3] (int64),
-    nodes numbered by first use. Returns (node keys [N][3], dofmap [ncells][K] uint32)."""
-    ref = refcell.lagrange_points(cell, p)  # [K][td] in [0, 1]
+    nodes numbered by first use. Returns (node keys [N][3], dofmap [ncells][K] uint32).
+    `lagrange_points(cell, p)` gives the reference nodes (the library's refcell by default)."""
+    ref = (lagrange_points or refcell.lagrange_points)(cell, p)  # [K][td] in [0, 1]
     r = np.rint(ref * p).astype(np.int64)
     assert np.allclose(r, ref * p), "equispaced nodes lie on the lattice"
     axes = verts[:, _axis_vertices(cell), :] - verts[:, :1, :]  # [ncells][td][3]
@@ -138,7 +139,7 @@ def _orient(cell: str, verts: np.ndarray) -> np.ndarray:
     return verts
 
 
-def cube_box(cell: str, n: int, p: int) -> HostMesh:
+def cube_box(cell: str, n: int, p: int, lagrange_points=None) -> HostMesh:
     """The unit cube in n^3 subcells of `cell` cells of degree p (boxes.rs:129-167)."""
     if n < 1 or p < 1:
         raise ValueError("a box needs n >= 1 and p >= 1")
@@ -162,7 +163,7 @@ def cube_box(cell: str, n: int, p: int) -> HostMesh:
     else:
         raise ValueError(f"cube_box has no {cell} cells in this build")
     verts = _orient(cell, verts.copy())
-    keys, dofmap = _assemble(cell, p, verts, 3, res)
+    keys, dofmap = _assemble(cell, p, verts, 3, res, lagrange_points)
     return HostMesh(3, keys.astype(np.float64) / res, [HostBlock(cell, p, dofmap)])
 
 
@@ -207,10 +208,11 @@ def jitter_interior(x: np.ndarray, boundary_of: np.ndarray, amplitude: float, se
     return out
 
 
-def curved_box(cell: str, n: int, p: int, jitter: float, seed: int = 2026, amplitude: float = 0.05) -> HostMesh:
+def curved_box(cell: str, n: int, p: int, jitter: float, seed: int = 2026, amplitude: float = 0.05,
+               lagrange_points=None) -> HostMesh:
     """The benchmark boxes: cube_box mapped by `sin_map`, then interior nodes jittered by
     `jitter` * h (h = 1 / n)."""
-    m = cube_box(cell, n, p)
+    m = cube_box(cell, n, p, lagrange_points)
     x = sin_map(m.nodes, amplitude) if amplitude else m.nodes
     m.nodes = jitter_interior(x, m.nodes, jitter / n, seed) if jitter else x
     return m

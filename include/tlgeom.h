@@ -274,6 +274,12 @@ tlg_status tlg_vjp_batch_create(const tlg_tables* const* tables, const tlg_block
                                 const uint32_t* const* offsets, const uint32_t* const* entries,
                                 int64_t num_nodes, int gdim, double* grad, int num_blocks,
                                 tlg_vjp_batch** out);
+/* Forward fields from other tables: with forward[i] set (num_blocks tables, or NULL to undo), block
+ * i's branch runs tlg_eval_block(forward[i], ...) for the batch's forward outputs, then the adjoint
+ * from the batch's tables with no forward outputs; e.g. TLG_DF64 tables (f64-accurate fields) with
+ * TLG_SPLIT32 adjoint tables (FP32 contributions summed per node in f64). Recaptures on the next
+ * launch. No counterpart in the reference, which has no adjoint. */
+tlg_status tlg_vjp_batch_set_forward(tlg_vjp_batch* batch, const tlg_tables* const* forward);
 tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* batch, void* stream);
 tlg_status tlg_vjp_batch_destroy(tlg_vjp_batch* batch);
 

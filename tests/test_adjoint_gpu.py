@@ -405,6 +405,39 @@ def test_adjoint_batch_equals_the_blocks(cuda, precision):
     assert torch.equal(batch.grad, want)
 
 
+def test_adjoint_batch_with_double_float_forward(cuda):
+    """precision="df64": each block's forward fields from the double-float kernels (bit for bit
+    the fields of tlg_eval_block with df64 tables, and within 1e-12 of the oracle's f64 values),
+    its adjoint the split-precision one (bit for bit the node cotangents of the split batch)."""
+    mesh = meshes.hybrid_box(300, 120, 60)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    rule = tg.QuadRule([tg.PointSet("Hexahedron", *tg.refcell.gauss_rule("Hexahedron", 4)),
+                        tg.PointSet("Prism", *tg.refcell.collapsed_rule("Prism", (3, 1, 7))),
+                        tg.PointSet("Tetrahedron", *tg.refcell.collapsed_rule("Tetrahedron", (4, 3, 2)))])
+    rng = np.random.default_rng(37)
+    cts = []
+    for blk in g.blocks:
+        ct, _ = cotangent_fields(rng, blk.num_cells, len(rule.get(blk.element.cell)), torch.float32)
+        cts.append(ct)
+    names = ("points", "jacobian", "detj", "pinv")
+    batch = tg.AdjointBatch(g, rule, cts, precision="df64", forward=names)
+    batch.launch()
+    split = tg.AdjointBatch(g, rule, cts, precision="split")
+    split.launch()
+    torch.cuda.synchronize()
+    assert torch.equal(batch.grad, split.grad)
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
+    for b, blk in enumerate(g.blocks):
+        ps = rule.get(blk.element.cell)
+        want = tg.geometric_factors_block(g, b, ps, names, precision="df64")
+        oracle = orc.eval_block(blk.element.cell, blk.element.degree, absx, mesh.blocks[b].cells, ps.points)
+        for k, ok in zip(names, ("x", "j", "detj", "k")):
+            got = batch.fields[b][k]
+            assert got.chunks[0].data.dtype == torch.float64
+            assert torch.equal(got.chunks[0].data, want[k].chunks[0].data), (b, k)
+            assert orc.rel_err(got.to_host_cell_major(), oracle[ok]) < 1e-12, (b, k)
+
+
 def test_csr_with_long_runs_of_unused_nodes(cuda):
     """Offsets across long runs of nodes without entries (a block's nodes in the middle of a large
     node array, as in a mesh of several blocks) against the host's stable sort."""
