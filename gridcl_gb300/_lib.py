@@ -94,6 +94,7 @@ SIGNATURES = [
     ("tlg_tables_num_points", _L, [_P]),
     ("tlg_tables_device_status", _I, [_P, _P]),
     ("tlg_tables_nodes_per_cell", _L, [_P]),
+    ("tlg_tables_set_wait", _I, [_P, _L, _I]),
     ("tlg_eval_block", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs), _P]),
     ("tlg_batch_create", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs), _I, _P]),
     ("tlg_batch_destroy", _I, [_P]),

@@ -1277,6 +1277,16 @@ tlg_status tlg_tables_destroy(tlg_tables* t) {
   return ok();
 }
 
+tlg_status tlg_tables_set_wait(tlg_tables* t, int64_t polls, int issue_copy) {
+  if (!t || polls < 0 || polls > INT32_MAX || (issue_copy != 0 && issue_copy != 1))
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_set_wait: NULL tables, polls outside 0 .. 2^31 - 1 or "
+                                          "issue_copy not 0 or 1");
+  const int words[2] = {(int)polls, issue_copy ? 0 : 1};
+  cudaError_t e = cudaMemcpy(t->err + 1, words, sizeof(words), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_tables_set_wait");
+  return ok();
+}
+
 int64_t tlg_tables_num_points(const tlg_tables* t) { return t ? t->q : -1; }
 
 int64_t tlg_tables_nodes_per_cell(const tlg_tables* t) { return t ? t->k : -1; }

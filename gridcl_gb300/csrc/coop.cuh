@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kEvalThreads) coop_kernel(const __grid_constan
   extern __shared__ __align__(16) unsigned char smem[];
   const unsigned char* tabs = a.tab;
   if (!a.tab_global) {
-    stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+    if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
     tabs = smem;
   }
   const F* phi = reinterpret_cast<const F*>(tabs);

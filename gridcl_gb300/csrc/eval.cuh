@@ -97,7 +97,7 @@ struct PairArgs {
 // ----------------------------------------------------------------------------------------
 // Table staging: one elected thread issues a bulk copy into shared memory; all threads wait on
 // the mbarrier with a bounded number of polls. On expiry the CTA records an error and does a
-// second bounded wait for its copy before it lets the caller continue.
+// second bounded wait for its copy; a CTA whose tables never arrived returns without computing.
 
 __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   uint32_t done;
@@ -111,16 +111,23 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
   return done != 0;
 }
 
+// err[0] is the error word; err[1] overrides the number of polls of each bounded wait (0: the
+// default 2^22) and err[2] = 1 leaves the copy unissued, so that the wait runs out with nothing in
+// flight (the tables' test hook, tlg_tables_set_wait). Returns whether the tables arrived, the
+// same for every thread of the CTA; a CTA whose tables did not arrive computes nothing.
 __device__ __forceinline__ bool stage_table(const unsigned char* src, unsigned char* dst,
                                             uint32_t bytes, uint64_t* bar, int* err) {
   const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(bar);
   const uint32_t dst_s = (uint32_t)__cvta_generic_to_shared(dst);
+  const int limit = err ? err[1] : 0;
+  const bool issue = !err || err[2] != 1;
+  const int polls = limit > 0 ? limit : (1 << 22);
   if (threadIdx.x == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && issue) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_s), "r"(bytes)
                  : "memory");
     asm volatile(
@@ -129,14 +136,16 @@ __device__ __forceinline__ bool stage_table(const unsigned char* src, unsigned c
         "l"(src), "r"(bytes), "r"(bar_s)
         : "memory");
   }
-  // Bounded poll: try_wait itself suspends for a hardware-defined interval per call.
-  const int kPolls = 1 << 22;
-  for (int i = 0; i < kPolls; ++i)
-    if (mbar_try_wait(bar_s, 0)) return true;
-  if (err) atomicExch(err, 1);
-  for (int i = 0; i < kPolls; ++i)
-    if (mbar_try_wait(bar_s, 0)) break;
-  return false;
+  // Bounded poll: try_wait itself suspends for a hardware-defined interval per call. On expiry
+  // the error word is set and a second bounded wait gives the copy time to land (the CTA must
+  // not exit with its copy in flight).
+  bool done = false;
+  for (int i = 0; i < polls && !done; ++i) done = mbar_try_wait(bar_s, 0);
+  if (!done) {
+    if (err) atomicExch(err, 1);
+    for (int i = 0; i < polls && !done; ++i) done = mbar_try_wait(bar_s, 0);
+  }
+  return __syncthreads_and(done) != 0;
 }
 
 // ----------------------------------------------------------------------------------------
@@ -669,7 +678,7 @@ template <bool SPLIT, int TD, int GD, int K, bool MEAS = false>
 __global__ void __launch_bounds__(kEvalThreads) eval_pair_kernel(const __grid_constant__ PairArgs a) {
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   pair_cells<SPLIT, TD, GD, K, MEAS>(a, smem, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, a.padded,
                                (int64_t)gridDim.x * blockDim.x);
 }
@@ -785,7 +794,7 @@ template <typename F, int TD, int GD, int K, int TILE>
 __global__ void __launch_bounds__(kEvalThreads) eval_direct_kernel(const __grid_constant__ EvalArgs<F> a) {
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   direct_cells<F, TD, GD, K, TILE>(a, smem, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, a.padded,
                                    (int64_t)gridDim.x * blockDim.x);
 }
@@ -890,7 +899,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_loops_kernel(const __grid_c
   } else {
     __shared__ uint64_t bar;
     extern __shared__ __align__(16) unsigned char smem[];
-    stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+    if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
     loops_cells<F, TD, GD>(a, smem);
   }
 }
@@ -1043,7 +1052,7 @@ __global__ void __launch_bounds__(kEvalThreads) split_loops_kernel(const __grid_
   } else {
     __shared__ uint64_t bar;
     extern __shared__ __align__(16) unsigned char smem[];
-    stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+    if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
     split_loops_cells<TD, GD>(a, smem);
   }
 }

@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kEvalThreads) eval_df_kernel(const __grid_cons
   using M = Factors<D, TD, GD>;
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   const float4* rows = reinterpret_cast<const float4*>(smem + a.off_rows);
   const double* refn = reinterpret_cast<const double*>(smem + a.off_refn);
   float2* ys = reinterpret_cast<float2*>(smem + (a.tab_bytes + 15) / 16 * 16) + threadIdx.x;

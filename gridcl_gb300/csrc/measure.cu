@@ -181,7 +181,7 @@ tlg_status measure_into(const void* detj, int dtype, int64_t num_cells, int64_t 
                         const void* weights, void* scratch, void* result, cudaStream_t s);
 
 // Device address of g_measure_scratch for each device, found once per device (with that device
-// current) by the first call made on it.
+// current) by the first call made on it, and again after a device reset.
 std::mutex g_scratch_mutex;
 void* g_scratch_ptr[64] = {};
 
@@ -191,6 +191,15 @@ tlg_status static_scratch(void** ptr) {
   if (e != cudaSuccess) return tlg::cuda_fail(e, "tlg_measure_static: cudaGetDevice");
   if (dev < 0 || dev >= 64) return tlg::fail(TLG_ERR_INVALID_ARGUMENT, "tlg_measure_static: device ordinal above 63");
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (g_scratch_ptr[dev]) {
+    // The address found before belongs to the context of that time: after a device reset the
+    // library's module is loaded anew and the array lives elsewhere, so look it up again when the
+    // cached address is no longer this device's memory.
+    cudaPointerAttributes at;
+    const cudaError_t pe = cudaPointerGetAttributes(&at, g_scratch_ptr[dev]);
+    if (pe != cudaSuccess) cudaGetLastError();  // (not sticky: clear it)
+    if (pe != cudaSuccess || at.type != cudaMemoryTypeDevice || at.device != dev) g_scratch_ptr[dev] = nullptr;
+  }
   if (!g_scratch_ptr[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, tlg::g_measure_scratch);

@@ -142,15 +142,19 @@ FacetGraph facet_graph(int cell, const uint32_t* cells, int64_t n, int k) {
   FacetGraph g;
   g.start.assign((size_t)n + 1, 0);
   g.len.assign((size_t)n, 0);
+  // A cell's neighbours across a facet are the other cells of the facet's run (a degenerate cell
+  // with two facets on the same vertices does not neighbour itself, as in order.rs:147).
   for (const auto& r : runs)
-    for (size_t a = r.first; a < r.second; ++a) g.start[(size_t)entries[a].cell + 1] += (int64_t)(r.second - r.first - 1);
+    for (size_t a = r.first; a < r.second; ++a)
+      for (size_t b = r.first; b < r.second; ++b)
+        if (entries[b].cell != entries[a].cell) ++g.start[(size_t)entries[a].cell + 1];
   for (int64_t c = 0; c < n; ++c) g.start[(size_t)c + 1] += g.start[(size_t)c];
   g.nbr.resize((size_t)g.start[(size_t)n]);
   std::vector<int64_t> fill(g.start.begin(), g.start.end() - 1);
   for (const auto& r : runs)
     for (size_t a = r.first; a < r.second; ++a)
       for (size_t b = r.first; b < r.second; ++b)
-        if (a != b) g.nbr[(size_t)fill[(size_t)entries[a].cell]++] = entries[b].cell;
+        if (entries[b].cell != entries[a].cell) g.nbr[(size_t)fill[(size_t)entries[a].cell]++] = entries[b].cell;
   for (int64_t c = 0; c < n; ++c) {
     auto first = g.nbr.begin() + g.start[(size_t)c], last = g.nbr.begin() + g.start[(size_t)c + 1];
     std::sort(first, last);

@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_kernel(const __grid_cons
   constexpr int T = kEvalThreads;
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   F* xs = reinterpret_cast<F*>(smem + (a.tab_bytes + 15) / 16 * 16) + threadIdx.x;
   const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
   const SfBlock* blocks = reinterpret_cast<const SfBlock*>(smem);
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_prism_kernel(const __gri
   constexpr int T = kEvalThreads;
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   F* xs = reinterpret_cast<F*>(smem + (a.tab_bytes + 15) / 16 * 16) + threadIdx.x;
   const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
   const SfBlock* blocks = reinterpret_cast<const SfBlock*>(smem);
@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
   constexpr int T = kEvalThreads;  // compile-time slot strides: shared-memory offsets are immediates
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
   uint32_t* invperm = reinterpret_cast<uint32_t*>(smem + (a.tab_bytes + 15) / 16 * 16);
   for (int i = threadIdx.x; i < K; i += T) invperm[perm[i]] = i;

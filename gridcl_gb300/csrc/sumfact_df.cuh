@@ -139,7 +139,7 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_df_kernel(const __grid_c
   constexpr int T = kEvalThreads;
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   float2* ys = reinterpret_cast<float2*>(smem + (a.tab_bytes + 15) / 16 * 16) + threadIdx.x;
   const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
   const SfBlock* blocks = reinterpret_cast<const SfBlock*>(smem);
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kEvalThreads) sumfact_prism_df_kernel(const __
   constexpr int T = kEvalThreads;
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   float2* ys = reinterpret_cast<float2*>(smem + (a.tab_bytes + 15) / 16 * 16) + threadIdx.x;
   const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
   const SfBlock* blocks = reinterpret_cast<const SfBlock*>(smem);
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(kEvalThreads, MINB) sumfact_df3_kernel(const _
   constexpr int T = kEvalThreads;
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   float2* ys = reinterpret_cast<float2*>(smem + (a.tab_bytes + 15) / 16 * 16) + threadIdx.x;
   const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
   const SfBlock* blocks = reinterpret_cast<const SfBlock*>(smem);

@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(kEvalThreads, vjp_min_blocks(SPLIT, D, K))
   constexpr int R = vjp_row(D);
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
-  stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   const V* tab = reinterpret_cast<const V*>(smem);
   S* stage = reinterpret_cast<S*>(smem + (a.tab_bytes + 15) / 16 * 16) +
              (threadIdx.x / 32) * (kVjpCellsPerWarp * K * R);

@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_surface_kernel(const __grid_
   const unsigned char* tabs = a.tab;
   size_t slot_base = 0;
   if (!a.tab_global) {
-    stage_table(a.tab, smem, a.tab_bytes, &bar, a.err);
+    if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
     tabs = smem;
     slot_base = (a.tab_bytes + 15) / 16 * 16;
   }

@@ -121,6 +121,12 @@ int64_t tlg_tables_num_points(const tlg_tables* tables);
  * these tables gave up a bounded wait for its table copy; TLG_OK otherwise. */
 tlg_status tlg_tables_device_status(const tlg_tables* tables, void* stream);
 int64_t tlg_tables_nodes_per_cell(const tlg_tables* tables);
+/* The bounded wait for the table copy, for tests of the timeout path: each of the wait's two
+ * rounds polls `polls` times (0: the default 2^22); issue_copy = 0 leaves the copy unissued, so
+ * that the wait runs out with nothing in flight: the kernels that read these tables then record
+ * TLG_ERR_DEVICE_TIMEOUT (tlg_tables_device_status) and compute nothing, the context stays usable.
+ * (0, 1) restores the default. No counterpart in the reference. */
+tlg_status tlg_tables_set_wait(tlg_tables* tables, int64_t polls, int issue_copy);
 
 /* ---------------------------------------------------------------------------------------
  * One cell block of a Geometry (tetraloma-geometry/src/geometry.rs:187-288,
@@ -420,7 +426,9 @@ tlg_status tlg_sum(const void* x, int dtype, int64_t n, void* workspace, int64_t
  * loads the library holds until the process exits; chunks of more than
  * tlg_measure_static_max_cells() = 16,777,216 cells are rejected with
  * TLG_ERR_ALLOCATION_TOO_LARGE. The first call on each device looks up the array's device
- * address (with that device current); make that first call before any stream capture. Every call
+ * address (with that device current); make that first call before any stream capture. Later calls
+ * check that the address is still the device's (one runtime query) and look it up again after a
+ * device reset. Every call
  * shares the array: calls whose kernels may overlap on the GPU (other streams, other threads)
  * race and must be serialised by the caller. No value of the array needs to start at zero:
  * each is written before it is read. */

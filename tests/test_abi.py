@@ -35,6 +35,8 @@ def test_abi_version():
 def test_argument_errors_before_device_work():
     L = lib()
     assert L.tlg_eval_block(None, None, None, None) == 1
+    assert L.tlg_tables_set_wait(None, 16, 0) == 1
+    assert L.tlg_vjp_batch_set_forward(None, None) == 1
     b = TlgBlock()
     o = TlgOutputs()
     assert L.tlg_evector(ctypes.byref(b), 4, 0, 0, 16, None, None) == 1

@@ -479,3 +479,34 @@ def test_runtime_k_adjoint_for_elements_without_node_row_kernels(cuda, cell, n, 
     for k in names:  # the forward kernels sum in another order (cooperative or paired kernels)
         assert orc.rel_err(fused[k].to_host_cell_major(), plain[k].to_host_cell_major()) < (
             1e-13 if precision == "native" else 1e-5), k
+
+
+def test_split_node_sums_are_within_their_stated_bound(cuda):
+    """The node sums of f32 contribution rows (tlg_vjp_gather with local_dtype 4) are FP32 TwoSum
+    pairs, each addition's rounding error kept in the low part, rounded once to f64. Against the
+    f64 sums of the same rows the error stays within n^2 2^-48 sum |rows| per node and component (n
+    its entries: the low part's own roundings), bounded here by 2^-40 sum |rows| — far below the
+    2^-24 of FP32 sums and of the f32 contributions themselves."""
+    rng = np.random.default_rng(41)
+    ncells, k, nn = 20_000, 10, 9_000
+    cells = rng.integers(0, nn, size=(ncells, k)).astype(np.uint32)
+    mesh = meshes.HostMesh(3, rng.random((nn, 3)), [meshes.HostBlock("Tetrahedron", 2, cells)])
+    g = tg.Geometry.from_host(mesh)
+    inc = tg.node_incidence(g, 0)
+    # Rows of widely different magnitudes and signs (cancellation within a node's sum).
+    rows = (rng.standard_normal((ncells, k, 4)) * 10.0 ** rng.integers(-6, 3, size=(ncells, k, 1))).astype(np.float32)
+    rows[..., 3] = 0.0
+    local = torch.from_numpy(rows).cuda()
+    grad = torch.empty((nn, 3), dtype=torch.float64, device="cuda")
+    st = tg._lib.lib().tlg_vjp_gather(inc.offsets.data_ptr(), inc.entries.data_ptr(), nn, 3, local.data_ptr(), 4,
+                                      grad.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    exact = np.zeros((nn, 3))
+    mag = np.zeros((nn, 3))
+    r64 = rows[..., :3].astype(np.float64)
+    np.add.at(exact, cells.astype(np.int64).ravel(), r64.reshape(-1, 3))
+    np.add.at(mag, cells.astype(np.int64).ravel(), np.abs(r64).reshape(-1, 3))
+    err = np.abs(grad.cpu().numpy() - exact)
+    count = np.bincount(cells.astype(np.int64).ravel(), minlength=nn).astype(np.float64)[:, None]
+    assert np.all(err <= count ** 2 * 2.0 ** -48 * mag + 1e-300)
+    assert np.all(err <= 2.0 ** -40 * mag + 1e-300)
