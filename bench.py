@@ -50,8 +50,9 @@ METRIC = "Jacobian qpoints/s (fwd, fwd+adjoint) vs plain FP64 GPU path at stated
 # kernel on the 64^3 workload, measured on a GB300 by one-pass ncu captures of
 # `bench.py --no-extras --no-cpu-baseline --steps 3 --warmup 3 [--mode f64]` (-s 3 -c 1):
 # split eval_pair_kernel<1,3,3,10> 191.07 MB + 3.26 GB; f64 eval_direct_kernel<double,3,3,10,16>
-# 166.22 MB + 6.58 GB. Reported as roofline.traffic, scaled by quadrature points for other n.
-NCU_TRAFFIC_64 = {"split": 191.07e6 + 3.26e9, "f64": 166.22e6 + 6.58e9}
+# 166.22 MB + 6.58 GB; double-float eval_df_kernel<3,3,10> 171.69 MB + 6.581 GB. Reported as
+# roofline.traffic, scaled by quadrature points for other n.
+NCU_TRAFFIC_64 = {"split": 191.07e6 + 3.26e9, "f64": 166.22e6 + 6.58e9, "df64": 171.69e6 + 6.581e9}
 QPOINTS_64 = 64 ** 3 * 6 * 24
 
 
