@@ -13,6 +13,7 @@ _VERTS = {
     "Tetrahedron": [[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]],
     "Hexahedron": [[v & 1, (v >> 1) & 1, (v >> 2) & 1] for v in range(8)],
     "Prism": [[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [0, 1, 1]],
+    "Pyramid": [[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0], [0, 0, 1]],
 }
 # Facets (sub-entities of dimension tdim - 1) by sorted vertex lists, lexicographic.
 _FACETS = {
@@ -22,6 +23,7 @@ _FACETS = {
     "Tetrahedron": [[0, 1, 2], [0, 1, 3], [0, 2, 3], [1, 2, 3]],
     "Hexahedron": [[0, 1, 2, 3], [0, 1, 4, 5], [0, 2, 4, 6], [1, 3, 5, 7], [2, 3, 6, 7], [4, 5, 6, 7]],
     "Prism": [[0, 1, 2], [0, 1, 3, 4], [0, 2, 3, 5], [1, 2, 4, 5], [3, 4, 5]],
+    "Pyramid": [[0, 1, 2, 3], [0, 1, 4], [0, 2, 4], [1, 3, 4], [2, 3, 4]],
 }
 
 

@@ -983,8 +983,6 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
     *out = nullptr;
     if (!tlg::valid_cell(cell) || cell == tlg::kPoint)
       return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: no cell type " + std::to_string(cell));
-    if (cell == tlg::kPyramid)
-      return fail(TLG_ERR_UNSUPPORTED, "tlg_tables_create: pyramids are not supported by this build");
     const int td = tlg::tdim(cell);
     if (gdim < td || gdim > 3)
       return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_tables_create: gdim " + std::to_string(gdim) +
@@ -1029,7 +1027,7 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       t->off_dphi64 = (uint32_t)total;
       total = align16(total + std::max<size_t>(n_dphi, 1) * 8);
     }
-    if (df && k <= 27 && npoints > 0) {  // the double-float rows of the paired f64 kernels
+    if (df && k <= 30 && npoints > 0) {  // the double-float rows of the paired f64 kernels
       t->off_dfrows = (uint32_t)total;
       t->dfrows_bytes = (uint32_t)((size_t)qp * k * (1 + td) * 16);
       total = align16(total + t->dfrows_bytes);

@@ -17,6 +17,10 @@ cudaError_t launch_eval_df(int td, int gd, int k, const DfArgs& a, size_t smem, 
   TLG_DFK(3, 3, 27)
   TLG_DFK(3, 3, 6)
   TLG_DFK(3, 3, 18)
+  // Pyramids P1-P3.
+  TLG_DFK(3, 3, 5)
+  TLG_DFK(3, 3, 14)
+  TLG_DFK(3, 3, 30)
   // Triangles P1-P4 and quadrilaterals Q1-Q2, planar and embedded in 3D.
   TLG_DFK(2, 2, 3)
   TLG_DFK(2, 2, 6)

@@ -23,6 +23,10 @@ cudaError_t TLG_LAUNCH(int td, int gd, int k, const EvalArgs<TLG_F>& a, size_t s
   TLG_DIRECT(3, 3, 27)
   TLG_DIRECT(3, 3, 6)
   TLG_DIRECT(3, 3, 18)
+  // Pyramids P1-P3.
+  TLG_DIRECT(3, 3, 5)
+  TLG_DIRECT(3, 3, 14)
+  TLG_DIRECT(3, 3, 30)
   // Triangles P1-P4 and quadrilaterals Q1-Q2, planar and embedded in 3D.
   TLG_DIRECT(2, 2, 3)
   TLG_DIRECT(2, 2, 6)

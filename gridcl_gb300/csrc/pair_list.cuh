@@ -19,6 +19,10 @@ static cudaError_t launch_pair(int td, int gd, int k, const PairArgs& a, size_t 
   TLG_PAIR(3, 3, 27)
   TLG_PAIR(3, 3, 6)
   TLG_PAIR(3, 3, 18)
+  // Pyramids P1-P3.
+  TLG_PAIR(3, 3, 5)
+  TLG_PAIR(3, 3, 14)
+  TLG_PAIR(3, 3, 30)
   // Triangles P1-P4 and quadrilaterals Q1-Q2, planar and embedded in 3D.
   TLG_PAIR(2, 2, 3)
   TLG_PAIR(2, 2, 6)

@@ -15,7 +15,10 @@
 // nodes; on triangles and tetrahedra (equispaced nodes) the barycentric product
 //   phi_alpha = prod_i prod_{j < alpha_i} (p lambda_i - j) / (j + 1),   |alpha| = p,
 // whose value is 1 at its node and 0 at the others; prisms multiply the triangle's by the
-// line's. The host stores per node its 1D indices or barycentric multi-index.
+// line's. The host stores per node its 1D indices or barycentric multi-index. Pyramids (a
+// rational space, no product form) go through the expansion, as the reference does: the host's
+// orthogonal rationomials evaluated at xi by their recurrences, times the host's coefficient
+// matrix (the inverse of their Vandermonde matrix at the nodes).
 //
 // One cell per thread: the cell's node coordinates (relative to the origin) go to the thread's
 // interleaved slots in shared memory, then each point runs its iterations. Tile layout of the
@@ -45,10 +48,13 @@ namespace tlg {
 
 constexpr int kBasisMaxN = 16;    // 1D nodes (degree + 1)
 constexpr int kBasisMaxK = 1024;  // nodes per cell
+constexpr int kPyramidMaxP = 4;   // pyramid degrees of the pull-back
+constexpr int kPyramidMaxK = 55;  // (p + 1)(p + 2)(2p + 3) / 6 at p = 4
 
 // Device copy of the basis description.
-struct BasisData {
+struct alignas(16) BasisData {
   int cell, p, k, n;        // cell type, degree, nodes per cell, 1D nodes (p + 1)
+  const double* coef;       // pyramids: C [m][k] (m-major) after this header; else null
   double s[kBasisMaxN];     // sorted 1D nodes (tensor cells, the prism's line)
   uint8_t idx[kBasisMaxK][4];  // per node: 1D indices (tensor) or barycentric multi-index
                                // (simplex: lambda_0 .. lambda_TD; prism: alpha_0..2, line index)
@@ -106,10 +112,122 @@ __device__ void simplex_factors(int p, F lam, F* f, F* df) {
   }
 }
 
+// The pyramid's orthogonal rationomials at xi, in the host's order (i outer, then j, then k;
+// max(i, j) + k <= p): e[0][m] the values, e[1 + d][m] the derivatives. With s = 1 - z,
+//   Q_i(2x - s, s) Q_j(2y - s, s) / s^min(i,j) * P_k^(2 max(i,j) + 2, 0)(2z - 1),
+// Q_i the homogeneous Legendre recurrence Q_n = ((2n - 1) f Q_{n-1} - (n - 1) s^2 Q_{n-2}) / n
+// and P_k the Jacobi recurrence. At s = 0 the rational ones (min(i, j) >= 1) are 0 with a zero
+// gradient, their limit along the axis.
+template <typename F>
+__device__ void pyramid_set(int p, const F* xi, F (*e)[kPyramidMaxK]) {
+  const F s = F(1) - xi[2];
+  F q[2][kPyramidMaxP + 1], qd[2][kPyramidMaxP + 1], qz[2][kPyramidMaxP + 1];
+  for (int v = 0; v < 2; ++v) {
+    const F f = F(2) * xi[v] - s;  // d/dx_v = 2, d/dz = 1
+    q[v][0] = F(1);
+    qd[v][0] = qz[v][0] = F(0);
+    if (p >= 1) {
+      q[v][1] = f;
+      qd[v][1] = F(2);
+      qz[v][1] = F(1);
+    }
+    for (int n = 2; n <= p; ++n) {
+      const F a = F(2 * n - 1) / F(n), c = F(n - 1) / F(n);
+      q[v][n] = a * f * q[v][n - 1] - c * s * s * q[v][n - 2];
+      qd[v][n] = a * (F(2) * q[v][n - 1] + f * qd[v][n - 1]) - c * s * s * qd[v][n - 2];
+      qz[v][n] = a * (q[v][n - 1] + f * qz[v][n - 1]) - c * (s * s * qz[v][n - 2] - F(2) * s * q[v][n - 2]);
+    }
+  }
+  const F t = F(2) * xi[2] - F(1);
+  int m = 0;
+  for (int i = 0; i <= p; ++i)
+    for (int j = 0; j <= p; ++j) {
+      const int mx = i > j ? i : j, mn = i < j ? i : j;
+      F f = F(0), fx = F(0), fy = F(0), fz = F(0);
+      if (mn == 0 || s != F(0)) {
+        F sn = F(1);
+        for (int r = 0; r < mn; ++r) sn *= s;
+        const F r = F(1) / sn;
+        const F rz = mn ? F(mn) * r / s : F(0);  // d(s^-mn)/dz
+        f = q[0][i] * q[1][j] * r;
+        fx = qd[0][i] * q[1][j] * r;
+        fy = q[0][i] * qd[1][j] * r;
+        fz = (qz[0][i] * q[1][j] + q[0][i] * qz[1][j]) * r + q[0][i] * q[1][j] * rz;
+      }
+      const F al = F(2 * mx + 2);
+      F j2 = F(0), dj2 = F(0), j1 = F(1), dj1 = F(0);  // P_{k-2}, P_{k-1}
+      for (int k = 0; k + mx <= p; ++k) {
+        F jk, djk;
+        if (k == 0) {
+          jk = F(1);
+          djk = F(0);
+        } else if (k == 1) {
+          jk = F(0.5) * ((al + F(2)) * t + al);
+          djk = al + F(2);
+        } else {
+          const F kk = F(k);
+          const F D = F(2) * kk * (kk + al) * (F(2) * kk + al - F(2));
+          const F A = (F(2) * kk + al - F(1)) * (F(2) * kk + al) * (F(2) * kk + al - F(2)) / D;
+          const F B = (F(2) * kk + al - F(1)) * al * al / D;
+          const F C = F(2) * (kk + al - F(1)) * (kk - F(1)) * (F(2) * kk + al) / D;
+          jk = (A * t + B) * j1 - C * j2;
+          djk = F(2) * A * j1 + (A * t + B) * dj1 - C * dj2;
+        }
+        if (k >= 1) {
+          j2 = j1;
+          dj2 = dj1;
+        }
+        j1 = jk;
+        dj1 = djk;
+        e[0][m] = f * jk;
+        e[1][m] = fx * jk;
+        e[2][m] = fy * jk;
+        e[3][m] = fz * jk + f * djk;
+        ++m;
+      }
+    }
+}
+
+// X and J of a pyramid at xi through the expansion coefficients.
+template <typename F, int GD, bool WANT_J>
+__device__ void map_at_pyramid(const BasisData& b, const F* xs, int T, const F* xi, F* X, F* J) {
+  F e[4][kPyramidMaxK];
+  pyramid_set<F>(b.p, xi, e);
+#pragma unroll
+  for (int g = 0; g < GD; ++g) X[g] = F(0);
+  if constexpr (WANT_J)
+#pragma unroll
+    for (int i = 0; i < 3 * GD; ++i) J[i] = F(0);
+  for (int k = 0; k < b.k; ++k) {
+    F phi = F(0), grad[3] = {F(0), F(0), F(0)};
+    for (int m = 0; m < b.k; ++m) {
+      const F c = F(__ldg(b.coef + (size_t)m * b.k + k));
+      phi = fma(e[0][m], c, phi);
+      if constexpr (WANT_J)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) grad[d] = fma(e[1 + d][m], c, grad[d]);
+    }
+#pragma unroll
+    for (int g = 0; g < GD; ++g) {
+      const F xk = xs[(k * GD + g) * T];
+      X[g] = fma(xk, phi, X[g]);
+      if constexpr (WANT_J)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) J[d * GD + g] = fma(xk, grad[d], J[d * GD + g]);
+    }
+  }
+}
+
 // X (GD) and, with WANT_J, J (J(g, d) at d * GD + g) at xi from the node coordinates in the
 // thread's slots.
 template <typename F, int TD, int GD, bool WANT_J = true>
 __device__ void map_at(const BasisData& b, const F* xs, int T, const F* xi, F* X, F* J) {
+  if constexpr (TD == 3) {
+    if (b.cell == kPyramid) {
+      map_at_pyramid<F, GD, WANT_J>(b, xs, T, xi, X, J);
+      return;
+    }
+  }
   constexpr int MAXN = kBasisMaxN;
   F v[3][MAXN], dv[3][MAXN];
   const int cell = b.cell;
@@ -238,6 +356,9 @@ __device__ __forceinline__ void centroid_f32(int cell, float* start) {
   else if (cell == kPrism) {
     start[0] = start[1] = third;
     start[2] = 0.5f;
+  } else if (cell == kPyramid) {
+    start[0] = start[1] = 0.4f;
+    start[2] = 0.2f;
   } else start[0] = start[1] = start[2] = 0.5f;
 }
 
@@ -420,10 +541,12 @@ tlg_status basis_fail(tlg_status s, const std::string& m) { return tlg::fail(s, 
 tlg_status tlg_basis_create(int cell, int degree, int family, tlg_basis** out) {
   if (!out) return basis_fail(TLG_ERR_INVALID_ARGUMENT, "tlg_basis_create: out is NULL");
   *out = nullptr;
-  if (!tlg::valid_cell(cell) || cell == tlg::kPoint || cell == tlg::kPyramid)
+  if (!tlg::valid_cell(cell) || cell == tlg::kPoint)
     return basis_fail(TLG_ERR_UNSUPPORTED, "tlg_basis_create: no basis for cell " + std::to_string(cell));
   if (degree < 1 || degree + 1 > tlg::kBasisMaxN)
     return basis_fail(TLG_ERR_UNSUPPORTED, "tlg_basis_create: degree must be 1 .. 15");
+  if (cell == tlg::kPyramid && degree > tlg::kPyramidMaxP)
+    return basis_fail(TLG_ERR_UNSUPPORTED, "tlg_basis_create: pyramid degrees 1 .. 4");
   try {
     const int td = tlg::tdim(cell);
     const int64_t k = tlg::num_lagrange_nodes(cell, degree);
@@ -454,7 +577,8 @@ tlg_status tlg_basis_create(int cell, int degree, int family, tlg_basis** out) {
         throw std::invalid_argument("tlg_basis_create: a node off the barycentric lattice");
       return (int)m;
     };
-    for (int64_t kk = 0; kk < k; ++kk) {
+    const bool pyramid = cell == tlg::kPyramid;
+    for (int64_t kk = 0; kk < k && !pyramid; ++kk) {
       const double* x = &lp[kk * td];
       if (tensor) {
         for (int d = 0; d < td; ++d) h.idx[kk][d] = (uint8_t)index_1d(x[d]);
@@ -474,8 +598,16 @@ tlg_status tlg_basis_create(int cell, int degree, int family, tlg_basis** out) {
     b->family = family;
     b->td = td;
     b->k = k;
-    cudaError_t e = cudaMalloc(&b->dev, sizeof(tlg::BasisData));
+    // Pyramids: the expansion coefficients follow the header.
+    const std::vector<double> coef =
+        pyramid ? tlg::expansion_coefficients(cell, degree, family) : std::vector<double>();
+    static_assert(sizeof(tlg::BasisData) % 16 == 0, "the coefficients start 16-byte aligned");
+    cudaError_t e = cudaMalloc(&b->dev, sizeof(tlg::BasisData) + coef.size() * sizeof(double));
+    if (e == cudaSuccess && pyramid) h.coef = reinterpret_cast<const double*>(b->dev + sizeof(tlg::BasisData));
     if (e == cudaSuccess) e = cudaMemcpy(b->dev, &h, sizeof(h), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && pyramid)
+      e = cudaMemcpy(b->dev + sizeof(tlg::BasisData), coef.data(), coef.size() * sizeof(double),
+                     cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
       if (b->dev) cudaFree(b->dev);
       delete b;

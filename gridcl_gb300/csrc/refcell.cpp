@@ -15,7 +15,12 @@
 //    prisms), and the generalised Vandermonde matrix is inverted by LU with partial pivoting.
 //    Both span the same space, so the Lagrange functions agree to rounding; orthogonality keeps
 //    the Vandermonde matrix well conditioned at high degree.
-// Pyramids (a rational space) are not supported by this build.
+//  - pyramids: the space of tetraloma-refcell/src/polynomials/pyramid.rs:1-17 (rational:
+//    x^a y^b z^c / (1 - z)^min(a,b), a + c <= p, b + c <= p), expanded in the orthogonal
+//    rationomials Q_i(2x - s, s) Q_j(2y - s, s) / s^min(i,j) * P_k^(2 max(i,j) + 2, 0)(2z - 1),
+//    s = 1 - z, max(i, j) + k <= p, with Q_i the scaled Legendre polynomials (not normalised).
+//    At the apex (s = 0) the functions with min(i, j) >= 1 are 0 with a zero gradient, the limit
+//    along the pyramid's axis, as the reference returns there.
 #include "refcell.h"
 
 #include <algorithm>
@@ -213,9 +218,44 @@ void dubiner_point(int cell, int p, const double* x, const std::vector<std::arra
   }
 }
 
-// Exponent triples of the expansion set of (cell, p).
+// The pyramid's orthogonal rationomials (i, j, k) of `sp` at one point, values and gradients.
+void pyramid_point(int p, const double* x, const std::vector<std::array<int, 3>>& sp, double* val,
+                   double* grad /* [j][3] */) {
+  const double s = 1.0 - x[2];
+  const double zero[3] = {0.0, 0.0, 0.0};
+  // Q_i(2x - s, s) and Q_j(2y - s, s): d(2x - s) = (2, 0, 1), d(2y - s) = (0, 2, 1), ds = (0, 0, -1).
+  const double dfx[3] = {2.0, 0.0, 1.0}, dfy[3] = {0.0, 2.0, 1.0}, ds[3] = {0.0, 0.0, -1.0};
+  std::vector<double> qx(p + 1), dqx((p + 1) * 3), qy(p + 1), dqy((p + 1) * 3);
+  scaled_jacobi(p, 0.0, 2.0 * x[0] - s, dfx, s, ds, 3, qx.data(), dqx.data());
+  scaled_jacobi(p, 0.0, 2.0 * x[1] - s, dfy, s, ds, 3, qy.data(), dqy.data());
+  std::vector<double> t(p + 1), dt((p + 1) * 3);
+  const double dfz[3] = {0.0, 0.0, 2.0};
+  for (size_t m = 0; m < sp.size(); ++m) {
+    const int i = sp[m][0], j = sp[m][1], k = sp[m][2];
+    const int n = std::min(i, j);
+    double f = 0.0, gf[3] = {0.0, 0.0, 0.0};
+    if (n == 0 || s != 0.0) {
+      const double r = n ? std::pow(s, -n) : 1.0;
+      const double rz = n ? n * r / s : 0.0;  // d(s^-n)/dz
+      f = qx[i] * qy[j] * r;
+      for (int d = 0; d < 3; ++d) gf[d] = (dqx[i * 3 + d] * qy[j] + qx[i] * dqy[j * 3 + d]) * r;
+      gf[2] += qx[i] * qy[j] * rz;
+    }
+    scaled_jacobi(k, 2.0 * std::max(i, j) + 2.0, 2.0 * x[2] - 1.0, dfz, 1.0, zero, 3, t.data(), dt.data());
+    val[m] = f * t[k];
+    for (int d = 0; d < 3; ++d) grad[m * 3 + d] = gf[d] * t[k] + f * dt[k * 3 + d];
+  }
+}
+
+// Exponent triples of the expansion set of (cell, p); on pyramids the (i, j, k) above.
 std::vector<std::array<int, 3>> space(int cell, int p) {
   std::vector<std::array<int, 3>> s;
+  if (cell == kPyramid) {
+    for (int i = 0; i <= p; ++i)
+      for (int j = 0; j <= p; ++j)
+        for (int k = 0; k + std::max(i, j) <= p; ++k) s.push_back({i, j, k});
+    return s;
+  }
   for (int c = 0; c <= p; ++c)
     for (int b = 0; b <= p; ++b)
       for (int a = 0; a <= p; ++a) {
@@ -245,8 +285,11 @@ std::vector<double> basis(int cell, int p, const double* pts, long npts, int nde
   const bool collapsed = cell == kTriangle || cell == kTetrahedron || cell == kPrism;
   std::vector<double> v1(nb), g1((size_t)nb * 3);
   for (long q = 0; q < npts; ++q) {
-    if (collapsed) {
-      dubiner_point(cell, p, pts + q * td, sp, v1.data(), g1.data());
+    if (collapsed || cell == kPyramid) {
+      if (cell == kPyramid)
+        pyramid_point(p, pts + q * td, sp, v1.data(), g1.data());
+      else
+        dubiner_point(cell, p, pts + q * td, sp, v1.data(), g1.data());
       for (long j = 0; j < nb; ++j) {
         out[q * nb + j] = v1[j];
         if (nderivs)
@@ -519,10 +562,7 @@ void collapsed_rule(int cell, const int* counts, std::vector<double>& points,
   }
 }
 
-std::vector<double> tabulate(int cell, int degree, int family, const double* points, long npoints,
-                             int nderivs) {
-  if (nderivs < 0 || nderivs > 1) throw std::invalid_argument("derivative order must be 0 or 1");
-  const int td = tdim(cell);
+std::vector<double> expansion_coefficients(int cell, int degree, int family) {
   const std::vector<double> nodes = lagrange_points(cell, degree, family);
   const int n = (int)num_lagrange_nodes(cell, degree);
   // V[i][m] = basis_m(node_i); coefficients C = V^-1 (V C = I).
@@ -530,6 +570,15 @@ std::vector<double> tabulate(int cell, int degree, int family, const double* poi
   std::vector<double> c((size_t)n * n, 0.0);
   for (int i = 0; i < n; ++i) c[(size_t)i * n + i] = 1.0;
   lu_solve(v, n, c, n);
+  return c;
+}
+
+std::vector<double> tabulate(int cell, int degree, int family, const double* points, long npoints,
+                             int nderivs) {
+  if (nderivs < 0 || nderivs > 1) throw std::invalid_argument("derivative order must be 0 or 1");
+  const int td = tdim(cell);
+  const int n = (int)num_lagrange_nodes(cell, degree);
+  const std::vector<double> c = expansion_coefficients(cell, degree, family);
   const std::vector<double> phi = basis(cell, degree, points, npoints, nderivs);
   const int rows = 1 + (nderivs ? td : 0);
   std::vector<double> out((size_t)rows * npoints * n, 0.0);

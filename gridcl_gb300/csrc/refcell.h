@@ -24,6 +24,9 @@ void gauss_jacobi(int m, double alpha, std::vector<double>& x, std::vector<doubl
 std::vector<double> gll_points(int m);
 void collapsed_rule(int cell, const int* counts, std::vector<double>& points,
                     std::vector<double>& weights);
+// C [m][k] (m-major): Lagrange function k = sum_m C[m][k] e_m, e_m the expansion set (on
+// pyramids the orthogonal rationomials (i, j, k), i outer, j, then k, max(i, j) + k <= degree).
+std::vector<double> expansion_coefficients(int cell, int degree, int family);
 // [deriv][q][k]
 std::vector<double> tabulate(int cell, int degree, int family, const double* points, long npoints,
                              int nderivs);

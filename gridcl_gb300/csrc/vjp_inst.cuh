@@ -25,6 +25,9 @@ cudaError_t TLG_VJP_LAUNCH(int d, int k, const VjpArgs& a, size_t smem, cudaStre
   TLG_VJP(3, 27)
   TLG_VJP(3, 6)
   TLG_VJP(3, 18)
+  TLG_VJP(3, 5)
+  TLG_VJP(3, 14)
+  TLG_VJP(3, 30)
   TLG_VJP(2, 3)
   TLG_VJP(2, 6)
   TLG_VJP(2, 10)

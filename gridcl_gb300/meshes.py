@@ -6,8 +6,10 @@ Restates (paths inside the reference project):
 - ``cube_box`` / ``square_box``: tetraloma-testing/src/meshes/boxes.rs:96-151 — the unit box in
   n^d subcells on the integer lattice of resolution 2 n p, cells numbered x fastest, then y,
   then z, the cells of one subcell consecutive; tetrahedra by the Kuhn split (one per path
-  0 -> e_a -> e_a + e_b -> 7), prisms by the z-face diagonal (0,0)-(1,1), each cell oriented
-  positively (swap of vertices 1 and 2, and 4 and 5 on prisms);
+  0 -> e_a -> e_a + e_b -> 7), prisms by the z-face diagonal (0,0)-(1,1), pyramids one per
+  face of the subcell (faces in the hexahedron's sub-entity order) with the apex at its centre
+  (boxes.rs:44-58, 182-187), each cell oriented positively (swap of vertices 1 and 2, and 4
+  and 5 on prisms);
 - node numbering: the order of first use by the cells, with shared high-order nodes found
   exactly through their lattice keys (meshes/lattice.rs:95-230);
 - the Lagrange nodes of a cell are the equispaced reference nodes mapped affinely through its
@@ -28,7 +30,7 @@ import numpy as np
 from . import refcell
 
 _TDIM = {"Interval": 1, "Triangle": 2, "Quadrilateral": 2, "Tetrahedron": 3, "Hexahedron": 3,
-         "Prism": 3}
+         "Prism": 3, "Pyramid": 3}
 
 
 @dataclasses.dataclass
@@ -92,30 +94,69 @@ def uniform(seed: int, shape) -> np.ndarray:
 
 def _axis_vertices(cell: str):
     return {"Interval": [1], "Triangle": [1, 2], "Quadrilateral": [1, 2],
-            "Tetrahedron": [1, 2, 3], "Prism": [1, 2, 3], "Hexahedron": [1, 2, 4]}[cell]
+            "Tetrahedron": [1, 2, 3], "Prism": [1, 2, 3], "Hexahedron": [1, 2, 4],
+            "Pyramid": [1, 2, 4]}[cell]
 
 
-def _assemble(cell: str, p: int, verts: np.ndarray, gdim: int, resolution: int, lagrange_points=None):
-    """Lagrange-node lattice keys of cells given by vertex keys `verts` [ncells][nv][3] (int64),
-    nodes numbered by first use. Returns (node keys [N][3], dofmap [ncells][K] uint32).
-    `lagrange_points(cell, p)` gives the reference nodes (the library's refcell by default)."""
+def _node_keys(cell: str, p: int, verts: np.ndarray, lagrange_points=None) -> np.ndarray:
+    """Lattice keys [ncells][K][3] of the Lagrange nodes of cells given by vertex keys `verts`
+    [ncells][nv][3] (int64): the reference nodes mapped affinely through the vertices 0 and the
+    axis vertices. `lagrange_points(cell, p)` gives the reference nodes (the library's refcell by
+    default)."""
     ref = (lagrange_points or refcell.lagrange_points)(cell, p)  # [K][td] in [0, 1]
     r = np.rint(ref * p).astype(np.int64)
     assert np.allclose(r, ref * p), "equispaced nodes lie on the lattice"
     axes = verts[:, _axis_vertices(cell), :] - verts[:, :1, :]  # [ncells][td][3]
     s = np.einsum("kt,ctg->ckg", r, axes)
     assert np.all(s % p == 0)
-    keys = verts[:, :1, :] + s // p  # [ncells][K][3]
-    side = resolution + 1
-    flat = (keys[..., 0] * side + keys[..., 1]) * side + keys[..., 2]
-    uniq, first, inverse = np.unique(flat.ravel(), return_index=True, return_inverse=True)
+    return verts[:, :1, :] + s // p
+
+
+def _number(flat: np.ndarray, side: int):
+    """First-use numbering of the flat keys (in the order given). Returns (node keys [N][3],
+    node index of every key)."""
+    uniq, first, inverse = np.unique(flat, return_index=True, return_inverse=True)
     order = np.argsort(first, kind="stable")  # unique keys in order of first use
     rank = np.empty_like(order)
     rank[order] = np.arange(order.size)
-    dofmap = rank[inverse].reshape(flat.shape).astype(np.uint32)
     node_keys = np.stack([uniq[order] // (side * side), (uniq[order] // side) % side,
                           uniq[order] % side], axis=1)
-    return node_keys, dofmap
+    return node_keys, rank[inverse]
+
+
+def _assemble(cell: str, p: int, verts: np.ndarray, gdim: int, resolution: int, lagrange_points=None):
+    """Lagrange-node lattice keys of cells given by vertex keys `verts` [ncells][nv][3] (int64),
+    nodes numbered by first use. Returns (node keys [N][3], dofmap [ncells][K] uint32)."""
+    keys = _node_keys(cell, p, verts, lagrange_points)
+    side = resolution + 1
+    flat = (keys[..., 0] * side + keys[..., 1]) * side + keys[..., 2]
+    node_keys, idx = _number(flat.ravel(), side)
+    return node_keys, idx.reshape(flat.shape).astype(np.uint32)
+
+
+_CELL_ORDER = ("Interval", "Triangle", "Quadrilateral", "Tetrahedron", "Hexahedron", "Prism", "Pyramid")
+
+
+def _assemble_blocks(parts, p: int, resolution: int) -> HostMesh:
+    """A mesh of several cell types: `parts` maps a cell type to (vertex keys [n][nv][3], the
+    cells' positions in the generation order [n]). Nodes are numbered by first use over all
+    cells in generation order; blocks follow the cell-type order (meshes/lattice.rs:95-230)."""
+    side = resolution + 1
+    cells = sorted(parts, key=_CELL_ORDER.index)
+    keys = {c: _node_keys(c, p, parts[c][0]) for c in cells}
+    flat = {c: (k[..., 0] * side + k[..., 1]) * side + k[..., 2] for c, k in keys.items()}
+    seq = np.concatenate([np.repeat(parts[c][1], flat[c].shape[1]) for c in cells])
+    allk = np.concatenate([flat[c].ravel() for c in cells])
+    order = np.argsort(seq, kind="stable")  # cells in generation order, nodes in local order
+    node_keys, idx_sorted = _number(allk[order], side)
+    idx = np.empty_like(idx_sorted)
+    idx[order] = idx_sorted
+    blocks, at = [], 0
+    for c in cells:
+        n = flat[c].size
+        blocks.append(HostBlock(c, p, idx[at: at + n].reshape(flat[c].shape).astype(np.uint32)))
+        at += n
+    return HostMesh(3, node_keys.astype(np.float64) / resolution, blocks)
 
 
 def _orient(cell: str, verts: np.ndarray) -> np.ndarray:
@@ -125,7 +166,7 @@ def _orient(cell: str, verts: np.ndarray) -> np.ndarray:
     det = np.linalg.det(axes[:, :, :td]) if td > 1 else axes[:, 0, 0]
     neg = det < 0
     if np.any(neg):
-        if cell in ("Triangle", "Tetrahedron"):
+        if cell in ("Triangle", "Tetrahedron", "Pyramid"):
             v = verts[neg]
             v[:, [1, 2]] = v[:, [2, 1]]
             verts[neg] = v
@@ -160,11 +201,93 @@ def cube_box(cell: str, n: int, p: int, lagrange_points=None) -> HostMesh:
     elif cell == "Prism":
         sel = [[a, b, d, a + 4, b + 4, d + 4] for a, b, d in ([0, 1, 3], [0, 3, 2])]
         verts = corners[:, sel, :].reshape(-1, 6, 3)
+    elif cell == "Pyramid":
+        verts = _pyramids(corners, origin + p).reshape(-1, 5, 3)
     else:
         raise ValueError(f"cube_box has no {cell} cells in this build")
     verts = _orient(cell, verts.copy())
     keys, dofmap = _assemble(cell, p, verts, 3, res, lagrange_points)
     return HostMesh(3, keys.astype(np.float64) / res, [HostBlock(cell, p, dofmap)])
+
+
+_HEX_FACES = [[0, 1, 2, 3], [0, 1, 4, 5], [0, 2, 4, 6], [1, 3, 5, 7], [2, 3, 6, 7], [4, 5, 6, 7]]
+
+
+def _subcells(n: int, p: int):
+    """Per subcell (x fastest, then y, then z): its index (i, j, k), its 8 corner keys in tensor
+    order and its centre key, on the lattice of resolution 2 n p."""
+    h = 2 * p
+    i, j, k = np.meshgrid(np.arange(n), np.arange(n), np.arange(n), indexing="ij")
+    ijk = np.stack([i.transpose(2, 1, 0).ravel(), j.transpose(2, 1, 0).ravel(),
+                    k.transpose(2, 1, 0).ravel()], axis=1).astype(np.int64)
+    bits = np.array([[(v >> b) & 1 for b in range(3)] for v in range(8)], dtype=np.int64)
+    corners = ijk[:, None, :] * h + bits[None, :, :] * h
+    return ijk, corners, ijk * h + p
+
+
+def _pyramids(corners: np.ndarray, centres: np.ndarray, faces=_HEX_FACES) -> np.ndarray:
+    """[n][len(faces)][5][3]: the pyramid on each face with the apex at the centre."""
+    base = corners[:, faces, :]
+    apex = np.broadcast_to(centres[:, None, None, :], base.shape[:2] + (1, 3))
+    return np.concatenate([base, apex], axis=2)
+
+
+def mixed_box(n: int, p: int) -> HostMesh:
+    """The conforming tetrahedron/hexahedron/pyramid box (boxes.rs:194-245): subcells with an
+    even index sum split into six pyramids around their centre, the pyramid on the face x = 0 of
+    the subcells at i = 0 split into two tetrahedra along its base diagonal v0-v3; the other
+    subcells stay hexahedra. Blocks: tetrahedra, hexahedra, pyramids."""
+    if n < 1 or p < 1:
+        raise ValueError("a box needs n >= 1 and p >= 1")
+    ijk, corners, centres = _subcells(n, p)
+    even = ijk.sum(1) % 2 == 0
+    # Generation order: per subcell, its cells; six slots per subcell (the split pyramid's two
+    # tetrahedra share its slot, the hexahedron takes slot 0).
+    base_seq = np.arange(ijk.shape[0]) * 6
+    hexes = corners[~even]
+    pyr = _pyramids(corners[even], centres[even])  # [ne][6][5][3]
+    pseq = base_seq[even][:, None] + np.arange(6)[None, :]
+    split = np.zeros(pyr.shape[:2], dtype=bool)
+    split[:, 2] = ijk[even][:, 0] == 0  # face 2 is x = 0 (vertices 0, 2, 4, 6)
+    tets = []
+    for a, b, d in ((0, 1, 3), (0, 3, 2)):
+        t = pyr[split][:, [a, b, d, 4], :]
+        tets.append(t)
+    tv = np.stack(tets, axis=1).reshape(-1, 4, 3) if split.any() else np.zeros((0, 4, 3), np.int64)
+    tseq = np.repeat(pseq[split], 2)
+    parts = {}
+    if tv.shape[0]:
+        parts["Tetrahedron"] = (_orient("Tetrahedron", tv.copy()), tseq)
+    if hexes.shape[0]:
+        parts["Hexahedron"] = (hexes, base_seq[~even])
+    parts["Pyramid"] = (_orient("Pyramid", pyr[~split].copy()), pseq[~split])
+    return _assemble_blocks(parts, p, 2 * n * p)
+
+
+def hex_prism_pyramid_box(n: int, p: int) -> HostMesh:
+    """The conforming hexahedron/prism/pyramid box (boxes.rs:247-302): the subcells of the
+    columns i < n // 3 split into two prisms each (as `cube_box`'s prisms), of the others those
+    with an even index sum into six pyramids around their centre, the rest hexahedra."""
+    if n < 1 or p < 1:
+        raise ValueError("a box needs n >= 1 and p >= 1")
+    ijk, corners, centres = _subcells(n, p)
+    prism_col = ijk[:, 0] < n // 3
+    even = (ijk.sum(1) % 2 == 0) & ~prism_col
+    hexa = ~prism_col & ~even
+    seq = np.arange(ijk.shape[0]) * 6
+    parts = {}
+    if hexa.any():
+        parts["Hexahedron"] = (corners[hexa], seq[hexa])
+    if prism_col.any():
+        sel = [[a, b, d, a + 4, b + 4, d + 4] for a, b, d in ([0, 1, 3], [0, 3, 2])]
+        pv = corners[prism_col][:, sel, :].reshape(-1, 6, 3)
+        parts["Prism"] = (_orient("Prism", pv.copy()),
+                          (seq[prism_col][:, None] + np.arange(2)[None, :]).ravel())
+    if even.any():
+        pyr = _pyramids(corners[even], centres[even]).reshape(-1, 5, 3)
+        parts["Pyramid"] = (_orient("Pyramid", pyr.copy()),
+                            (seq[even][:, None] + np.arange(6)[None, :]).ravel())
+    return _assemble_blocks(parts, p, 2 * n * p)
 
 
 def square_box(cell: str, n: int, p: int) -> HostMesh:

@@ -142,7 +142,8 @@ def vjp(cell: str, degree: int, nodes_abs: np.ndarray, dofmap: np.ndarray, point
 
 
 CENTROID = {"Interval": (0.5,), "Triangle": (1 / 3, 1 / 3), "Quadrilateral": (0.5, 0.5),
-            "Tetrahedron": (0.25, 0.25, 0.25), "Hexahedron": (0.5, 0.5, 0.5), "Prism": (1 / 3, 1 / 3, 0.5)}
+            "Tetrahedron": (0.25, 0.25, 0.25), "Hexahedron": (0.5, 0.5, 0.5), "Prism": (1 / 3, 1 / 3, 0.5),
+            "Pyramid": (0.4, 0.4, 0.2)}
 
 
 def pull_back(cell: str, degree: int, nodes_abs: np.ndarray, dofmap: np.ndarray, x_abs: np.ndarray,

@@ -22,12 +22,21 @@ What is restated, and from where (paths inside the reference project):
   matrix inverse: products of 1D Lagrange polynomials on intervals, quadrilaterals and
   hexahedra, the classical equispaced barycentric products on triangles and tetrahedra, and
   their product on prisms. This is exact up to rounding at every degree.
-
-Pyramids (a rational space) are not restated: no workload of this path uses them.
+- pyramids: the Lagrange space is rational (``tetraloma-refcell/src/polynomials/pyramid.rs:1-17``,
+  spanned by x^a y^b z^c / (1 - z)^min(a,b) with a + c <= p and b + c <= p, the set of
+  ``tabulation.rs:418-460``). There is no product form, so this module expands the Lagrange
+  functions in the centred rationomials u^a v^b w^c / s^min(a,b), s = 1 - z, u = 2x - s,
+  v = 2y - s, w = 2z - 1 (the same space: x^a = ((u + s) / 2)^a, and the powers of s and w
+  are polynomials in z of no higher degree), where the reference uses an orthonormal set, and
+  inverts their Vandermonde matrix at the equispaced nodes exactly, in rational arithmetic.
+  At the apex (s = 0) every value and first derivative is its limit along the pyramid's axis
+  u = v = 0, as the reference returns there (``pyramid.rs:12-16``).
 """
 
 from __future__ import annotations
 
+import fractions
+import functools
 import math
 
 import numpy as np
@@ -352,6 +361,85 @@ def _simplex(td: int, p: int, nodes: np.ndarray, pts: np.ndarray):
     return out
 
 
+def pyramid_exponents(p: int) -> list[tuple[int, int, int]]:
+    """(a, b, c) with a + c <= p and b + c <= p: the exponents of the rationomials
+    x^a y^b z^c / (1 - z)^min(a,b) spanning the pyramid's Lagrange space (tabulation.rs:446-460),
+    and of the centred ones this module expands in."""
+    return [(a, b, c) for c in range(p + 1) for b in range(p + 1 - c) for a in range(p + 1 - c)]
+
+
+def _centred_exact(e, x) -> fractions.Fraction:
+    """u^a v^b w^c / s^r (r = min(a, b)) at a point of exact fractions; 0 at s = 0 when r >= 1
+    (there u = v = 0 inside the cell: the limit along the axis)."""
+    a, b, c = e
+    r = min(a, b)
+    s = 1 - x[2]
+    if s == 0 and r > 0:
+        return fractions.Fraction(0)
+    return (2 * x[0] - s) ** a * (2 * x[1] - s) ** b * (2 * x[2] - 1) ** c / s ** r
+
+
+@functools.lru_cache(maxsize=None)
+def pyramid_coefficients(p: int) -> np.ndarray:
+    """C [m][k]: the pyramid's Lagrange function k is sum_m C[m][k] f_m, f_m the centred
+    rationomials of `pyramid_exponents(p)`; the Vandermonde matrix V[i][m] = f_m(node_i) at the
+    equispaced nodes (i0/p, i1/p, i2/p) is inverted exactly (Gauss-Jordan over fractions), then
+    rounded."""
+    exps = pyramid_exponents(p)
+    nodes = [[fractions.Fraction(int(round(v * p)), p) for v in row] for row in lagrange_points("Pyramid", p)]
+    n = len(nodes)
+    assert len(exps) == n
+    a = [[_centred_exact(e, x) for e in exps] + [fractions.Fraction(int(i == j)) for j in range(n)]
+         for i, x in enumerate(nodes)]
+    for col in range(n):
+        piv = next(r for r in range(col, n) if a[r][col] != 0)
+        a[col], a[piv] = a[piv], a[col]
+        inv = 1 / a[col][col]
+        a[col] = [v * inv for v in a[col]]
+        for r in range(n):
+            if r != col and a[r][col] != 0:
+                f = a[r][col]
+                a[r] = [v - f * w for v, w in zip(a[r], a[col])]
+    return np.array([[float(v) for v in row[n:]] for row in a])
+
+
+def _centred_terms(e):
+    """The value and the three first derivatives of u^a v^b w^c s^-r as lists of terms
+    (coefficient, (eu, ev, ew, es)); du = (2, 0, 1), dv = (0, 2, 1), dw = (0, 0, 2), ds = (0, 0, -1)."""
+    a, b, c = e
+    r = min(a, b)
+    out = [[(1.0, (a, b, c, -r))], [], [], []]
+    if a:
+        out[1].append((2.0 * a, (a - 1, b, c, -r)))
+        out[3].append((float(a), (a - 1, b, c, -r)))
+    if b:
+        out[2].append((2.0 * b, (a, b - 1, c, -r)))
+        out[3].append((float(b), (a, b - 1, c, -r)))
+    if c:
+        out[3].append((2.0 * c, (a, b, c - 1, -r)))
+    if r:
+        out[3].append((float(r), (a, b, c, -r - 1)))
+    return out
+
+
+def _pyramid(p: int, pts: np.ndarray) -> np.ndarray:
+    exps = pyramid_exponents(p)
+    coef = pyramid_coefficients(p)
+    s = 1.0 - pts[:, 2]
+    u, v, w = 2.0 * pts[:, 0] - s, 2.0 * pts[:, 1] - s, 2.0 * pts[:, 2] - 1.0
+    apex = s == 0.0
+    safe = np.where(apex, 1.0, s)
+    f = np.zeros((4, pts.shape[0], len(exps)))
+    for m, e in enumerate(exps):
+        for d, terms in enumerate(_centred_terms(e)):
+            for c, (eu, ev, ew, es) in terms:
+                val = c * u ** eu * v ** ev * w ** ew * safe ** es
+                # On the axis (u = v = 0) a term with eu = ev = 0 has es = 0: its limit is c w^ew.
+                lim = c * w ** ew if eu == 0 and ev == 0 and es == 0 else 0.0
+                f[d, :, m] += np.where(apex, lim, val)
+    return f @ coef
+
+
 def tabulate(cell: str, degree: int, points, nderivs: int = 1, family: str = "Equispaced") -> np.ndarray:
     """``[deriv][q][k]``: values (deriv 0) and d/dxi_d (deriv 1 + d) of the Lagrange functions of
     (cell, degree, family) at `points`, like ``Tabulation::get`` (tabulation.rs:266). The
@@ -387,6 +475,10 @@ def tabulate(cell: str, degree: int, points, nderivs: int = 1, family: str = "Eq
             out[1, :, k] = tri[1, :, it] * fz[0]
             out[2, :, k] = tri[2, :, it] * fz[0]
             out[3, :, k] = tri[0, :, it] * fz[1]
+    elif cell == "Pyramid":
+        if family != "Equispaced":
+            raise ValueError("pyramids have equispaced nodes only")
+        out = _pyramid(p, pts)
     else:
         raise NotImplementedError(f"{cell} is not restated by the oracle")
     return out if nderivs else out[:1]

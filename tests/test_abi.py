@@ -43,10 +43,10 @@ def test_argument_errors_before_device_work():
     h = ctypes.c_void_p()
     pts = np.zeros((1, 3))
     p = pts.ctypes.data_as(ctypes.c_void_p)
-    # gdim below tdim, unknown dtype, pyramids, degree 0: all rejected on the host
+    # gdim below tdim, unknown dtype, GLL nodes on pyramids, degree 0: all rejected on the host
     assert L.tlg_tables_create(4, 1, 0, 2, 8, p, 1, None, ctypes.byref(h)) == 1
     assert L.tlg_tables_create(4, 1, 0, 3, 2, p, 1, None, ctypes.byref(h)) == 1
-    assert L.tlg_tables_create(7, 1, 0, 3, 8, p, 1, None, ctypes.byref(h)) == 4
+    assert L.tlg_tables_create(7, 2, 1, 3, 8, p, 1, None, ctypes.byref(h)) == 1
     assert L.tlg_tables_create(4, 0, 0, 3, 8, p, 1, None, ctypes.byref(h)) == 1
     assert b"degree" in L.tlg_last_error()
     assert h.value is None

@@ -95,6 +95,70 @@ def test_tabulation_is_lagrange(cell):
             assert np.abs(grad - want).max() < 1e-10
 
 
+def test_pyramid_interior_nodes():
+    """lagrange.rs's interior block of the P4 pyramid: i2 = 1 gives i0, i1 in 1..=2 (i0 fastest),
+    i2 = 2 gives (1, 1)."""
+    pts = rc.lagrange_points("Pyramid", 4)
+    want = np.array([[1, 1, 1], [2, 1, 1], [1, 2, 1], [2, 2, 1], [1, 1, 2]]) / 4.0
+    assert pts.shape == (55, 3)
+    assert np.array_equal(pts[-5:], want)
+
+
+def _rationomial(a, b, c, x):
+    """x^a y^b z^c / (1 - z)^min(a, b) and its gradient, strictly inside the pyramid (the value
+    also at the apex, where it is 0 for min(a, b) >= 1)."""
+    r = min(a, b)
+    s = 1.0 - x[:, 2]
+    pw = lambda v, k: v ** k if k >= 0 else np.zeros_like(v)
+    base = pw(x[:, 0], a) * pw(x[:, 1], b) * pw(x[:, 2], c)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        v = np.where(s == 0.0, 0.0 if r else base, base / np.where(s == 0.0, 1.0, s) ** r)
+    dx = a * pw(x[:, 0], a - 1) * pw(x[:, 1], b) * pw(x[:, 2], c) / s ** r
+    dy = b * pw(x[:, 0], a) * pw(x[:, 1], b - 1) * pw(x[:, 2], c) / s ** r
+    dz = c * pw(x[:, 0], a) * pw(x[:, 1], b) * pw(x[:, 2], c - 1) / s ** r + r * base / s ** (r + 1)
+    return v, np.stack([dx, dy, dz])
+
+
+def test_pyramid_space_is_reproduced():
+    """tabulation.rs:418-520: Kronecker at the nodes; the interpolant of every rationomial of the
+    space reproduces its values and first derivatives at the points of gauss_rule(Pyramid, 2p)
+    (1e-10 relative to the largest derivative there), p = 1..5."""
+    for p in range(1, 6):
+        e = rc.LagrangeElement("Pyramid", p)
+        assert np.abs(e.tabulate(e.points, 0)[0] - np.eye(e.dim)).max() < 1e-12
+        pts, _ = rc.gauss_rule("Pyramid", 2 * p)
+        t = e.tabulate(pts, 1)
+        for a, b, c in rc.pyramid_exponents(p):
+            fn, _ = _rationomial(a, b, c, e.points)
+            v, g = _rationomial(a, b, c, pts)
+            assert np.abs(t[0] @ fn - v).max() <= 1e-12 * max(1.0, np.abs(v).max())
+            if (a, b, c) != (0, 0, 0):
+                assert np.abs(t[1:] @ fn - g).max() <= 1e-10 * np.abs(g).max(), (p, a, b, c)
+
+
+def test_pyramid_apex_is_the_axis_limit():
+    """pyramid.rs:176-200: the values and derivatives at the apex are the limits along the axis
+    x = y = (1 - z) / 2 (a power of two apart, so the near point is exact)."""
+    eps = 2.0 ** -40
+    for p in range(1, 5):
+        apex = rc.tabulate("Pyramid", p, np.array([[0.0, 0.0, 1.0]]), 1)
+        near = rc.tabulate("Pyramid", p, np.array([[eps / 2, eps / 2, 1.0 - eps]]), 1)
+        assert np.abs(apex - near).max() <= 1e-6 * max(1.0, np.abs(near).max()), p
+
+
+def test_pyramid_rules_integrate_the_space():
+    """quadrature.rs:39-41: gauss_rule(Pyramid, p) is exact for the rationomials of degree p:
+    the integral of x^a y^b z^c / (1 - z)^r over the pyramid (x = xi s, y = eta s) is
+    c! q! / (c + q + 1)! / ((a + 1)(b + 1)) with q = a + b - r + 2."""
+    for p in range(0, 9):
+        pts, w = rc.gauss_rule("Pyramid", p)
+        for a, b, c in rc.pyramid_exponents(p):
+            q = a + b - min(a, b) + 2
+            exact = math.factorial(c) * math.factorial(q) / math.factorial(c + q + 1) / ((a + 1) * (b + 1))
+            v, _ = _rationomial(a, b, c, pts)
+            assert abs(np.dot(w, v) - exact) <= 1e-14 * 10, (p, a, b, c)
+
+
 def test_pinv_is_a_left_inverse():
     """tetraloma-testing/src/reference.rs:907-929, through the C oracle's per-point math."""
     cases = [(1, 1, [2.0]), (1, 3, [1.0, 2.0, 0.5]), (2, 2, [1.0, 0.2, -0.3, 2.0]),
@@ -142,7 +206,7 @@ def test_unit_volume_and_constant_affine_detj():
     """unit_volume.rs (1e-12) and factors.rs:151-185 (det J constant on affine cells)."""
     from gridcl_gb300 import meshes
 
-    for cell in ("Tetrahedron", "Hexahedron", "Prism"):
+    for cell in ("Tetrahedron", "Hexahedron", "Prism", "Pyramid"):
         m = meshes.cube_box(cell, 3, 1)
         b = m.blocks[0]
         pts, w = rc.gauss_rule(cell, 2)
