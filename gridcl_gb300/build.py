@@ -21,7 +21,7 @@ OUT_DIR = HERE / "_build"
 LIB = HERE / "libtlgeom.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "coop.cu", "csr.cu", "eval_df.cu", "eval_f32.cu", "eval_f64.cu", "eval_pair.cu", "eval_pair_meas.cu", "measure.cu", "order.cpp",
-           "pullback.cu", "refcell.cpp", "sumfact.cu", "sumfact_df.cu", "sumfact_fn.cu", "tc.cu", "vjp_f64.cu", "vjp_split.cu", "vjp_surface.cu"]
+           "pullback.cu", "refcell.cpp", "sumfact.cu", "sumfact_df.cu", "sumfact_fn.cu", "tc.cu", "umma.cu", "vjp_f64.cu", "vjp_split.cu", "vjp_surface.cu"]
 
 
 def nvcc() -> str:

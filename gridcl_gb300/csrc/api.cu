@@ -23,6 +23,7 @@
 #include "status.h"
 #include "coop.cuh"
 #include "tc.cuh"
+#include "umma.cuh"
 #include "sumfact.cuh"
 #include "eval_df.cuh"
 #include "sumfact_df.cuh"
@@ -83,6 +84,13 @@ struct tlg_tables {
   // (b0 head, b1 head, b0 tail, b1 tail) of B[k][4 q + r] (r = 0 phi, 1 + d dphi_d).
   uint64_t off_tc = 0;
   int tc_ksteps = 0, tc_col_tiles = 0;
+  // Section of the tcgen05 kernel (f32 and split tables of volume cells in 3D, 20 < K <= 88): per
+  // chunk of 8 points the TF32 heads, then the tails, of B[32 x kpad] (column 4 p + r of point
+  // 8 chunk + p, r = 0 phi, 1 + d dphi_d; node k) in the canonical K-major layout of the MMA
+  // operands (8-row x 16-byte core matrices, 128 bytes apart along K, kpad * 32 bytes apart along
+  // the columns), copied into shared memory chunk by chunk.
+  uint64_t off_umma = 0;
+  int umma_kpad = 0, umma_chunks = 0;
   int* err = nullptr;
   std::vector<unsigned char> host;  // host copy of the device bytes
 };
@@ -281,6 +289,9 @@ bool coop_preferred(const tlg_tables* t) { return t->k > 27; }
 // kernel at P4/P5 tetrahedra and slower at P6 (f32 1.42 ms cooperative, 2.03 ms tensor), with up
 // to 5x the cooperative kernel's error (3xTF32 rounds the tails at 2^-22).
 bool tc_preferred(const tlg_tables*) { return false; }
+
+// The tcgen05 kernel: not taken by AUTO until measured against the cooperative kernel.
+bool umma_preferred(const tlg_tables*) { return false; }
 
 // The sum-factorised kernel; `found` is false when it does not apply (no tensor structure, facet
 // normals, split precision at a tile other than 16, or no instantiation): nothing is launched.
@@ -542,6 +553,50 @@ tlg_status eval_tc(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o
   a.col_tiles = t->tc_col_tiles;
   cudaError_t e = tlg::launch_tc(split, t->td, t->gd, a, smem, stream, found);
   if (!*found) return TLG_ERR_UNSUPPORTED;
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
+  g_last_family = TLG_STRATEGY_TENSOR;
+  return ok();
+}
+
+// The tcgen05 kernel (f32 and split tables of volume cells in 3D with 20 < K <= 88, tile 16);
+// `found` is false where it does not apply (nothing launched).
+tlg_status eval_umma(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, uint32_t mask,
+                     cudaStream_t stream, bool* found) {
+  *found = false;
+  if (t->umma_kpad == 0 || o->tile != 16 || (t->dtype != TLG_F32 && t->dtype != TLG_SPLIT32) ||
+      (mask & tlg::kOutNormals))
+    return TLG_ERR_UNSUPPORTED;
+  // At least 80 KiB, so that at most two CTAs (2 x 256 tensor-memory columns) share an SM.
+  const size_t smem = std::max<size_t>(tlg::umma_smem_bytes(t->umma_kpad), (size_t)80 * 1024);
+  if (smem > (size_t)227 * 1024) return TLG_ERR_UNSUPPORTED;
+  const bool split = t->dtype == TLG_SPLIT32;
+  tlg::UmmaArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = b->nodes;
+  a.dofmap = b->dofmap;
+  a.flags = b->flags;
+  a.btab = t->dev + t->off_umma;
+  a.refn = reinterpret_cast<const float*>(t->dev + t->off_refn);
+  a.dphi64 = split ? reinterpret_cast<const double*>(t->dev + t->off_dphi64) : nullptr;
+  void* outs[6] = {o->points, o->jacobian, o->detj, o->pinv, o->normals, o->facet_normals};
+  for (int i = 0; i < 6; ++i) a.out[i] = outs[i];
+  a.err = t->err;
+  a.recomputed = split ? o->recomputed : nullptr;
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + 15) / 16 * 16;
+  a.range_cells = o->num_cells;
+  a.out_first_cell = o->out_first_cell;
+  a.last_cell = b->num_cells - 1;
+  for (int g = 0; g < 3; ++g) a.origin[g] = b->origin[g];
+  a.cond_limit = o->cond_limit > 0 ? (float)o->cond_limit : 256.0f;
+  a.last_node = (uint32_t)(b->num_nodes - 1);
+  a.mask = mask;
+  a.k = (int)t->k;
+  a.kpad = t->umma_kpad;
+  a.num_points = (int)t->q;
+  a.chunks = t->umma_chunks;
+  *found = true;
+  cudaError_t e = tlg::launch_umma(split, a, smem, stream);
   if (e != cudaSuccess) return cuda_fail(e, "tlg_eval_block launch");
   g_last_family = TLG_STRATEGY_TENSOR;
   return ok();
@@ -1111,6 +1166,13 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       t->off_tc = align16(host_bytes);
       host_bytes = t->off_tc + (size_t)t->tc_col_tiles * t->tc_ksteps * 32 * 16;
     }
+    if (dtype != TLG_F64 && td == 3 && gdim == 3 && k > 20 && (k + 7) / 8 * 8 <= tlg::kUmmaMaxKpad &&
+        npoints > 0) {
+      t->umma_kpad = (int)((k + 7) / 8 * 8);
+      t->umma_chunks = (int)((npoints + tlg::kUmmaPoints - 1) / tlg::kUmmaPoints);
+      t->off_umma = align16(host_bytes);
+      host_bytes = t->off_umma + (size_t)t->umma_chunks * 2 * tlg::kUmmaN * t->umma_kpad * 4;
+    }
     t->host.assign(host_bytes, 0);
     if (t->sf_ok) {
       std::memcpy(t->host.data() + t->off_sf, heads.data(), heads.size() * sizeof(tlg::SfBlock));
@@ -1210,6 +1272,20 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
           std::memcpy(&h, &u, 4);
           return h;
         };
+        if (t->umma_kpad > 0) {
+          const int kp = t->umma_kpad;
+          const size_t half = (size_t)tlg::kUmmaN * kp;  // floats
+          float* ub = reinterpret_cast<float*>(t->host.data() + t->off_umma);
+          for (int ch = 0; ch < t->umma_chunks; ++ch)
+            for (int n = 0; n < tlg::kUmmaN; ++n)
+              for (int kk = 0; kk < kp; ++kk) {
+                const float v = bval(kk, (int64_t)ch * tlg::kUmmaN + n);
+                const float h = head(v);
+                const size_t off = (size_t)(n >> 3) * (kp * 8) + (size_t)(kk >> 2) * 32 + (n & 7) * 4 + (kk & 3);
+                ub[ch * 2 * half + off] = h;
+                ub[ch * 2 * half + half + off] = head(v - h);
+              }
+        }
         float* dst = reinterpret_cast<float*>(t->host.data() + t->off_tc);
         for (int j = 0; j < t->tc_col_tiles; ++j)
           for (int ks = 0; ks < t->tc_ksteps; ++ks)
@@ -1320,6 +1396,11 @@ tlg_status eval_dispatch(const tlg_tables* t, const tlg_block* b, const tlg_outp
   if (strategy == TLG_STRATEGY_SUMFACT || (is_auto && sumfact_preferred(t))) {
     bool found = false;
     tlg_status st = eval_sumfact(t, b, o, mask, s, &found);
+    if (found) return st;
+  }
+  if (strategy == TLG_STRATEGY_TENSOR || (is_auto && umma_preferred(t))) {
+    bool found = false;
+    tlg_status st = eval_umma(t, b, o, mask, s, &found);
     if (found) return st;
   }
   if (strategy == TLG_STRATEGY_TENSOR || (is_auto && tc_preferred(t))) {
