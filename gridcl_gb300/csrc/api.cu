@@ -285,13 +285,16 @@ bool sumfact_preferred(const tlg_tables* t) { return t->sf_ok && (t->dtype == TL
 // cell): the cooperative kernel instead of the loops kernel.
 bool coop_preferred(const tlg_tables* t) { return t->k > 27; }
 
-// The tensor-core kernel is not in the policy: on GB300 it measured level with the cooperative
-// kernel at P4/P5 tetrahedra and slower at P6 (f32 1.42 ms cooperative, 2.03 ms tensor), with up
-// to 5x the cooperative kernel's error (3xTF32 rounds the tails at 2^-22).
+// The mma.sync kernel is not in the policy: on GB300 it measured level with the cooperative
+// kernel at P4/P5 tetrahedra and slower at P6 (f32 1.42 ms cooperative, 2.03 ms mma.sync), with
+// up to 5x the cooperative kernel's error (3xTF32 rounds the tails at 2^-22).
 bool tc_preferred(const tlg_tables*) { return false; }
 
-// The tcgen05 kernel: not taken by AUTO until measured against the cooperative kernel.
-bool umma_preferred(const tlg_tables*) { return false; }
+// The tcgen05 kernel replaces the cooperative kernel where it applies (f32 and split tables of
+// volume cells in 3D, 27 < K <= 88). GB300, curved tetrahedra 6 x 16^3 at Gauss rules of degree
+// 2p, ms (tcgen05 / cooperative): f32 P4 0.180 / 0.197, P5 0.313 / 0.691, P6 0.629 / 1.436;
+// split P4 0.201 / 0.215, P5 0.465 / 0.765, P6 0.897 / 2.750.
+bool umma_preferred(const tlg_tables* t) { return t->umma_kpad > 0 && t->k > 27; }
 
 // The sum-factorised kernel; `found` is false when it does not apply (no tensor structure, facet
 // normals, split precision at a tile other than 16, or no instantiation): nothing is launched.

@@ -40,6 +40,7 @@ constexpr int kUmmaN = 32;          // columns per chunk: 8 points x (phi, dphi_
 constexpr int kUmmaThreads = 256;
 constexpr int kUmmaTmemCols = 256;  // 2 buffers x 3 coordinates x 32 columns, rounded to a power of 2
 constexpr int kUmmaMaxKpad = 88;
+constexpr int kUmmaFix = 1024;      // split: ill-conditioned points queued per tile
 
 struct UmmaArgs {
   const void* nodes;
@@ -59,10 +60,10 @@ struct UmmaArgs {
 };
 
 // Shared memory: A (3 x 128 x kpad), B (2 buffers x head and tail x 32 x kpad), the exchange
-// (2 directions x 2 warp pairs x 24 values x 64 cells), 4 mbarriers and the tensor-memory
-// address, 1 KiB of alignment slack.
+// (2 directions x 2 warp pairs x 24 values x 64 cells), 4 mbarriers, the tensor-memory address
+// and the queue's count, the queue of ill-conditioned points, 1 KiB of alignment slack.
 inline size_t umma_smem_bytes(int kpad) {
-  return 1024 + (size_t)3 * 128 * kpad * 4 + (size_t)4 * kUmmaN * kpad * 4 + 2 * 48 * 64 * 4 + 64;
+  return 1024 + (size_t)3 * 128 * kpad * 4 + (size_t)4 * kUmmaN * kpad * 4 + 2 * 48 * 64 * 4 + 64 + kUmmaFix * 4;
 }
 
 __device__ __forceinline__ uint32_t umma_tf32_head(float x) {
@@ -191,6 +192,8 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
   float* xch = reinterpret_cast<float*>(smem + 3 * a_bytes + 4 * b_half);  // [2][48][64]
   uint64_t* bars = reinterpret_cast<uint64_t*>(xch + 2 * 48 * 64);         // B[2], MMA[2]
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 4);
+  uint32_t* fix_n = tslot + 1;                                   // queued points of this tile
+  uint32_t* fix = reinterpret_cast<uint32_t*>(bars + 8);         // [kUmmaFix]: (cell << 16) | point
   const uint32_t a_s = (uint32_t)__cvta_generic_to_shared(smem);
   const uint32_t b_s = a_s + 3 * a_bytes;
   const uint32_t bar_s = (uint32_t)__cvta_generic_to_shared(bars);
@@ -211,6 +214,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
   }
   if (tid == 0) {
     for (int i = 0; i < 4; ++i) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_s + 8 * i) : "memory");
+    *fix_n = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   tmem_fence_before();
@@ -390,12 +394,24 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
         float kk[LJ];
         M::pinv(jm, kk);
         float dj = M::detj(jm);
+        bool deferred = false;
         if constexpr (SPLIT) {
-          // Ill-conditioned points: J from the f64 nodes and table, the warp's lanes splitting the
-          // nodes, one flagged lane at a time; det J and K from it in FP64.
+          // Ill-conditioned points go to the tile's queue (J, det J, K and facet normals from
+          // FP64 at the end of the tile); beyond its capacity J comes from the f64 nodes and
+          // table here, the warp's lanes splitting the nodes, one flagged lane at a time.
           const float kap = M::condition(jm, kk);
           const bool need = store && !(kap <= a.cond_limit) && (mask & (kOutJacobian | kOutDetJ | kOutPinv));
-          uint32_t flagged = __ballot_sync(0xFFFFFFFFu, need);
+          bool here = false;
+          if (need) {
+            const uint32_t slot = atomicAdd(fix_n, 1u);
+            if (slot < (uint32_t)kUmmaFix) {
+              fix[slot] = ((uint32_t)c << 16) | (uint32_t)q;
+              deferred = true;
+            } else {
+              here = true;
+            }
+          }
+          uint32_t flagged = __ballot_sync(0xFFFFFFFFu, here);
           while (flagged) {
             const int src = __ffs(flagged) - 1;
             flagged &= flagged - 1;
@@ -417,7 +433,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
             }
           }
         }
-        if (!store) continue;
+        if (!store || deferred) continue;
         if (mask & kOutJacobian) store_point(static_cast<float*>(a.out[1]), tile_idx, q, nq, LJ, tl, 4, jm, LJ);
         if (mask & kOutDetJ) store_point(static_cast<float*>(a.out[2]), tile_idx, q, nq, 1, tl, 4, &dj, 1);
         if (mask & kOutPinv) store_point(static_cast<float*>(a.out[3]), tile_idx, q, nq, LJ, tl, 4, kk, LJ);
@@ -431,6 +447,34 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
       tmem_fence_before();
       __syncthreads();
       tmem_fence_after();
+    }
+    if constexpr (SPLIT) {
+      // The tile's queued points, one per thread: J, det J, K (and facet normals) from FP64.
+      if (good) {
+        const int nfix = min((int)*fix_n, kUmmaFix);
+        __syncthreads();
+        if (tid == 0) *fix_n = 0;  // the next tile's gather ends with a barrier
+        for (int e = tid; e < nfix; e += kUmmaThreads) {
+          const int fc = (int)(fix[e] >> 16), fq = (int)(fix[e] & 0xFFFFu);
+          const int64_t fcr = tile * kUmmaCells + fc;
+          const int64_t fcell = min(a.first_cell + fcr, a.last_cell);
+          float jr[LJ], kr[LJ], dr;
+          recompute_f64_rt<TD, GD>(static_cast<const double*>(a.nodes), a.dofmap + fcell * K, K, a.last_node,
+                                   a.dphi64 + (int64_t)fq * K * TD, jr, &dr, kr, 1);
+          const int64_t fo = a.out_first_cell + fcr;
+          const int64_t ft = fo >> 4;
+          const int fl = (int)(fo & 15);
+          if (mask & kOutJacobian) store_point(static_cast<float*>(a.out[1]), ft, fq, nq, LJ, fl, 4, jr, LJ);
+          if (mask & kOutDetJ) store_point(static_cast<float*>(a.out[2]), ft, fq, nq, 1, fl, 4, &dr, 1);
+          if (mask & kOutPinv) store_point(static_cast<float*>(a.out[3]), ft, fq, nq, LJ, fl, 4, kr, LJ);
+          if (mask & kOutFacetNormals) {
+            float n[GD];
+            M::facet_normal(kr, a.refn + fq * TD, n);
+            store_point(static_cast<float*>(a.out[5]), ft, fq, nq, GD, fl, 4, n, GD);
+          }
+          if (a.recomputed && fcr < a.range_cells) atomicAdd(a.recomputed, 1ull);
+        }
+      }
     }
   }
   if (!good) {
