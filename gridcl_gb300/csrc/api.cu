@@ -1174,7 +1174,8 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       t->umma_kpad = (int)((k + 7) / 8 * 8);
       t->umma_chunks = (int)((npoints + tlg::kUmmaPoints - 1) / tlg::kUmmaPoints);
       t->off_umma = align16(host_bytes);
-      host_bytes = t->off_umma + (size_t)t->umma_chunks * 2 * tlg::kUmmaN * t->umma_kpad * 4;
+      // Zero chunks after the last, for work items whose last group runs past it.
+      host_bytes = t->off_umma + (size_t)(t->umma_chunks + tlg::kUmmaMaxGroups - 1) * 2 * tlg::kUmmaN * t->umma_kpad * 4;
     }
     t->host.assign(host_bytes, 0);
     if (t->sf_ok) {

@@ -18,9 +18,9 @@
 // in the canonical K-major layout without swizzle (8-row x 16-byte core matrices; core matrices
 // along K 128 bytes apart, 8-row blocks kpad * 32 bytes apart); the tables are laid out on the host
 // in the same form per chunk of 8 points and copied in by cp.async.bulk (double-buffered, an
-// mbarrier per buffer). One thread issues the MMAs of the next chunk into the second accumulator
-// buffer while all threads run the epilogue of the current one; tcgen05.commit arrives on the
-// chunk's mbarrier. Tensor memory: 2 buffers x 3 coordinates x 32 columns, allocated as 256
+// mbarrier per buffer). A ninth warp issues the copies, and the MMAs of the next chunk into the
+// second accumulator buffer while the other eight run the epilogue of the current one;
+// tcgen05.commit arrives on the chunk's mbarrier. Tensor memory: 2 buffers x 3 coordinates x 32 columns, allocated as 256
 // columns; the launch's shared memory keeps at most two CTAs on an SM, so that the allocations
 // never wait. Every wait is bounded: on expiry the CTA records an error, waits (bounded) for what
 // it has in flight, frees its tensor memory and returns.
@@ -37,7 +37,9 @@ namespace tlg {
 constexpr int kUmmaCells = 64;      // cells per tile
 constexpr int kUmmaPoints = 8;      // points per chunk
 constexpr int kUmmaN = 32;          // columns per chunk: 8 points x (phi, dphi_0, dphi_1, dphi_2)
-constexpr int kUmmaThreads = 256;
+constexpr int kUmmaEpi = 256;       // eight epilogue warps
+constexpr int kUmmaThreads = 288;   // and one warp that issues the copies and the MMAs
+constexpr int kUmmaIssuer = 256;    // its first thread
 constexpr int kUmmaTmemCols = 256;  // 2 buffers x 3 coordinates x 32 columns, rounded to a power of 2
 constexpr int kUmmaMaxKpad = 88;
 constexpr int kUmmaFix = 1024;      // split: ill-conditioned points queued per tile
@@ -57,7 +59,12 @@ struct UmmaArgs {
   float cond_limit;
   uint32_t last_node, mask;
   int k, kpad, num_points, chunks;
+  // Work items: each tile's chunks in `groups` groups of `per_group` (the last ones padded with
+  // zero tables; the table section holds chunks + kUmmaMaxGroups - 1 chunks).
+  int groups, per_group;
 };
+
+constexpr int kUmmaMaxGroups = 8;
 
 // Shared memory: A (3 x 128 x kpad), B (2 buffers x head and tail x 32 x kpad), the exchange
 // (2 directions x 2 warp pairs x 24 values x 64 cells), 4 mbarriers, the tensor-memory address
@@ -185,7 +192,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
   // 1 KiB-aligned base (the operands' descriptors address 16-byte units).
   const uint32_t raw_s = (uint32_t)__cvta_generic_to_shared(smem_raw);
   unsigned char* smem = smem_raw + (((raw_s + 1023u) & ~1023u) - raw_s);
-  const int kpad = a.kpad, K = a.k, nq = a.num_points, nch = a.chunks;
+  const int kpad = a.kpad, K = a.k, nq = a.num_points;
   const uint32_t a_bytes = 128u * kpad * 4u;      // one coordinate's A
   const uint32_t b_half = (uint32_t)kUmmaN * kpad * 4u;  // head or tail of one B chunk
   const uint32_t sbo = (uint32_t)kpad * 32u;        // 8-row blocks
@@ -203,6 +210,8 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
   const NT* nodes = static_cast<const NT*>(a.nodes);
   const uint32_t mask = a.mask;
   const int64_t tiles = (a.padded + kUmmaCells - 1) / kUmmaCells;
+  const int cpg = a.per_group;
+  const int64_t items = tiles * a.groups;
   constexpr uint32_t kIdesc = umma_idesc(128, kUmmaN);
 
   if (warp == 0) {
@@ -222,16 +231,18 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
   tmem_fence_after();
   const uint32_t tmem = *tslot;
 
-  // Chunk sequence of this CTA: chunk j of its i-th tile is number i * nch + j; it uses B and
-  // accumulator buffer (number & 1).
-  auto exists = [&](int64_t seq) { return (int64_t)blockIdx.x + (seq / nch) * (int64_t)gridDim.x < tiles; };
+  // Chunk sequence of this CTA: chunk j of its i-th work item is number i * cpg + j; it uses B and
+  // accumulator buffer (number & 1). Item t covers tile t / groups, chunks (t % groups) * cpg + j.
+  auto item_of = [&](int64_t seq) { return (int64_t)blockIdx.x + (seq / cpg) * (int64_t)gridDim.x; };
+  auto exists = [&](int64_t seq) { return item_of(seq) < items; };
+  auto chunk_of = [&](int64_t seq) { return (int)(item_of(seq) % a.groups) * cpg + (int)(seq % cpg); };
   uint32_t ph_b[2] = {0u, 0u}, ph_m[2] = {0u, 0u};
   bool pend_b[2] = {false, false}, pend_m[2] = {false, false};  // thread 0: in flight
   const uint32_t bbytes = 2 * b_half;
-  if (tid == 0 && issue_copies) {
+  if (tid == kUmmaIssuer && issue_copies) {
     for (int s = 0; s < 2; ++s)
       if (exists(s)) {
-        umma_load_b(a, b_s + s * bbytes, bar_s + 8 * s, s % nch, bbytes);
+        umma_load_b(a, b_s + s * bbytes, bar_s + 8 * s, chunk_of(s), bbytes);
         pend_b[s] = true;
       }
   }
@@ -261,7 +272,8 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
   // tail-row warps 4-7, two per warp (w / 4 picks which two); each sends its rows' values of the
   // two points its partner (the warp with the other rows of the same cells and the same w / 4)
   // finishes.
-  const int qd = warp & 3, sub = warp >> 2;
+  const bool mma_warp = warp == kUmmaEpi / 32;
+  const int qd = warp & 3, sub = (warp >> 2) & 1;
   const bool top = qd < 2;
   const int c = (qd & 1) * 32 + lane;              // this thread's cell in the tile
   const int own0 = (top ? 0 : 4) + 2 * sub;        // first of the two points this warp finishes
@@ -270,10 +282,12 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
   const float* xs_in = xch + (top ? 3072 : 0) + sub * 1536;
   bool good = true;
   int64_t seq = 0;
-  for (int64_t tile = blockIdx.x; tile < tiles && good; tile += gridDim.x) {
-    // Gather: thread (cell tid % 64, nodes k = tid / 64 (mod threads / 64)) writes heads to row
-    // c, tails to row 64 + c of each coordinate's A.
-    {
+  for (int64_t item = blockIdx.x; item < items && good; item += gridDim.x) {
+    const int64_t tile = item / a.groups;
+    const int chunk0 = (int)(item % a.groups) * cpg;
+    // Gather: epilogue thread (cell tid % 64, nodes k = tid / 64 (mod 4)) writes heads to row c,
+    // tails to row 64 + c of each coordinate's A.
+    if (tid < kUmmaEpi) {
       const int gc = tid & 63;
       const int64_t cell = min(a.first_cell + tile * kUmmaCells + gc, a.last_cell);
       const uint32_t* row = a.dofmap + cell * K;
@@ -281,7 +295,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
       const uint32_t n0 = min(__ldg(row), a.last_node);
 #pragma unroll
       for (int g = 0; g < GD; ++g) x0[g] = __ldg(nodes + (int64_t)n0 * GD + g);
-      for (int k = tid >> 6; k < kpad; k += kUmmaThreads / 64) {
+      for (int k = tid >> 6; k < kpad; k += kUmmaEpi / 64) {
         float y[GD];
         if (k < K) {
           const uint32_t n = min(__ldg(row + k), a.last_node);
@@ -311,7 +325,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
     __syncthreads();
     tmem_fence_after();
     int ok = 1;
-    if (tid == 0) ok = issue(seq);
+    if (tid == kUmmaIssuer) ok = issue(seq);
 
     // This thread's cell: its first node plus the origin (split: as an f32 pair), its output slot.
     const int64_t cr = tile * kUmmaCells + c;  // cell index in the range
@@ -336,23 +350,22 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
     const int64_t tile_idx = o >> 4;
     const int tl = (int)(o & 15);
 
-    for (int j = 0; j < nch; ++j, ++seq) {
+    for (int j = 0; j < cpg; ++j, ++seq) {
       const int buf = (int)(seq & 1);
-      if (tid == 0 && ok && j + 1 < nch) ok = issue(seq + 1);
       // Chunk j's accumulators (and its B buffer free again). The tensor-memory loads are
       // warp-collective: a warp loads only when all its lanes saw the chunk complete.
       bool done = ok && umma_wait(bar_s + 16 + 8 * buf, ph_m[buf], polls);
       if (done) {
         ph_m[buf] ^= 1u;
-        if (tid == 0) pend_m[buf] = false;
+        if (tid == kUmmaIssuer) pend_m[buf] = false;
       }
       tmem_fence_after();
-      if (tid == 0 && done && issue_copies && exists(seq + 2)) {
-        umma_load_b(a, b_s + buf * bbytes, bar_s + 8 * buf, (int)((seq + 2) % nch), bbytes);
+      if (tid == kUmmaIssuer && done && issue_copies && exists(seq + 2)) {
+        umma_load_b(a, b_s + buf * bbytes, bar_s + 8 * buf, chunk_of(seq + 2), bbytes);
         pend_b[buf] = true;
       }
       const uint32_t trow = tmem + ((uint32_t)(qd * 32) << 16) + (uint32_t)(buf * 96);
-      if (__all_sync(0xFFFFFFFFu, done)) {
+      if (!mma_warp && __all_sync(0xFFFFFFFFu, done)) {
 #pragma unroll
         for (int g = 0; g < GD; ++g) {
           float v[8];
@@ -365,6 +378,15 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
         good = false;
         break;
       }
+      if (mma_warp) {
+        // The next chunk's MMAs while the epilogue warps finish this one (its accumulator buffer
+        // was freed by the previous chunk's closing barrier, its tables copied a chunk ago).
+        if (tid == kUmmaIssuer && ok && j + 1 < cpg) ok = issue(seq + 1);
+        tmem_fence_before();
+        __syncthreads();
+        tmem_fence_after();
+        continue;
+      }
       float u[GD][8];  // column 4 p + r of this warp's two points: r = 0 phi, 1 + d dphi_d
 #pragma unroll
       for (int g = 0; g < GD; ++g) {
@@ -374,7 +396,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
       }
 #pragma unroll
       for (int p = 0; p < 2; ++p) {
-        const int q = j * kUmmaPoints + own0 + p;
+        const int q = (chunk0 + j) * kUmmaPoints + own0 + p;
         if (q >= nq) continue;  // the same for the whole warp
         float x[GD], jm[LJ];
 #pragma unroll
@@ -454,7 +476,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
         const int nfix = min((int)*fix_n, kUmmaFix);
         __syncthreads();
         if (tid == 0) *fix_n = 0;  // the next tile's gather ends with a barrier
-        for (int e = tid; e < nfix; e += kUmmaThreads) {
+        for (int e = tid; e < nfix; e += kUmmaThreads) {  // the issuing warp too
           const int fc = (int)(fix[e] >> 16), fq = (int)(fix[e] & 0xFFFFu);
           const int64_t fcr = tile * kUmmaCells + fc;
           const int64_t fcell = min(a.first_cell + fcr, a.last_cell);
@@ -480,7 +502,7 @@ __global__ void __launch_bounds__(kUmmaThreads, 1) umma_eval_kernel(const __grid
   if (!good) {
     // A wait expired: record it, let what is in flight land (bounded), then free the tensor
     // memory.
-    if (tid == 0) {
+    if (tid == kUmmaIssuer) {
       if (a.err) atomicExch(a.err, 1);
       for (int b = 0; b < 2; ++b) {
         if (pend_m[b]) umma_wait(bar_s + 16 + 8 * b, ph_m[b], polls);
