@@ -74,6 +74,8 @@ def parse():
     p.add_argument("--fd-nodes", type=int, default=1000, help="nodes of the adjoint's central-difference check")
     p.add_argument("--hex-n", type=int, default=64, help="hexahedra per direction (hex_strategies)")
     p.add_argument("--ho-n", type=int, default=16, help="subcells per direction (high_order)")
+    p.add_argument("--ho-degree", type=int, default=6, help="degree (high_order_case)")
+    p.add_argument("--ho-precision", default="f32", choices=("f32", "split", "f64"), help="(high_order_case)")
     return p.parse_args()
 
 
@@ -707,11 +709,13 @@ def extra_hex_strategies(n: int = 64, cell: str = "Hexahedron"):
     return out
 
 
-def extra_high_order(n: int = 16):
+def extra_high_order(n: int = 16, full: bool = True):
     """Curved tetrahedra P4-P6 (6 n^3 cells, 35 / 56 / 84 nodes) at the collapsed Gauss rules of
-    degree 2p, x/J/detJ/K, under the loops (global tables), shared (staged tables), cooperative
-    and tensor-core kernels and AUTO, in split precision, f64 and f32: ms per launch and the family.
-    Run with --workload high_order (not part of the default run)."""
+    degree 2p, x/J/detJ/K: ms per launch and the family that ran, with the stores' bandwidth
+    (Q points x 22 f32 outputs). `full`: the loops (global tables), shared (staged tables),
+    cooperative and tensor-core kernels and AUTO in split precision, f64 and f32 (run with
+    --workload high_order); otherwise (the default run) the tcgen05 and cooperative kernels and AUTO
+    in split precision and f32."""
     import torch
 
     import gridcl_gb300 as tg
@@ -719,27 +723,55 @@ def extra_high_order(n: int = 16):
 
     names = ("points", "jacobian", "detj", "pinv")
     out = {"workload": f"curved tetrahedra P4-P6, 6x{n}^3 cells, Gauss rules of degree 2p, x/J/detJ/K"}
+    precisions = ((("split", torch.float64), ("native", torch.float64), ("native", torch.float32)) if full
+                  else (("split", torch.float64), ("native", torch.float32)))
+    strategies = ("loops", "shared", "cooperative", "tensor", "auto") if full else ("cooperative", "tensor", "auto")
     for degree in (4, 5, 6):
         mesh = meshes.curved_box("Tetrahedron", n, degree, jitter=0.02)
         pts, w = tg.refcell.gauss_rule("Tetrahedron", 2 * degree)
         ps = tg.PointSet("Tetrahedron", pts, w)
         qpts = mesh.blocks[0].num_cells * len(ps)
-        for prec, dt in (("split", torch.float64), ("native", torch.float64), ("native", torch.float32)):
+        for prec, dt in precisions:
             g = tg.Geometry.from_host(mesh, dtype=dt)
             row = {"qpoints": int(qpts)}
-            for strat in ("loops", "shared", "cooperative", "tensor", "auto"):
+            for strat in strategies:
                 with tg.with_strategy(strat):
                     f = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
                     fam = tg.last_kernel_family()
                     ms = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, names, out=f, precision=prec),
                                   reps=3, warm=1)
-                row[strat] = {"family": fam, "ms": ms, "gpts_per_s": qpts / (ms * 1e-3) / 1e9}
+                ob = 8 if (dt == torch.float64 and prec == "native") else 4
+                row[strat] = {"family": fam, "ms": ms, "gpts_per_s": qpts / (ms * 1e-3) / 1e9,
+                              "store_gbs": qpts * 22 * ob / (ms * 1e-3) / 1e9}
                 del f
+            if "tensor" in row and "cooperative" in row:
+                row["tensor_over_cooperative"] = row["cooperative"]["ms"] / row["tensor"]["ms"]
             label = "split" if prec == "split" else ("f64" if dt == torch.float64 else "f32")
             out[f"P{degree}_{label}"] = row
             del g
             torch.cuda.empty_cache()
     return out
+
+
+def extra_high_order_case(n: int, degree: int, precision: str):
+    """One high-order case for profiling: curved P`degree` tetrahedra 6 n^3, Gauss rule of degree
+    2p, x/J/detJ/K under AUTO (the tcgen05 kernel for f32 and split), four launches; the family
+    and the last launch's ms."""
+    import torch
+
+    import gridcl_gb300 as tg
+    from gridcl_gb300 import meshes
+
+    mesh = meshes.curved_box("Tetrahedron", n, degree, jitter=0.02)
+    pts, w = tg.refcell.gauss_rule("Tetrahedron", 2 * degree)
+    ps = tg.PointSet("Tetrahedron", pts, w)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float32 if precision == "f32" else torch.float64)
+    prec = "split" if precision == "split" else "native"
+    names = ("points", "jacobian", "detj", "pinv")
+    f = tg.geometric_factors_block(g, 0, ps, names, precision=prec)
+    ms = event_ms(lambda: tg.geometric_factors_block(g, 0, ps, names, out=f, precision=prec), reps=1, warm=2)
+    return {"workload": f"curved P{degree} tetrahedra 6x{n}^3, {len(ps)} points, {precision}",
+            "family": tg.last_kernel_family(), "ms": ms}
 
 
 def extra_p1_box():
@@ -949,7 +981,7 @@ def run_ours(args):
                              ("sphere_surface", extra_sphere),
                              ("q2_forward_adjoint", lambda: extra_adjoint(args.adjoint_n, args.fd_nodes)),
                              ("pull_back", extra_pull_back), ("ordering", extra_ordering),
-                             ("p1_box", extra_p1_box)):
+                             ("p1_box", extra_p1_box), ("high_order", lambda: extra_high_order(args.ho_n, False))):
                 try:
                     workloads[name] = fn()
                 except Exception as exc:  # reported, not fatal: the main line stands
@@ -966,7 +998,7 @@ def run_ours(args):
 
 
 EXTRAS = ("hybrid_batched", "sphere_surface", "q2_forward_adjoint", "pull_back", "ordering", "p1_box",
-          "hex_strategies", "prism_strategies", "high_order", "hybrid_forward_adjoint")
+          "hex_strategies", "prism_strategies", "high_order", "hybrid_forward_adjoint", "high_order_case")
 
 
 def run_extra(args):
@@ -980,6 +1012,7 @@ def run_extra(args):
           "hex_strategies": lambda: extra_hex_strategies(args.hex_n),
           "prism_strategies": lambda: extra_hex_strategies(args.hex_n, "Prism"),
           "high_order": lambda: extra_high_order(args.ho_n),
+          "high_order_case": lambda: extra_high_order_case(args.ho_n, args.ho_degree, args.ho_precision),
           "hybrid_forward_adjoint": extra_hybrid_adjoint}[args.workload]
     print(json.dumps(fn()), flush=True)
 
