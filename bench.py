@@ -331,6 +331,23 @@ def event_ms(fn, reps: int = 5, warm: int = 2) -> float:
     return a.elapsed_time(b) / reps
 
 
+def median_launch_ms(fn, n: int = 15) -> float:
+    """The median of `n` launches timed one by one with CUDA events (after two untimed ones)."""
+    import torch
+
+    fn()
+    fn()
+    times = []
+    for _ in range(n):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return float(np.median(times))
+
+
 def rel_err_fields(a: dict, b: dict) -> dict:
     out = {}
     for k in a:
@@ -376,10 +393,12 @@ def extra_hybrid():
         b: errors_vs_oracle(plain_out[b], want[b], samples[b]) for b in range(len(g.blocks))}
     for precision in ("native", "df64", "split"):
         batch = tg.Batch(g, rule, factors=factors, precision=precision)
-        grids = batch.tune()
+        batch.tune()
         ms = event_ms(batch.launch, reps=10)
+        single = median_launch_ms(batch.launch, 15)
         key = {"native": "batched_fp64_graph", "df64": "batched_df64_graph", "split": "batched_split_graph"}[precision]
-        res[key] = {"ms": ms, "value": qpts / (ms * 1e-3), "tuned_grids": grids,
+        res[key] = {"ms": ms, "value": qpts / (ms * 1e-3), "tuning": batch.tuning(),
+                    "median_single_launch_ms": single,
                     "speedup_vs_plain_fp64": plain_ms / ms,
                     "error_vs_oracle": {b: errors_vs_oracle(batch.fields[b], want[b], samples[b])
                                         for b in range(len(g.blocks))}}

@@ -35,6 +35,7 @@ struct tlg_batch {
   std::vector<tlg_outputs> outputs;
   std::vector<int> grid;  // launch grid per block (0: the kernel's persistent default)
   bool serial = false;    // the blocks one after another instead of parallel graph branches
+  float tuned_ms = 0.0f;  // the tuner's median time of the chosen graph (0: not tuned here)
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> events;  // fork, then one join per block
   cudaStream_t capture = nullptr;
@@ -1921,7 +1922,7 @@ std::string tune_key(const tlg_tables* t, const tlg_outputs* o, int64_t cells) {
   int bucket = 0;
   while ((int64_t(1) << bucket) < cells) ++bucket;
   char buf[160];
-  std::snprintf(buf, sizeof(buf), "d%d t%d g%d k%lld q%lld c%d o%d%d%d%d%d%d", t->dtype, t->td, t->gd,
+  std::snprintf(buf, sizeof(buf), "d%d%s t%d g%d k%lld q%lld c%d o%d%d%d%d%d%d", t->dtype, t->df ? "df" : "", t->td, t->gd,
                 (long long)t->k, (long long)t->q, bucket, o->points != nullptr, o->jacobian != nullptr,
                 o->detj != nullptr, o->pinv != nullptr, o->normals != nullptr, o->facet_normals != nullptr);
   return buf;
@@ -1995,23 +1996,30 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
   cudaEvent_t t0, t1;
   cudaEventCreate(&t0);
   cudaEventCreate(&t1);
-  // The median of five launches timed one by one (after `fn` has run once untimed): robust
+  // The median of `n` launches timed one by one (after `fn` has run once untimed): robust
   // against a launch slowed by a clock or power transition, which an average of back-to-back
   // launches is not.
-  auto median_ms = [&](auto fn, float* ms) -> tlg_status {
+  auto median_ms = [&](auto fn, float* ms, int n = 7) -> tlg_status {
     tlg_status st = fn();
-    float t[5] = {0, 0, 0, 0, 0};
-    for (int r = 0; r < 5 && st == TLG_OK; ++r) {
+    float t[15];
+    n = std::min(n, 15);
+    for (int r = 0; r < n && st == TLG_OK; ++r) {
       cudaEventRecord(t0, s);
       st = fn();
       cudaEventRecord(t1, s);
       cudaEventSynchronize(t1);
       cudaEventElapsedTime(&t[r], t0, t1);
     }
-    std::sort(t, t + 5);
-    *ms = t[2];
+    std::sort(t, t + n);
+    *ms = t[n / 2];
     return st;
   };
+  auto finish = [&](tlg_status st) {
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    return st;
+  };
+  const int cands[] = {0, 1, 2, 3, 4, 6, 8};  // CTAs per SM of the persistent grid (0: occupancy)
   for (size_t i = 0; i < b->tables.size(); ++i) {
     const std::string key = tune_key(b->tables[i], &b->outputs[i], b->outputs[i].num_cells);
     int mult = -1;
@@ -2021,20 +2029,15 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
       if (it != g_tune_cache.end()) mult = it->second;
     }
     if (mult < 0) {
-      // Candidates: CTAs per SM of the persistent grid (0: the occupancy limit).
-      const int cands[] = {0, 1, 2, 3, 4, 6, 8};
       float best = 1e30f;
       mult = 0;
       for (int c : cands) {
         const int grid = c == 0 ? 0 : c * sms;
         float ms = 0.0f;
         tlg_status st = median_ms([&] { return eval_with_grid(b, i, s, grid); }, &ms);
-        if (st != TLG_OK) {
-          cudaEventDestroy(t0);
-          cudaEventDestroy(t1);
-          return st;
-        }
-        if (ms < best) {
+        if (st != TLG_OK) return finish(st);
+        // A candidate replaces the occupancy default only when more than 1 % faster.
+        if (ms < (c == 0 ? best : 0.99f * best)) {
           best = ms;
           mult = c;
         }
@@ -2044,9 +2047,13 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
     }
     b->grid[i] = mult == 0 ? 0 : mult * sms;
   }
-  // Joint pass: the graph runs the blocks concurrently, so each block's best grid alone is only
-  // the start. One round of coordinate descent over each block's candidates, timing the whole
-  // graph (the median of five launches), keeps a change only when the graph gets faster.
+  // Joint pass: the graph runs the blocks concurrently (or in turn), so each block's best grid
+  // alone is only the start. Every comparison times the whole graph, the median of 9 launches,
+  // and a change is kept only when more than 1 % faster, so that run-to-run noise does not pick
+  // the configuration: parallel branches against a serial chain (the concurrent branches of
+  // persistent kernels share the SMs in an order the hardware picks; the chain is kept unless
+  // the branches are more than 3 % faster), one round of coordinate descent over each block's
+  // grid candidates, and the result against every block at its occupancy default.
   std::string batch_key;
   for (size_t i = 0; i < b->tables.size(); ++i)
     batch_key += tune_key(b->tables[i], &b->outputs[i], b->outputs[i].num_cells) + ";";
@@ -2056,26 +2063,24 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
     auto it = g_joint_cache.find(batch_key);
     if (it != g_joint_cache.end()) joint = it->second;
   }
+  auto time_graph = [&](float* ms) -> tlg_status {
+    destroy_graph(b);
+    return median_ms([&] { return tlg_batch_launch(b, s); }, ms, 9);
+  };
   if (joint.size() == b->tables.size() + 1) {
     for (size_t i = 0; i < b->tables.size(); ++i) b->grid[i] = joint[i];
     b->serial = joint.back() != 0;
   } else if (b->tables.size() > 1) {
-    auto time_graph = [&](float* ms) -> tlg_status {
-      destroy_graph(b);
-      return median_ms([&] { return tlg_batch_launch(b, s); }, ms);
-    };
-    // Parallel branches or a serial chain: the concurrent branches of persistent kernels share
-    // the SMs in an order the hardware picks, which can cost more than running them in turn.
-    float best = 0.0f, serial_ms = 0.0f;
-    b->serial = false;
-    tlg_status st = time_graph(&best);
+    float serial_ms = 0.0f, par_ms = 0.0f, best = 0.0f;
+    b->serial = true;
+    tlg_status st = time_graph(&serial_ms);
     if (st == TLG_OK) {
-      b->serial = true;
-      st = time_graph(&serial_ms);
-      if (serial_ms < best) best = serial_ms;
-      else b->serial = false;
+      b->serial = false;
+      st = time_graph(&par_ms);
     }
-    const int cands[] = {0, 1, 2, 3, 4, 6, 8};
+    if (st != TLG_OK) return finish(st);
+    b->serial = !(par_ms < 0.97f * serial_ms);
+    best = b->serial ? serial_ms : par_ms;
     for (size_t i = 0; i < b->tables.size() && st == TLG_OK; ++i) {
       const int keep = b->grid[i];
       int chosen = keep;
@@ -2086,30 +2091,53 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
         float ms = 0.0f;
         st = time_graph(&ms);
         if (st != TLG_OK) break;
-        if (ms < best) {
+        if (ms < 0.99f * best) {
           best = ms;
           chosen = grid;
         }
       }
       b->grid[i] = chosen;
     }
-    if (st != TLG_OK) {
-      cudaEventDestroy(t0);
-      cudaEventDestroy(t1);
-      return st;
+    if (st != TLG_OK) return finish(st);
+    // The untuned graph (occupancy grids, serial chain) against the result, timed again.
+    const std::vector<int> tuned = b->grid;
+    const bool tuned_serial = b->serial;
+    float base_ms = 0.0f, again_ms = 0.0f;
+    for (auto& gi : b->grid) gi = 0;
+    b->serial = true;
+    st = time_graph(&base_ms);
+    b->grid = tuned;
+    b->serial = tuned_serial;
+    if (st == TLG_OK) st = time_graph(&again_ms);
+    if (st != TLG_OK) return finish(st);
+    if (!(again_ms < 0.99f * base_ms)) {
+      for (auto& gi : b->grid) gi = 0;
+      b->serial = true;
     }
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     std::vector<int> rec = b->grid;
     rec.push_back(b->serial ? 1 : 0);
     g_joint_cache[batch_key] = rec;
   }
+  if (!b->tables.empty()) {
+    float ms = 0.0f;
+    tlg_status st = time_graph(&ms);
+    if (st != TLG_OK) return finish(st);
+    b->tuned_ms = ms;
+  }
   if (grids)
     for (size_t i = 0; i < b->tables.size(); ++i) grids[i] = b->grid[i];
-  cudaEventDestroy(t0);
-  cudaEventDestroy(t1);
+  finish(TLG_OK);
   destroy_graph(b);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "tlg_batch_tune");
+  return ok();
+}
+
+tlg_status tlg_batch_tuning(const tlg_batch* b, int* serial, float* ms) {
+  if (!b) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_batch_tuning: NULL batch");
+  if (serial) *serial = b->serial ? 1 : 0;
+  if (ms) *ms = b->tuned_ms;
   return ok();
 }
 

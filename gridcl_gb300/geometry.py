@@ -692,6 +692,13 @@ class Batch:
         self.grids = list(grids)[: len(self.fields)]
         return self.grids
 
+    def tuning(self) -> dict:
+        """The tuner's choice: ``{"grids", "serial" (a chain rather than parallel branches),
+        "tuned_ms" (its median time of the chosen graph)}``."""
+        serial, ms = ctypes.c_int(0), ctypes.c_float(0.0)
+        check(lib().tlg_batch_tuning(self.handle, ctypes.byref(serial), ctypes.byref(ms)))
+        return {"grids": list(self.grids), "serial": bool(serial.value), "tuned_ms": float(ms.value)}
+
     def launch(self) -> None:
         check(lib().tlg_batch_launch(self.handle, current_stream_handle()))
 

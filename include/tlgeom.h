@@ -194,14 +194,21 @@ tlg_status tlg_batch_create(const tlg_tables* const* tables, const tlg_block* bl
                             const tlg_outputs* outputs, int num_blocks, tlg_batch** out);
 tlg_status tlg_batch_destroy(tlg_batch* batch);
 
-/* Times candidate persistent grids (0 and 1..8 CTAs per SM) for each block on `stream`, keeps the
- * fastest, and caches the choice per launch shape for the process; then times the whole graph
- * with the blocks as parallel branches and as a serial chain, keeps the faster, and runs one
- * round of coordinate descent over each block's candidates timing the whole graph (cached per
- * batch shape). grids[i] (may be NULL) receives block i's grid (0: the
- * occupancy limit). Runs the blocks' kernels; call it outside stream capture. Rebuilds the graph
- * on the next launch. */
+/* Times candidate persistent grids (0 and 1..8 CTAs per SM) for each block on `stream` (the
+ * median of 7 launches), keeps the fastest (a grid replaces the occupancy limit only when more
+ * than 1 % faster), and caches the choice per launch shape for the process; then, timing the
+ * whole graph (the median of 9 launches), takes parallel branches over a serial chain only when
+ * more than 3 % faster, runs one round of coordinate descent over each block's candidates
+ * (changes kept when more than 1 % faster), and keeps the result only when more than 1 % faster
+ * than every block at its occupancy limit in a serial chain (cached per batch shape). grids[i]
+ * (may be NULL) receives block i's grid (0: the occupancy limit). Runs the blocks' kernels; call
+ * it outside stream capture. Rebuilds the graph on the next launch. */
 tlg_status tlg_batch_tune(tlg_batch* batch, void* stream, int* grids);
+
+/* After tlg_batch_tune: whether the graph runs the blocks as a serial chain (1) or as parallel
+ * branches (0), and the tuner's median time of the chosen graph in ms. No counterpart in the
+ * reference. */
+tlg_status tlg_batch_tuning(const tlg_batch* batch, int* serial, float* ms);
 
 /* Evaluates every block: one launch of a CUDA graph (captured on the first call). */
 tlg_status tlg_batch_launch(tlg_batch* batch, void* stream);
