@@ -111,7 +111,10 @@ typedef struct tlg_tables tlg_tables;
 
 /* `points` `[q][tdim]` in reference coordinates; `ref_normals` `[q][tdim]` or NULL (the
  * per-point reference facet normals of a FacetPointSet, facet_rule.rs). gdim is the
- * geometric dimension of the grids the tables will serve. Allocates device memory. */
+ * geometric dimension of the grids the tables will serve. Every cell type but the point, pyramids
+ * included (their rational Lagrange space, tetraloma-refcell/src/polynomials/pyramid.rs; GLL
+ * nodes on intervals, quadrilaterals and hexahedra only, as the reference). Allocates device
+ * memory. */
 tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dtype,
                              const double* points, int64_t npoints, const double* ref_normals,
                              tlg_tables** out);
