@@ -1999,7 +1999,7 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
   // The median of `n` launches timed one by one (after `fn` has run once untimed): robust
   // against a launch slowed by a clock or power transition, which an average of back-to-back
   // launches is not.
-  auto median_ms = [&](auto fn, float* ms, int n = 7) -> tlg_status {
+  auto median_ms = [&](auto fn, float* ms, int n = 7, float* mean = nullptr) -> tlg_status {
     tlg_status st = fn();
     float t[15];
     n = std::min(n, 15);
@@ -2012,6 +2012,11 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
     }
     std::sort(t, t + n);
     *ms = t[n / 2];
+    if (mean) {
+      float sum = 0.0f;
+      for (int r = 0; r < n; ++r) sum += t[r];
+      *mean = sum / n;
+    }
     return st;
   };
   auto finish = [&](tlg_status st) {
@@ -2063,23 +2068,24 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
     auto it = g_joint_cache.find(batch_key);
     if (it != g_joint_cache.end()) joint = it->second;
   }
-  auto time_graph = [&](float* ms) -> tlg_status {
+  auto time_graph = [&](float* ms, float* mean = nullptr) -> tlg_status {
     destroy_graph(b);
-    return median_ms([&] { return tlg_batch_launch(b, s); }, ms, 9);
+    return median_ms([&] { return tlg_batch_launch(b, s); }, ms, 9, mean);
   };
   if (joint.size() == b->tables.size() + 1) {
     for (size_t i = 0; i < b->tables.size(); ++i) b->grid[i] = joint[i];
     b->serial = joint.back() != 0;
   } else if (b->tables.size() > 1) {
-    float serial_ms = 0.0f, par_ms = 0.0f, best = 0.0f;
+    float serial_ms = 0.0f, par_ms = 0.0f, serial_mean = 0.0f, par_mean = 0.0f, best = 0.0f;
     b->serial = true;
-    tlg_status st = time_graph(&serial_ms);
+    tlg_status st = time_graph(&serial_ms, &serial_mean);
     if (st == TLG_OK) {
       b->serial = false;
-      st = time_graph(&par_ms);
+      st = time_graph(&par_ms, &par_mean);
     }
     if (st != TLG_OK) return finish(st);
-    b->serial = !(par_ms < 0.97f * serial_ms);
+    // Branches only when faster in the median and in the mean (their times spread more).
+    b->serial = !(par_ms < 0.97f * serial_ms && par_mean < 0.97f * serial_mean);
     best = b->serial ? serial_ms : par_ms;
     for (size_t i = 0; i < b->tables.size() && st == TLG_OK; ++i) {
       const int keep = b->grid[i];

@@ -201,7 +201,7 @@ tlg_status tlg_batch_destroy(tlg_batch* batch);
  * median of 7 launches), keeps the fastest (a grid replaces the occupancy limit only when more
  * than 1 % faster), and caches the choice per launch shape for the process; then, timing the
  * whole graph (the median of 9 launches), takes parallel branches over a serial chain only when
- * more than 3 % faster, runs one round of coordinate descent over each block's candidates
+ * more than 3 % faster in the median and in the mean of those launches, runs one round of coordinate descent over each block's candidates
  * (changes kept when more than 1 % faster), and keeps the result only when more than 1 % faster
  * than every block at its occupancy limit in a serial chain (cached per batch shape). grids[i]
  * (may be NULL) receives block i's grid (0: the occupancy limit). Runs the blocks' kernels; call
