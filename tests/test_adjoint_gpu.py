@@ -405,6 +405,39 @@ def test_adjoint_batch_equals_the_blocks(cuda, precision):
     assert torch.equal(batch.grad, want)
 
 
+@pytest.mark.parametrize("precision", ["native", "split"])
+def test_adjoint_batch_on_the_mixed_box(cuda, precision):
+    """The tetrahedron/hexahedron/pyramid box (P2, sin-mapped and jittered) in one adjoint graph:
+    the node cotangents equal the per-block adjoints summed in block order, bit for bit, and the
+    FP64 ones match the oracle's restated adjoint."""
+    mesh = meshes.mixed_box(3, 2)
+    x = meshes.sin_map(mesh.nodes, 0.05)
+    mesh.nodes = meshes.jitter_interior(x, mesh.nodes, 0.02 / 3, 2026)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    rule = tg.QuadRule([tg.PointSet(c, *tg.refcell.gauss_rule(c, 4)) for c in ("Tetrahedron", "Hexahedron", "Pyramid")])
+    dt = torch.float64 if precision == "native" else torch.float32
+    rng = np.random.default_rng(37)
+    cts, hosts = [], []
+    for blk in g.blocks:
+        ct, host = cotangent_fields(rng, blk.num_cells, len(rule.get(blk.element.cell)), dt)
+        cts.append(ct)
+        hosts.append(host)
+    batch = tg.AdjointBatch(g, rule, cts, precision=precision)
+    batch.launch()
+    want = torch.zeros_like(batch.grad)
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
+    oracle = np.zeros(want.shape)
+    for b, blk in enumerate(g.blocks):
+        pts = rule.get(blk.element.cell)
+        grad, _ = tg.vjp_block(g, b, pts, cts[b], precision=precision)
+        want += grad
+        h = hosts[b]
+        oracle += orc.vjp(blk.element.cell, 2, absx, mesh.blocks[b].cells, pts.points, h["points"],
+                          h["detj"][..., 0], h["pinv"])
+    assert torch.equal(batch.grad, want)
+    assert orc.rel_err(batch.grad.cpu().numpy(), oracle) < (1e-11 if precision == "native" else 2e-5)
+
+
 def test_adjoint_batch_with_double_float_forward(cuda):
     """precision="df64": each block's forward fields from the double-float kernels (bit for bit
     the fields of tlg_eval_block with df64 tables, and within 1e-12 of the oracle's f64 values),

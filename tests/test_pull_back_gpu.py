@@ -24,8 +24,23 @@ def quad_or_tri(cell, n, degree):
 
 CELLS = [
     ("Tetrahedron", 1), ("Tetrahedron", 2), ("Tetrahedron", 3), ("Hexahedron", 1), ("Hexahedron", 2),
-    ("Prism", 1), ("Prism", 2), ("Triangle", 2), ("Quadrilateral", 3),
+    ("Prism", 1), ("Prism", 2), ("Pyramid", 2), ("Pyramid", 3), ("Triangle", 2), ("Quadrilateral", 3),
 ]
+
+
+def inside(cell, xi, eps=1e-9):
+    """Whether reference points `[..., td]` lie in the reference cell (up to eps)."""
+    x = [xi[..., d] for d in range(xi.shape[-1])]
+    lo = np.all(xi >= -eps, axis=-1)
+    if cell in ("Interval", "Quadrilateral", "Hexahedron"):
+        return lo & np.all(xi <= 1 + eps, axis=-1)
+    if cell in ("Triangle", "Tetrahedron"):
+        return lo & (xi.sum(axis=-1) <= 1 + eps)
+    if cell == "Prism":
+        return lo & (x[0] + x[1] <= 1 + eps) & (x[2] <= 1 + eps)
+    if cell == "Pyramid":
+        return lo & (x[0] + x[2] <= 1 + eps) & (x[1] + x[2] <= 1 + eps)
+    raise ValueError(cell)
 
 
 def mesh_for(cell, degree, n=2):
@@ -59,10 +74,13 @@ def test_gauss_points_come_back(cuda, cell, degree, dtype):
     tol = 1e-13 if dtype == F64 else 1e-5
     conv = step.to_host_cell_major()[..., 0] <= tol
     # Newton from the centroid can leave strongly curved cells for points near a vertex (the
-    # reference's algorithm, and the oracle's, flag those as not converged); every converged
-    # point is the Gauss point.
-    assert conv.mean() > 0.99
-    assert np.abs(got - pts[None])[conv].max() < (1e-11 if dtype == F64 else 2e-5)
+    # reference's algorithm, and the oracle's, flag those as not converged), and near the apex of
+    # a curved P3 pyramid it can converge to the map's second preimage beyond the apex (the
+    # oracle finds the same one); every point converged inside the reference cell is the Gauss
+    # point.
+    conv_in = conv & inside(cell, got, 1e-6)
+    assert conv_in.mean() > 0.99
+    assert np.abs(got - pts[None])[conv_in].max() < (1e-11 if dtype == F64 else 2e-5)
 
 
 @pytest.mark.parametrize("cell,degree", CELLS)
@@ -152,12 +170,15 @@ def test_split_pull_back_matches_f64(cuda, cell, degree):
     xis, sts = tg.pull_back_block(g, 0, field, precision="split")
     xi64, st64 = xi64.to_host_cell_major(), st64.to_host_cell_major()[..., 0]
     xis, sts = xis.to_host_cell_major(), sts.to_host_cell_major()[..., 0]
-    both = (st64 <= 1e-13) & (sts <= 1e-13)
+    # Both converged, the f64 one inside the reference cell (near a curved P3 pyramid's apex the
+    # iteration can reach the map's second preimage beyond it, and the two precisions need not
+    # reach the same one).
+    both = (st64 <= 1e-13) & (sts <= 1e-13) & inside(cell, xi64) & inside(cell, xis)
     assert both.any()
     assert np.abs(xis[both] - xi64[both]).max() < 1e-12
     # Points converged in f64 well inside the box converge in mixed precision too.
-    inside = (st64 <= 1e-13) & np.all((xi64 > 0.0) & (xi64 < 1.0), axis=2)
-    assert np.all(sts[inside] <= 1e-13)
+    in_box = (st64 <= 1e-13) & np.all((xi64 > 0.0) & (xi64 < 1.0), axis=2)
+    assert np.all(sts[in_box] <= 1e-13)
 
 
 def test_split_pull_back_needs_f64(cuda):
