@@ -818,13 +818,38 @@ def extra_p1_box():
     return res
 
 
-def _roofline(alg: int, ms: float, peaks: dict, traffic):
+# What binds each mode's kernel, from its ncu capture (the profiles of the P2 tetrahedra): the
+# double-float and FP64 kernels are bound by an arithmetic pipe, not by HBM.
+BINDING = {
+    "df64": "FP32 pipe: FMA 62.8 %, ALU 35.2 %, issue 56.5 % of active cycles (ncu, 32^3 x 6 case)",
+    "f64": "FP64 pipe: 93.7 % of active cycles (ncu)",
+    "split": "HBM: stores of the f32 fields (ncu traffic 1.004 x the algorithmic bytes)",
+    "f32": "HBM: stores of the f32 fields",
+}
+# Algorithmic FP64 operations per point of the curved P2 tetrahedra (x: 3 x 10 FMAs, J: 9 x 10
+# FMAs, det J and K about 50): the dense direct count; and the FP64 FMA rate measured on this
+# GB300 (a dependent-FMA loop over every SM, 1/64 of the FP32 rate).
+FLOPS_PER_QPOINT_P2 = 290
+FP64_TFLOPS_MEASURED = 1.18
+
+
+def _roofline(alg: int, ms: float, peaks: dict, traffic, mode: str = "", qpts: int = 0):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     achieved = alg / (ms * 1e-3) / 1e9
-    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "algorithmic_bytes_per_launch": int(alg),
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy), of measured" if "hbm_gbs" in peaks
-            else "fallback 6800 GB/s"}
+    out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+           "traffic": traffic, "algorithmic_bytes_per_launch": int(alg),
+           "peak_source": "MEASURED_PEAKS.json hbm_gbs (burst copy), of measured" if "hbm_gbs" in peaks
+           else "fallback 6800 GB/s"}
+    if mode in BINDING:
+        out["binding"] = BINDING[mode]
+    if mode in ("df64", "f64") and qpts:
+        # f64-accurate results per second, in FP64 operations: the double-float path against the
+        # FP64 pipe's own peak.
+        tf = FLOPS_PER_QPOINT_P2 * qpts / (ms * 1e-3) / 1e12
+        out["f64_equivalent"] = {"tflops": tf, "fp64_peak_tflops": FP64_TFLOPS_MEASURED,
+                                 "frac_of_fp64_peak": tf / FP64_TFLOPS_MEASURED,
+                                 "flops_per_qpoint": FLOPS_PER_QPOINT_P2}
+    return out
 
 
 def run_ours(args):
@@ -983,7 +1008,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "error_vs_oracle": main_err,
             "error_sample": f"{len(sample)} seeded cells x {nq} points against the oracle (f64)",
-            "roofline": _roofline(alg, ms, peaks, traffic),
+            "roofline": _roofline(alg, ms, peaks, traffic, args.mode, qpts),
             "e2e": {"value": whole_job_rate(qpts, world, e2e_ms), "unit": "qpoints/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": out_es, "ms_per_step": e2e_ms,
                     "measure": vol, "steps": e2e_steps,
