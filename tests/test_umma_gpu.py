@@ -81,6 +81,17 @@ def test_many_tiles_match_the_oracle(cuda, precision):
     check(g, mesh, "Tetrahedron", 4, pts, got, precision)
 
 
+@pytest.mark.parametrize("precision", ["f32", "split"])
+def test_fewer_cells_than_a_tile(cuda, precision):
+    """6 P5 tetrahedra (one tile of 64 mostly padding, its 27 chunks in work-item groups) against
+    the oracle."""
+    mesh = meshes.curved_box("Tetrahedron", 1, 5, jitter=0.0)
+    pts, _ = tg.refcell.gauss_rule("Tetrahedron", 10)
+    g, got, family = run(mesh, "Tetrahedron", pts, precision)
+    assert family == "tensor"
+    check(g, mesh, "Tetrahedron", 5, pts, got, precision)
+
+
 def test_ranges_and_facet_normals(cuda):
     """Chunks of 48 cells (tiles of 64 cut short, outputs at 16-cell boundaries) give the fields
     of one launch; facet normals of a facet rule against the oracle."""
