@@ -99,7 +99,7 @@ SIGNATURES = [
     ("tlg_batch_create", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs), _I, _P]),
     ("tlg_batch_destroy", _I, [_P]),
     ("tlg_batch_tune", _I, [_P, _P, _P]),
-    ("tlg_batch_tuning", _I, [_P, _P, _P]),
+    ("tlg_batch_tuning", _I, [_P, _P, _P, _P]),
     ("tlg_batch_launch", _I, [_P, _P]),
     ("tlg_evector", _I, [ctypes.POINTER(TlgBlock), _I, _L, _L, _L, _P, _P]),
     ("tlg_csr_workspace_bytes", _L, [_L, _I]),

@@ -34,6 +34,7 @@ struct tlg_batch {
   std::vector<tlg_block> blocks;
   std::vector<tlg_outputs> outputs;
   std::vector<int> grid;  // launch grid per block (0: the kernel's persistent default)
+  std::vector<int> strategy;  // per block: TLG_STRATEGY_* forced on every family, -1 the caller's
   bool serial = false;    // the blocks one after another instead of parallel graph branches
   float tuned_ms = 0.0f;  // the tuner's median time of the chosen graph (0: not tuned here)
   std::vector<cudaStream_t> streams;
@@ -1914,7 +1915,7 @@ extern "C" {
 namespace {
 
 std::mutex g_tune_mutex;
-std::map<std::string, int> g_tune_cache;  // launch-shape key -> grid multiplier
+std::map<std::string, std::pair<int, int>> g_tune_cache;  // launch-shape key -> (strategy, grid multiplier)
 std::map<std::string, std::vector<int>> g_joint_cache;  // batch key -> grids after the joint pass,
                                                         // then 1 for a serial chain, 0 for branches
 
@@ -1933,11 +1934,35 @@ void destroy_graph(tlg_batch* b) {
   b->exec = nullptr;
 }
 
+// Block i's launch with its grid and strategy (every family's override set for the launch and
+// restored after it).
 tlg_status eval_with_grid(tlg_batch* b, size_t i, cudaStream_t s, int grid) {
+  const int forced = b->strategy[i];
+  int saved[kFamilies];
+  if (forced >= 0)
+    for (int f = 0; f < kFamilies; ++f) {
+      saved[f] = g_override[f];
+      g_override[f] = forced;
+    }
   tlg::g_grid_override = grid;
   tlg_status st = tlg_eval_block(b->tables[i], &b->blocks[i], &b->outputs[i], s);
   tlg::g_grid_override = 0;
+  if (forced >= 0)
+    for (int f = 0; f < kFamilies; ++f) g_override[f] = saved[f];
   return st;
+}
+
+// The strategies worth timing for a block: the policy, and the forced strategies whose kernels
+// apply to its tables (the others would run the loops kernel): the unrolled or paired kernels,
+// sum factorisation (tensor-product point sets), the cooperative kernel (not for double-float
+// tables, which it runs in FP64), the tensor-core kernels (f32 and split tables).
+std::vector<int> strategy_candidates(const tlg_tables* t) {
+  std::vector<int> c = {-1, TLG_STRATEGY_DIRECT};
+  if (t->sf_ok) c.push_back(TLG_STRATEGY_SUMFACT);
+  if (t->td >= 2 && t->k <= 128 && !t->df) c.push_back(TLG_STRATEGY_COOPERATIVE);
+  if ((t->umma_kpad > 0 || t->tc_ksteps > 0) && (t->dtype == TLG_F32 || t->dtype == TLG_SPLIT32))
+    c.push_back(TLG_STRATEGY_TENSOR);
+  return c;
 }
 
 }  // namespace
@@ -1957,6 +1982,7 @@ tlg_status tlg_batch_create(const tlg_tables* const* tables, const tlg_block* bl
     b->blocks.push_back(blocks[i]);
     b->outputs.push_back(outputs[i]);
     b->grid.push_back(0);
+    b->strategy.push_back(-1);
   }
   cudaError_t e = cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking);
   for (int i = 0; i < num_blocks && e == cudaSuccess; ++i) {
@@ -2025,41 +2051,73 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
     return st;
   };
   const int cands[] = {0, 1, 2, 3, 4, 6, 8};  // CTAs per SM of the persistent grid (0: occupancy)
+  // A strategy set by the caller (a scoped override or TLG_GEOM_STRATEGY) is kept; otherwise each
+  // block's strategy is a candidate too: the kernel families tile the work differently (paired
+  // kernels: 16-cell tiles, two points per instruction; sum factorisation: a cell's planes and
+  // rows per thread; cooperative: four lanes per cell; tcgen05: 64-cell tiles by 8-point chunks).
+  int fixed = TLG_STRATEGY_AUTO;
+  if (!wanted_strategy(TLG_FAMILY_JACOBIAN, &fixed)) return finish(TLG_ERR_INVALID_ARGUMENT);
+  bool caller_fixed = fixed != TLG_STRATEGY_AUTO;
+  for (int f = 0; f < kFamilies; ++f) caller_fixed = caller_fixed || g_override[f] >= 0;
   for (size_t i = 0; i < b->tables.size(); ++i) {
-    const std::string key = tune_key(b->tables[i], &b->outputs[i], b->outputs[i].num_cells);
-    int mult = -1;
+    const std::string key = tune_key(b->tables[i], &b->outputs[i], b->outputs[i].num_cells) +
+                            (caller_fixed ? " fixed" : "");
+    std::pair<int, int> choice(-1, -1);
     {
       std::lock_guard<std::mutex> lock(g_tune_mutex);
       auto it = g_tune_cache.find(key);
-      if (it != g_tune_cache.end()) mult = it->second;
+      if (it != g_tune_cache.end()) choice = it->second;
     }
-    if (mult < 0) {
+    if (choice.second < 0) {
+      // The strategy at the occupancy grid (a forced strategy replaces the policy only when more
+      // than 1 % faster), then the grid for it.
+      b->grid[i] = 0;
       float best = 1e30f;
-      mult = 0;
+      int strat = -1;
+      const std::vector<int> strats = caller_fixed ? std::vector<int>{-1} : strategy_candidates(b->tables[i]);
+      for (int c : strats) {
+        b->strategy[i] = c;
+        float ms = 0.0f;
+        tlg_status st = median_ms([&] { return eval_with_grid(b, i, s, 0); }, &ms);
+        if (st != TLG_OK) {
+          b->strategy[i] = -1;
+          return finish(st);
+        }
+        if (ms < (c == -1 ? best : 0.97f * best)) {  // a forced strategy: more than 3 % faster
+          best = ms;
+          strat = c;
+        }
+      }
+      b->strategy[i] = strat;
+      int mult = 0;
       for (int c : cands) {
-        const int grid = c == 0 ? 0 : c * sms;
+        if (c == 0) continue;  // timed above
+        const int grid = c * sms;
         float ms = 0.0f;
         tlg_status st = median_ms([&] { return eval_with_grid(b, i, s, grid); }, &ms);
         if (st != TLG_OK) return finish(st);
         // A candidate replaces the occupancy default only when more than 1 % faster.
-        if (ms < (c == 0 ? best : 0.99f * best)) {
+        if (ms < 0.99f * best) {
           best = ms;
           mult = c;
         }
       }
+      choice = {strat, mult};
       std::lock_guard<std::mutex> lock(g_tune_mutex);
-      g_tune_cache[key] = mult;
+      g_tune_cache[key] = choice;
     }
-    b->grid[i] = mult == 0 ? 0 : mult * sms;
+    b->strategy[i] = choice.first;
+    b->grid[i] = choice.second == 0 ? 0 : choice.second * sms;
   }
   // Joint pass: the graph runs the blocks concurrently (or in turn), so each block's best grid
-  // alone is only the start. Every comparison times the whole graph, the median of 9 launches,
-  // and a change is kept only when more than 1 % faster, so that run-to-run noise does not pick
-  // the configuration: parallel branches against a serial chain (the concurrent branches of
+  // alone is only the start. Every comparison times the whole graph (time_graph), and a change
+  // is kept only when more than 1 % faster, so that run-to-run noise does not pick the
+  // configuration: parallel branches against a serial chain (the concurrent branches of
   // persistent kernels share the SMs in an order the hardware picks; the chain is kept unless
-  // the branches are more than 3 % faster), one round of coordinate descent over each block's
-  // grid candidates, and the result against every block at its occupancy default.
-  std::string batch_key;
+  // the branches are more than 3 % faster in the median and the slowest round), one round of
+  // coordinate descent over each block's grid candidates, and the result against every block at
+  // its occupancy default.
+  std::string batch_key = caller_fixed ? "fixed;" : "";
   for (size_t i = 0; i < b->tables.size(); ++i)
     batch_key += tune_key(b->tables[i], &b->outputs[i], b->outputs[i].num_cells) + ";";
   std::vector<int> joint;
@@ -2068,24 +2126,42 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
     auto it = g_joint_cache.find(batch_key);
     if (it != g_joint_cache.end()) joint = it->second;
   }
-  auto time_graph = [&](float* ms, float* mean = nullptr) -> tlg_status {
+  // A graph is timed as it runs in use, launch after launch: the median over five rounds of the
+  // mean of four back-to-back launches (consecutive graphs with parallel branches can interfere,
+  // which launches timed one by one do not show; the median of rounds still drops a round slowed
+  // by a clock or power transition).
+  auto time_graph = [&](float* ms, float* spread = nullptr) -> tlg_status {
     destroy_graph(b);
-    return median_ms([&] { return tlg_batch_launch(b, s); }, ms, 9, mean);
+    tlg_status st = tlg_batch_launch(b, s);
+    float r[5];
+    for (int k = 0; k < 5 && st == TLG_OK; ++k) {
+      cudaEventRecord(t0, s);
+      for (int l = 0; l < 4 && st == TLG_OK; ++l) st = tlg_batch_launch(b, s);
+      cudaEventRecord(t1, s);
+      cudaEventSynchronize(t1);
+      cudaEventElapsedTime(&r[k], t0, t1);
+      r[k] /= 4.0f;
+    }
+    if (st != TLG_OK) return st;
+    std::sort(r, r + 5);
+    *ms = r[2];
+    if (spread) *spread = r[4];
+    return st;
   };
   if (joint.size() == b->tables.size() + 1) {
     for (size_t i = 0; i < b->tables.size(); ++i) b->grid[i] = joint[i];
     b->serial = joint.back() != 0;
   } else if (b->tables.size() > 1) {
-    float serial_ms = 0.0f, par_ms = 0.0f, serial_mean = 0.0f, par_mean = 0.0f, best = 0.0f;
+    float serial_ms = 0.0f, par_ms = 0.0f, serial_max = 0.0f, par_max = 0.0f, best = 0.0f;
     b->serial = true;
-    tlg_status st = time_graph(&serial_ms, &serial_mean);
+    tlg_status st = time_graph(&serial_ms, &serial_max);
     if (st == TLG_OK) {
       b->serial = false;
-      st = time_graph(&par_ms, &par_mean);
+      st = time_graph(&par_ms, &par_max);
     }
     if (st != TLG_OK) return finish(st);
-    // Branches only when faster in the median and in the mean (their times spread more).
-    b->serial = !(par_ms < 0.97f * serial_ms && par_mean < 0.97f * serial_mean);
+    // Branches only when faster in the median and in the slowest round (their times spread more).
+    b->serial = !(par_ms < 0.97f * serial_ms && par_max < 0.97f * serial_max);
     best = b->serial ? serial_ms : par_ms;
     for (size_t i = 0; i < b->tables.size() && st == TLG_OK; ++i) {
       const int keep = b->grid[i];
@@ -2140,10 +2216,12 @@ tlg_status tlg_batch_tune(tlg_batch* b, void* stream, int* grids) {
   return ok();
 }
 
-tlg_status tlg_batch_tuning(const tlg_batch* b, int* serial, float* ms) {
+tlg_status tlg_batch_tuning(const tlg_batch* b, int* serial, float* ms, int* strategies) {
   if (!b) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_batch_tuning: NULL batch");
   if (serial) *serial = b->serial ? 1 : 0;
   if (ms) *ms = b->tuned_ms;
+  if (strategies)
+    for (size_t i = 0; i < b->strategy.size(); ++i) strategies[i] = b->strategy[i];
   return ok();
 }
 

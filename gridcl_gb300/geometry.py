@@ -693,11 +693,17 @@ class Batch:
         return self.grids
 
     def tuning(self) -> dict:
-        """The tuner's choice: ``{"grids", "serial" (a chain rather than parallel branches),
-        "tuned_ms" (its median time of the chosen graph)}``."""
+        """The tuner's choice: ``{"grids", "strategies" (per block the strategy name its launch
+        forces, "caller" for the override or policy in effect), "serial" (a chain rather than
+        parallel branches), "tuned_ms" (its median time of the chosen graph)}``."""
         serial, ms = ctypes.c_int(0), ctypes.c_float(0.0)
-        check(lib().tlg_batch_tuning(self.handle, ctypes.byref(serial), ctypes.byref(ms)))
-        return {"grids": list(self.grids), "serial": bool(serial.value), "tuned_ms": float(ms.value)}
+        n = len(self.fields)
+        codes = (ctypes.c_int * max(n, 1))()
+        check(lib().tlg_batch_tuning(self.handle, ctypes.byref(serial), ctypes.byref(ms), codes))
+        names = {-1: "caller", 0: "auto", 1: "direct", 2: "loops", 3: "sumfact", 4: "shared", 5: "cooperative",
+                 6: "tensor"}
+        return {"grids": list(self.grids), "strategies": [names.get(c, str(c)) for c in list(codes)[:n]],
+                "serial": bool(serial.value), "tuned_ms": float(ms.value)}
 
     def launch(self) -> None:
         check(lib().tlg_batch_launch(self.handle, current_stream_handle()))

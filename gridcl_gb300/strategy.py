@@ -5,11 +5,13 @@ this thread's scoped setting (:func:`with_strategy`), then the environment varia
 ``TLG_GEOM_STRATEGY`` (one strategy for every family, or ``Family=strategy,...``), then the
 built-in policy ("policy"/"auto": sum factorisation for quadrilaterals, hexahedra and prisms at
 tensor-product rules in f64 and above the degrees with paired kernels, else the paired or
-unrolled kernels where compiled, the cooperative kernel above 27 nodes per cell, loops
-otherwise). "loops" reads the tables from global
+unrolled kernels where compiled (the double-float ones for double-float tables), above 27 nodes
+per cell the tcgen05 tensor-core kernel for f32 and split volume cells of at most 88 nodes and
+the cooperative kernel otherwise, loops otherwise). "loops" reads the tables from global
 memory, "shared" stages them in shared memory, "cooperative" splits each cell's node sums over
 four lanes, "tensor" (an extension of the reference's five) runs the node-by-basis contraction on
-the tensor cores (3xTF32). A forced strategy that does not apply runs "loops", as in the
+the tensor cores (tcgen05 UMMAs with tensor-memory accumulators for volume cells of 21-88 nodes,
+mma.sync 3xTF32 for the others). A forced strategy that does not apply runs "loops", as in the
 reference. A fused launch follows its principal family: Jacobian when J, det J or K is among its
 outputs, else Normals, FacetNormals, Points."""
 

@@ -197,11 +197,15 @@ tlg_status tlg_batch_create(const tlg_tables* const* tables, const tlg_block* bl
                             const tlg_outputs* outputs, int num_blocks, tlg_batch** out);
 tlg_status tlg_batch_destroy(tlg_batch* batch);
 
-/* Times candidate persistent grids (0 and 1..8 CTAs per SM) for each block on `stream` (the
- * median of 7 launches), keeps the fastest (a grid replaces the occupancy limit only when more
- * than 1 % faster), and caches the choice per launch shape for the process; then, timing the
- * whole graph (the median of 9 launches), takes parallel branches over a serial chain only when
- * more than 3 % faster in the median and in the mean of those launches, runs one round of coordinate descent over each block's candidates
+/* Times, for each block on `stream` (the median of 7 launches), the strategies whose kernels
+ * apply to its tables (the policy, direct, sumfact, cooperative, tensor; none when the caller has
+ * set a strategy: an override on this thread or TLG_GEOM_STRATEGY), keeps the fastest (a forced
+ * strategy replaces the policy only when more than 3 % faster), then candidate persistent grids
+ * (0 and 1..8 CTAs per SM) for it (a grid replaces the occupancy limit only when more than 1 %
+ * faster), and caches the choice per launch shape for the process; then, timing the
+ * whole graph as it runs in use (the median over 5 rounds of the mean of 4 back-to-back
+ * launches), takes parallel branches over a serial chain only when more than 3 % faster in the
+ * median and in the slowest round, runs one round of coordinate descent over each block's candidates
  * (changes kept when more than 1 % faster), and keeps the result only when more than 1 % faster
  * than every block at its occupancy limit in a serial chain (cached per batch shape). grids[i]
  * (may be NULL) receives block i's grid (0: the occupancy limit). Runs the blocks' kernels; call
@@ -209,9 +213,11 @@ tlg_status tlg_batch_destroy(tlg_batch* batch);
 tlg_status tlg_batch_tune(tlg_batch* batch, void* stream, int* grids);
 
 /* After tlg_batch_tune: whether the graph runs the blocks as a serial chain (1) or as parallel
- * branches (0), and the tuner's median time of the chosen graph in ms. No counterpart in the
- * reference. */
-tlg_status tlg_batch_tuning(const tlg_batch* batch, int* serial, float* ms);
+ * branches (0), the tuner's median time of the chosen graph in ms, and per block (strategies may
+ * be NULL) the strategy its launch forces on every kernel family (TLG_STRATEGY_*; -1: the
+ * caller's, i.e. the override or TLG_GEOM_STRATEGY in effect, else the policy). No counterpart in
+ * the reference. */
+tlg_status tlg_batch_tuning(const tlg_batch* batch, int* serial, float* ms, int* strategies);
 
 /* Evaluates every block: one launch of a CUDA graph (captured on the first call). */
 tlg_status tlg_batch_launch(tlg_batch* batch, void* stream);
