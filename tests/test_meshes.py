@@ -13,6 +13,8 @@ from oracle import refcell as rc
     ("Tetrahedron", 4, 2, 384, 9 ** 3),
     ("Hexahedron", 3, 2, 27, 7 ** 3),
     ("Prism", 3, 2, 54, 7 ** 3),
+    ("Pyramid", 2, 1, 48, 27 + 8),
+    ("Pyramid", 1, 2, 6, 27 + 8),  # the 3^3 P2 lattice of the cube, the 8 corner-to-apex midpoints
 ])
 def test_cube_box_counts(cell, n, p, cells, nodes):
     m = meshes.cube_box(cell, n, p)
@@ -24,7 +26,7 @@ def test_cube_box_counts(cell, n, p, cells, nodes):
     assert np.all(np.diff(first) > 0)
 
 
-@pytest.mark.parametrize("cell", ["Tetrahedron", "Hexahedron", "Prism"])
+@pytest.mark.parametrize("cell", ["Tetrahedron", "Hexahedron", "Prism", "Pyramid"])
 def test_cells_are_positively_oriented(cell):
     m = meshes.curved_box(cell, 3, 2, jitter=0.02)
     pts, _ = rc.gauss_rule(cell, 4)
@@ -57,3 +59,36 @@ def test_splitmix64_first_values():
     z = meshes.splitmix64(0, 2)
     assert int(z[0]) == 0xE220A8397B1DCDAF
     assert int(z[1]) == 0x6E789E6AA1B965F4
+
+
+def test_mixed_boxes_match_the_reference_examples():
+    """boxes.rs's documented examples: mixed_box(2, 1) has 4 tetrahedra, 4 hexahedra and 22
+    pyramids on 27 corners and 4 centres; hex_prism_pyramid_box(3, 1) 9 hexahedra, 18 prisms and
+    54 pyramids."""
+    m = meshes.mixed_box(2, 1)
+    assert [(b.cell, b.num_cells) for b in m.blocks] == [("Tetrahedron", 4), ("Hexahedron", 4), ("Pyramid", 22)]
+    assert m.num_nodes == 27 + 4
+    h = meshes.hex_prism_pyramid_box(3, 1)
+    assert [(b.cell, b.num_cells) for b in h.blocks] == [("Hexahedron", 9), ("Prism", 18), ("Pyramid", 54)]
+
+
+@pytest.mark.parametrize("p", [1, 2, 3])
+def test_mixed_boxes_are_conforming_with_unit_volume(p):
+    """Every node used, numbered by first use over the cells in generation order; no two nodes
+    at the same point (shared high-order nodes found across blocks); positive det J at Gauss
+    points; volume 1 by the oracle (rule degree 3p integrates the pyramids' rational det J of
+    these affine maps exactly)."""
+    for m in (meshes.mixed_box(3, p), meshes.hex_prism_pyramid_box(3, p)):
+        used = np.zeros(m.num_nodes, dtype=bool)
+        for b in m.blocks:
+            used[b.cells.ravel()] = True
+        assert used.all()
+        keys = np.rint(m.nodes * (2 * 3 * p)).astype(np.int64)
+        assert np.unique(keys, axis=0).shape[0] == m.num_nodes
+        vol = 0.0
+        for b in m.blocks:
+            pts, w = rc.gauss_rule(b.cell, 3 * p)
+            d = orc.eval_block(b.cell, p, m.nodes, b.cells, pts, factors=("detj",))["detj"][..., 0]
+            assert d.min() > 0, b.cell
+            vol += orc.measure(d, w)
+        assert abs(vol - 1.0) < 1e-12
