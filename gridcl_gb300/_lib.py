@@ -113,6 +113,8 @@ SIGNATURES = [
     ("tlg_vjp_batch_create", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs),
                                   ctypes.POINTER(TlgCotangents), _P, _P, _P, _P, _L, _I, _P, _I, _P]),
     ("tlg_vjp_batch_set_forward", _I, [_P, _P]),
+    ("tlg_vjp_batch_set_two_pass", _I, [_P, _I]),
+    ("tlg_vjp_block_from_fields", _I, [_P, ctypes.POINTER(TlgBlock), ctypes.POINTER(TlgOutputs), ctypes.POINTER(TlgCotangents), _P, _L, _P]),
     ("tlg_vjp_batch_launch", _I, [_P, _P]),
     ("tlg_vjp_batch_destroy", _I, [_P]),
     ("tlg_measure_cell_sums", _I, [_P, _I, _L, _L, _I, _P, _P, _P]),

@@ -1605,6 +1605,55 @@ tlg_status vjp_sumfact(const tlg_tables* t, const tlg::VjpArgs& v, cudaStream_t 
   return ok();
 }
 
+// The sum-factorised adjoint from forward fields already written (det J and K in o->detj and
+// o->pinv, read); `found` is false where it does not apply.
+tlg_status vjp_sumfact_from_fields(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o,
+                                   const tlg_cotangents* ct, void* local, cudaStream_t s, bool* found) {
+  *found = false;
+  if (!vjp_sumfact_preferred(t) || !o->detj || !o->pinv) return TLG_ERR_UNSUPPORTED;
+  const bool split = t->dtype == TLG_SPLIT32;
+  const size_t fbytes = split ? 4 : 8;
+  const int threads = tlg::kEvalThreads;
+  // The tile kernel where a tile's points and plane sums fit, else one thread per cell.
+  const size_t stab = (t->sf_bytes + 15) / 16 * 16;
+  const size_t smem_tile = stab + tlg::vjp_sumfact_tile_extra_bytes(t->sf_n, (int)t->q, t->sf_block0.m[2], fbytes);
+  const bool tiled = smem_tile <= (size_t)227 * 1024;
+  const size_t smem = tiled ? smem_tile : stab + tlg::vjp_sumfact_bwd_extra_bytes(t->sf_n, threads, fbytes);
+  if (smem > (size_t)227 * 1024) return TLG_ERR_UNSUPPORTED;
+  tlg::VjpSfArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.nodes = b->nodes;
+  a.dofmap = b->dofmap;
+  a.tab = t->dev + t->off_sf;
+  a.ct[0] = ct->points;
+  a.ct[1] = ct->detj;
+  a.ct[2] = ct->pinv;
+  a.out[2] = o->detj;
+  a.out[3] = o->pinv;
+  a.local = local;
+  a.err = t->err;
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + 15) / 16 * 16;
+  a.out_first_cell = o->out_first_cell;
+  a.last_cell = b->num_cells - 1;
+  a.range_end = o->first_cell + o->num_cells;
+  a.last_node = (uint32_t)(b->num_nodes - 1);
+  a.tab_bytes = t->sf_bytes;
+  for (int d = 0; d < 3; ++d) {
+    a.off_b[d] = t->sf_block0.off_b[d];
+    a.off_d[d] = t->sf_block0.off_d[d];
+    a.m[d] = t->sf_block0.m[d];
+  }
+  a.off_perm = t->sf_offperm;
+  a.num_points = (int)t->q;
+  cudaError_t e = tiled ? tlg::launch_vjp_sumfact_tile(split, t->sf_n, a, smem, s, found)
+                        : tlg::launch_vjp_sumfact_bwd(split, t->sf_n, a, smem, threads, s, found);
+  if (!*found) return TLG_ERR_UNSUPPORTED;
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_block_from_fields launch");
+  g_last_family = TLG_STRATEGY_SUMFACT;
+  return ok();
+}
+
 // The adjoint below codimension 0 (vjp_surface.cu) from the node-row kernel's arguments: phi and
 // dphi staged when they and the thread slots (2 K GD values per thread) fit, else read from global
 // memory; 32 to 128 threads per CTA.
@@ -1730,6 +1779,30 @@ tlg_status tlg_vjp_block(const tlg_tables* t, const tlg_block* b, const tlg_outp
   return ok();
 }
 
+tlg_status tlg_vjp_block_from_fields(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o,
+                                     const tlg_cotangents* ct, void* local, int64_t local_cells, void* stream) {
+  if (!t || !b || !o || !ct) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block_from_fields: NULL argument");
+  if (t->dtype != TLG_F64 && t->dtype != TLG_SPLIT32)
+    return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block_from_fields: f64 or split-precision tables");
+  if (b->gdim != t->gd || t->td != t->gd)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block_from_fields: codimension 0, block and tables alike");
+  if (o->tile != 16) return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block_from_fields: tile 16");
+  if (!o->detj || !o->pinv)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block_from_fields: the det J and K fields are the inputs");
+  if (o->first_cell < 0 || o->num_cells < 0 || o->first_cell + o->num_cells > b->num_cells ||
+      o->out_first_cell < 0 || o->out_first_cell % 16 != 0)
+    return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block_from_fields: bad cell range");
+  if (local_cells < b->num_cells)
+    return fail(TLG_ERR_LENGTH_MISMATCH, "tlg_vjp_block_from_fields: local_cells below the block's cells");
+  if (o->num_cells == 0 || t->q == 0) return ok();
+  if (!local) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block_from_fields: NULL local");
+  bool found = false;
+  tlg_status st = vjp_sumfact_from_fields(t, b, o, ct, local, static_cast<cudaStream_t>(stream), &found);
+  if (!found)
+    return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block_from_fields: hexahedra Q1/Q2 at tensor-product rules only");
+  return st;
+}
+
 tlg_status tlg_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int gdim,
                           const void* local, int local_dtype, double* grad, void* stream) {
   if (!offsets || !grad || num_nodes < 0 || gdim < 1 || gdim > 3 || (local_dtype != 4 && local_dtype != 8))
@@ -1768,6 +1841,9 @@ struct tlg_vjp_batch {
   std::vector<const uint32_t*> offsets, entries;
   // Tables of a separate forward evaluation per block (tlg_vjp_batch_set_forward), or empty.
   std::vector<const tlg_tables*> forward;
+  // tlg_vjp_batch_set_two_pass: blocks whose adjoint can read det J and K back run the policy's
+  // forward, then the adjoint from those fields.
+  bool two_pass = false;
   int64_t num_nodes = 0;
   int gdim = 0;
   double* grad = nullptr;
@@ -1790,9 +1866,11 @@ tlg_status tlg_vjp_batch_create(const tlg_tables* const* tables, const tlg_block
   *out = nullptr;
   auto b = new tlg_vjp_batch();
   for (int i = 0; i < num_blocks; ++i) {
-    if (!tables[i] || !offsets[i] || tables[i]->gd != gdim) {
+    if (!tables[i] || !offsets[i] || tables[i]->gd != gdim ||
+        (tables[i]->dtype == TLG_SPLIT32) != (tables[0]->dtype == TLG_SPLIT32)) {
       delete b;
-      return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_batch_create: NULL tables or CSR, or another gdim");
+      return fail(TLG_ERR_INVALID_ARGUMENT,
+                  "tlg_vjp_batch_create: NULL tables or CSR, another gdim, or split and f64 tables mixed");
     }
     b->tables.push_back(tables[i]);
     b->blocks.push_back(blocks[i]);
@@ -1851,6 +1929,14 @@ tlg_status tlg_vjp_batch_set_forward(tlg_vjp_batch* b, const tlg_tables* const* 
   return ok();
 }
 
+tlg_status tlg_vjp_batch_set_two_pass(tlg_vjp_batch* b, int on) {
+  if (!b || (on != 0 && on != 1)) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_batch_set_two_pass: NULL batch or not 0/1");
+  b->two_pass = on != 0;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->exec = nullptr;
+  return ok();
+}
+
 tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* b, void* stream) {
   if (!b) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_batch_launch: NULL batch");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -1876,6 +1962,11 @@ tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* b, void* stream) {
         if (st == TLG_OK)
           st = tlg_vjp_block(b->tables[i], &b->blocks[i], &adj, &b->cotangents[i], b->locals[i], b->local_cells[i],
                              b->streams[i]);
+      } else if (b->two_pass && vjp_sumfact_preferred(b->tables[i]) && b->outputs[i].detj && b->outputs[i].pinv) {
+        st = tlg_eval_block(b->tables[i], &b->blocks[i], &b->outputs[i], b->streams[i]);
+        if (st == TLG_OK)
+          st = tlg_vjp_block_from_fields(b->tables[i], &b->blocks[i], &b->outputs[i], &b->cotangents[i], b->locals[i],
+                                         b->local_cells[i], b->streams[i]);
       } else {
         st = tlg_vjp_block(b->tables[i], &b->blocks[i], &b->outputs[i], &b->cotangents[i], b->locals[i],
                            b->local_cells[i], b->streams[i]);
@@ -1883,10 +1974,21 @@ tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* b, void* stream) {
       if (st == TLG_OK) e = cudaEventRecord(b->events[i], b->streams[i]);
       if (e == cudaSuccess && st == TLG_OK) e = cudaStreamWaitEvent(b->capture, b->events[i], 0);
     }
-    for (size_t i = 0; i < nb && e == cudaSuccess && st == TLG_OK; ++i) {
-      const int ldt = b->tables[i]->dtype == TLG_SPLIT32 ? 4 : 8;
-      st = (i == 0 ? tlg_vjp_gather : tlg_vjp_gather_add)(b->offsets[i], b->entries[i], b->num_nodes, b->gdim,
-                                                          b->locals[i], ldt, b->grad, b->capture);
+    // The node sums in groups of up to kGatherMaxBlocks blocks per pass over the nodes (rows of
+    // one dtype: a batch has one precision), the first group writing the gradient.
+    for (size_t i0 = 0; i0 < nb && e == cudaSuccess && st == TLG_OK && b->num_nodes > 0;
+         i0 += tlg::kGatherMaxBlocks) {
+      tlg::GatherBlocks gb;
+      std::memset(&gb, 0, sizeof(gb));
+      const size_t i1 = std::min(nb, i0 + (size_t)tlg::kGatherMaxBlocks);
+      for (size_t i = i0; i < i1; ++i) {
+        gb.offsets[i - i0] = b->offsets[i];
+        gb.entries[i - i0] = b->entries[i];
+        gb.local[i - i0] = b->locals[i];
+      }
+      gb.count = (int)(i1 - i0);
+      const int ldt = b->tables[i0]->dtype == TLG_SPLIT32 ? 4 : 8;
+      e = tlg::launch_vjp_gather_blocks(gb, b->num_nodes, b->gdim, ldt, b->grad, b->capture, i0 > 0);
     }
     cudaGraph_t graph = nullptr;
     const std::string msg = tlg_last_error();

@@ -89,6 +89,13 @@ struct VjpSfArgs;
 // N nodes per direction, `threads` per CTA; `found` is false when none is compiled for n.
 cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t smem, int threads, cudaStream_t s,
                                bool* found);
+// Defined in sumfact.cu: the same adjoint from forward fields already written (det J and K read
+// back, vjp_sumfact_bwd_kernel).
+cudaError_t launch_vjp_sumfact_bwd(bool split, int n, const VjpSfArgs& a, size_t smem, int threads, cudaStream_t s,
+                                   bool* found);
+// Defined in sumfact.cu: the same with a 16-cell tile spread over the CTA (vjp_sumfact_tile_kernel;
+// 128 threads; work over a.padded / 16 tiles).
+cudaError_t launch_vjp_sumfact_tile(bool split, int n, const VjpSfArgs& a, size_t smem, cudaStream_t s, bool* found);
 // Defined in sumfact.cu: the sum-factorised kernel for precision 4 (f32), 8 (f64) or 12 (split),
 // N nodes per direction; `found` is false when none is compiled for (td, gd, n).
 cudaError_t launch_sumfact(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
@@ -123,5 +130,10 @@ cudaError_t launch_vjp_f64(int d, int k, const VjpArgs& a, size_t smem, cudaStre
 cudaError_t launch_vjp_split(int d, int k, const VjpArgs& a, size_t smem, cudaStream_t s, bool* found);
 cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int d,
                               const void* local, int local_dtype, double* grad, cudaStream_t s, bool add = false);
+struct GatherBlocks;
+// Defined in vjp_split.cu: the node sums of up to kGatherMaxBlocks blocks in one pass
+// (vjp_gather_blocks_kernel), rows of one dtype.
+cudaError_t launch_vjp_gather_blocks(const GatherBlocks& gb, int64_t num_nodes, int d, int local_dtype, double* grad,
+                                     cudaStream_t s, bool add);
 
 }  // namespace tlg

@@ -38,6 +38,58 @@ cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t sme
   return cudaSuccess;
 }
 
+cudaError_t launch_vjp_sumfact_bwd(bool split, int n, const VjpSfArgs& a, size_t smem, int threads, cudaStream_t s,
+                                   bool* found) {
+  *found = true;
+#define TLG_VSB(F, NN) \
+  if (n == NN) { \
+    auto kern = a.m[0] == NN ? vjp_sumfact_bwd_kernel<F, NN, NN> : vjp_sumfact_bwd_kernel<F, NN, 0>; \
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e != cudaSuccess) return e; \
+    const int grid = persistent_grid(kern, smem, a.padded, threads); \
+    kern<<<grid, threads, smem, s>>>(a); \
+    return cudaGetLastError(); \
+  }
+  if (split) {
+    TLG_VSB(float, 2)
+    TLG_VSB(float, 3)
+  } else {
+    TLG_VSB(double, 2)
+    TLG_VSB(double, 3)
+  }
+#undef TLG_VSB
+  *found = false;
+  return cudaSuccess;
+}
+
+cudaError_t launch_vjp_sumfact_tile(bool split, int n, const VjpSfArgs& a, size_t smem, cudaStream_t s, bool* found) {
+  *found = true;
+  const bool cube = a.m[0] == a.m[1] && a.m[1] == a.m[2];
+#define TLG_VST(F, NN, MM) \
+  if (n == NN && (MM == 0 || (cube && a.m[0] == MM))) { \
+    auto kern = vjp_sumfact_tile_kernel<F, NN, MM>; \
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e != cudaSuccess) return e; \
+    const int grid = persistent_grid(kern, smem, a.padded / 16 * kEvalThreads, kEvalThreads); \
+    kern<<<grid, kEvalThreads, smem, s>>>(a); \
+    return cudaGetLastError(); \
+  }
+  if (split) {
+    TLG_VST(float, 2, 2)
+    TLG_VST(float, 3, 3)
+    TLG_VST(float, 2, 0)
+    TLG_VST(float, 3, 0)
+  } else {
+    TLG_VST(double, 2, 2)
+    TLG_VST(double, 3, 3)
+    TLG_VST(double, 2, 0)
+    TLG_VST(double, 3, 0)
+  }
+#undef TLG_VST
+  *found = false;
+  return cudaSuccess;
+}
+
 cudaError_t launch_sumfact(int precision, int td, int gd, int n, const SfArgs& a, size_t smem, cudaStream_t s,
                            bool* found) {
   if (a.mask & kOutFacetNormals) return launch_sumfact_fn(precision, td, gd, n, a, smem, s, found);

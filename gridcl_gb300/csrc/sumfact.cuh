@@ -778,4 +778,380 @@ __global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_kernel(const __grid_
   }
 }
 
+
+// The adjoint of hexahedra at tensor-product rules from forward fields already written: det J and
+// K read back per point (the pinv layout K(t, h) at h * D + t, as the fused kernel writes it)
+// instead of recomputed, so no coordinates, no forward contraction and no coordinate slots; the
+// transposed contraction, its accumulation order and the contribution rows exactly as
+// vjp_sumfact_kernel's. `a.out[2]` (det J) and `a.out[3]` (K) are the inputs here.
+template <typename F, int N, int M0>
+__global__ void __launch_bounds__(kEvalThreads) vjp_sumfact_bwd_kernel(const __grid_constant__ VjpSfArgs a) {
+  using A = Ar<F>;
+  constexpr int D = 3, K = N * N * N, LJ = 9, R = 4, TILE = 16;
+  constexpr int T = kEvalThreads;
+  constexpr int NV = D + 1 + LJ + 1 + LJ;  // xbar, dbar, Kbar, det J, K of a point
+  __shared__ uint64_t bar;
+  extern __shared__ __align__(16) unsigned char smem[];
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
+  const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
+  uint32_t* invperm = reinterpret_cast<uint32_t*>(smem + (a.tab_bytes + 15) / 16 * 16);
+  for (int i = threadIdx.x; i < K; i += T) invperm[perm[i]] = i;
+  __syncthreads();
+  F* slots = reinterpret_cast<F*>(reinterpret_cast<unsigned char*>(invperm) + (K * 4 + 15) / 16 * 16);
+  constexpr int S = T + 1;                              // stride of the contribution slots
+  F* Ps = slots + threadIdx.x;                          // [2][3][N][N] plane accumulators
+  F* Lw = slots + (size_t)2 * D * N * N * T;            // [K][3] contributions
+  F* Ls = Lw + threadIdx.x;
+  const F* B0 = reinterpret_cast<const F*>(smem + a.off_b[0]);
+  const F* D0 = reinterpret_cast<const F*>(smem + a.off_d[0]);
+  const F* B1 = reinterpret_cast<const F*>(smem + a.off_b[1]);
+  const F* D1 = reinterpret_cast<const F*>(smem + a.off_d[1]);
+  const F* B2 = reinterpret_cast<const F*>(smem + a.off_b[2]);
+  const F* D2 = reinterpret_cast<const F*>(smem + a.off_d[2]);
+  const F* ctx = static_cast<const F*>(a.ct[0]);
+  const F* ctd = static_cast<const F*>(a.ct[1]);
+  const F* ctk = static_cast<const F*>(a.ct[2]);
+  const F* fdet = static_cast<const F*>(a.out[2]);
+  const F* fk = static_cast<const F*>(a.out[3]);
+  const int m0 = a.m[0], m1 = a.m[1], m2 = a.m[2];
+  const int nq = a.num_points;
+  const int lane = threadIdx.x % 32;
+  const int64_t step = (int64_t)gridDim.x * T;
+
+  for (int64_t cw = (int64_t)blockIdx.x * T + (threadIdx.x & ~31); cw < a.padded; cw += step) {
+    const int64_t c = cw + lane;
+    const bool live = c < a.padded;
+#pragma unroll 4
+    for (int l = 0; l < K; ++l)
+#pragma unroll
+      for (int g = 0; g < D; ++g) Ls[(l * D + g) * S] = F(0);
+    // Lanes past the padded range read the values of the last padded cell.
+    const int64_t o = a.out_first_cell + (live ? c : a.padded - 1);
+    const int64_t tq = (o / TILE) * nq;
+    const int l16 = (int)(o % TILE);
+#define TLG_AT(q, len, comp) (((tq + (q)) * (len) + (comp)) * TILE + l16)
+    // A point's values, loaded PF points ahead (points run in rule order).
+    auto load_pt = [&](int q, F* v) {
+#pragma unroll
+      for (int g = 0; g < D; ++g) v[g] = ctx ? __ldg(ctx + TLG_AT(q, D, g)) : F(0);
+      v[D] = ctd ? __ldg(ctd + TLG_AT(q, 1, 0)) : F(0);
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) v[D + 1 + i] = ctk ? __ldg(ctk + TLG_AT(q, LJ, i)) : F(0);
+      v[D + 1 + LJ] = __ldg(fdet + TLG_AT(q, 1, 0));
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) v[D + 2 + LJ + i] = __ldg(fk + TLG_AT(q, LJ, i));
+    };
+    constexpr int PF = sizeof(F) == 4 ? 2 : 1;
+    F buf[PF][NV];
+#pragma unroll
+    for (int p = 0; p < PF; ++p) load_pt(min(p, nq - 1), buf[p]);
+
+    for (int c2 = 0; c2 < m2; ++c2) {
+#pragma unroll
+      for (int g = 0; g < D; ++g)
+#pragma unroll
+        for (int jj = 0; jj < N; ++jj)
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            Ps[((0 * D + g) * N * N + jj * N + i) * T] = F(0);
+            Ps[((1 * D + g) * N * N + jj * N + i) * T] = F(0);
+          }
+      for (int b1 = 0; b1 < m1; ++b1) {
+        F RU[D][N], RD1[D][N], RD2[D][N];
+#pragma unroll
+        for (int g = 0; g < D; ++g)
+#pragma unroll
+          for (int i = 0; i < N; ++i) RU[g][i] = RD1[g][i] = RD2[g][i] = F(0);
+#pragma unroll
+        for (int a0 = 0; a0 < (M0 > 0 ? M0 : m0); ++a0) {
+          const int q = a0 + m0 * (b1 + m1 * c2);
+          F nxt[NV];
+          load_pt(min(q + PF, nq - 1), nxt);
+          const F* cur = buf[0];
+          const F det = cur[D + 1 + LJ];
+          const F* kinv = cur + D + 2 + LJ;
+          // Jbar(g, d) at g * D + d; K(t, h) and Kbar(t, h) at h * D + t.
+          F jb[LJ];
+          const F s = A::mul(cur[D], det);
+#pragma unroll
+          for (int g = 0; g < D; ++g)
+#pragma unroll
+            for (int d = 0; d < D; ++d) jb[g * D + d] = A::mul(s, kinv[g * D + d]);
+          if (ctk) {
+            const F* kb = cur + D + 1;
+#pragma unroll
+            for (int t = 0; t < D; ++t)
+#pragma unroll
+              for (int d = 0; d < D; ++d) {
+                F mt = A::mul(kb[t], kinv[d]);
+#pragma unroll
+                for (int h = 1; h < D; ++h) mt = A::fma(kb[h * D + t], kinv[h * D + d], mt);
+#pragma unroll
+                for (int g = 0; g < D; ++g) jb[g * D + d] = A::fma(A::neg(kinv[g * D + t]), mt, jb[g * D + d]);
+              }
+          }
+          const F* xb = cur;
+#pragma unroll
+          for (int i = 0; i < N; ++i) {
+            const F bi = B0[a0 * N + i], di = D0[a0 * N + i];
+#pragma unroll
+            for (int g = 0; g < D; ++g) {
+              RU[g][i] = A::fma(bi, xb[g], A::fma(di, jb[g * D + 0], RU[g][i]));
+              RD1[g][i] = A::fma(bi, jb[g * D + 1], RD1[g][i]);
+              RD2[g][i] = A::fma(bi, jb[g * D + 2], RD2[g][i]);
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < NV; ++i) {
+#pragma unroll
+            for (int p = 0; p + 1 < PF; ++p) buf[p][i] = buf[p + 1][i];
+            buf[PF - 1][i] = nxt[i];
+          }
+        }
+        // The row into the plane accumulators.
+#pragma unroll
+        for (int jj = 0; jj < N; ++jj) {
+          const F bj = B1[b1 * N + jj], dj = D1[b1 * N + jj];
+#pragma unroll
+          for (int g = 0; g < D; ++g)
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              F* pu = Ps + ((0 * D + g) * N * N + jj * N + i) * T;
+              F* pv = Ps + ((1 * D + g) * N * N + jj * N + i) * T;
+              *pu = A::fma(bj, RU[g][i], A::fma(dj, RD1[g][i], *pu));
+              *pv = A::fma(bj, RD2[g][i], *pv);
+            }
+        }
+      }
+      // The plane into the contributions.
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        const F bk = B2[c2 * N + k], dk = D2[c2 * N + k];
+#pragma unroll
+        for (int jj = 0; jj < N; ++jj)
+#pragma unroll
+          for (int i = 0; i < N; ++i)
+#pragma unroll
+            for (int g = 0; g < D; ++g) {
+              F* lp = Ls + ((i + N * (jj + N * k)) * D + g) * S;
+              const F pu = Ps[((0 * D + g) * N * N + jj * N + i) * T];
+              const F pv = Ps[((1 * D + g) * N * N + jj * N + i) * T];
+              *lp = A::fma(bk, pu, A::fma(dk, pv, *lp));
+            }
+      }
+    }
+#undef TLG_AT
+    // The warp's cells' rows, Lagrange node order, as one run.
+    __syncwarp();
+    const int64_t cell0 = a.first_cell + cw;
+    const int64_t nreal = min((int64_t)32, a.range_end - cell0);
+    if (nreal > 0) {
+      F* dst = static_cast<F*>(a.local) + cell0 * (K * R);
+      const F* lw = Lw + (threadIdx.x & ~31);
+      for (int t = lane; t < nreal * K; t += 32) {
+        const int cl = t / K;
+        const int kk = t - cl * K;
+        const F* src = lw + (int)invperm[kk] * D * S + cl;
+        F* row4 = dst + (int64_t)t * R;
+        if constexpr (sizeof(F) == 4) {
+          *reinterpret_cast<float4*>(row4) = make_float4(src[0], src[S], src[2 * S], 0.0f);
+        } else {
+          reinterpret_cast<double2*>(row4)[0] = make_double2(src[0], src[S]);
+          reinterpret_cast<double2*>(row4)[1] = make_double2(src[2 * S], 0.0);
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Shared memory past the tables of the kernel above: the inverse permutation, the plane
+// accumulators (2 * 3 * N^2, stride `threads`) and the contribution slots (K * 3, stride
+// threads + 1), of F.
+inline size_t vjp_sumfact_bwd_extra_bytes(int n, int threads, size_t f_bytes) {
+  const size_t k = (size_t)n * n * n;
+  return (k * 4 + 15) / 16 * 16 + f_bytes * ((size_t)threads * 2 * 3 * n * n + (size_t)(threads + 1) * k * 3);
+}
+
+// ----------------------------------------------------------------------------------------
+// Tile kernels: the work of a 16-cell tile of the fields spread over the CTA, one phase after
+// another with a barrier between, each phase's work items (point and cell, cell and node, ...)
+// over the threads with the cell index fastest, so that the loads and stores of the fields are
+// coalesced and the shared-memory slots of one cell per lane are bank-spread (odd strides). Every
+// sum runs in vjp_sumfact_kernel's order, so fields and contribution rows are that kernel's bit
+// for bit.
+
+constexpr int kTileCells = 16;
+constexpr int kTileQS = 13 * kTileCells;  // per point: x̄ (3) and J̄ (9) of the tile's cells, padded
+
+// J̄(g, d) at g * 3 + d of a point from its cotangents (d̄ = db, K̄ = kb or null for zero) and its
+// det J and K (K(t, h) at h * 3 + t).
+template <typename F>
+__device__ __forceinline__ void tile_jbar(F db, const F* kb, F det, const F* kinv, F* jb) {
+  using A = Ar<F>;
+  constexpr int D = 3;
+  const F s = A::mul(db, det);
+#pragma unroll
+  for (int g = 0; g < D; ++g)
+#pragma unroll
+    for (int d = 0; d < D; ++d) jb[g * D + d] = A::mul(s, kinv[g * D + d]);
+  if (kb) {
+#pragma unroll
+    for (int t = 0; t < D; ++t)
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        F mt = A::mul(kb[t], kinv[d]);
+#pragma unroll
+        for (int h = 1; h < D; ++h) mt = A::fma(kb[h * D + t], kinv[h * D + d], mt);
+#pragma unroll
+        for (int g = 0; g < D; ++g) jb[g * D + d] = A::fma(A::neg(kinv[g * D + t]), mt, jb[g * D + d]);
+      }
+  }
+}
+
+// The transposed contraction of a tile along ξ0 (rows of m0 points) and ξ1 (planes of m1 rows):
+// one item per (cell, plane c2, coordinate g, node index i), from x̄ and J̄ in V into the plane
+// sums P ([cell * ps + ((c2 * 3 + g) * N + j) * N + i) * 2 + (u, v)]).
+template <typename F, int N, int M, int T>
+__device__ __forceinline__ void tile_planes(const F* V, F* P, int ps, const F* B0, const F* D0, const F* B1,
+                                            const F* D1, int m0, int m1, int m2) {
+  using A = Ar<F>;
+  constexpr int D = 3, TILE = kTileCells, QS = kTileQS;
+  for (int it = threadIdx.x; it < m2 * D * N * TILE; it += T) {
+    const int l = it % TILE;
+    int r = it / TILE;
+    const int i = r % N;
+    r /= N;
+    const int g = r % D, c2 = r / D;
+    F pu[N], pv[N];
+#pragma unroll
+    for (int j = 0; j < N; ++j) pu[j] = pv[j] = F(0);
+    for (int b1 = 0; b1 < m1; ++b1) {
+      F ru = F(0), rd1 = F(0), rd2 = F(0);
+#pragma unroll
+      for (int a0 = 0; a0 < (M > 0 ? M : m0); ++a0) {
+        const F* vq = V + (a0 + m0 * (b1 + m1 * c2)) * QS + l;
+        const F bi = B0[a0 * N + i], di = D0[a0 * N + i];
+        ru = A::fma(bi, vq[g * TILE], A::fma(di, vq[(D + g * D) * TILE], ru));
+        rd1 = A::fma(bi, vq[(D + g * D + 1) * TILE], rd1);
+        rd2 = A::fma(bi, vq[(D + g * D + 2) * TILE], rd2);
+      }
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const F bj = B1[b1 * N + j], dj = D1[b1 * N + j];
+        pu[j] = A::fma(bj, ru, A::fma(dj, rd1, pu[j]));
+        pv[j] = A::fma(bj, rd2, pv[j]);
+      }
+    }
+    F* pl = P + l * ps + (c2 * D + g) * N * N * 2;
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      pl[(j * N + i) * 2] = pu[j];
+      pl[(j * N + i) * 2 + 1] = pv[j];
+    }
+  }
+}
+
+// Along ξ2: the contribution row of each (cell, node) of the tile, Lagrange node order, one item
+// per (cell, node) with the node fastest (consecutive items, consecutive rows).
+template <typename F, int N, int T>
+__device__ __forceinline__ void tile_rows(const VjpSfArgs& a, const F* P, int ps, const uint32_t* invperm,
+                                          const F* B2, const F* D2, int m2, int64_t tile) {
+  using A = Ar<F>;
+  constexpr int D = 3, K = N * N * N, R = 4, TILE = kTileCells;
+  const int64_t cell0 = a.first_cell + tile * TILE;
+  for (int it = threadIdx.x; it < K * TILE; it += T) {
+    const int l = it / K, kk = it - (it / K) * K;
+    const int64_t cell = cell0 + l;
+    if (cell >= a.range_end) continue;
+    const int t = (int)invperm[kk];
+    const int i = t % N, j = (t / N) % N, k = t / (N * N);
+    F v[D];
+#pragma unroll
+    for (int g = 0; g < D; ++g) {
+      F acc = F(0);
+      for (int c2 = 0; c2 < m2; ++c2) {
+        const F* pp = P + l * ps + ((c2 * D + g) * N * N + j * N + i) * 2;
+        acc = A::fma(B2[c2 * N + k], pp[0], A::fma(D2[c2 * N + k], pp[1], acc));
+      }
+      v[g] = acc;
+    }
+    F* row4 = static_cast<F*>(a.local) + (cell * K + kk) * R;
+    if constexpr (sizeof(F) == 4) {
+      *reinterpret_cast<float4*>(row4) = make_float4(v[0], v[1], v[2], 0.0f);
+    } else {
+      reinterpret_cast<double2*>(row4)[0] = make_double2(v[0], v[1]);
+      reinterpret_cast<double2*>(row4)[1] = make_double2(v[2], 0.0);
+    }
+  }
+}
+
+// The adjoint from forward fields already written (vjp_sumfact_bwd_kernel's work, tiled):
+// `a.out[2]` (det J) and `a.out[3]` (K) are read per (point, cell) with the cotangents, x̄ and J̄
+// put in shared memory; then tile_planes and tile_rows. Two barriers per tile. M > 0: M points
+// in each direction.
+template <typename F, int N, int M>
+__global__ void __launch_bounds__(kEvalThreads, 4) vjp_sumfact_tile_kernel(const __grid_constant__ VjpSfArgs a) {
+  constexpr int D = 3, K = N * N * N, LJ = 9, TILE = kTileCells, T = kEvalThreads, QS = kTileQS;
+  __shared__ uint64_t bar;
+  extern __shared__ __align__(16) unsigned char smem[];
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
+  const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
+  uint32_t* invperm = reinterpret_cast<uint32_t*>(smem + (a.tab_bytes + 15) / 16 * 16);
+  for (int i = threadIdx.x; i < K; i += T) invperm[perm[i]] = i;
+  const int m0 = M > 0 ? M : a.m[0], m1 = M > 0 ? M : a.m[1], m2 = M > 0 ? M : a.m[2];
+  const int nq = a.num_points;
+  const int ps = m2 * D * N * N * 2 + 1;
+  F* V = reinterpret_cast<F*>(reinterpret_cast<unsigned char*>(invperm) + (K * 4 + 15) / 16 * 16);
+  F* P = V + (size_t)nq * QS;
+  const F* B0 = reinterpret_cast<const F*>(smem + a.off_b[0]);
+  const F* D0 = reinterpret_cast<const F*>(smem + a.off_d[0]);
+  const F* B1 = reinterpret_cast<const F*>(smem + a.off_b[1]);
+  const F* D1 = reinterpret_cast<const F*>(smem + a.off_d[1]);
+  const F* B2 = reinterpret_cast<const F*>(smem + a.off_b[2]);
+  const F* D2 = reinterpret_cast<const F*>(smem + a.off_d[2]);
+  const F* ctx = static_cast<const F*>(a.ct[0]);
+  const F* ctd = static_cast<const F*>(a.ct[1]);
+  const F* ctk = static_cast<const F*>(a.ct[2]);
+  const F* fdet = static_cast<const F*>(a.out[2]);
+  const F* fk = static_cast<const F*>(a.out[3]);
+  __syncthreads();
+  const int64_t ntiles = a.padded / TILE;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t tq = (a.out_first_cell / TILE + tile) * nq;
+    for (int it = threadIdx.x; it < nq * TILE; it += T) {
+      const int q = it / TILE, l = it % TILE;
+#define TLG_AT(len, comp) (((tq + q) * (len) + (comp)) * TILE + l)
+      F xb[D], kb[LJ], kinv[LJ], jb[LJ];
+#pragma unroll
+      for (int g = 0; g < D; ++g) xb[g] = ctx ? __ldg(ctx + TLG_AT(D, g)) : F(0);
+      const F db = ctd ? __ldg(ctd + TLG_AT(1, 0)) : F(0);
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) kb[i] = ctk ? __ldg(ctk + TLG_AT(LJ, i)) : F(0);
+      const F det = __ldg(fdet + TLG_AT(1, 0));
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) kinv[i] = __ldg(fk + TLG_AT(LJ, i));
+#undef TLG_AT
+      tile_jbar<F>(db, ctk ? kb : nullptr, det, kinv, jb);
+      F* vq = V + q * QS + l;
+#pragma unroll
+      for (int g = 0; g < D; ++g) vq[g * TILE] = xb[g];
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) vq[(D + i) * TILE] = jb[i];
+    }
+    __syncthreads();
+    tile_planes<F, N, M, T>(V, P, ps, B0, D0, B1, D1, m0, m1, m2);
+    __syncthreads();
+    tile_rows<F, N, T>(a, P, ps, invperm, B2, D2, m2, tile);
+  }
+}
+
+// Shared memory past the tables of the kernel above: the inverse permutation, x̄ and J̄ of a
+// tile's points (13 * 16 per point) and the tile's plane sums (16 cells x (2 * 3 * N^2 * m2 + 1)),
+// of F.
+inline size_t vjp_sumfact_tile_extra_bytes(int n, int num_points, int m2, size_t f_bytes) {
+  const size_t k = (size_t)n * n * n;
+  return (k * 4 + 15) / 16 * 16 + f_bytes * ((size_t)num_points * 13 * 16 + 16 * ((size_t)m2 * 3 * n * n * 2 + 1));
+}
+
 }  // namespace tlg

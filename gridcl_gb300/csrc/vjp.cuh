@@ -468,4 +468,82 @@ __global__ void __launch_bounds__(kGatherNodes) vjp_gather_kernel(const uint32_t
   }
 }
 
+// The node sums of several blocks in one pass over the nodes (an adjoint batch's blocks in block
+// order): per node, the first block's sum (zero without entries) or, with `add`, the gradient's
+// value, then each further block's sum added where the node has entries, with the sums and their
+// order of vjp_gather_kernel's launches one block after another, so the gradient is the same bit
+// for bit; written once. A CTA skips a block none of its nodes has entries in.
+constexpr int kGatherMaxBlocks = 8;
+
+struct GatherBlocks {
+  const uint32_t* offsets[kGatherMaxBlocks];
+  const uint32_t* entries[kGatherMaxBlocks];
+  const void* local[kGatherMaxBlocks];
+  int count;
+};
+
+template <typename L, int D>
+__global__ void __launch_bounds__(kGatherNodes) vjp_gather_blocks_kernel(const __grid_constant__ GatherBlocks gb,
+                                                                         int64_t num_nodes, double* grad, int add) {
+  constexpr int R = vjp_row(D);
+  using Row = VjpRow<L, R>;
+  __shared__ typename Row::T rows[kGatherChunk];
+  for (int64_t n0 = (int64_t)blockIdx.x * kGatherNodes; n0 < num_nodes; n0 += (int64_t)gridDim.x * kGatherNodes) {
+    const int64_t n = n0 + threadIdx.x;
+    const int64_t n_end = min(n0 + kGatherNodes, num_nodes);
+    double v[D];
+#pragma unroll
+    for (int g = 0; g < D; ++g) v[g] = 0.0;
+    bool have = false;  // add: v holds the gradient's value
+    for (int bi = 0; bi < gb.count; ++bi) {
+      const uint32_t* offsets = gb.offsets[bi];
+      const uint32_t* entries = gb.entries[bi];
+      const L* local = static_cast<const L*>(gb.local[bi]);
+      const uint32_t e0 = offsets[n0], e1 = offsets[n_end];
+      uint32_t b = e0, e = e0;
+      if (e1 > e0 && n < num_nodes) {
+        b = offsets[n];
+        e = offsets[n + 1];
+      }
+      GatherSum<L> acc[D];
+      for (uint32_t c = e0; c < e1; c += kGatherChunk) {
+        const uint32_t cn = min((uint32_t)kGatherChunk, e1 - c);
+        uint32_t ent[kGatherChunk / kGatherNodes];
+#pragma unroll
+        for (int u = 0; u < kGatherChunk / kGatherNodes; ++u) {
+          const uint32_t i = threadIdx.x + kGatherNodes * u;
+          ent[u] = i < cn ? entries[c + i] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < kGatherChunk / kGatherNodes; ++u) {
+          const uint32_t i = threadIdx.x + kGatherNodes * u;
+          if (i < cn) rows[i] = Row::load(local + (int64_t)ent[u] * R);
+        }
+        __syncthreads();
+        const uint32_t lo = max(b, c), hi = min(e, c + cn);
+        for (uint32_t i = lo; i < hi; ++i)
+#pragma unroll
+          for (int g = 0; g < D; ++g) acc[g].add(Row::get(rows[i - c], g));
+        __syncthreads();
+      }
+      if (n >= num_nodes) continue;
+      if (bi == 0 && !add) {
+#pragma unroll
+        for (int g = 0; g < D; ++g) v[g] = acc[g].value();
+      } else if (e > b) {
+        if (add && !have) {
+#pragma unroll
+          for (int g = 0; g < D; ++g) v[g] = grad[n * D + g];
+          have = true;
+        }
+#pragma unroll
+        for (int g = 0; g < D; ++g) v[g] = __dadd_rn(v[g], acc[g].value());
+      }
+    }
+    if (n < num_nodes && (!add || have))
+#pragma unroll
+      for (int g = 0; g < D; ++g) grad[n * D + g] = v[g];
+  }
+}
+
 }  // namespace tlg

@@ -26,4 +26,24 @@ cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, 
   return cudaGetLastError();
 }
 
+cudaError_t launch_vjp_gather_blocks(const GatherBlocks& gb, int64_t num_nodes, int d, int local_dtype, double* grad,
+                                     cudaStream_t s, bool add) {
+  int64_t blocks = (num_nodes + kGatherNodes - 1) / kGatherNodes;
+  if (blocks < 1) blocks = 1;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+#define TLG_GATHER(L, DD) \
+  vjp_gather_blocks_kernel<L, DD><<<(unsigned)blocks, kGatherNodes, 0, s>>>(gb, num_nodes, grad, add ? 1 : 0)
+  if (local_dtype == 4) {
+    if (d == 1) TLG_GATHER(float, 1);
+    else if (d == 2) TLG_GATHER(float, 2);
+    else TLG_GATHER(float, 3);
+  } else {
+    if (d == 1) TLG_GATHER(double, 1);
+    else if (d == 2) TLG_GATHER(double, 2);
+    else TLG_GATHER(double, 3);
+  }
+#undef TLG_GATHER
+  return cudaGetLastError();
+}
+
 }  // namespace tlg

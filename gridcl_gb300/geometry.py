@@ -581,13 +581,18 @@ def node_incidence(g: Geometry, b: int) -> NodeIncidence:
 
 
 def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: str = "native",
-              forward=(), out: dict | None = None, local: torch.Tensor | None = None):
+              forward=(), out: dict | None = None, local: torch.Tensor | None = None,
+              from_fields: dict | None = None):
     """Cotangents of the node coordinates (``[node][GD]`` f64) for the cotangent fields
     ``{"points", "detj", "pinv", "normals"}`` (QuadFields of tile 16, f64, or f32 with
     ``precision="split"``; missing entries are zero; "detj" is the area element and "normals"
     the unit normals of curves and surfaces, TD + 1 = GD) of block b. J, det J and K are
     recomputed. The factors named in `forward` are evaluated in the same pass (fused forward +
-    adjoint) and returned: ``(grad, fields)``."""
+    adjoint) and returned: ``(grad, fields)``.
+
+    `from_fields`: the "detj" and "pinv" fields of a forward evaluation of the same block and
+    points already run (tile 16, the adjoint's field dtype); the adjoint reads them instead of
+    recomputing them (``tlg_vjp_block_from_fields``: hexahedra Q1/Q2 at tensor-product rules)."""
     from ._lib import TlgCotangents
 
     blk = g.blocks[b]
@@ -626,8 +631,21 @@ def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: s
         setattr(o, name, f.chunks[0].data.data_ptr())
     desc = g.block_desc(b)
     stream = current_stream_handle()
-    check(lib().tlg_vjp_block(tables.handle, ctypes.byref(desc), ctypes.byref(o), ctypes.byref(ct),
-                              local.data_ptr(), local.shape[0], stream))
+    if from_fields is not None:
+        if forward:
+            raise GridError(1, "from_fields reads the forward fields: no fused forward")
+        for name in ("detj", "pinv"):
+            f = from_fields.get(name)
+            if f is None or f.tile != GPU_QUAD_TILE or len(f.chunks) != 1 or f.chunks[0].data.dtype != fdt:
+                raise GridError(1, f"from_fields {name}: one chunk of tile 16 and dtype {fdt} expected")
+            if f.num_cells != blk.num_cells or f.num_points != nq:
+                raise GridError(2, f"from_fields {name}: another block's or point set's field")
+            setattr(o, name, f.chunks[0].data.data_ptr())
+        check(lib().tlg_vjp_block_from_fields(tables.handle, ctypes.byref(desc), ctypes.byref(o), ctypes.byref(ct),
+                                              local.data_ptr(), local.shape[0], stream))
+    else:
+        check(lib().tlg_vjp_block(tables.handle, ctypes.byref(desc), ctypes.byref(o), ctypes.byref(ct),
+                                  local.data_ptr(), local.shape[0], stream))
     _note_launch()
     inc = node_incidence(g, b)
     grad = torch.empty((g.nodes.shape[0], gd), dtype=torch.float64, device=dev)
@@ -732,9 +750,14 @@ class AdjointBatch:
 
     ``precision="df64"``: the forward fields are f64 and come from the double-float kernels
     (f64-accurate), each block's adjoint is the split-precision one (f32 cotangents, FP32
-    contributions summed per node in f64), both on the block's branch of the graph."""
+    contributions summed per node in f64), both on the block's branch of the graph.
 
-    def __init__(self, g: Geometry, rule: "QuadRule", cotangents: list, precision: str = "split", forward=()):
+    ``two_pass=True`` (``tlg_vjp_batch_set_two_pass``; det J and K among `forward`): blocks of
+    hexahedra at tensor-product rules run the policy's forward kernel, then the adjoint from the
+    det J and K fields it wrote; the others the fused pass."""
+
+    def __init__(self, g: Geometry, rule: "QuadRule", cotangents: list, precision: str = "split", forward=(),
+                 two_pass: bool = False):
         from ._lib import TlgCotangents
 
         if g.dtype != torch.float64:
@@ -797,6 +820,8 @@ class AdjointBatch:
                 fwd[b] = rule.get(blk.element.cell).tables(blk.element, gd, DF64).handle
             self._fwd = fwd
             check(lib().tlg_vjp_batch_set_forward(h, fwd))
+        if two_pass:
+            check(lib().tlg_vjp_batch_set_two_pass(h, 1))
 
     def launch(self) -> None:
         check(lib().tlg_vjp_batch_launch(self.handle, current_stream_handle()))

@@ -271,6 +271,17 @@ tlg_status tlg_vjp_block(const tlg_tables* tables, const tlg_block* block, const
                          const tlg_cotangents* cotangents, void* local, int64_t local_cells,
                          void* stream);
 
+/* The contributions of tlg_vjp_block from forward fields already written: outputs->detj and
+ * outputs->pinv (det J and K of the range, tiled as tlg_eval_block writes them) are read instead
+ * of recomputed, the other output pointers are ignored; the transposed contraction and the rows
+ * as tlg_vjp_block's sum-factorised adjoint (hexahedra Q1/Q2 at tensor-product rules in one
+ * block, f64 or split-precision tables; TLG_ERR_UNSUPPORTED otherwise). A forward pass on the
+ * paired or unrolled kernels plus this adjoint moves more bytes than the fused pass but needs
+ * neither the coordinates nor their slots here. No counterpart in the reference. */
+tlg_status tlg_vjp_block_from_fields(const tlg_tables* tables, const tlg_block* block, const tlg_outputs* outputs,
+                                     const tlg_cotangents* cotangents, void* local, int64_t local_cells,
+                                     void* stream);
+
 /* grad[n * gdim + g] = sum over node n's CSR entries e, in entry order, of local[e * R + g]
  * (R as in tlg_vjp_block; local_dtype 4 or 8 is the contributions' type): f64 sums of f64
  * contributions; f32 contributions summed as an FP32 TwoSum pair (about 48 significant bits)
@@ -285,10 +296,12 @@ tlg_status tlg_vjp_gather_add(const uint32_t* offsets, const uint32_t* entries, 
 /* Adjoint batches (the hybrid mesh's fused forward + adjoint in one CUDA graph launch): per block
  * its tables, block, outputs (forward fields or none), cotangents, contribution rows (local,
  * local_cells as in tlg_vjp_block) and node CSR (tlg_csr_build of its dofmap over num_nodes
- * nodes); grad [num_nodes][gdim] f64. The graph runs every block's tlg_vjp_block on its own
- * branch, then tlg_vjp_gather for the first block (every node written, zero where the block has no
- * entries) and tlg_vjp_gather_add for the others, block by block (no blocks: grad zeroed).
- * Captured on the first launch; the pointers are used as given at every launch. */
+ * nodes); grad [num_nodes][gdim] f64; the tables all TLG_SPLIT32 or none. The graph runs every
+ * block's tlg_vjp_block on its own branch, then the node sums of tlg_vjp_gather for the first block
+ * (every node written, zero where the block has no entries) and of tlg_vjp_gather_add for the
+ * others, in block order, eight blocks to a pass over the nodes (the same gradient bit for bit as
+ * those calls one after another; no blocks: grad zeroed). Captured on the first launch; the
+ * pointers are used as given at every launch. */
 typedef struct tlg_vjp_batch tlg_vjp_batch;
 tlg_status tlg_vjp_batch_create(const tlg_tables* const* tables, const tlg_block* blocks,
                                 const tlg_outputs* outputs, const tlg_cotangents* cotangents,
@@ -302,6 +315,11 @@ tlg_status tlg_vjp_batch_create(const tlg_tables* const* tables, const tlg_block
  * TLG_SPLIT32 adjoint tables (FP32 contributions summed per node in f64). Recaptures on the next
  * launch. No counterpart in the reference, which has no adjoint. */
 tlg_status tlg_vjp_batch_set_forward(tlg_vjp_batch* batch, const tlg_tables* const* forward);
+/* on = 1: blocks whose adjoint tlg_vjp_block_from_fields serves (and whose outputs include det J
+ * and K) run tlg_eval_block (the policy's forward kernel) and then that adjoint on their branch;
+ * the others, and every block while forward tables are set, the fused pass. Recaptures on the
+ * next launch. No counterpart in the reference. */
+tlg_status tlg_vjp_batch_set_two_pass(tlg_vjp_batch* batch, int on);
 tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* batch, void* stream);
 tlg_status tlg_vjp_batch_destroy(tlg_vjp_batch* batch);
 

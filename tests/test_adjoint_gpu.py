@@ -406,6 +406,29 @@ def test_adjoint_batch_equals_the_blocks(cuda, precision):
 
 
 @pytest.mark.parametrize("precision", ["native", "split"])
+def test_adjoint_batch_with_more_blocks_than_a_gather_pass(cuda, precision):
+    """11 blocks (slices of one P2 tetrahedron mesh, sharing nodes): the node sums run as a pass of
+    eight blocks writing the gradient and a pass of three adding onto it; the gradient equals the
+    per-block adjoints summed in block order, bit for bit."""
+    base = meshes.curved_box("Tetrahedron", 3, 2, jitter=0.02)
+    parts = np.array_split(base.blocks[0].cells, 11)
+    mesh = meshes.HostMesh(3, base.nodes, [meshes.HostBlock("Tetrahedron", 2, np.ascontiguousarray(c)) for c in parts])
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    ps = tg.PointSet("Tetrahedron", *tg.refcell.gauss_rule("Tetrahedron", 4))
+    dt = torch.float64 if precision == "native" else torch.float32
+    rng = np.random.default_rng(47)
+    cts = [cotangent_fields(rng, blk.num_cells, len(ps), dt)[0] for blk in g.blocks]
+    batch = tg.AdjointBatch(g, tg.QuadRule([ps]), cts, precision=precision)
+    batch.grad.fill_(float("nan"))
+    batch.launch()
+    want = torch.zeros_like(batch.grad)
+    for b in range(len(g.blocks)):
+        grad, _ = tg.vjp_block(g, b, ps, cts[b], precision=precision)
+        want += grad
+    assert torch.equal(batch.grad, want)
+
+
+@pytest.mark.parametrize("precision", ["native", "split"])
 def test_adjoint_batch_on_the_mixed_box(cuda, precision):
     """The tetrahedron/hexahedron/pyramid box (P2, sin-mapped and jittered) in one adjoint graph:
     the node cotangents equal the per-block adjoints summed in block order, bit for bit, and the
@@ -436,6 +459,76 @@ def test_adjoint_batch_on_the_mixed_box(cuda, precision):
                           h["detj"][..., 0], h["pinv"])
     assert torch.equal(batch.grad, want)
     assert orc.rel_err(batch.grad.cpu().numpy(), oracle) < (1e-11 if precision == "native" else 2e-5)
+
+
+@pytest.mark.parametrize("precision", ["native", "split"])
+def test_two_pass_adjoint_batch(cuda, precision):
+    """two_pass: the hexahedra's forward fields from the policy's kernel, then the adjoint from det
+    J and K read back (tlg_vjp_block_from_fields); the prisms and tetrahedra fused. The node
+    cotangents against the one-pass batch (the forward kernels differ only in rounding) and the
+    oracle; the forward fields those of tlg_eval_block."""
+    mesh = meshes.hybrid_box(300, 120, 60)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    rule = tg.QuadRule([tg.PointSet("Hexahedron", *tg.refcell.gauss_rule("Hexahedron", 4)),
+                        tg.PointSet("Prism", *tg.refcell.collapsed_rule("Prism", (3, 1, 7))),
+                        tg.PointSet("Tetrahedron", *tg.refcell.collapsed_rule("Tetrahedron", (4, 3, 2)))])
+    dt = torch.float64 if precision == "native" else torch.float32
+    rng = np.random.default_rng(41)
+    cts, hosts = [], []
+    for blk in g.blocks:
+        ct, host = cotangent_fields(rng, blk.num_cells, len(rule.get(blk.element.cell)), dt)
+        cts.append(ct)
+        hosts.append(host)
+    names = ("points", "jacobian", "detj", "pinv")
+    one = tg.AdjointBatch(g, rule, cts, precision=precision, forward=names)
+    one.launch()
+    two = tg.AdjointBatch(g, rule, cts, precision=precision, forward=names, two_pass=True)
+    two.launch()
+    two.launch()
+    tol = 1e-12 if precision == "native" else 2e-5
+    assert orc.rel_err(two.grad.cpu().numpy(), one.grad.cpu().numpy()) < tol
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
+    want = np.zeros(two.grad.shape)
+    for b, blk in enumerate(g.blocks):
+        h = hosts[b]
+        pts = rule.get(blk.element.cell).points
+        want += orc.vjp(blk.element.cell, blk.element.degree, absx, mesh.blocks[b].cells, pts, h["points"],
+                        h["detj"][..., 0], h["pinv"])
+    assert orc.rel_err(two.grad.cpu().numpy(), want) < (1e-11 if precision == "native" else 2e-5)
+    fwd = tg.geometric_factors_block(g, 0, rule.get("Hexahedron"), names,
+                                     precision="split" if precision == "split" else "native")
+    for k in names:
+        assert torch.equal(two.fields[0][k].chunks[0].data, fwd[k].chunks[0].data), k
+
+
+@pytest.mark.parametrize("precision", ["native", "split"])
+@pytest.mark.parametrize("degree,counts,missing", [(2, (3, 3, 3), None), (2, (2, 3, 4), "points"),
+                                                   (2, (3, 3, 3), "pinv"), (1, (2, 2, 2), None),
+                                                   (1, (3, 2, 2), "detj"), (2, (5, 5, 5), None)])
+def test_two_pass_adjoint_on_hexahedra(cuda, precision, degree, counts, missing):
+    """The adjoint from det J and K read back on 27 hexahedra (a whole tile of 16 and a partial
+    one), cube and anisotropic tensor rules, a missing cotangent counted as zero: against the
+    oracle and the fused one-pass batch. vjp_sumfact_tile_kernel, except FP64 at 125 points, whose
+    tile does not fit in shared memory (vjp_sumfact_bwd_kernel, one thread per cell)."""
+    mesh = meshes.curved_box("Hexahedron", 3, degree, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    ps = tg.PointSet("Hexahedron", *tg.refcell.collapsed_rule("Hexahedron", counts))
+    dt = torch.float64 if precision == "native" else torch.float32
+    ct, host = cotangent_fields(np.random.default_rng(43), mesh.blocks[0].num_cells, len(ps), dt)
+    if missing:
+        del ct[missing]
+        host[missing] = np.zeros_like(host[missing])
+    names = ("detj", "pinv")
+    two = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct], precision=precision, forward=names, two_pass=True)
+    two.launch()
+    one = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct], precision=precision, forward=names)
+    one.launch()
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
+    want = orc.vjp("Hexahedron", degree, absx, mesh.blocks[0].cells, ps.points, host["points"],
+                   host["detj"][..., 0], host["pinv"])
+    tol = 1e-11 if precision == "native" else 2e-5
+    assert orc.rel_err(two.grad.cpu().numpy(), want) < tol
+    assert orc.rel_err(two.grad.cpu().numpy(), one.grad.cpu().numpy()) < tol
 
 
 def test_adjoint_batch_with_double_float_forward(cuda):
