@@ -1654,6 +1654,50 @@ tlg_status vjp_sumfact_from_fields(const tlg_tables* t, const tlg_block* b, cons
   return ok();
 }
 
+// The adjoint of volume cells of any kind from forward fields already written (vjp_tile_kernel):
+// the node rows staged, then 13 * 16 values of F per point; `found` is false where it does not
+// apply (no node-row table, or more than the shared memory holds).
+size_t vjp_tile_smem(const tlg_tables* t) {
+  const size_t fbytes = t->dtype == TLG_SPLIT32 ? 4 : 8;
+  return (size_t)(t->vjp_bytes + 15) / 16 * 16 + (size_t)t->q * 13 * 16 * fbytes;
+}
+
+bool vjp_tile_applies(const tlg_tables* t) {
+  return t->td == 3 && t->gd == 3 && t->vjp_bytes > 0 && t->k <= 1024 && vjp_tile_smem(t) <= (size_t)227 * 1024;
+}
+
+tlg_status vjp_tile_from_fields(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o, const tlg_cotangents* ct,
+                                void* local, cudaStream_t s, bool* found) {
+  *found = false;
+  if (!vjp_tile_applies(t) || !o->detj || !o->pinv) return TLG_ERR_UNSUPPORTED;
+  *found = true;
+  tlg::VjpArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.tab = t->dev + t->off_vjp;
+  a.ct[0] = ct->points;
+  a.ct[1] = ct->detj;
+  a.ct[2] = ct->pinv;
+  a.out[2] = o->detj;
+  a.out[3] = o->pinv;
+  a.local = local;
+  a.err = t->err;
+  a.first_cell = o->first_cell;
+  a.padded = (o->num_cells + 15) / 16 * 16;
+  a.out_first_cell = o->out_first_cell;
+  a.last_cell = b->num_cells - 1;
+  a.range_end = o->first_cell + o->num_cells;
+  a.tab_bytes = t->vjp_bytes;
+  a.num_points = (int)t->q;
+  a.k_runtime = (int)t->k;
+  cudaError_t e = tlg::launch_vjp_tile(t->dtype == TLG_SPLIT32, a, vjp_tile_smem(t), s);
+  if (e != cudaSuccess) return cuda_fail(e, "tlg_vjp_block_from_fields launch");
+  g_last_family = TLG_STRATEGY_DIRECT;
+  return ok();
+}
+
+// Whether tlg_vjp_block_from_fields serves the tables.
+bool from_fields_applies(const tlg_tables* t) { return vjp_sumfact_preferred(t) || vjp_tile_applies(t); }
+
 // The adjoint below codimension 0 (vjp_surface.cu) from the node-row kernel's arguments: phi and
 // dphi staged when they and the thread slots (2 K GD values per thread) fit, else read from global
 // memory; 32 to 128 threads per CTA.
@@ -1797,9 +1841,12 @@ tlg_status tlg_vjp_block_from_fields(const tlg_tables* t, const tlg_block* b, co
   if (o->num_cells == 0 || t->q == 0) return ok();
   if (!local) return fail(TLG_ERR_INVALID_ARGUMENT, "tlg_vjp_block_from_fields: NULL local");
   bool found = false;
-  tlg_status st = vjp_sumfact_from_fields(t, b, o, ct, local, static_cast<cudaStream_t>(stream), &found);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  tlg_status st = vjp_sumfact_from_fields(t, b, o, ct, local, s, &found);
+  if (!found) st = vjp_tile_from_fields(t, b, o, ct, local, s, &found);
   if (!found)
-    return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block_from_fields: hexahedra Q1/Q2 at tensor-product rules only");
+    return fail(TLG_ERR_UNSUPPORTED, "tlg_vjp_block_from_fields: no kernel for the element and rule (volume cells "
+                                     "whose node rows and point slots fit in shared memory)");
   return st;
 }
 
@@ -1962,7 +2009,7 @@ tlg_status tlg_vjp_batch_launch(tlg_vjp_batch* b, void* stream) {
         if (st == TLG_OK)
           st = tlg_vjp_block(b->tables[i], &b->blocks[i], &adj, &b->cotangents[i], b->locals[i], b->local_cells[i],
                              b->streams[i]);
-      } else if (b->two_pass && vjp_sumfact_preferred(b->tables[i]) && b->outputs[i].detj && b->outputs[i].pinv) {
+      } else if (b->two_pass && from_fields_applies(b->tables[i]) && b->outputs[i].detj && b->outputs[i].pinv) {
         st = tlg_eval_block(b->tables[i], &b->blocks[i], &b->outputs[i], b->streams[i]);
         if (st == TLG_OK)
           st = tlg_vjp_block_from_fields(b->tables[i], &b->blocks[i], &b->outputs[i], &b->cotangents[i], b->locals[i],

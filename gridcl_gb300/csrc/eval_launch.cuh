@@ -94,7 +94,7 @@ cudaError_t launch_vjp_sumfact(bool split, int n, const VjpSfArgs& a, size_t sme
 cudaError_t launch_vjp_sumfact_bwd(bool split, int n, const VjpSfArgs& a, size_t smem, int threads, cudaStream_t s,
                                    bool* found);
 // Defined in sumfact.cu: the same with a 16-cell tile spread over the CTA (vjp_sumfact_tile_kernel;
-// 128 threads; work over a.padded / 16 tiles).
+// kTileBwdThreads threads; work over a.padded / 16 tiles).
 cudaError_t launch_vjp_sumfact_tile(bool split, int n, const VjpSfArgs& a, size_t smem, cudaStream_t s, bool* found);
 // Defined in sumfact.cu: the sum-factorised kernel for precision 4 (f32), 8 (f64) or 12 (split),
 // N nodes per direction; `found` is false when none is compiled for (td, gd, n).
@@ -130,6 +130,9 @@ cudaError_t launch_vjp_f64(int d, int k, const VjpArgs& a, size_t smem, cudaStre
 cudaError_t launch_vjp_split(int d, int k, const VjpArgs& a, size_t smem, cudaStream_t s, bool* found);
 cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int d,
                               const void* local, int local_dtype, double* grad, cudaStream_t s, bool add = false);
+// Defined in vjp_split.cu: the adjoint from det J and K fields for volume cells of any kind
+// (vjp_tile_kernel; a.k_runtime = K; smem: the node rows, then 13 * 16 values per point).
+cudaError_t launch_vjp_tile(bool split, const VjpArgs& a, size_t smem, cudaStream_t s);
 struct GatherBlocks;
 // Defined in vjp_split.cu: the node sums of up to kGatherMaxBlocks blocks in one pass
 // (vjp_gather_blocks_kernel), rows of one dtype.

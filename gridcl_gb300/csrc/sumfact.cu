@@ -70,8 +70,8 @@ cudaError_t launch_vjp_sumfact_tile(bool split, int n, const VjpSfArgs& a, size_
     auto kern = vjp_sumfact_tile_kernel<F, NN, MM>; \
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
     if (e != cudaSuccess) return e; \
-    const int grid = persistent_grid(kern, smem, a.padded / 16 * kEvalThreads, kEvalThreads); \
-    kern<<<grid, kEvalThreads, smem, s>>>(a); \
+    const int grid = persistent_grid(kern, smem, a.padded / 16 * kTileBwdThreads, kTileBwdThreads); \
+    kern<<<grid, kTileBwdThreads, smem, s>>>(a); \
     return cudaGetLastError(); \
   }
   if (split) {

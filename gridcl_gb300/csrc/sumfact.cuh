@@ -1010,99 +1010,119 @@ __device__ __forceinline__ void tile_jbar(F db, const F* kb, F det, const F* kin
 }
 
 // The transposed contraction of a tile along ξ0 (rows of m0 points) and ξ1 (planes of m1 rows):
-// one item per (cell, plane c2, coordinate g, node index i), from x̄ and J̄ in V into the plane
-// sums P ([cell * ps + ((c2 * 3 + g) * N + j) * N + i) * 2 + (u, v)]).
+// one item per (cell, plane c2, coordinate g), all node indices (j, i) of the plane at once, so that
+// each point's x̄ and J̄ are read once; from V into the plane sums P ([cell * ps + ((c2 * 3 + g)
+// * N + j) * N + i) * 2 + (u, v)]).
 template <typename F, int N, int M, int T>
 __device__ __forceinline__ void tile_planes(const F* V, F* P, int ps, const F* B0, const F* D0, const F* B1,
                                             const F* D1, int m0, int m1, int m2) {
   using A = Ar<F>;
   constexpr int D = 3, TILE = kTileCells, QS = kTileQS;
-  for (int it = threadIdx.x; it < m2 * D * N * TILE; it += T) {
-    const int l = it % TILE;
-    int r = it / TILE;
-    const int i = r % N;
-    r /= N;
+  for (int it = threadIdx.x; it < m2 * D * TILE; it += T) {
+    const int l = it % TILE, r = it / TILE;
     const int g = r % D, c2 = r / D;
-    F pu[N], pv[N];
+    F pu[N][N], pv[N][N];
 #pragma unroll
-    for (int j = 0; j < N; ++j) pu[j] = pv[j] = F(0);
+    for (int j = 0; j < N; ++j)
+#pragma unroll
+      for (int i = 0; i < N; ++i) pu[j][i] = pv[j][i] = F(0);
     for (int b1 = 0; b1 < m1; ++b1) {
-      F ru = F(0), rd1 = F(0), rd2 = F(0);
+      F ru[N], rd1[N], rd2[N];
+#pragma unroll
+      for (int i = 0; i < N; ++i) ru[i] = rd1[i] = rd2[i] = F(0);
 #pragma unroll
       for (int a0 = 0; a0 < (M > 0 ? M : m0); ++a0) {
         const F* vq = V + (a0 + m0 * (b1 + m1 * c2)) * QS + l;
-        const F bi = B0[a0 * N + i], di = D0[a0 * N + i];
-        ru = A::fma(bi, vq[g * TILE], A::fma(di, vq[(D + g * D) * TILE], ru));
-        rd1 = A::fma(bi, vq[(D + g * D + 1) * TILE], rd1);
-        rd2 = A::fma(bi, vq[(D + g * D + 2) * TILE], rd2);
+        const F xb = vq[g * TILE], j0 = vq[(D + g * D) * TILE];
+        const F j1 = vq[(D + g * D + 1) * TILE], j2 = vq[(D + g * D + 2) * TILE];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const F bi = B0[a0 * N + i], di = D0[a0 * N + i];
+          ru[i] = A::fma(bi, xb, A::fma(di, j0, ru[i]));
+          rd1[i] = A::fma(bi, j1, rd1[i]);
+          rd2[i] = A::fma(bi, j2, rd2[i]);
+        }
       }
 #pragma unroll
       for (int j = 0; j < N; ++j) {
         const F bj = B1[b1 * N + j], dj = D1[b1 * N + j];
-        pu[j] = A::fma(bj, ru, A::fma(dj, rd1, pu[j]));
-        pv[j] = A::fma(bj, rd2, pv[j]);
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          pu[j][i] = A::fma(bj, ru[i], A::fma(dj, rd1[i], pu[j][i]));
+          pv[j][i] = A::fma(bj, rd2[i], pv[j][i]);
+        }
       }
     }
     F* pl = P + l * ps + (c2 * D + g) * N * N * 2;
 #pragma unroll
-    for (int j = 0; j < N; ++j) {
-      pl[(j * N + i) * 2] = pu[j];
-      pl[(j * N + i) * 2 + 1] = pv[j];
-    }
+    for (int j = 0; j < N; ++j)
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        pl[(j * N + i) * 2] = pu[j][i];
+        pl[(j * N + i) * 2 + 1] = pv[j][i];
+      }
   }
 }
 
-// Along ξ2: the contribution row of each (cell, node) of the tile, Lagrange node order, one item
-// per (cell, node) with the node fastest (consecutive items, consecutive rows).
-template <typename F, int N, int T>
-__device__ __forceinline__ void tile_rows(const VjpSfArgs& a, const F* P, int ps, const uint32_t* invperm,
+// Along ξ2: one item per (cell, node indices j, i), the cell slowest, which forms the rows of the
+// N nodes (i, j, k) and writes them at their Lagrange positions (perm: tensor slot to Lagrange
+// node).
+template <typename F, int N, int M, int T>
+__device__ __forceinline__ void tile_rows(const VjpSfArgs& a, const F* P, int ps, const uint32_t* perm,
                                           const F* B2, const F* D2, int m2, int64_t tile) {
   using A = Ar<F>;
   constexpr int D = 3, K = N * N * N, R = 4, TILE = kTileCells;
   const int64_t cell0 = a.first_cell + tile * TILE;
-  for (int it = threadIdx.x; it < K * TILE; it += T) {
-    const int l = it / K, kk = it - (it / K) * K;
+  for (int it = threadIdx.x; it < N * N * TILE; it += T) {
+    const int l = it / (N * N), r = it % (N * N);
+    const int i = r % N, j = r / N;
     const int64_t cell = cell0 + l;
     if (cell >= a.range_end) continue;
-    const int t = (int)invperm[kk];
-    const int i = t % N, j = (t / N) % N, k = t / (N * N);
-    F v[D];
+    F acc[N][D];
 #pragma unroll
-    for (int g = 0; g < D; ++g) {
-      F acc = F(0);
-      for (int c2 = 0; c2 < m2; ++c2) {
+    for (int k = 0; k < N; ++k)
+#pragma unroll
+      for (int g = 0; g < D; ++g) acc[k][g] = F(0);
+#pragma unroll
+    for (int c2 = 0; c2 < (M > 0 ? M : m2); ++c2)
+#pragma unroll
+      for (int g = 0; g < D; ++g) {
         const F* pp = P + l * ps + ((c2 * D + g) * N * N + j * N + i) * 2;
-        acc = A::fma(B2[c2 * N + k], pp[0], A::fma(D2[c2 * N + k], pp[1], acc));
+        const F pu = pp[0], pv = pp[1];
+#pragma unroll
+        for (int k = 0; k < N; ++k) acc[k][g] = A::fma(B2[c2 * N + k], pu, A::fma(D2[c2 * N + k], pv, acc[k][g]));
       }
-      v[g] = acc;
-    }
-    F* row4 = static_cast<F*>(a.local) + (cell * K + kk) * R;
-    if constexpr (sizeof(F) == 4) {
-      *reinterpret_cast<float4*>(row4) = make_float4(v[0], v[1], v[2], 0.0f);
-    } else {
-      reinterpret_cast<double2*>(row4)[0] = make_double2(v[0], v[1]);
-      reinterpret_cast<double2*>(row4)[1] = make_double2(v[2], 0.0);
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      F* row4 = static_cast<F*>(a.local) + (cell * K + perm[i + N * (j + N * k)]) * R;
+      if constexpr (sizeof(F) == 4) {
+        *reinterpret_cast<float4*>(row4) = make_float4(acc[k][0], acc[k][1], acc[k][2], 0.0f);
+      } else {
+        reinterpret_cast<double2*>(row4)[0] = make_double2(acc[k][0], acc[k][1]);
+        reinterpret_cast<double2*>(row4)[1] = make_double2(acc[k][2], 0.0);
+      }
     }
   }
 }
 
-// The adjoint from forward fields already written (vjp_sumfact_bwd_kernel's work, tiled):
+// The adjoint from forward fields already written (vjp_sumfact_bwd_kernel's work, tiled; 144
+// threads, so that each phase of a Q2 tile at 27 points is whole rounds of items):
 // `a.out[2]` (det J) and `a.out[3]` (K) are read per (point, cell) with the cotangents, x̄ and J̄
 // put in shared memory; then tile_planes and tile_rows. Two barriers per tile. M > 0: M points
 // in each direction.
+constexpr int kTileBwdThreads = 144;
+
 template <typename F, int N, int M>
-__global__ void __launch_bounds__(kEvalThreads, 4) vjp_sumfact_tile_kernel(const __grid_constant__ VjpSfArgs a) {
-  constexpr int D = 3, K = N * N * N, LJ = 9, TILE = kTileCells, T = kEvalThreads, QS = kTileQS;
+__global__ void __launch_bounds__(kTileBwdThreads, sizeof(F) == 4 ? 5 : 3) vjp_sumfact_tile_kernel(const __grid_constant__ VjpSfArgs a) {
+  constexpr int D = 3, LJ = 9, TILE = kTileCells, T = kTileBwdThreads, QS = kTileQS;
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
   if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   const uint32_t* perm = reinterpret_cast<const uint32_t*>(smem + a.off_perm);
-  uint32_t* invperm = reinterpret_cast<uint32_t*>(smem + (a.tab_bytes + 15) / 16 * 16);
-  for (int i = threadIdx.x; i < K; i += T) invperm[perm[i]] = i;
   const int m0 = M > 0 ? M : a.m[0], m1 = M > 0 ? M : a.m[1], m2 = M > 0 ? M : a.m[2];
   const int nq = a.num_points;
   const int ps = m2 * D * N * N * 2 + 1;
-  F* V = reinterpret_cast<F*>(reinterpret_cast<unsigned char*>(invperm) + (K * 4 + 15) / 16 * 16);
+  F* V = reinterpret_cast<F*>(smem + (a.tab_bytes + 15) / 16 * 16);
   F* P = V + (size_t)nq * QS;
   const F* B0 = reinterpret_cast<const F*>(smem + a.off_b[0]);
   const F* D0 = reinterpret_cast<const F*>(smem + a.off_d[0]);
@@ -1142,16 +1162,14 @@ __global__ void __launch_bounds__(kEvalThreads, 4) vjp_sumfact_tile_kernel(const
     __syncthreads();
     tile_planes<F, N, M, T>(V, P, ps, B0, D0, B1, D1, m0, m1, m2);
     __syncthreads();
-    tile_rows<F, N, T>(a, P, ps, invperm, B2, D2, m2, tile);
+    tile_rows<F, N, M, T>(a, P, ps, perm, B2, D2, m2, tile);
   }
 }
 
-// Shared memory past the tables of the kernel above: the inverse permutation, x̄ and J̄ of a
-// tile's points (13 * 16 per point) and the tile's plane sums (16 cells x (2 * 3 * N^2 * m2 + 1)),
-// of F.
+// Shared memory past the tables of the kernel above: x̄ and J̄ of a tile's points (13 * 16 per
+// point) and the tile's plane sums (16 cells x (2 * 3 * N^2 * m2 + 1)), of F.
 inline size_t vjp_sumfact_tile_extra_bytes(int n, int num_points, int m2, size_t f_bytes) {
-  const size_t k = (size_t)n * n * n;
-  return (k * 4 + 15) / 16 * 16 + f_bytes * ((size_t)num_points * 13 * 16 + 16 * ((size_t)m2 * 3 * n * n * 2 + 1));
+  return f_bytes * ((size_t)num_points * 13 * 16 + 16 * ((size_t)m2 * 3 * n * n * 2 + 1));
 }
 
 }  // namespace tlg

@@ -64,6 +64,7 @@ struct VjpArgs {
   double origin[3];
   uint32_t last_node, tab_bytes;
   int num_points;
+  int k_runtime;  // K (vjp_tile_kernel)
 };
 
 constexpr int kVjpGroup = 4;
@@ -465,6 +466,141 @@ __global__ void __launch_bounds__(kGatherNodes) vjp_gather_kernel(const uint32_t
     if (n < num_nodes && (!add || e > b))
 #pragma unroll
       for (int g = 0; g < D; ++g) grad[n * D + g] = add ? __dadd_rn(grad[n * D + g], acc[g].value()) : acc[g].value();
+  }
+}
+
+// The adjoint from forward fields already written, for volume cells of any kind (D = 3, K at run
+// time): det J and K read back instead of recomputed, so no coordinates and no forward
+// contraction. A 16-cell tile of the fields per CTA step: one item per (point, cell) reads the
+// cotangents, det J and K (coalesced, the cell fastest) and puts x̄ and J̄ (J̄(g, d) = d̄ det J
+// K(d, g) - (K^T K̄ K^T)(g, d)) in shared memory; one item per (cell, node pair k, k + ceil(K/2)),
+// the node fastest, sums over the points phi_k x̄ + sum_d dphi_k[d] J̄(., d) from the staged node
+// rows and writes the two contribution rows. Two barriers per tile.
+constexpr int kVjpTileThreads = 128;
+
+template <typename F>
+__global__ void __launch_bounds__(kVjpTileThreads) vjp_tile_kernel(const __grid_constant__ VjpArgs a) {
+  using A = Ar<F>;
+  constexpr int D = 3, LJ = 9, TILE = 16, T = kVjpTileThreads, QS = 13 * TILE, R = 4;
+  constexpr int PN = sizeof(F) == 4 ? 2 : 1;  // points per node row (split: point pairs)
+  __shared__ uint64_t bar;
+  extern __shared__ __align__(16) unsigned char smem[];
+  if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
+  const F* tab = reinterpret_cast<const F*>(smem);
+  F* V = reinterpret_cast<F*>(smem + (a.tab_bytes + 15) / 16 * 16);
+  const int K = a.k_runtime, KH = (K + 1) / 2, nq = a.num_points;
+  const F* ctx = static_cast<const F*>(a.ct[0]);
+  const F* ctd = static_cast<const F*>(a.ct[1]);
+  const F* ctk = static_cast<const F*>(a.ct[2]);
+  const F* fdet = static_cast<const F*>(a.out[2]);
+  const F* fk = static_cast<const F*>(a.out[3]);
+  // The 8 values of node k's row at point pair (or point) r: phi, dphi_0..2, PN points each.
+  auto row = [&](int r, int k, F* t) {
+    if constexpr (PN == 2) {
+      const float4* p = reinterpret_cast<const float4*>(tab + ((size_t)r * K + k) * 8);
+      const float4 u = p[0], v = p[1];
+      t[0] = u.x; t[1] = u.y; t[2] = u.z; t[3] = u.w;
+      t[4] = v.x; t[5] = v.y; t[6] = v.z; t[7] = v.w;
+    } else {
+      const double2* p = reinterpret_cast<const double2*>(tab + ((size_t)r * K + k) * 4);
+      const double2 u = p[0], v = p[1];
+      t[0] = u.x; t[1] = u.y; t[2] = v.x; t[3] = v.y;
+    }
+  };
+  const int64_t ntiles = a.padded / TILE;
+  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int64_t tq = (a.out_first_cell / TILE + tile) * nq;
+    for (int it = threadIdx.x; it < nq * TILE; it += T) {
+      const int q = it / TILE, l = it % TILE;
+#define TLG_AT(len, comp) (((tq + q) * (len) + (comp)) * TILE + l)
+      F xb[D], kb[LJ], kinv[LJ], jb[LJ];
+#pragma unroll
+      for (int g = 0; g < D; ++g) xb[g] = ctx ? __ldg(ctx + TLG_AT(D, g)) : F(0);
+      const F db = ctd ? __ldg(ctd + TLG_AT(1, 0)) : F(0);
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) kb[i] = ctk ? __ldg(ctk + TLG_AT(LJ, i)) : F(0);
+      const F det = __ldg(fdet + TLG_AT(1, 0));
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) kinv[i] = __ldg(fk + TLG_AT(LJ, i));
+#undef TLG_AT
+      // J̄(g, d) at g * D + d; K(t, h) and K̄(t, h) at h * D + t.
+      const F s = A::mul(db, det);
+#pragma unroll
+      for (int g = 0; g < D; ++g)
+#pragma unroll
+        for (int d = 0; d < D; ++d) jb[g * D + d] = A::mul(s, kinv[g * D + d]);
+      if (ctk) {
+#pragma unroll
+        for (int t = 0; t < D; ++t)
+#pragma unroll
+          for (int d = 0; d < D; ++d) {
+            F mt = A::mul(kb[t], kinv[d]);
+#pragma unroll
+            for (int h = 1; h < D; ++h) mt = A::fma(kb[h * D + t], kinv[h * D + d], mt);
+#pragma unroll
+            for (int g = 0; g < D; ++g) jb[g * D + d] = A::fma(A::neg(kinv[g * D + t]), mt, jb[g * D + d]);
+          }
+      }
+      F* vq = V + q * QS + l;
+#pragma unroll
+      for (int g = 0; g < D; ++g) vq[g * TILE] = xb[g];
+#pragma unroll
+      for (int i = 0; i < LJ; ++i) vq[(D + i) * TILE] = jb[i];
+    }
+    __syncthreads();
+    const int64_t cell0 = a.first_cell + tile * TILE;
+    for (int it = threadIdx.x; it < KH * TILE; it += T) {
+      const int l = it / KH, k0 = it - (it / KH) * KH, k1 = k0 + KH;
+      const bool two = k1 < K;
+      const int64_t cell = cell0 + l;
+      if (cell >= a.range_end) continue;
+      F acc0[D], acc1[D];
+#pragma unroll
+      for (int g = 0; g < D; ++g) acc0[g] = acc1[g] = F(0);
+      for (int r = 0; r < (nq + PN - 1) / PN; ++r) {
+        F t0[4 * PN], t1[4 * PN];
+        row(r, k0, t0);
+        if (two) row(r, k1, t1);
+#pragma unroll
+        for (int h = 0; h < PN; ++h) {
+          const int q = r * PN + h;
+          if (q >= nq) break;
+          const F* vq = V + q * QS + l;
+          F v[D + LJ];
+#pragma unroll
+          for (int i = 0; i < D + LJ; ++i) v[i] = vq[i * TILE];
+#pragma unroll
+          for (int g = 0; g < D; ++g) {
+            F s0 = A::fma(t0[h], v[g], acc0[g]);
+#pragma unroll
+            for (int d = 0; d < D; ++d) s0 = A::fma(t0[(1 + d) * PN + h], v[D + g * D + d], s0);
+            acc0[g] = s0;
+          }
+          if (two) {
+#pragma unroll
+            for (int g = 0; g < D; ++g) {
+              F s1 = A::fma(t1[h], v[g], acc1[g]);
+#pragma unroll
+              for (int d = 0; d < D; ++d) s1 = A::fma(t1[(1 + d) * PN + h], v[D + g * D + d], s1);
+              acc1[g] = s1;
+            }
+          }
+        }
+      }
+      F* base = static_cast<F*>(a.local) + cell * K * R;
+      if constexpr (sizeof(F) == 4) {
+        *reinterpret_cast<float4*>(base + k0 * R) = make_float4(acc0[0], acc0[1], acc0[2], 0.0f);
+        if (two) *reinterpret_cast<float4*>(base + k1 * R) = make_float4(acc1[0], acc1[1], acc1[2], 0.0f);
+      } else {
+        reinterpret_cast<double2*>(base + k0 * R)[0] = make_double2(acc0[0], acc0[1]);
+        reinterpret_cast<double2*>(base + k0 * R)[1] = make_double2(acc0[2], 0.0);
+        if (two) {
+          reinterpret_cast<double2*>(base + k1 * R)[0] = make_double2(acc1[0], acc1[1]);
+          reinterpret_cast<double2*>(base + k1 * R)[1] = make_double2(acc1[2], 0.0);
+        }
+      }
+    }
+    __syncthreads();
   }
 }
 

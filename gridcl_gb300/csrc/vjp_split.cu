@@ -26,6 +26,17 @@ cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, 
   return cudaGetLastError();
 }
 
+cudaError_t launch_vjp_tile(bool split, const VjpArgs& a, size_t smem, cudaStream_t s) {
+  auto launch = [&](auto kern) -> cudaError_t {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int grid = persistent_grid(kern, smem, a.padded / 16 * kVjpTileThreads, kVjpTileThreads);
+    kern<<<grid, kVjpTileThreads, smem, s>>>(a);
+    return cudaGetLastError();
+  };
+  return split ? launch(vjp_tile_kernel<float>) : launch(vjp_tile_kernel<double>);
+}
+
 cudaError_t launch_vjp_gather_blocks(const GatherBlocks& gb, int64_t num_nodes, int d, int local_dtype, double* grad,
                                      cudaStream_t s, bool add) {
   int64_t blocks = (num_nodes + kGatherNodes - 1) / kGatherNodes;

@@ -592,7 +592,7 @@ def vjp_block(g: Geometry, b: int, pts: PointSet, cotangents: dict, precision: s
 
     `from_fields`: the "detj" and "pinv" fields of a forward evaluation of the same block and
     points already run (tile 16, the adjoint's field dtype); the adjoint reads them instead of
-    recomputing them (``tlg_vjp_block_from_fields``: hexahedra Q1/Q2 at tensor-product rules)."""
+    recomputing them (``tlg_vjp_block_from_fields``: volume cells)."""
     from ._lib import TlgCotangents
 
     blk = g.blocks[b]
@@ -753,8 +753,8 @@ class AdjointBatch:
     contributions summed per node in f64), both on the block's branch of the graph.
 
     ``two_pass=True`` (``tlg_vjp_batch_set_two_pass``; det J and K among `forward`): blocks of
-    hexahedra at tensor-product rules run the policy's forward kernel, then the adjoint from the
-    det J and K fields it wrote; the others the fused pass."""
+    volume cells run the policy's forward kernel, then the adjoint from the det J and K fields it
+    wrote (``tlg_vjp_block_from_fields``); the others the fused pass."""
 
     def __init__(self, g: Geometry, rule: "QuadRule", cotangents: list, precision: str = "split", forward=(),
                  two_pass: bool = False):

@@ -273,11 +273,13 @@ tlg_status tlg_vjp_block(const tlg_tables* tables, const tlg_block* block, const
 
 /* The contributions of tlg_vjp_block from forward fields already written: outputs->detj and
  * outputs->pinv (det J and K of the range, tiled as tlg_eval_block writes them) are read instead
- * of recomputed, the other output pointers are ignored; the transposed contraction and the rows
- * as tlg_vjp_block's sum-factorised adjoint (hexahedra Q1/Q2 at tensor-product rules in one
- * block, f64 or split-precision tables; TLG_ERR_UNSUPPORTED otherwise). A forward pass on the
- * paired or unrolled kernels plus this adjoint moves more bytes than the fused pass but needs
- * neither the coordinates nor their slots here. No counterpart in the reference. */
+ * of recomputed, the other output pointers are ignored. Volume cells (TD = GD = 3), f64 or
+ * split-precision tables: hexahedra Q1/Q2 at tensor-product rules by the sum-factorised
+ * transposed contraction (rows as tlg_vjp_block's sum-factorised adjoint, bit for bit), other
+ * cells and rules from the tables' node rows where they and 13 * 16 values per point fit in
+ * shared memory; TLG_ERR_UNSUPPORTED otherwise. A forward pass plus this adjoint moves more bytes
+ * than the fused pass but needs neither the coordinates nor the forward contraction here. No
+ * counterpart in the reference. */
 tlg_status tlg_vjp_block_from_fields(const tlg_tables* tables, const tlg_block* block, const tlg_outputs* outputs,
                                      const tlg_cotangents* cotangents, void* local, int64_t local_cells,
                                      void* stream);

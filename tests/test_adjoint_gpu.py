@@ -531,6 +531,37 @@ def test_two_pass_adjoint_on_hexahedra(cuda, precision, degree, counts, missing)
     assert orc.rel_err(two.grad.cpu().numpy(), one.grad.cpu().numpy()) < tol
 
 
+@pytest.mark.parametrize("precision", ["native", "split"])
+@pytest.mark.parametrize("cell,degree,rdeg,missing", [("Tetrahedron", 2, 4, None), ("Tetrahedron", 3, 6, "points"),
+                                                      ("Prism", 2, 4, None), ("Pyramid", 2, 4, "pinv"),
+                                                      ("Hexahedron", 2, 4, None), ("Tetrahedron", 1, 3, "detj")])
+def test_two_pass_adjoint_on_volume_cells(cuda, precision, cell, degree, rdeg, missing):
+    """The adjoint from det J and K read back through the node rows (vjp_tile_kernel): tetrahedra,
+    prisms, pyramids and hexahedra at a rule in no tensor order, odd and even point counts, a
+    missing cotangent counted as zero; against the oracle and the fused one-pass batch."""
+    mesh = meshes.curved_box(cell, 2, degree, jitter=0.02)
+    g = tg.Geometry.from_host(mesh, dtype=torch.float64)
+    pts, w = tg.refcell.gauss_rule(cell, rdeg)
+    order = np.random.default_rng(5).permutation(len(pts))
+    ps = tg.PointSet(cell, pts[order], w[order])
+    dt = torch.float64 if precision == "native" else torch.float32
+    ct, host = cotangent_fields(np.random.default_rng(53), mesh.blocks[0].num_cells, len(ps), dt)
+    if missing:
+        del ct[missing]
+        host[missing] = np.zeros_like(host[missing])
+    names = ("detj", "pinv")
+    two = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct], precision=precision, forward=names, two_pass=True)
+    two.launch()
+    one = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct], precision=precision, forward=names)
+    one.launch()
+    absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
+    want = orc.vjp(cell, degree, absx, mesh.blocks[0].cells, ps.points, host["points"], host["detj"][..., 0],
+                   host["pinv"])
+    tol = 1e-11 if precision == "native" else 2e-5
+    assert orc.rel_err(two.grad.cpu().numpy(), want) < tol
+    assert orc.rel_err(two.grad.cpu().numpy(), one.grad.cpu().numpy()) < tol
+
+
 def test_adjoint_batch_with_double_float_forward(cuda):
     """precision="df64": each block's forward fields from the double-float kernels (bit for bit
     the fields of tlg_eval_block with df64 tables, and within 1e-12 of the oracle's f64 values),
