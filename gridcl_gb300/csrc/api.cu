@@ -1655,11 +1655,11 @@ tlg_status vjp_sumfact_from_fields(const tlg_tables* t, const tlg_block* b, cons
 }
 
 // The adjoint of volume cells of any kind from forward fields already written (vjp_tile_kernel):
-// the node rows staged, then 13 * 16 values of F per point; `found` is false where it does not
+// the node rows staged, then 12 * 16 values of F per point; `found` is false where it does not
 // apply (no node-row table, or more than the shared memory holds).
 size_t vjp_tile_smem(const tlg_tables* t) {
   const size_t fbytes = t->dtype == TLG_SPLIT32 ? 4 : 8;
-  return (size_t)(t->vjp_bytes + 15) / 16 * 16 + (size_t)t->q * 13 * 16 * fbytes;
+  return (size_t)(t->vjp_bytes + 15) / 16 * 16 + (size_t)t->q * tlg::kVjpTileRec * 16 * fbytes;
 }
 
 bool vjp_tile_applies(const tlg_tables* t) {

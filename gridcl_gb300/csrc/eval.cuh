@@ -199,6 +199,37 @@ struct Ar<float2> {
   __device__ static float2 sqrt(float2 a) { return make_float2(__fsqrt_rn(a.x), __fsqrt_rn(a.y)); }
 };
 
+// Four values of F at a 16-byte-aligned address in one 16-byte access (f32) or two (f64).
+template <typename F>
+struct Vec4;
+template <>
+struct Vec4<float> {
+  __device__ __forceinline__ static void put(float* p, float a, float b, float c, float d) {
+    *reinterpret_cast<float4*>(p) = make_float4(a, b, c, d);
+  }
+  __device__ __forceinline__ static void get(const float* p, float* v) {
+    const float4 u = *reinterpret_cast<const float4*>(p);
+    v[0] = u.x;
+    v[1] = u.y;
+    v[2] = u.z;
+    v[3] = u.w;
+  }
+};
+template <>
+struct Vec4<double> {
+  __device__ __forceinline__ static void put(double* p, double a, double b, double c, double d) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(a, b);
+    reinterpret_cast<double2*>(p)[1] = make_double2(c, d);
+  }
+  __device__ __forceinline__ static void get(const double* p, double* v) {
+    const double2 u = reinterpret_cast<const double2*>(p)[0], w = reinterpret_cast<const double2*>(p)[1];
+    v[0] = u.x;
+    v[1] = u.y;
+    v[2] = w.x;
+    v[3] = w.y;
+  }
+};
+
 // ----------------------------------------------------------------------------------------
 // Factor math on J (column-major GD x TD), tetraloma-geometry/src/layout.rs:166-369, in the
 // value type V. a*b - c*d is fma(a, b, -(c*d)) throughout.

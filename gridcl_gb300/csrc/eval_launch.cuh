@@ -131,7 +131,7 @@ cudaError_t launch_vjp_split(int d, int k, const VjpArgs& a, size_t smem, cudaSt
 cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, int64_t num_nodes, int d,
                               const void* local, int local_dtype, double* grad, cudaStream_t s, bool add = false);
 // Defined in vjp_split.cu: the adjoint from det J and K fields for volume cells of any kind
-// (vjp_tile_kernel; a.k_runtime = K; smem: the node rows, then 13 * 16 values per point).
+// (vjp_tile_kernel; a.k_runtime = K, the group and CTA sizes from vjp_tile_shape; smem: the node rows, then 12 * 16 values per point).
 cudaError_t launch_vjp_tile(bool split, const VjpArgs& a, size_t smem, cudaStream_t s);
 struct GatherBlocks;
 // Defined in vjp_split.cu: the node sums of up to kGatherMaxBlocks blocks in one pass

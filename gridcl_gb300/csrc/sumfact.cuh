@@ -977,12 +977,20 @@ inline size_t vjp_sumfact_bwd_extra_bytes(int n, int threads, size_t f_bytes) {
 // Tile kernels: the work of a 16-cell tile of the fields spread over the CTA, one phase after
 // another with a barrier between, each phase's work items (point and cell, cell and node, ...)
 // over the threads with the cell index fastest, so that the loads and stores of the fields are
-// coalesced and the shared-memory slots of one cell per lane are bank-spread (odd strides). Every
-// sum runs in vjp_sumfact_kernel's order, so fields and contribution rows are that kernel's bit
-// for bit.
+// coalesced. A point's x̄ and J̄ of one cell are a record of three 4-vectors (x̄_g, J̄(g, 0),
+// J̄(g, 1), J̄(g, 2)), [point][cell][12], each moved by one 16-byte access (f32); the plane sums
+// of a cell sit at an odd stride. Every sum runs in vjp_sumfact_kernel's order, so the
+// contribution rows are that kernel's bit for bit.
 
 constexpr int kTileCells = 16;
-constexpr int kTileQS = 13 * kTileCells;  // per point: x̄ (3) and J̄ (9) of the tile's cells, padded
+constexpr int kTileRec = 12;                       // x̄ and J̄ of a point and cell
+constexpr int kTileQS = kTileRec * kTileCells;     // per point: the tile's records
+
+template <typename F>
+__device__ __forceinline__ void tile_put_record(F* rec, const F* xb, const F* jb) {
+#pragma unroll
+  for (int g = 0; g < 3; ++g) Vec4<F>::put(rec + 4 * g, xb[g], jb[g * 3], jb[g * 3 + 1], jb[g * 3 + 2]);
+}
 
 // J̄(g, d) at g * 3 + d of a point from its cotangents (d̄ = db, K̄ = kb or null for zero) and its
 // det J and K (K(t, h) at h * 3 + t).
@@ -1032,9 +1040,9 @@ __device__ __forceinline__ void tile_planes(const F* V, F* P, int ps, const F* B
       for (int i = 0; i < N; ++i) ru[i] = rd1[i] = rd2[i] = F(0);
 #pragma unroll
       for (int a0 = 0; a0 < (M > 0 ? M : m0); ++a0) {
-        const F* vq = V + (a0 + m0 * (b1 + m1 * c2)) * QS + l;
-        const F xb = vq[g * TILE], j0 = vq[(D + g * D) * TILE];
-        const F j1 = vq[(D + g * D + 1) * TILE], j2 = vq[(D + g * D + 2) * TILE];
+        F v[4];
+        Vec4<F>::get(V + (size_t)(a0 + m0 * (b1 + m1 * c2)) * QS + l * kTileRec + 4 * g, v);
+        const F xb = v[0], j0 = v[1], j1 = v[2], j2 = v[3];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
           const F bi = B0[a0 * N + i], di = D0[a0 * N + i];
@@ -1153,11 +1161,7 @@ __global__ void __launch_bounds__(kTileBwdThreads, sizeof(F) == 4 ? 5 : 3) vjp_s
       for (int i = 0; i < LJ; ++i) kinv[i] = __ldg(fk + TLG_AT(LJ, i));
 #undef TLG_AT
       tile_jbar<F>(db, ctk ? kb : nullptr, det, kinv, jb);
-      F* vq = V + q * QS + l;
-#pragma unroll
-      for (int g = 0; g < D; ++g) vq[g * TILE] = xb[g];
-#pragma unroll
-      for (int i = 0; i < LJ; ++i) vq[(D + i) * TILE] = jb[i];
+      tile_put_record<F>(V + (size_t)q * QS + l * kTileRec, xb, jb);
     }
     __syncthreads();
     tile_planes<F, N, M, T>(V, P, ps, B0, D0, B1, D1, m0, m1, m2);
@@ -1166,10 +1170,10 @@ __global__ void __launch_bounds__(kTileBwdThreads, sizeof(F) == 4 ? 5 : 3) vjp_s
   }
 }
 
-// Shared memory past the tables of the kernel above: x̄ and J̄ of a tile's points (13 * 16 per
+// Shared memory past the tables of the kernel above: x̄ and J̄ of a tile's points (12 * 16 per
 // point) and the tile's plane sums (16 cells x (2 * 3 * N^2 * m2 + 1)), of F.
 inline size_t vjp_sumfact_tile_extra_bytes(int n, int num_points, int m2, size_t f_bytes) {
-  return f_bytes * ((size_t)num_points * 13 * 16 + 16 * ((size_t)m2 * 3 * n * n * 2 + 1));
+  return f_bytes * ((size_t)num_points * kTileQS + 16 * ((size_t)m2 * 3 * n * n * 2 + 1));
 }
 
 }  // namespace tlg

@@ -65,6 +65,7 @@ struct VjpArgs {
   uint32_t last_node, tab_bytes;
   int num_points;
   int k_runtime;  // K (vjp_tile_kernel)
+  int group;      // nodes per item (vjp_tile_kernel)
 };
 
 constexpr int kVjpGroup = 4;
@@ -473,40 +474,33 @@ __global__ void __launch_bounds__(kGatherNodes) vjp_gather_kernel(const uint32_t
 // time): det J and K read back instead of recomputed, so no coordinates and no forward
 // contraction. A 16-cell tile of the fields per CTA step: one item per (point, cell) reads the
 // cotangents, det J and K (coalesced, the cell fastest) and puts x̄ and J̄ (J̄(g, d) = d̄ det J
-// K(d, g) - (K^T K̄ K^T)(g, d)) in shared memory; one item per (cell, node pair k, k + ceil(K/2)),
-// the node fastest, sums over the points phi_k x̄ + sum_d dphi_k[d] J̄(., d) from the staged node
-// rows and writes the two contribution rows. Two barriers per tile.
-constexpr int kVjpTileThreads = 128;
+// K(d, g) - (K^T K̄ K^T)(g, d)) in shared memory as a record of three 4-vectors (x̄_g, J̄(g, 0..2));
+// one item per (cell, group of a.group consecutive nodes), the group fastest, sums over the points
+// phi_k x̄ + sum_d dphi_k[d] J̄(., d) from the staged node rows (the record read once per point for
+// the group's nodes; split precision's point pairs as two 16-byte loads) and writes the group's
+// rows. The host picks the group size and the CTA size (blockDim.x) so that the items fill whole
+// warps. Two barriers per tile.
+constexpr int kVjpTileMaxGroup = 6;
+constexpr int kVjpTileRec = 12;
 
 template <typename F>
-__global__ void __launch_bounds__(kVjpTileThreads) vjp_tile_kernel(const __grid_constant__ VjpArgs a) {
+__global__ void __launch_bounds__(256) vjp_tile_kernel(const __grid_constant__ VjpArgs a) {
   using A = Ar<F>;
-  constexpr int D = 3, LJ = 9, TILE = 16, T = kVjpTileThreads, QS = 13 * TILE, R = 4;
+  constexpr int D = 3, LJ = 9, TILE = 16, R = 4, G = kVjpTileMaxGroup, RS = kVjpTileRec;
   constexpr int PN = sizeof(F) == 4 ? 2 : 1;  // points per node row (split: point pairs)
+  const int T = blockDim.x;
   __shared__ uint64_t bar;
   extern __shared__ __align__(16) unsigned char smem[];
   if (!stage_table(a.tab, smem, a.tab_bytes, &bar, a.err)) return;
   const F* tab = reinterpret_cast<const F*>(smem);
   F* V = reinterpret_cast<F*>(smem + (a.tab_bytes + 15) / 16 * 16);
-  const int K = a.k_runtime, KH = (K + 1) / 2, nq = a.num_points;
+  const int K = a.k_runtime, nq = a.num_points, grp = a.group;
+  const int ngroups = (K + grp - 1) / grp;
   const F* ctx = static_cast<const F*>(a.ct[0]);
   const F* ctd = static_cast<const F*>(a.ct[1]);
   const F* ctk = static_cast<const F*>(a.ct[2]);
   const F* fdet = static_cast<const F*>(a.out[2]);
   const F* fk = static_cast<const F*>(a.out[3]);
-  // The 8 values of node k's row at point pair (or point) r: phi, dphi_0..2, PN points each.
-  auto row = [&](int r, int k, F* t) {
-    if constexpr (PN == 2) {
-      const float4* p = reinterpret_cast<const float4*>(tab + ((size_t)r * K + k) * 8);
-      const float4 u = p[0], v = p[1];
-      t[0] = u.x; t[1] = u.y; t[2] = u.z; t[3] = u.w;
-      t[4] = v.x; t[5] = v.y; t[6] = v.z; t[7] = v.w;
-    } else {
-      const double2* p = reinterpret_cast<const double2*>(tab + ((size_t)r * K + k) * 4);
-      const double2 u = p[0], v = p[1];
-      t[0] = u.x; t[1] = u.y; t[2] = v.x; t[3] = v.y;
-    }
-  };
   const int64_t ntiles = a.padded / TILE;
   for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int64_t tq = (a.out_first_cell / TILE + tile) * nq;
@@ -541,66 +535,79 @@ __global__ void __launch_bounds__(kVjpTileThreads) vjp_tile_kernel(const __grid_
             for (int g = 0; g < D; ++g) jb[g * D + d] = A::fma(A::neg(kinv[g * D + t]), mt, jb[g * D + d]);
           }
       }
-      F* vq = V + q * QS + l;
+      F* rec = V + ((size_t)q * TILE + l) * RS;
 #pragma unroll
-      for (int g = 0; g < D; ++g) vq[g * TILE] = xb[g];
-#pragma unroll
-      for (int i = 0; i < LJ; ++i) vq[(D + i) * TILE] = jb[i];
+      for (int g = 0; g < D; ++g) Vec4<F>::put(rec + 4 * g, xb[g], jb[g * D], jb[g * D + 1], jb[g * D + 2]);
     }
     __syncthreads();
     const int64_t cell0 = a.first_cell + tile * TILE;
-    for (int it = threadIdx.x; it < KH * TILE; it += T) {
-      const int l = it / KH, k0 = it - (it / KH) * KH, k1 = k0 + KH;
-      const bool two = k1 < K;
+    for (int it = threadIdx.x; it < ngroups * TILE; it += T) {
+      const int l = it / ngroups, gi = it - (it / ngroups) * ngroups;
+      const int k0 = gi * grp;
       const int64_t cell = cell0 + l;
       if (cell >= a.range_end) continue;
-      F acc0[D], acc1[D];
+      F acc[G][D];
 #pragma unroll
-      for (int g = 0; g < D; ++g) acc0[g] = acc1[g] = F(0);
+      for (int u = 0; u < G; ++u)
+#pragma unroll
+        for (int g = 0; g < D; ++g) acc[u][g] = F(0);
       for (int r = 0; r < (nq + PN - 1) / PN; ++r) {
-        F t0[4 * PN], t1[4 * PN];
-        row(r, k0, t0);
-        if (two) row(r, k1, t1);
 #pragma unroll
         for (int h = 0; h < PN; ++h) {
           const int q = r * PN + h;
           if (q >= nq) break;
-          const F* vq = V + q * QS + l;
-          F v[D + LJ];
+          F v[RS];
+          const F* rec = V + ((size_t)q * TILE + l) * RS;
 #pragma unroll
-          for (int i = 0; i < D + LJ; ++i) v[i] = vq[i * TILE];
+          for (int g = 0; g < D; ++g) Vec4<F>::get(rec + 4 * g, v + 4 * g);
 #pragma unroll
-          for (int g = 0; g < D; ++g) {
-            F s0 = A::fma(t0[h], v[g], acc0[g]);
+          for (int u = 0; u < G; ++u) {
+            if (u < grp && k0 + u < K) {
+              // Node k0 + u's row at pair r: phi, dphi_0..2, PN points each.
+              F t[4 * PN];
+              const F* row = tab + ((size_t)r * K + k0 + u) * 4 * PN;
+              Vec4<F>::get(row, t);
+              if constexpr (PN == 2) Vec4<F>::get(row + 4, t + 4);
 #pragma unroll
-            for (int d = 0; d < D; ++d) s0 = A::fma(t0[(1 + d) * PN + h], v[D + g * D + d], s0);
-            acc0[g] = s0;
-          }
-          if (two) {
+              for (int g = 0; g < D; ++g) {
+                F s0 = A::fma(t[h], v[4 * g], acc[u][g]);
 #pragma unroll
-            for (int g = 0; g < D; ++g) {
-              F s1 = A::fma(t1[h], v[g], acc1[g]);
-#pragma unroll
-              for (int d = 0; d < D; ++d) s1 = A::fma(t1[(1 + d) * PN + h], v[D + g * D + d], s1);
-              acc1[g] = s1;
+                for (int d = 0; d < D; ++d) s0 = A::fma(t[(1 + d) * PN + h], v[4 * g + 1 + d], s0);
+                acc[u][g] = s0;
+              }
             }
           }
         }
       }
-      F* base = static_cast<F*>(a.local) + cell * K * R;
-      if constexpr (sizeof(F) == 4) {
-        *reinterpret_cast<float4*>(base + k0 * R) = make_float4(acc0[0], acc0[1], acc0[2], 0.0f);
-        if (two) *reinterpret_cast<float4*>(base + k1 * R) = make_float4(acc1[0], acc1[1], acc1[2], 0.0f);
-      } else {
-        reinterpret_cast<double2*>(base + k0 * R)[0] = make_double2(acc0[0], acc0[1]);
-        reinterpret_cast<double2*>(base + k0 * R)[1] = make_double2(acc0[2], 0.0);
-        if (two) {
-          reinterpret_cast<double2*>(base + k1 * R)[0] = make_double2(acc1[0], acc1[1]);
-          reinterpret_cast<double2*>(base + k1 * R)[1] = make_double2(acc1[2], 0.0);
-        }
-      }
+      F* base = static_cast<F*>(a.local) + (cell * K + k0) * R;
+#pragma unroll
+      for (int u = 0; u < G; ++u)
+        if (u < grp && k0 + u < K) Vec4<F>::put(base + u * R, acc[u][0], acc[u][1], acc[u][2], F(0));
     }
     __syncthreads();
+  }
+}
+
+// The group size and CTA size of vjp_tile_kernel for K nodes: the pair with the most useful work
+// per issued instruction — the share of whole warps its items (16 cells x groups) fill, times the
+// share of its groups' node slots that are nodes, times the share of a node's per-point
+// instructions (12 FMA and a row load) that are not the record's three loads split over the group —
+// ties to the larger group.
+inline void vjp_tile_shape(int k, int* group, int* threads) {
+  double best = -1.0;
+  *group = 1;
+  *threads = 32;
+  for (int g = 1; g <= kVjpTileMaxGroup; ++g) {
+    const int groups = (k + g - 1) / g;
+    const int items = 16 * groups;
+    const int t = items >= 256 ? 256 : (items + 31) / 32 * 32;
+    const int rounds = (items + t - 1) / t;
+    const double score = (double)items / (rounds * t) * ((double)k / (groups * g)) * (13.0 / (13.0 + 3.0 / g));
+    if (score >= best - 1e-12) {
+      best = score;
+      *group = g;
+      *threads = t;
+    }
   }
 }
 

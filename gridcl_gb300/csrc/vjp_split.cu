@@ -27,11 +27,15 @@ cudaError_t launch_vjp_gather(const uint32_t* offsets, const uint32_t* entries, 
 }
 
 cudaError_t launch_vjp_tile(bool split, const VjpArgs& a, size_t smem, cudaStream_t s) {
+  int group = 1, threads = 32;
+  vjp_tile_shape(a.k_runtime, &group, &threads);
+  VjpArgs b = a;
+  b.group = group;
   auto launch = [&](auto kern) -> cudaError_t {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int grid = persistent_grid(kern, smem, a.padded / 16 * kVjpTileThreads, kVjpTileThreads);
-    kern<<<grid, kVjpTileThreads, smem, s>>>(a);
+    const int grid = persistent_grid(kern, smem, a.padded / 16 * threads, threads);
+    kern<<<grid, threads, smem, s>>>(b);
     return cudaGetLastError();
   };
   return split ? launch(vjp_tile_kernel<float>) : launch(vjp_tile_kernel<double>);

@@ -276,7 +276,7 @@ tlg_status tlg_vjp_block(const tlg_tables* tables, const tlg_block* block, const
  * of recomputed, the other output pointers are ignored. Volume cells (TD = GD = 3), f64 or
  * split-precision tables: hexahedra Q1/Q2 at tensor-product rules by the sum-factorised
  * transposed contraction (rows as tlg_vjp_block's sum-factorised adjoint, bit for bit), other
- * cells and rules from the tables' node rows where they and 13 * 16 values per point fit in
+ * cells and rules from the tables' node rows where they and 12 * 16 values per point fit in
  * shared memory; TLG_ERR_UNSUPPORTED otherwise. A forward pass plus this adjoint moves more bytes
  * than the fused pass but needs neither the coordinates nor the forward contraction here. No
  * counterpart in the reference. */
