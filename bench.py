@@ -481,8 +481,9 @@ def extra_hybrid_adjoint():
            "plain_fp64_per_block_fwd_then_vjp": {"ms": plain_ms, "value": qpts / (plain_ms * 1e-3)},
            "error_sample": "forward fields on 16,384 seeded cells per block against the oracle (f64); node "
                            "cotangents against the plain FP64 path's"}
-    # two_pass: the hexahedra's forward on the policy's kernel, their adjoint from the det J and K
-    # fields read back (the re-read is not counted as compulsory).
+    # two_pass (AdjointBatch's default in split precision): each block's forward on the policy's
+    # kernel, its adjoint from the det J and K fields read back (the re-read is not counted as
+    # compulsory); the fused pass for comparison.
     for precision, key, es, two in (("df64", "batched_df64_forward_split_adjoint_graph", 8, False),
                                     ("split", "batched_fused_split_graph", 4, False),
                                     ("split", "batched_two_pass_split_graph", 4, True)):

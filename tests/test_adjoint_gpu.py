@@ -392,7 +392,7 @@ def test_adjoint_batch_equals_the_blocks(cuda, precision):
         ct, _ = cotangent_fields(rng, blk.num_cells, len(rule.get(blk.element.cell)), dt)
         cts.append(ct)
     names = ("points", "jacobian", "detj", "pinv")
-    batch = tg.AdjointBatch(g, rule, cts, precision=precision, forward=names)
+    batch = tg.AdjointBatch(g, rule, cts, precision=precision, forward=names, two_pass=False)
     batch.grad.fill_(float("nan"))  # the first block's sums overwrite every node
     batch.launch()
     batch.launch()  # a second launch replays the graph
@@ -480,11 +480,14 @@ def test_two_pass_adjoint_batch(cuda, precision):
         cts.append(ct)
         hosts.append(host)
     names = ("points", "jacobian", "detj", "pinv")
-    one = tg.AdjointBatch(g, rule, cts, precision=precision, forward=names)
+    one = tg.AdjointBatch(g, rule, cts, precision=precision, forward=names, two_pass=False)
     one.launch()
     two = tg.AdjointBatch(g, rule, cts, precision=precision, forward=names, two_pass=True)
     two.launch()
     two.launch()
+    # The default: two passes in split precision with det J and K among the forward fields.
+    assert tg.AdjointBatch(g, rule, cts, precision=precision, forward=names).two_pass == (precision == "split")
+    assert not tg.AdjointBatch(g, rule, cts, precision=precision, forward=("points",)).two_pass
     tol = 1e-12 if precision == "native" else 2e-5
     assert orc.rel_err(two.grad.cpu().numpy(), one.grad.cpu().numpy()) < tol
     absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
@@ -521,7 +524,7 @@ def test_two_pass_adjoint_on_hexahedra(cuda, precision, degree, counts, missing)
     names = ("detj", "pinv")
     two = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct], precision=precision, forward=names, two_pass=True)
     two.launch()
-    one = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct], precision=precision, forward=names)
+    one = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct], precision=precision, forward=names, two_pass=False)
     one.launch()
     absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
     want = orc.vjp("Hexahedron", degree, absx, mesh.blocks[0].cells, ps.points, host["points"],
@@ -552,7 +555,7 @@ def test_two_pass_adjoint_on_volume_cells(cuda, precision, cell, degree, rdeg, m
     names = ("detj", "pinv")
     two = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct], precision=precision, forward=names, two_pass=True)
     two.launch()
-    one = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct], precision=precision, forward=names)
+    one = tg.AdjointBatch(g, tg.QuadRule([ps]), [ct], precision=precision, forward=names, two_pass=False)
     one.launch()
     absx = g.nodes.cpu().numpy() + np.array(g.origin[:3])
     want = orc.vjp(cell, degree, absx, mesh.blocks[0].cells, ps.points, host["points"], host["detj"][..., 0],
