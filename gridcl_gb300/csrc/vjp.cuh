@@ -626,7 +626,7 @@ struct GatherBlocks {
 };
 
 template <typename L, int D>
-__global__ void __launch_bounds__(kGatherNodes) vjp_gather_blocks_kernel(const __grid_constant__ GatherBlocks gb,
+__global__ void __launch_bounds__(kGatherNodes, 6) vjp_gather_blocks_kernel(const __grid_constant__ GatherBlocks gb,
                                                                          int64_t num_nodes, double* grad, int add) {
   constexpr int R = vjp_row(D);
   using Row = VjpRow<L, R>;
@@ -638,11 +638,24 @@ __global__ void __launch_bounds__(kGatherNodes) vjp_gather_blocks_kernel(const _
 #pragma unroll
     for (int g = 0; g < D; ++g) v[g] = 0.0;
     bool have = false;  // add: v holds the gradient's value
-    for (int bi = 0; bi < gb.count; ++bi) {
+    // The blocks' CSR ranges of this CTA's nodes, loaded together before the blocks' passes (one
+    // latency, not one per block: most blocks of a batch have no entries in most CTAs' ranges).
+    uint32_t E0[kGatherMaxBlocks], E1[kGatherMaxBlocks];
+#pragma unroll
+    for (int bi = 0; bi < kGatherMaxBlocks; ++bi) {
+      E0[bi] = E1[bi] = 0u;
+      if (bi < gb.count) {
+        E0[bi] = gb.offsets[bi][n0];
+        E1[bi] = gb.offsets[bi][n_end];
+      }
+    }
+#pragma unroll
+    for (int bi = 0; bi < kGatherMaxBlocks; ++bi) {
+      if (bi >= gb.count) break;
       const uint32_t* offsets = gb.offsets[bi];
       const uint32_t* entries = gb.entries[bi];
       const L* local = static_cast<const L*>(gb.local[bi]);
-      const uint32_t e0 = offsets[n0], e1 = offsets[n_end];
+      const uint32_t e0 = E0[bi], e1 = E1[bi];
       uint32_t b = e0, e = e0;
       if (e1 > e0 && n < num_nodes) {
         b = offsets[n];
