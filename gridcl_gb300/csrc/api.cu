@@ -3,6 +3,7 @@
 // strategy settings and policy, and the launches of the evaluation, E-vector and adjoint kernels,
 // singly and as CUDA-graph batches.
 #include <algorithm>
+#include <array>
 #include <cctype>
 #include <cmath>
 #include <cstdlib>
@@ -59,6 +60,10 @@ struct tlg_tables {
   // (head of point 2p, head of point 2p + 1, tail of 2p, tail of 2p + 1); an odd last point pairs
   // with itself.
   uint32_t off_dfrows = 0, dfrows_bytes = 0;
+  // The double-float monomial form (tetrahedra P1-P3): dfrows hold the monomials' rows, off_dfmono
+  // the expansion C [k][m] (f32 head, tail) and the monomials' direction masks.
+  uint32_t off_dfmono = 0;
+  bool df_mono = false;
   // The adjoint's table after the error word (codimension 0, f64 or split tables; 0 bytes when
   // absent or too large to stage): per node of each point (f64) or point pair (split) the 32
   // bytes phi, dphi_0 .. dphi_{TD-1}, zero padding, as f64 values or f32 pairs.
@@ -463,7 +468,9 @@ tlg_status eval_df(const tlg_tables* t, const tlg_block* b, const tlg_outputs* o
   a.off_refn = t->off_refn;
   a.mask = mask;
   a.num_points = (int)t->q;
-  const size_t smem = (size_t)(t->bytes + 15) / 16 * 16 + tlg::df_slot_bytes((int)t->k, t->gd);
+  a.off_mono = t->off_dfmono;
+  a.mono = t->df_mono ? 1 : 0;
+  const size_t smem = (size_t)(t->bytes + 15) / 16 * 16 + tlg::df_slot_bytes((int)t->k, t->gd, t->df_mono);
   if (smem > (size_t)227 * 1024) return TLG_ERR_UNSUPPORTED;
   cudaError_t e = tlg::launch_eval_df(t->td, t->gd, (int)t->k, a, smem, stream, found);
   if (!*found) return TLG_ERR_UNSUPPORTED;
@@ -668,6 +675,106 @@ void record_launch(int family, int strategy) {
 }
 
 }  // namespace tlg
+
+// The double-float monomial form of a tetrahedron's tables (P1-P3): the monomials x^a, |a| <= p,
+// the expansion C = V^-1 of the Lagrange functions in them (V[j][m] = x_j^(a_m) at the Lagrange
+// points, Gauss-Jordan with partial pivoting), checked against the tabulation at every point
+// (values and derivatives within 1e-11); on success the double-float rows are overwritten with the
+// monomials' (the same layout: per point pair and monomial, x^a and its derivatives as heads and
+// tails of both points) and the expansion and direction masks written at off_dfmono.
+void df_monomial_form(tlg_tables* t, const double* points, int64_t npoints, const std::vector<double>& phi,
+                      const std::vector<double>& dphi) {
+  const int k = (int)t->k, td = t->td, p = t->degree;
+  std::vector<std::array<int, 3>> al;
+  for (int s = 0; s <= p; ++s)
+    for (int a = s; a >= 0; --a)
+      for (int b = s - a; b >= 0; --b) al.push_back({a, b, s - a - b});
+  if ((int)al.size() != k || td != 3) return;
+  auto mono = [&](const double* x, int m) {
+    double v = 1.0;
+    for (int d = 0; d < 3; ++d)
+      for (int e = 0; e < al[m][d]; ++e) v *= x[d];
+    return v;
+  };
+  auto dmono = [&](const double* x, int m, int d) {
+    if (al[m][d] == 0) return 0.0;
+    double v = (double)al[m][d];
+    for (int e = 0; e < 3; ++e)
+      for (int i = 0; i < al[m][e] - (e == d ? 1 : 0); ++i) v *= x[e];
+    return v;
+  };
+  const std::vector<double> lp = tlg::lagrange_points(t->cell, p, t->family);
+  // [V | I] -> [I | V^-1]
+  std::vector<double> a((size_t)k * 2 * k, 0.0);
+  for (int j = 0; j < k; ++j) {
+    for (int m = 0; m < k; ++m) a[(size_t)j * 2 * k + m] = mono(&lp[(size_t)j * 3], m);
+    a[(size_t)j * 2 * k + k + j] = 1.0;
+  }
+  for (int c = 0; c < k; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < k; ++r)
+      if (std::fabs(a[(size_t)r * 2 * k + c]) > std::fabs(a[(size_t)piv * 2 * k + c])) piv = r;
+    if (std::fabs(a[(size_t)piv * 2 * k + c]) < 1e-12) return;
+    if (piv != c)
+      for (int e = 0; e < 2 * k; ++e) std::swap(a[(size_t)piv * 2 * k + e], a[(size_t)c * 2 * k + e]);
+    const double inv = 1.0 / a[(size_t)c * 2 * k + c];
+    for (int e = 0; e < 2 * k; ++e) a[(size_t)c * 2 * k + e] *= inv;
+    for (int r = 0; r < k; ++r) {
+      if (r == c) continue;
+      const double f = a[(size_t)r * 2 * k + c];
+      if (f != 0.0)
+        for (int e = 0; e < 2 * k; ++e) a[(size_t)r * 2 * k + e] -= f * a[(size_t)c * 2 * k + e];
+    }
+  }
+  // V C = I: C[m][kk] = (V^-1)[m][kk].
+  std::vector<double> C((size_t)k * k);
+  for (int m = 0; m < k; ++m)
+    for (int kk = 0; kk < k; ++kk) {
+      double v = a[(size_t)m * 2 * k + k + kk];
+      if (std::fabs(v) < 1e-13) v = 0.0;
+      C[(size_t)m * k + kk] = v;
+    }
+  double err = 0.0;
+  for (int64_t q = 0; q < npoints; ++q)
+    for (int kk = 0; kk < k; ++kk) {
+      double v = 0.0, dv[3] = {0.0, 0.0, 0.0};
+      for (int m = 0; m < k; ++m) {
+        const double cm = C[(size_t)m * k + kk];
+        v += cm * mono(points + q * 3, m);
+        for (int d = 0; d < 3; ++d) dv[d] += cm * dmono(points + q * 3, m, d);
+      }
+      err = std::max(err, std::fabs(v - phi[(size_t)q * k + kk]));
+      for (int d = 0; d < 3; ++d) err = std::max(err, std::fabs(dv[d] - dphi[((size_t)q * k + kk) * 3 + d]));
+    }
+  if (!(err <= 1e-11)) return;
+  const int64_t qp = (npoints + 1) / 2;
+  float* rows = reinterpret_cast<float*>(t->host.data() + t->off_dfrows);
+  for (int64_t pp = 0; pp < qp; ++pp)
+    for (int m = 0; m < k; ++m)
+      for (int r = 0; r <= td; ++r)
+        for (int h = 0; h < 2; ++h) {
+          const int64_t q = std::min<int64_t>(2 * pp + h, npoints - 1);
+          const double v = r == 0 ? mono(points + q * 3, m) : dmono(points + q * 3, m, r - 1);
+          float* e = rows + ((pp * k + m) * (1 + td) + r) * 4;
+          e[h] = (float)v;
+          e[2 + h] = (float)(v - (double)(float)v);
+        }
+  float* coef = reinterpret_cast<float*>(t->host.data() + t->off_dfmono);
+  for (int kk = 0; kk < k; ++kk)
+    for (int m = 0; m < k; ++m) {
+      const double v = C[(size_t)m * k + kk];
+      coef[((size_t)kk * k + m) * 2] = (float)v;
+      coef[((size_t)kk * k + m) * 2 + 1] = (float)(v - (double)(float)v);
+    }
+  uint32_t* mask = reinterpret_cast<uint32_t*>(t->host.data() + t->off_dfmono + (size_t)k * k * 8);
+  for (int m = 0; m < k; ++m) {
+    uint32_t bits = 0;
+    for (int d = 0; d < 3; ++d)
+      if (al[m][d] > 0) bits |= 1u << d;
+    mask[m] = bits;
+  }
+  t->df_mono = true;
+}
 
 extern "C" {
 
@@ -1091,6 +1198,10 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
       t->off_dfrows = (uint32_t)total;
       t->dfrows_bytes = (uint32_t)((size_t)qp * k * (1 + td) * 16);
       total = align16(total + t->dfrows_bytes);
+      if (cell == tlg::kTetrahedron && gdim == 3 && (k == 4 || k == 10 || k == 20)) {
+        t->off_dfmono = (uint32_t)total;
+        total = align16(total + (size_t)k * k * 8 + (size_t)k * 4);
+      }
     }
     // Tables beyond the shared-memory budget stay in global memory: the loops kernels read them
     // there (L1/L2-cached) instead of staging them.
@@ -1250,6 +1361,7 @@ tlg_status tlg_tables_create(int cell, int degree, int family, int gdim, int dty
               e[2 + h] = (float)(v - (double)(float)v);
             }
     }
+    if (t->off_dfmono) df_monomial_form(t, points, npoints, phi, dphi);
     if (dtype != TLG_F64) {
       std::vector<double> rows2((size_t)qp * k * rw, 0.0);
       for (int64_t p = 0; p < qp; ++p)

@@ -7,6 +7,17 @@ namespace tlg {
 
 cudaError_t launch_eval_df(int td, int gd, int k, const DfArgs& a, size_t smem, cudaStream_t s, bool* found) {
   *found = true;
+  if (a.mono) {
+    // The monomial form (its rows are not the nodes'): tetrahedra P1-P3 only.
+#define TLG_DFM(TD, GD, K) \
+  if (td == TD && gd == GD && k == K) return launch_persistent(eval_df_kernel<TD, GD, K, true>, a, a.padded, smem, s);
+    TLG_DFM(3, 3, 4)
+    TLG_DFM(3, 3, 10)
+    TLG_DFM(3, 3, 20)
+#undef TLG_DFM
+    *found = false;
+    return cudaSuccess;
+  }
 #define TLG_DFK(TD, GD, K) \
   if (td == TD && gd == GD && k == K) return launch_persistent(eval_df_kernel<TD, GD, K>, a, a.padded, smem, s);
   // Tetrahedra P1-P3, hexahedra Q1-Q2, prisms P1-P2.

@@ -31,6 +31,11 @@ struct DfArgs {
   double origin[3];
   uint32_t last_node, tab_bytes, off_rows, off_refn, mask;
   int num_points;
+  // Monomial form (tetrahedra P1-P3): the rows at off_rows are those of the monomials x^a of the
+  // Lagrange space, and off_mono holds the expansion C [k][m] (f32 head, tail) and per monomial
+  // the mask of the directions it depends on (u32 bits).
+  uint32_t off_mono;
+  int mono;
 };
 
 // Output cursor of an f64 field (tile 16): point pairs of double-floats, assembled into f64.
@@ -53,10 +58,18 @@ struct DfCursor {
 
 // Shared memory past the staged tables: per thread the double-float coordinates y_k (k >= 1) as
 // (head, tail) f32 pairs, [k - 1][g] with stride kEvalThreads (the lanes of a warp read
-// consecutive 8-byte slots).
-inline size_t df_slot_bytes(int k, int gd) { return (size_t)(k - 1) * gd * kEvalThreads * 8; }
+// consecutive 8-byte slots); in the monomial form the K coefficient vectors c_m, [m][g].
+inline size_t df_slot_bytes(int k, int gd, bool mono = false) {
+  return (size_t)(mono ? k : k - 1) * gd * kEvalThreads * 8;
+}
 
-template <int TD, int GD, int K>
+// MONO: the monomial form. The map of a cell is x_0 + sum_m c_m x^(a_m) with c_m = sum_k C[m][k]
+// y_k, formed once per cell (double-float sums over the nonzero C[m][k]; accumulated in the slots
+// and normalised there). At a point J(:, d) = sum over the monomials that depend on x_d of
+// c_m d(x^(a_m))/dx_d: for a P2 tetrahedron 12 (monomial, direction) terms instead of the 27 of
+// the nine nodes k >= 1, about a third fewer double-float terms per point with x; the same
+// epilogue.
+template <int TD, int GD, int K, bool MONO = false>
 __global__ void __launch_bounds__(kEvalThreads) eval_df_kernel(const __grid_constant__ DfArgs a) {
   constexpr int TILE = 16;
   constexpr int LJ = TD * GD;
@@ -88,15 +101,51 @@ __global__ void __launch_bounds__(kEvalThreads) eval_df_kernel(const __grid_cons
     const uint32_t n0 = min(idx[0], a.last_node);
 #pragma unroll
     for (int g = 0; g < GD; ++g) x0[g] = __ldg(a.nodes + (int64_t)n0 * GD + g);
-    // y_k = x_k - x_0 (k >= 1) into this thread's slots; the k = 0 term of every sum vanishes.
+    if constexpr (MONO) {
+      // c_m = sum_k C[m][k] y_k (y_0 = 0), accumulated in the slots as (sum, error) pairs.
+      const float2* coef = reinterpret_cast<const float2*>(smem + a.off_mono);
 #pragma unroll
-    for (int k = 1; k < K; ++k) {
-      const uint32_t n = min(idx[k], a.last_node);
+      for (int i = 0; i < K * GD; ++i) ys[i * T] = make_float2(0.0f, 0.0f);
+#pragma unroll 1
+      for (int k = 1; k < K; ++k) {
+        // The row again through L1 (a rolled loop cannot index idx[] in registers).
+        const uint32_t n = min(__ldg(a.dofmap + cell * K + k), a.last_node);
+        float yh[GD], yl[GD];
 #pragma unroll
-      for (int g = 0; g < GD; ++g) {
-        float h, l;
-        df_split(__dsub_rn(__ldg(a.nodes + (int64_t)n * GD + g), x0[g]), h, l);
-        ys[((k - 1) * GD + g) * T] = make_float2(h, l);
+        for (int g = 0; g < GD; ++g) df_split(__dsub_rn(__ldg(a.nodes + (int64_t)n * GD + g), x0[g]), yh[g], yl[g]);
+#pragma unroll
+        for (int m = 0; m < K; ++m) {
+          const float2 cm = coef[k * K + m];
+          if (cm.x != 0.0f) {
+#pragma unroll
+            for (int g = 0; g < GD; ++g) {
+              const float2 st = ys[(m * GD + g) * T];
+              DfAcc<float> acc;
+              acc.s = st.x;
+              acc.c = st.y;
+              acc.add(yh[g], yl[g], cm.x, cm.y);
+              ys[(m * GD + g) * T] = make_float2(acc.s, acc.c);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < K * GD; ++i) {
+        const float2 st = ys[i * T];
+        const DF<float> v = Ar<DF<float>>::fast_two_sum(st.x, st.y);
+        ys[i * T] = make_float2(v.h, v.l);
+      }
+    } else {
+      // y_k = x_k - x_0 (k >= 1) into this thread's slots; the k = 0 term of every sum vanishes.
+#pragma unroll
+      for (int k = 1; k < K; ++k) {
+        const uint32_t n = min(idx[k], a.last_node);
+#pragma unroll
+        for (int g = 0; g < GD; ++g) {
+          float h, l;
+          df_split(__dsub_rn(__ldg(a.nodes + (int64_t)n * GD + g), x0[g]), h, l);
+          ys[((k - 1) * GD + g) * T] = make_float2(h, l);
+        }
       }
     }
     float oh[GD], ol[GD];  // x_0 + origin
@@ -130,11 +179,13 @@ __global__ void __launch_bounds__(kEvalThreads) eval_df_kernel(const __grid_cons
       for (int g = 0; g < GD; ++g) ax[g].zero();
 #pragma unroll
       for (int i = 0; i < LJ; ++i) aj[i].zero();
+      // (MONO: monomial m's rows, its coefficients in slot m, the directions it depends on.)
+      const uint32_t* mmask = reinterpret_cast<const uint32_t*>(smem + a.off_mono + K * K * 8);
 #pragma unroll 1
-      for (int k = 1; k < K; ++k) {
+      for (int k = MONO ? 0 : 1; k < K; ++k) {
         float2 y[GD];
 #pragma unroll
-        for (int g = 0; g < GD; ++g) y[g] = ys[((k - 1) * GD + g) * T];
+        for (int g = 0; g < GD; ++g) y[g] = ys[((MONO ? k : k - 1) * GD + g) * T];
         if (want_x) {
           const float4 r = rq[k * RW];
 #pragma unroll
@@ -142,8 +193,10 @@ __global__ void __launch_bounds__(kEvalThreads) eval_df_kernel(const __grid_cons
             ax[g].add(B::splat(y[g].x), B::splat(y[g].y), make_float2(r.x, r.y), make_float2(r.z, r.w));
         }
         if (want_j) {
+          const uint32_t dep = MONO ? mmask[k] : ~0u;
 #pragma unroll
           for (int d = 0; d < TD; ++d) {
+            if (!((dep >> d) & 1u)) continue;
             const float4 r = rq[k * RW + 1 + d];
             const V th = make_float2(r.x, r.y), tl = make_float2(r.z, r.w);
 #pragma unroll
