@@ -839,7 +839,7 @@ def extra_p1_box():
 # What binds each mode's kernel, from its ncu capture (the profiles of the P2 tetrahedra): the
 # double-float and FP64 kernels are bound by an arithmetic pipe, not by HBM.
 BINDING = {
-    "df64": "FP32 pipe: FMA 62.8 %, ALU 35.2 %, issue 56.5 % of active cycles (ncu, 32^3 x 6 case)",
+    "df64": "FP32 pipes: FMA 54.8 %, ALU 45.5 %, issue 59.9 % of active cycles (ncu, 32^3 x 6 case, monomial form)",
     "f64": "FP64 pipe: 93.7 % of active cycles (ncu)",
     "split": "HBM: stores of the f32 fields (ncu traffic 1.004 x the algorithmic bytes)",
     "f32": "HBM: stores of the f32 fields",
